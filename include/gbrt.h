@@ -1,0 +1,284 @@
+/*
+ * gbrt.h — C ABI of the GB300 unidirectional path-tracing hot path.
+ *
+ * This is the drop-in boundary for the renderer's PerPixelRenderer ->
+ * UniDiPathTracingIntegrator path. Every entry point takes plain pointers and
+ * sizes; no C++ or torch types cross it, and no C++ exception escapes it.
+ *
+ * Conventions shared with the renderer being replaced:
+ *   - Spectra (material colours, light intensities, film) are stored in BGR
+ *     channel order, as cv::Vec3f is in the renderer (src/sceneast.cpp:410-414,
+ *     src/mathhelper.cpp:102-105). The scene-file parser swaps RGB->BGR.
+ *   - A miss is reported as t = NaN (src/hitrecord.h:62-64, :111-114).
+ *   - A hit on the environment map is reported at t = +inf with the map's
+ *     primitive id (src/environmentmap.cpp:73-83).
+ *   - The film is H x W x 3 float, row-major, row 0 at the top of the image
+ *     (src/perpixelrenderer.cpp:62-96, src/camera.cpp:50-58).
+ *
+ * Primitive ids. The renderer renders IntersectableList(lights..., scene)
+ * (src/sceneast.cpp:673-695) and flattens nested lists into BVH leaves
+ * (src/intersectable.cpp:6-14, src/intersectablelist.cpp:67-78). gbrt numbers
+ * leaves in that spirit with a fixed type order:
+ *   [0, n_lights)                       lights (area lights and the env map are
+ *                                       hittable; point lights never are)
+ *   [+0, +n_tri)                        triangles
+ *   [+0, +n_quads)                      quads (one id per quad, like the
+ *                                       renderer's Quad object, src/quad.h:32)
+ *   [+0, +n_spheres)                    spheres
+ *   [+0, +n_planes)                     planes
+ *
+ * Threading: calls on one gbrt_ctx are serialised by the caller; distinct
+ * contexts are independent. All device memory is owned by the library.
+ */
+#ifndef GBRT_H
+#define GBRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBRT_ABI_VERSION 1
+
+typedef enum gbrt_status {
+  GBRT_OK = 0,
+  GBRT_ERR_INVALID_ARG = 1,
+  GBRT_ERR_OOM = 2,
+  GBRT_ERR_CUDA = 3,
+  GBRT_ERR_CANCELLED = 4,
+  GBRT_ERR_TIMEOUT = 5,
+  GBRT_ERR_NUMERIC = 6,
+  GBRT_ERR_PARSE = 7,
+  GBRT_ERR_IO = 8,
+  GBRT_ERR_UNSUPPORTED = 9
+} gbrt_status;
+
+/* Material kinds: src/material.h:30-50 and its subclasses. */
+typedef enum gbrt_material_type {
+  GBRT_MAT_DARK = 0,        /* DarkMatter, src/darkmatter.cpp:32-39          */
+  GBRT_MAT_DIFFUSE = 1,     /* DiffuseMaterial, src/diffusematerial.cpp:25-28 */
+  GBRT_MAT_MIRROR = 2,      /* MirrorMaterial, src/mirrormaterial.cpp:31-41   */
+  GBRT_MAT_PHONG = 3,       /* PhongMaterial, src/phongmaterial.cpp:31-81     */
+  GBRT_MAT_BLINN = 4,       /* BlinnMaterial, src/blinnmaterial.cpp:34-84     */
+  GBRT_MAT_TRANSPARENT = 5  /* TransparentMaterial, src/transparentmaterial.cpp:34-80 */
+} gbrt_material_type;
+
+typedef struct gbrt_material {
+  int32_t type;      /* gbrt_material_type                                 */
+  float kd[3];       /* diffuse colour (BGR); phong/blinn/diffuse          */
+  float ks[3];       /* specular colour (BGR); phong/blinn                 */
+  float exponent;    /* phong/blinn exponent                               */
+  float ior;         /* transparent: refraction coefficient                */
+  float coefficient; /* mirror: coefficient (ignored, as in the renderer)  */
+} gbrt_material;
+
+/* Quad(p1,p2,p3,p4): triangles (p1,p2,p4) and (p4,p2,p3), src/quad.h:32. */
+typedef struct gbrt_quad {
+  float p[4][3];
+  int32_t material;
+} gbrt_quad;
+
+/* Sphere(center, radius), src/sphere.cpp:29-56. */
+typedef struct gbrt_sphere {
+  float center[3];
+  float radius;
+  int32_t material;
+} gbrt_sphere;
+
+/* Plane: points x with dot((x,1), plane) = 0, src/plane.cpp:27-40. */
+typedef struct gbrt_plane {
+  float plane[4];
+  int32_t material;
+} gbrt_plane;
+
+typedef enum gbrt_light_type {
+  GBRT_LIGHT_AREA = 0,   /* AreaLight(origin,u,v,Le), src/arealight.cpp:31-118 */
+  GBRT_LIGHT_POINT = 1,  /* PointLight(pos,I), src/pointlight.cpp:29-70        */
+  GBRT_LIGHT_ENV = 2,    /* EnvironmentMap, src/environmentmap.cpp:16-108      */
+  GBRT_LIGHT_BLACK = 3   /* BlackLight (failed env map), src/blacklight.cpp:5-24 */
+} gbrt_light_type;
+
+typedef struct gbrt_light {
+  int32_t type;        /* gbrt_light_type                                  */
+  float origin[3];     /* area: corner; point: position                    */
+  float u[3];          /* area: first edge                                 */
+  float v[3];          /* area: second edge                                */
+  float intensity[3];  /* BGR; area: Le; point: I; env: coefficient        */
+} gbrt_light;
+
+typedef enum gbrt_env_mapping {
+  GBRT_ENV_ANGULAR = 0, /* angular light probe, src/environmentmap.cpp:57-65 */
+  GBRT_ENV_LATLONG = 1  /* equirectangular (extension for lat-long skies)   */
+} gbrt_env_mapping;
+
+/* Environment image, height x width x 3 float BGR, row-major. At most one per
+ * scene; a light of type GBRT_LIGHT_ENV refers to it. */
+typedef struct gbrt_env_map {
+  int32_t width, height;
+  int32_t mapping;        /* gbrt_env_mapping */
+  const float* texels;    /* host pointer, copied by gbrt_scene_create */
+} gbrt_env_map;
+
+typedef struct gbrt_scene_desc {
+  const gbrt_material* materials; int32_t n_materials;
+  /* triangle soup: n_tri x 9 positions (p1,p2,p3); optional n_tri x 9 normals
+   * (a triangle whose three normals are not all non-zero uses its geometric
+   * normal, src/sceneast.cpp:514-521); optional n_tri x 6 texcoords; material
+   * per triangle (NULL: all use material 0). */
+  const float* tri_pos; const float* tri_nrm; const float* tri_uv;
+  const int32_t* tri_mat; int64_t n_tri;
+  const gbrt_quad* quads; int32_t n_quads;
+  const gbrt_sphere* spheres; int32_t n_spheres;
+  const gbrt_plane* planes; int32_t n_planes;
+  const gbrt_light* lights; int32_t n_lights;
+  const gbrt_env_map* env;  /* NULL if no environment map */
+} gbrt_scene_desc;
+
+/* Camera(cop, lookAt, up, fov[radians, full vertical], resolution),
+ * src/camera.cpp:34-58. */
+typedef struct gbrt_camera {
+  float eye[3], look_at[3], up[3];
+  float fov;
+  int32_t width, height;
+} gbrt_camera;
+
+typedef enum gbrt_semantics {
+  /* the renderer's estimator with all of its quirks */
+  GBRT_SEM_REFERENCE = 0,
+  /* reserved: physically based estimator */
+  GBRT_SEM_PHYSICAL = 1
+} gbrt_semantics;
+
+/* Options of PerPixelRenderer (src/perpixelrenderer.cpp:103-112) plus the
+ * path-length cap, which the renderer fixes at compile time (MAX_DEPTH 5,
+ * src/renderer.h:38). */
+typedef struct gbrt_render_params {
+  int32_t x_samples;        /* --pt-x-samples (default 4)                  */
+  int32_t y_samples;        /* --pt-y-samples (default 4)                  */
+  float termination_prob;   /* --pt-termination-prob (default 0.5)         */
+  int32_t max_depth;        /* MAX_DEPTH (renderer: 5)                     */
+  uint64_t seed;            /* --seed                                      */
+  int32_t semantics;        /* gbrt_semantics                              */
+  int32_t batch_paths;      /* paths in flight per wavefront; 0 = auto     */
+} gbrt_render_params;
+
+typedef struct gbrt_stats {
+  uint64_t paths;           /* camera samples traced to termination        */
+  uint64_t extension_rays;  /* closest-hit rays (camera + bounce)          */
+  uint64_t shadow_rays;     /* any-hit rays                                */
+  uint64_t nonfinite;       /* samples whose radiance was NaN/inf (dropped)*/
+  double render_ms;         /* device time of the render loop              */
+  uint64_t kernel_launches; /* kernels launched by the render loop         */
+} gbrt_stats;
+
+/* Ray(origin, direction, from, to), src/ray.h:36-57. 32 bytes. */
+typedef struct gbrt_ray {
+  float org[3]; float tmin;
+  float dir[3]; float tmax;
+} gbrt_ray;
+
+/* HitRecord essentials, src/hitrecord.h:35-60. 16 bytes. */
+typedef struct gbrt_hit {
+  float t;          /* NaN on a miss, +inf on the environment map         */
+  int32_t prim;     /* primitive id (see above); -1 on a miss             */
+  float u, v;       /* barycentrics of the hit (triangles/quads)          */
+} gbrt_hit;
+
+typedef struct gbrt_ctx gbrt_ctx;
+typedef struct gbrt_scene gbrt_scene;
+
+/* ---- library ---------------------------------------------------------- */
+int32_t gbrt_abi_version(void);
+/* NUL-terminated message of the last failing call on ctx (or a global one
+ * when ctx is NULL). Valid until the next call on that context. */
+const char* gbrt_last_error(const gbrt_ctx* ctx);
+
+/* ---- context (replaces RenderingManager/Renderer set-up,
+ *      src/renderingmanager.cpp:8-59, src/renderer.cpp:131-145) ---------- */
+gbrt_status gbrt_ctx_create(int32_t device, gbrt_ctx** out);
+gbrt_status gbrt_ctx_destroy(gbrt_ctx* ctx);
+
+/* ---- scene (replaces scene_builder::getScene + Intersectable::createBVH,
+ *      src/sceneast.cpp:673-695, src/intersectable.cpp:11-14,
+ *      src/bvh.cpp:67-94). Deep-copies desc to the device and builds the
+ *      BVH. ------------------------------------------------------------- */
+gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* desc,
+                              gbrt_scene** out);
+gbrt_status gbrt_scene_destroy(gbrt_scene* scene);
+/* BVH statistics: nodes, leaves, max depth, SAH cost, build milliseconds. */
+gbrt_status gbrt_scene_info(const gbrt_scene* scene, int64_t* n_nodes,
+                            int64_t* n_leaves, int32_t* max_depth,
+                            double* sah_cost, double* build_ms);
+
+/* ---- ray queries (batched Intersectable::intersect, src/intersectable.h:40;
+ *      BVHNode::intersect, src/bvh.cpp:135-149) ------------------------- */
+/* Host pointers; copies in and out inside the call. */
+gbrt_status gbrt_trace_closest(gbrt_scene* scene, const gbrt_ray* rays,
+                               int64_t n, gbrt_hit* hits);
+/* Any-hit occlusion: occluded[i] = 1 if some primitive other than
+ * ignore_prim[i] (may be NULL) is hit in [tmin, tmax]. The environment map
+ * never occludes. Host pointers. (src/arealight.cpp:41-46,
+ * src/pointlight.cpp:55-60, src/environmentmap.cpp:44-50) */
+gbrt_status gbrt_trace_any(gbrt_scene* scene, const gbrt_ray* rays,
+                           const int32_t* ignore_prim, int64_t n,
+                           uint8_t* occluded);
+/* Device-pointer variants, enqueued on the context's stream (stream may be
+ * NULL for the context stream, else a cudaStream_t). Asynchronous. */
+gbrt_status gbrt_trace_closest_device(gbrt_scene* scene, const gbrt_ray* d_rays,
+                                      int64_t n, gbrt_hit* d_hits, void* stream);
+gbrt_status gbrt_trace_any_device(gbrt_scene* scene, const gbrt_ray* d_rays,
+                                  const int32_t* d_ignore_prim, int64_t n,
+                                  uint8_t* d_occluded, void* stream);
+
+/* ---- render (PerPixelRenderer::render + UniDiPathTracingIntegrator,
+ *      src/perpixelrenderer.cpp:43-101, src/unidipathtracingintegrator.cpp:34-107,
+ *      src/renderer.cpp:47-106) ----------------------------------------- */
+/* film_bgr: H x W x 3 float host buffer, overwritten with the per-pixel
+ * mean. opt_sum / opt_sumsq: optional H x W x 3 double host buffers that
+ * receive the per-pixel sum and sum of squares of the per-sample radiance
+ * (for variance / z-tests). stop_flag: optional host flag polled between
+ * wavefront batches (the renderer's doStop, src/renderer.h:71); a set flag
+ * ends the call with GBRT_ERR_CANCELLED. stats may be NULL. */
+gbrt_status gbrt_render(gbrt_scene* scene, const gbrt_camera* camera,
+                        const gbrt_render_params* params, float* film_bgr,
+                        double* opt_sum, double* opt_sumsq,
+                        const volatile int32_t* stop_flag, gbrt_stats* stats);
+/* Device-resident variant: d_film_bgr (float) and the optional d_sum /
+ * d_sumsq (double) are device pointers of H x W x 3. Synchronous. */
+gbrt_status gbrt_render_device(gbrt_scene* scene, const gbrt_camera* camera,
+                               const gbrt_render_params* params,
+                               float* d_film_bgr, double* d_sum,
+                               double* d_sumsq, gbrt_stats* stats);
+
+/* ---- scene files (SceneGrammar::parse + resolveVars + buildScene,
+ *      src/sceneparser.cpp:36-156, src/sceneast.cpp:673-747,
+ *      src/objreader.cpp:142-366) --------------------------------------- */
+typedef struct gbrt_parsed_scene gbrt_parsed_scene;
+/* Parses a scene file (the renderer's scene language) with its OBJ/MTL files
+ * and its environment map (Radiance .hdr or .pfm). Pure host code. */
+gbrt_status gbrt_parse_scene_file(const char* path, gbrt_parsed_scene** out,
+                                  char* err, int32_t err_len);
+gbrt_status gbrt_parse_scene_string(const char* text, const char* base_dir,
+                                    gbrt_parsed_scene** out, char* err,
+                                    int32_t err_len);
+/* Borrowed views, valid until gbrt_parsed_scene_free. has_camera is 0 when
+ * the file defines no variable named "camera". */
+gbrt_status gbrt_parsed_scene_desc(const gbrt_parsed_scene* ps,
+                                   gbrt_scene_desc* desc, gbrt_camera* camera,
+                                   int32_t* has_camera);
+void gbrt_parsed_scene_free(gbrt_parsed_scene* ps);
+
+/* Radiance RGBE (.hdr) reader: returns H x W x 3 float BGR in a buffer the
+ * caller frees with gbrt_free. (Replaces cv::imread in
+ * src/environmentmap.cpp:20-33.) */
+gbrt_status gbrt_read_hdr(const char* path, float** texels_bgr,
+                          int32_t* width, int32_t* height);
+void gbrt_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBRT_H */

@@ -1,0 +1,111 @@
+"""ctypes binding of oracle/_build/liboracle.so (TEST INFRASTRUCTURE ONLY).
+
+Builds the library on first use when it is missing (oracle/build.sh).
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from renderer_gb300 import _abi
+from renderer_gb300.runtime import HIT_DTYPE, RAY_DTYPE
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+_lib = None
+
+
+def build():
+    subprocess.run(["sh", os.path.join(HERE, "build.sh")], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        L.orc_scene_create.restype = P
+        L.orc_scene_create.argtypes = [C.POINTER(_abi.SceneDesc), C.c_int]
+        L.orc_scene_destroy.argtypes = [P]
+        L.orc_scene_prims.restype = C.c_int
+        L.orc_scene_prims.argtypes = [P]
+        L.orc_trace_closest.argtypes = [P, P, C.c_int64, P, C.c_int]
+        L.orc_trace_any.argtypes = [P, P, P, C.c_int64, P, C.c_int]
+        L.orc_render.restype = C.c_int
+        L.orc_render.argtypes = [P, C.POINTER(_abi.Camera), C.POINTER(_abi.RenderParams), C.c_int, C.c_int, C.c_int,
+                                 P, P, P, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                 C.POINTER(C.c_uint64)]
+        L.orc_camera_ray.argtypes = [C.POINTER(_abi.Camera), C.c_double, C.c_double, P]
+        L.orc_stream_u.restype = C.c_float
+        L.orc_stream_u.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class OracleScene:
+    """The renderer's scene (IntersectableList of lights + geometry, median-split
+    BVH or a plain list) restated on the CPU."""
+
+    def __init__(self, data, use_bvh=True):
+        desc, keep = data.to_desc()
+        self.data = data
+        self.handle = lib().orc_scene_create(C.byref(desc), 1 if use_bvh else 0)
+        if not self.handle:
+            raise RuntimeError("orc_scene_create failed")
+
+    def intersect(self, rays, threads=0):
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        hits = np.zeros(len(rays), HIT_DTYPE)
+        lib().orc_trace_closest(self.handle, _ptr(rays), len(rays), _ptr(hits), threads)
+        return hits
+
+    def occluded(self, rays, ignore_prim=None, threads=0):
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        occ = np.zeros(len(rays), np.uint8)
+        ign = None if ignore_prim is None else np.ascontiguousarray(ignore_prim, np.int32)
+        lib().orc_trace_any(self.handle, _ptr(rays), _ptr(ign), len(rays), _ptr(occ), threads)
+        return occ.astype(bool)
+
+    def render(self, camera, params, rng_mode=0, rows=None, threads=0):
+        """Returns dict(film, sum, sumsq, paths, rays, shadow_rays) for rows
+        [r0, r1) (all rows by default)."""
+        H, W = camera.height, camera.width
+        r0, r1 = rows if rows is not None else (0, H)
+        film = np.zeros((H, W, 3), np.float32)
+        s = np.zeros((H, W, 3), np.float64)
+        q = np.zeros((H, W, 3), np.float64)
+        paths, rays, sh = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        rc = lib().orc_render(self.handle, C.byref(camera), C.byref(params), rng_mode, r0, r1, _ptr(film), _ptr(s),
+                              _ptr(q), threads, C.byref(paths), C.byref(rays), C.byref(sh))
+        if rc != 0:
+            raise RuntimeError("orc_render failed")
+        return dict(film=film, sum=s, sumsq=q, paths=paths.value, rays=rays.value, shadow_rays=sh.value)
+
+    def close(self):
+        if self.handle:
+            lib().orc_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def camera_ray(camera, px, py):
+    r = np.zeros(1, RAY_DTYPE)
+    lib().orc_camera_ray(C.byref(camera), px, py, _ptr(r))
+    return r[0]
+
+
+def stream_u(seed, sample_id, dim):
+    return lib().orc_stream_u(seed, sample_id, dim)

@@ -1,0 +1,117 @@
+"""ctypes mirror of include/gbrt.h (the C ABI of the GB300 path tracer).
+
+The structures here must match the header field for field; tests check the
+sizes against the C compiler's view of the same header.
+"""
+import ctypes as C
+
+F3 = C.c_float * 3
+
+
+class Material(C.Structure):
+    _fields_ = [("type", C.c_int32), ("kd", F3), ("ks", F3), ("exponent", C.c_float),
+                ("ior", C.c_float), ("coefficient", C.c_float)]
+
+
+class Quad(C.Structure):
+    _fields_ = [("p", F3 * 4), ("material", C.c_int32)]
+
+
+class Sphere(C.Structure):
+    _fields_ = [("center", F3), ("radius", C.c_float), ("material", C.c_int32)]
+
+
+class Plane(C.Structure):
+    _fields_ = [("plane", C.c_float * 4), ("material", C.c_int32)]
+
+
+class Light(C.Structure):
+    _fields_ = [("type", C.c_int32), ("origin", F3), ("u", F3), ("v", F3), ("intensity", F3)]
+
+
+class EnvMap(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("mapping", C.c_int32),
+                ("texels", C.POINTER(C.c_float))]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("materials", C.POINTER(Material)), ("n_materials", C.c_int32),
+                ("tri_pos", C.POINTER(C.c_float)), ("tri_nrm", C.POINTER(C.c_float)),
+                ("tri_uv", C.POINTER(C.c_float)), ("tri_mat", C.POINTER(C.c_int32)),
+                ("n_tri", C.c_int64),
+                ("quads", C.POINTER(Quad)), ("n_quads", C.c_int32),
+                ("spheres", C.POINTER(Sphere)), ("n_spheres", C.c_int32),
+                ("planes", C.POINTER(Plane)), ("n_planes", C.c_int32),
+                ("lights", C.POINTER(Light)), ("n_lights", C.c_int32),
+                ("env", C.POINTER(EnvMap))]
+
+
+class Camera(C.Structure):
+    _fields_ = [("eye", F3), ("look_at", F3), ("up", F3), ("fov", C.c_float),
+                ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("x_samples", C.c_int32), ("y_samples", C.c_int32),
+                ("termination_prob", C.c_float), ("max_depth", C.c_int32),
+                ("seed", C.c_uint64), ("semantics", C.c_int32), ("batch_paths", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("extension_rays", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("nonfinite", C.c_uint64),
+                ("render_ms", C.c_double), ("kernel_launches", C.c_uint64)]
+
+
+class Ray(C.Structure):
+    _fields_ = [("org", F3), ("tmin", C.c_float), ("dir", F3), ("tmax", C.c_float)]
+
+
+class Hit(C.Structure):
+    _fields_ = [("t", C.c_float), ("prim", C.c_int32), ("u", C.c_float), ("v", C.c_float)]
+
+
+# gbrt_status
+OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_CANCELLED, ERR_TIMEOUT, ERR_NUMERIC, ERR_PARSE, \
+    ERR_IO, ERR_UNSUPPORTED = range(10)
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "CANCELLED", 5: "TIMEOUT",
+                6: "NUMERIC", 7: "PARSE", 8: "IO", 9: "UNSUPPORTED"}
+
+# gbrt_material_type
+MAT_DARK, MAT_DIFFUSE, MAT_MIRROR, MAT_PHONG, MAT_BLINN, MAT_TRANSPARENT = range(6)
+# gbrt_light_type
+LIGHT_AREA, LIGHT_POINT, LIGHT_ENV, LIGHT_BLACK = range(4)
+# gbrt_env_mapping
+ENV_ANGULAR, ENV_LATLONG = range(2)
+# gbrt_semantics
+SEM_REFERENCE, SEM_PHYSICAL = range(2)
+
+P = C.c_void_p
+
+# (name, restype, argtypes) of every exported entry point declared in gbrt.h.
+SIGNATURES = [
+    ("gbrt_abi_version", C.c_int32, []),
+    ("gbrt_last_error", C.c_char_p, [P]),
+    ("gbrt_ctx_create", C.c_int, [C.c_int32, C.POINTER(P)]),
+    ("gbrt_ctx_destroy", C.c_int, [P]),
+    ("gbrt_scene_create", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(P)]),
+    ("gbrt_scene_destroy", C.c_int, [P]),
+    ("gbrt_scene_info", C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("gbrt_trace_closest", C.c_int, [P, P, C.c_int64, P]),
+    ("gbrt_trace_any", C.c_int, [P, P, P, C.c_int64, P]),
+    ("gbrt_trace_closest_device", C.c_int, [P, P, C.c_int64, P, P]),
+    ("gbrt_trace_any_device", C.c_int, [P, P, P, C.c_int64, P, P]),
+    ("gbrt_render", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), P, P, P, P,
+                              C.POINTER(Stats)]),
+    ("gbrt_render_device", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), P, P, P,
+                                     C.POINTER(Stats)]),
+    ("gbrt_parse_scene_file", C.c_int, [C.c_char_p, C.POINTER(P), C.c_char_p, C.c_int32]),
+    ("gbrt_parse_scene_string", C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(P), C.c_char_p, C.c_int32]),
+    ("gbrt_parsed_scene_desc", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(Camera),
+                                         C.POINTER(C.c_int32)]),
+    ("gbrt_parsed_scene_free", None, [P]),
+    ("gbrt_read_hdr", C.c_int, [C.c_char_p, C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.c_int32),
+                                C.POINTER(C.c_int32)]),
+    ("gbrt_free", None, [P]),
+]

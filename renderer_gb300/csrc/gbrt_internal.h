@@ -1,0 +1,47 @@
+// gbrt_internal.h — host-side objects behind the C ABI handles.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "gbrt_scene.h"
+
+struct gbrt_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  // Scratch for the ray-query entry points: one work counter and one error
+  // word, reused by every call on this context.
+  unsigned long long* d_work = nullptr;
+  int* d_err = nullptr;
+};
+
+struct gbrt_scene {
+  gbrt_ctx* ctx = nullptr;
+  gbrt::DeviceScene view{};
+  std::vector<void*> allocations;
+  int64_t n_leaves = 0;
+  int32_t max_depth = 0;
+  double sah_cost = 0;
+  double build_ms = 0;
+  int32_t n_prims = 0;  // primitive ids in use
+};
+
+namespace gbrt {
+
+// Records a failure message on ctx (or the global slot) and returns status.
+gbrt_status fail(gbrt_ctx* ctx, gbrt_status st, const std::string& msg);
+gbrt_status cuda_fail(gbrt_ctx* ctx, cudaError_t e, const char* what);
+void clear_error(gbrt_ctx* ctx);
+
+#define GBRT_CUDA_TRY(ctx, expr)                              \
+  do {                                                        \
+    cudaError_t e_ = (expr);                                  \
+    if (e_ != cudaSuccess) return gbrt::cuda_fail(ctx, e_, #expr); \
+  } while (0)
+
+}  // namespace gbrt

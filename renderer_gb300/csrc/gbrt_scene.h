@@ -1,0 +1,88 @@
+// gbrt_scene.h — device layout of a flattened scene, shared by the host code
+// that builds it and the kernels that read it.
+//
+// HBM layout (all arrays 16-byte aligned, read through the non-coherent
+// 128-bit load path):
+//   nodes  : n_nodes x 64 B   BVH2 nodes (bvh_build.h), root at 0
+//   recs   : n_recs x 48 B    primitive records in BVH leaf order, 3 float4:
+//              triangle      (p1, kind) (p2, -) (p3, prim)
+//              sphere        (centre, kind) (radius, 0, 0, -) (0, 0, 0, prim)
+//              parallelogram (origin, kind) (u, -) (v, prim)
+//            kind and prim are int bit patterns in the w lanes.
+//   meta   : n_recs x 16 B    (prim id, material, normal index or -1, light)
+//   tri_nrm: per smooth triangle 3 normals (9 floats, padded to 12)
+//   planes : n_planes x float4 plane vector; plane_meta (prim, material)
+//   materials, lights: small tables; env texels H x W x 3 float (BGR)
+// Planes have unbounded boxes and live outside the BVH; the environment map is
+// what a ray with tmax = +inf sees when it hits nothing else.
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/gbrt.h"
+
+namespace gbrt {
+
+enum RecKind : int32_t { kRecTriangle = 0, kRecSphere = 1, kRecParallelogram = 2 };
+
+// Material kinds on the device (gbrt_material_type plus the two emitters that
+// are their own material in the renderer: AreaLight and EnvironmentMap).
+enum DevMatKind : int32_t {
+  kMatDark = GBRT_MAT_DARK,
+  kMatDiffuse = GBRT_MAT_DIFFUSE,
+  kMatMirror = GBRT_MAT_MIRROR,
+  kMatPhong = GBRT_MAT_PHONG,
+  kMatBlinn = GBRT_MAT_BLINN,
+  kMatTransparent = GBRT_MAT_TRANSPARENT,
+};
+
+struct alignas(16) DevMaterial {
+  int32_t type;
+  float kd[3];
+  float ks[3];
+  float exponent;
+  float ior;
+  float rho_d, rho_s;  // lum(kd), lum(ks) for Phong lobe selection
+  float pad;
+};
+
+struct alignas(16) DevLight {
+  int32_t type;       // gbrt_light_type
+  int32_t prim;       // primitive id (== light index)
+  float origin[3];
+  float u[3], v[3];
+  float normal[3];    // u x v (unnormalised)
+  float normal_len;   // |u x v| (computed through double, like QVector3D::length)
+  float nhat[3];      // normalised normal
+  float intensity[3]; // BGR; for the env map: its coefficient
+};
+
+// Plain-old-data view of a scene on the device, passed by value to kernels.
+struct DeviceScene {
+  const float4* nodes;
+  const float4* recs;
+  const int4* meta;
+  const float* tri_nrm;  // 12 floats per smooth triangle
+  const float4* planes;
+  const int2* plane_meta;  // (prim, material)
+  const DevMaterial* materials;
+  const DevLight* lights;
+  const float* env_texels;
+  int64_t n_nodes, n_recs;
+  int32_t n_planes, n_materials, n_lights;
+  int32_t env_light;      // light index / prim id of the environment map, -1 if none
+  int32_t env_w, env_h, env_mapping;
+  float env_coef[3];
+};
+
+// Internal hit encoding of the traversal kernels.
+//   rec >= 0       BVH record index
+//   rec == -1      nothing hit (the environment, if any, when tmax = +inf)
+//   rec <= -2      plane number -2 - rec
+struct alignas(16) RawHit {
+  float t;
+  int32_t rec;
+  float u, v;
+};
+
+}  // namespace gbrt

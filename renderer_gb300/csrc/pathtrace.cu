@@ -1,0 +1,661 @@
+// pathtrace.cu — wavefront unidirectional path tracer (gbrt_render*).
+//
+// GPU restatement of PerPixelRenderer::render (src/perpixelrenderer.cpp:43-101)
+// driving UniDiPathTracingIntegrator (src/unidipathtracingintegrator.cpp:34-107)
+// over Renderer::createPath (src/renderer.cpp:47-106), in the renderer's own
+// estimator ("reference semantics", quirks included).
+//
+// The renderer first builds a whole path (a list of stored, non-specular
+// vertices with their throughputs) and then walks it, adding for every stored
+// vertex k either the emission of vertex k+1, when that vertex is an emitter,
+// or next-event estimation with light lightIndex[k]. Here the same estimator
+// is evaluated in streaming form: the last stored vertex is kept "pending" in
+// the path state; when the next stored vertex turns out to be an emitter its
+// emission is used for the pending vertex (no shadow ray), otherwise the
+// pending vertex gets its shadow ray. At most two shadow rays per path leave
+// one shade step (the pending vertex and a new vertex that ends the path).
+//
+// Per wavefront batch of B paths (path index g = pixel * spp + sample, so a
+// warp's camera rays are coherent):
+//   raygen      camera rays, path state, extension queue 0
+//   D times:    extend  (closest hit, persistent, shared-memory stacks)
+//               shade   (materials, emission, NEE; warp-aggregated pushes
+//                        into the next extension queue and the shadow queue)
+//               shadow  (any hit; unoccluded contributions added to the path)
+//   accumulate  per-pixel FP64 sum and sum of squares
+// Queue sizes live in device memory, so launch grids never depend on them.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <vector>
+
+#include "gbrt_internal.h"
+#include "shading.cuh"
+#include "traverse.cuh"
+
+namespace gbrt {
+
+struct CamDev {
+  float eye[3];
+  float u[3], v[3], w[3];
+  float l, r, t, b;
+  int W, H;
+};
+
+struct PTParams {
+  CamDev cam;
+  unsigned long long seed;
+  unsigned long long g0;   // first path index of the batch
+  int nb;                  // paths in the batch
+  int xs, ys, spp;
+  int D;                   // maximum path length
+  float rr_pdf;            // Russian-roulette compensation pdf
+  float term_p;            // termination probability
+};
+
+// Path state, structure of arrays indexed by slot (path index - g0).
+struct PTState {
+  float4* alpha;   // current throughput
+  float4* L;       // accumulated radiance
+  int4* ctl;       // (i, pathLength, nStored, pending)
+  float4* pv_p;    // pending vertex: point, material (int bits)
+  float4* pv_n;    // pending vertex: normal, stored index k (int bits)
+  float4* pv_d;    // pending vertex: incoming ray direction
+  float4* pv_a;    // pending vertex: throughput
+  float4* ext[2];  // extension queues: (o, tmin), (d, tmax) per entry
+  int* ext_slot[2];
+  RawHit* hits;
+  float4* sh_ray;  // shadow queue: (o, tmin), (d, tmax)
+  float4* sh_c;    // contribution, ignore prim in w (int bits)
+  int* sh_slot;
+  int* counts;     // [0], [1] extension counts, [2] shadow count
+  unsigned long long* work;   // work counters of the persistent kernels
+  unsigned long long* tally;  // [0] extension rays, [1] shadow rays, [2] non-finite samples
+  int* err;
+};
+
+// Warp-aggregated queue push: all 32 lanes must call it together.
+__device__ __forceinline__ int warp_push(int* counter, bool pred) {
+  const unsigned m = __ballot_sync(0xffffffffu, pred);
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (m) {
+    if (lane == __ffs(m) - 1) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+  }
+  return base + __popc(m & ((1u << lane) - 1u));
+}
+
+// ------------------------------------------------------------- raygen ----
+__global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
+  int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot == 0) st.counts[0] = P.nb;
+  if (slot >= P.nb) return;
+  unsigned long long g = P.g0 + (unsigned long long)slot;
+  int pixel = int(g / unsigned(P.spp));
+  int s = int(g % unsigned(P.spp));
+  int px = pixel % P.cam.W, py = pixel / P.cam.W;
+  int a = s / P.ys, b = s % P.ys;  // JitteredSampler strata: x outer, y inner
+  unsigned long long key = stream_key(P.seed, g);
+  float sxp = float(px) + (stream_u(key, 0) + float(a)) / float(P.xs);
+  float syp = float(py) + (stream_u(key, 1) + float(b)) / float(P.ys);
+  // Camera::getRay (src/camera.cpp:50-58): image plane at z = -1 in camera space.
+  float x = P.cam.l + (P.cam.r - P.cam.l) * (sxp + 0.5f) / float(P.cam.W);
+  float y = P.cam.t + (P.cam.b - P.cam.t) * (syp + 0.5f) / float(P.cam.H);
+  float dx = x * P.cam.u[0] + y * P.cam.v[0] - P.cam.w[0];
+  float dy = x * P.cam.u[1] + y * P.cam.v[1] - P.cam.w[1];
+  float dz = x * P.cam.u[2] + y * P.cam.v[2] - P.cam.w[2];
+  // Path length: min(3 + Geometric(p), D) (src/renderer.cpp:52-61).
+  int plen = P.D;
+  if (P.term_p > 0.f) {
+    int k = 0;
+    if (P.term_p < 1.f) {
+      // Geometric draw by inversion, in double like the CPU oracle.
+      double ul = double(stream_u(key, 2));
+      k = int(floor(log(1.0 - ul) / log(1.0 - double(P.term_p))));
+      k = max(k, 0);
+    }
+    plen = min(3 + k, P.D);
+  }
+  st.alpha[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
+  st.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+  st.ctl[slot] = make_int4(0, plen, 0, 0);
+  st.ext[0][2 * slot] = make_float4(P.cam.eye[0], P.cam.eye[1], P.cam.eye[2], kEps);
+  st.ext[0][2 * slot + 1] = make_float4(dx, dy, dz, CUDART_INF_F);
+  st.ext_slot[0][slot] = slot;
+}
+
+// ------------------------------------------------------------- extend ----
+__global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState st, int cur) {
+  __shared__ int s_stack[kStackSize * kTraceBlock];
+  int* stack = s_stack + threadIdx.x;
+  const int n = st.counts[cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) st.tally[0] += (unsigned long long)n;
+  const float4* rays = st.ext[cur];
+  unsigned long long* work = st.work + cur;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(work, 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= (unsigned long long)n) break;
+    int i = int(base) + lane;
+    if (i >= n) continue;
+    TRay r = make_tray(rays[2 * i], rays[2 * i + 1]);
+    RawHit h;
+    h.rec = trace_ray<false, false>(S, r, -1, stack, h.t, h.u, h.v, st.err, nullptr);
+    st.hits[i] = h;
+  }
+}
+
+// ------------------------------------------------------------- shadow ----
+__global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState st) {
+  __shared__ int s_stack[kStackSize * kTraceBlock];
+  int* stack = s_stack + threadIdx.x;
+  const int n = st.counts[2];
+  if (blockIdx.x == 0 && threadIdx.x == 0) st.tally[1] += (unsigned long long)n;
+  unsigned long long* work = st.work + 2;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(work, 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= (unsigned long long)n) break;
+    int i = int(base) + lane;
+    if (i >= n) continue;
+    float4 c = st.sh_c[i];
+    TRay r = make_tray(st.sh_ray[2 * i], st.sh_ray[2 * i + 1]);
+    float t, u, v;
+    int32_t rec = trace_ray<true, false>(S, r, __float_as_int(c.w), stack, t, u, v, st.err, nullptr);
+    if (rec == -1) {
+      float4* L = st.L + st.sh_slot[i];
+      atomicAdd(&L->x, c.x);
+      atomicAdd(&L->y, c.y);
+      atomicAdd(&L->z, c.z);
+    }
+  }
+}
+
+// -------------------------------------------------------------- shade ----
+struct ShadowOut {
+  bool valid;
+  float4 o, d, c;
+};
+
+// Next-event estimation at a stored vertex: UniDiPathTracingIntegrator lines
+// 83-99 with Light::getIntensity for light lightIndex[k].
+__device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, unsigned long long key, const Vertex& vx,
+                                    V3f alpha, int k, ShadowOut& out) {
+  out.valid = false;
+  if (S.n_lights <= 0 || vx.mat < 0) return;
+  unsigned dl = dim_light(P.D, k);
+  float lx = stream_u(key, dl), ly = stream_u(key, dl + 1), lu = stream_u(key, dl + 2);
+  int li = min(int(double(lu) * double(S.n_lights)), S.n_lights - 1);  // exact floor(u * n)
+  const DevLight& Lt = S.lights[li];
+  V3f dir, Le;
+  V3f so, sd;
+  float stmax;
+  int ignore = -1;
+  if (Lt.type == GBRT_LIGHT_AREA) {
+    V3f lp = ld3(Lt.origin) + lx * ld3(Lt.u) + ly * ld3(Lt.v);
+    dir = vx.p - lp;
+    Le = area_intensity(Lt, dir);
+    so = vx.p;
+    sd = -normalize(dir);
+    stmax = len(dir) - kEps;
+    ignore = Lt.prim;
+  } else if (Lt.type == GBRT_LIGHT_POINT) {
+    dir = vx.p - ld3(Lt.origin);
+    float inv = 1.f / len2(dir);
+    Le = v3(Lt.intensity[0] * inv, Lt.intensity[1] * inv, Lt.intensity[2] * inv);
+    so = vx.p;
+    sd = -normalize(dir);
+    stmax = len(dir) - kEps;
+  } else if (Lt.type == GBRT_LIGHT_ENV && S.env_light >= 0) {
+    float pdf;
+    V3f s = cosine_power_dir(vx.n, lx, ly, 1.f, pdf);
+    dir = -s;
+    V3f e = env_get(S, dir);
+    float ip = 1.f / pdf;
+    Le = v3(e.x * ip, e.y * ip, e.z * ip);
+    // Ray(at, -s, -inf, -EPSILON) of the renderer == Ray(at, s, EPSILON, inf).
+    so = vx.p;
+    sd = s;
+    stmax = CUDART_INF_F;
+  } else {
+    return;  // BlackLight
+  }
+  if (is_zero(Le)) return;
+  V3f f = brdf_eval(S.materials, vx, dir);
+  float inCos = dot(-normalize(dir), vx.n);
+  float outCos = dot(-normalize(vx.d), vx.n);
+  if (signum(inCos) != signum(outCos)) return;
+  float ac = fabsf(inCos);
+  V3f c = v3(alpha.x * f.x * Le.x * ac, alpha.y * f.y * Le.y * ac, alpha.z * f.z * Le.z * ac);
+  if (is_zero(c)) return;
+  out.valid = true;
+  out.o = make_float4(so.x, so.y, so.z, kEps);
+  out.d = make_float4(sd.x, sd.y, sd.z, stmax);
+  out.c = make_float4(c.x, c.y, c.z, __int_as_float(ignore));
+}
+
+__global__ void __launch_bounds__(256) k_shade(DeviceScene S, PTParams P, PTState st, int cur) {
+  const int n = st.counts[cur];
+  const int nxt = cur ^ 1;
+  const int stride = gridDim.x * blockDim.x;
+  const int nround = (n + 31) & ~31;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
+    bool active = q < n;
+    bool wantExt = false;
+    float4 eo = make_float4(0, 0, 0, 0), ed = make_float4(0, 0, 0, 0);
+    ShadowOut s1, s2;
+    s1.valid = s2.valid = false;
+    int slot = 0;
+    if (active) {
+      slot = st.ext_slot[cur][q];
+      RawHit h = st.hits[q];
+      float4 ro = st.ext[cur][2 * q], rd = st.ext[cur][2 * q + 1];
+      int4 c = st.ctl[slot];
+      int i = c.x, plen = c.y, nst = c.z;
+      bool pend = c.w != 0;
+      unsigned long long key = stream_key(P.seed, P.g0 + (unsigned long long)slot);
+      V3f o = v3(ro.x, ro.y, ro.z), d = v3(rd.x, rd.y, rd.z);
+      V3f alpha = v3(st.alpha[slot].x, st.alpha[slot].y, st.alpha[slot].z);
+      bool envHit = h.rec == -1 && S.env_light >= 0 && isinf(rd.w) && rd.w > 0.f;
+      bool done = false;
+      Vertex vx;
+      vx.d = d;
+      vx.mat = -1;
+      int light = -1;  // area light hit
+      if (h.rec == -1 && !envHit) {
+        done = true;  // the path leaves the scene
+      } else if (envHit) {
+        light = S.env_light;
+        vx.p = normalize(d);  // point at infinity (w = 0)
+        vx.n = -vx.p;
+      } else {
+        vx.p = o + h.t * d;
+        if (h.rec >= 0) {
+          int4 m = __ldg(&S.meta[h.rec]);
+          const float4* rp = S.recs + 3 * int64_t(h.rec);
+          float4 a = __ldg(rp), b = __ldg(rp + 1), cc = __ldg(rp + 2);
+          int kind = __float_as_int(a.w);
+          vx.mat = m.y;
+          light = m.w;
+          if (kind == kRecTriangle) {
+            if (m.z >= 0) {
+              const float* nn = S.tri_nrm + 12 * int64_t(m.z);
+              float w0 = 1.f - h.u - h.v;
+              vx.n = normalize(w0 * ld3(nn) + h.u * ld3(nn + 3) + h.v * ld3(nn + 6));
+            } else {
+              V3f p1 = v3(a.x, a.y, a.z), p2 = v3(b.x, b.y, b.z), p3 = v3(cc.x, cc.y, cc.z);
+              vx.n = normalize(cross(p1 - p2, p1 - p3));
+            }
+          } else if (kind == kRecSphere) {
+            vx.n = normalize(vx.p - v3(a.x, a.y, a.z));
+          } else {
+            vx.n = ld3(S.lights[light].nhat);
+          }
+        } else {
+          float4 pl = __ldg(&S.planes[-2 - h.rec]);
+          vx.n = normalize(v3(pl.x, pl.y, pl.z));
+          vx.mat = S.plane_meta[-2 - h.rec].y;
+        }
+      }
+      float4 L4 = st.L[slot];
+      if (!done && light >= 0) {
+        // Emitter. Its own next-event term is zero (Material::brdf of a light
+        // is zero), so only its emission matters.
+        V3f e;
+        if (light == S.env_light && envHit) e = env_get(S, vx.p);
+        else e = area_intensity(S.lights[light], -d);
+        if (nst == 0) {
+          // First stored vertex is an emitter: its emission is the sample.
+          L4.x = e.x; L4.y = e.y; L4.z = e.z;
+        } else if (pend) {
+          // The pending vertex sees this emitter (lines 70-81).
+          float4 pp = st.pv_p[slot], pn = st.pv_n[slot], pd = st.pv_d[slot], pa = st.pv_a[slot];
+          Vertex pv;
+          pv.p = v3(pp.x, pp.y, pp.z); pv.n = v3(pn.x, pn.y, pn.z); pv.d = v3(pd.x, pd.y, pd.z);
+          pv.mat = __float_as_int(pp.w);
+          V3f dir = envHit ? -vx.p : pv.p - vx.p;
+          V3f f = brdf_eval(S.materials, pv, dir);
+          float inCos = dot(-normalize(dir), pv.n);
+          float outCos = dot(-normalize(pv.d), pv.n);
+          if (signum(inCos) == signum(outCos)) {
+            float ac = fabsf(inCos);
+            L4.x += pa.x * f.x * e.x * ac;
+            L4.y += pa.y * f.y * e.y * ac;
+            L4.z += pa.z * f.z * e.z * ac;
+          }
+        }
+        st.L[slot] = L4;
+        done = true;
+        pend = false;
+      } else if (!done && mat_specular(S.materials, vx.mat)) {
+        float pdf;
+        V3f f;
+        V3f out = out_direction(S.materials, vx, stream_u(key, dim_path(i)), stream_u(key, dim_path(i) + 1), pdf, f);
+        if (i == plen - 1 && plen < P.D) plen++;
+        i++;
+        if (i < plen) {
+          wantExt = true;
+          eo = make_float4(vx.p.x, vx.p.y, vx.p.z, kEps);
+          ed = make_float4(out.x, out.y, out.z, CUDART_INF_F);
+        } else {
+          done = true;
+        }
+      } else if (!done) {
+        // Stored, non-specular vertex k = nst.
+        if (pend) {
+          float4 pp = st.pv_p[slot], pn = st.pv_n[slot], pd = st.pv_d[slot], pa = st.pv_a[slot];
+          Vertex pv;
+          pv.p = v3(pp.x, pp.y, pp.z); pv.n = v3(pn.x, pn.y, pn.z); pv.d = v3(pd.x, pd.y, pd.z);
+          pv.mat = __float_as_int(pp.w);
+          nee(S, P, key, pv, v3(pa.x, pa.y, pa.z), __float_as_int(pn.w), s1);
+        }
+        int k = nst++;
+        st.pv_p[slot] = make_float4(vx.p.x, vx.p.y, vx.p.z, __int_as_float(vx.mat));
+        st.pv_n[slot] = make_float4(vx.n.x, vx.n.y, vx.n.z, __int_as_float(k));
+        st.pv_d[slot] = make_float4(d.x, d.y, d.z, 0.f);
+        st.pv_a[slot] = make_float4(alpha.x, alpha.y, alpha.z, 0.f);
+        pend = true;
+        float pdf;
+        V3f f;
+        V3f out = out_direction(S.materials, vx, stream_u(key, dim_path(i)), stream_u(key, dim_path(i) + 1), pdf, f);
+        if (pdf == 0.f || is_zero(alpha)) {
+          done = true;
+        } else {
+          float cs = fabsf(dot(normalize(out), vx.n));
+          float sc = cs / pdf;
+          alpha = v3(alpha.x * f.x * sc, alpha.y * f.y * sc, alpha.z * f.z * sc);
+          if (i > 3) {
+            float ir = 1.f / P.rr_pdf;
+            alpha = v3(alpha.x * ir, alpha.y * ir, alpha.z * ir);
+          }
+          i++;
+          if (i < plen) {
+            wantExt = true;
+            eo = make_float4(vx.p.x, vx.p.y, vx.p.z, kEps);
+            ed = make_float4(out.x, out.y, out.z, CUDART_INF_F);
+          } else {
+            done = true;
+          }
+        }
+        st.alpha[slot] = make_float4(alpha.x, alpha.y, alpha.z, 0.f);
+      }
+      if (done && pend) {
+        // The last stored vertex gets next-event estimation (line 85).
+        float4 pp = st.pv_p[slot], pn = st.pv_n[slot], pd = st.pv_d[slot], pa = st.pv_a[slot];
+        Vertex pv;
+        pv.p = v3(pp.x, pp.y, pp.z); pv.n = v3(pn.x, pn.y, pn.z); pv.d = v3(pd.x, pd.y, pd.z);
+        pv.mat = __float_as_int(pp.w);
+        ShadowOut& so = s1.valid ? s2 : s1;
+        nee(S, P, key, pv, v3(pa.x, pa.y, pa.z), __float_as_int(pn.w), so);
+        pend = false;
+      }
+      st.ctl[slot] = make_int4(i, plen, nst, pend ? 1 : 0);
+    }
+    // Converged pushes.
+    int pe = warp_push(&st.counts[nxt], wantExt);
+    if (wantExt) {
+      st.ext[nxt][2 * pe] = eo;
+      st.ext[nxt][2 * pe + 1] = ed;
+      st.ext_slot[nxt][pe] = slot;
+    }
+    int p1 = warp_push(&st.counts[2], s1.valid);
+    if (s1.valid) {
+      st.sh_ray[2 * p1] = s1.o;
+      st.sh_ray[2 * p1 + 1] = s1.d;
+      st.sh_c[p1] = s1.c;
+      st.sh_slot[p1] = slot;
+    }
+    int p2 = warp_push(&st.counts[2], s2.valid);
+    if (s2.valid) {
+      st.sh_ray[2 * p2] = s2.o;
+      st.sh_ray[2 * p2 + 1] = s2.d;
+      st.sh_c[p2] = s2.c;
+      st.sh_slot[p2] = slot;
+    }
+  }
+}
+
+// --------------------------------------------------------- accumulate ----
+// One thread per pixel touched by the batch; samples of a pixel are
+// contiguous slots. FP64 sums; non-finite samples are counted and dropped.
+__global__ void __launch_bounds__(256) k_accumulate(PTParams P, PTState st, double* sum, double* sumsq) {
+  unsigned long long p0 = P.g0 / unsigned(P.spp);
+  unsigned long long p1 = (P.g0 + unsigned(P.nb) - 1) / unsigned(P.spp);
+  unsigned long long p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > p1) return;
+  unsigned long long gb = max(P.g0, p * unsigned(P.spp));
+  unsigned long long ge = min(P.g0 + unsigned(P.nb), (p + 1) * unsigned(P.spp));
+  double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0;
+  unsigned long long bad = 0;
+  for (unsigned long long g = gb; g < ge; ++g) {
+    float4 L = st.L[g - P.g0];
+    if (!isfinite(L.x) || !isfinite(L.y) || !isfinite(L.z)) { ++bad; continue; }
+    s0 += L.x; s1 += L.y; s2 += L.z;
+    q0 += double(L.x) * L.x; q1 += double(L.y) * L.y; q2 += double(L.z) * L.z;
+  }
+  if (bad) atomicAdd(&st.tally[2], bad);
+  size_t o = size_t(p) * 3;
+  sum[o] += s0; sum[o + 1] += s1; sum[o + 2] += s2;
+  if (sumsq) { sumsq[o] += q0; sumsq[o + 1] += q1; sumsq[o + 2] += q2; }
+}
+
+__global__ void k_finalize(const double* sum, float* film, size_t n3, double inv_spp) {
+  size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n3) film[i] = float(sum[i] * inv_spp);
+}
+
+// ------------------------------------------------------------- driver ----
+static CamDev make_camera(const gbrt_camera& c) {
+  // Camera::init (src/camera.cpp:34-48) in float with double-length
+  // normalisation like QVector3D.
+  auto nrm = [](double x, double y, double z, float out[3]) {
+    float fx = float(x), fy = float(y), fz = float(z);
+    double l = double(fx) * fx + double(fy) * fy + double(fz) * fz;
+    if (std::fabs(l - 1.0) <= 1e-12) { out[0] = fx; out[1] = fy; out[2] = fz; return; }
+    double s = l > 1e-12 ? std::sqrt(l) : 0.0;
+    out[0] = s > 0 ? float(fx / s) : 0.f;
+    out[1] = s > 0 ? float(fy / s) : 0.f;
+    out[2] = s > 0 ? float(fz / s) : 0.f;
+  };
+  CamDev d;
+  for (int k = 0; k < 3; ++k) d.eye[k] = c.eye[k];
+  float w[3], u[3], v[3];
+  nrm(float(c.eye[0] - c.look_at[0]), float(c.eye[1] - c.look_at[1]), float(c.eye[2] - c.look_at[2]), w);
+  float cu[3] = {c.up[1] * w[2] - c.up[2] * w[1], c.up[2] * w[0] - c.up[0] * w[2], c.up[0] * w[1] - c.up[1] * w[0]};
+  nrm(cu[0], cu[1], cu[2], u);
+  v[0] = w[1] * u[2] - w[2] * u[1];
+  v[1] = w[2] * u[0] - w[0] * u[2];
+  v[2] = w[0] * u[1] - w[1] * u[0];
+  for (int k = 0; k < 3; ++k) { d.u[k] = u[k]; d.v[k] = v[k]; d.w[k] = w[k]; }
+  float aspect = float(c.width) / float(c.height);
+  d.t = float(std::tan(double(c.fov / 2)));
+  d.b = -d.t;
+  d.r = aspect * d.t;
+  d.l = -d.r;
+  d.W = c.width;
+  d.H = c.height;
+  return d;
+}
+
+struct Buffers {
+  std::vector<void*> ptrs;
+  cudaStream_t stream;
+  explicit Buffers(cudaStream_t s) : stream(s) {}
+  ~Buffers() {
+    for (void* p : ptrs) cudaFreeAsync(p, stream);
+  }
+  template <typename T>
+  cudaError_t alloc(T** out, size_t count) {
+    void* p = nullptr;
+    cudaError_t e = cudaMallocAsync(&p, std::max<size_t>(count, 1) * sizeof(T), stream);
+    if (e == cudaSuccess) ptrs.push_back(p);
+    *out = static_cast<T*>(p);
+    return e;
+  }
+};
+
+static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render_params* prm, float* d_film,
+                               double* d_sum_in, double* d_sumsq, const volatile int32_t* stop, gbrt_stats* stats) {
+  gbrt_ctx* ctx = s->ctx;
+  if (!cam || !prm || !d_film) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render: NULL argument");
+  if (cam->width <= 0 || cam->height <= 0 || prm->x_samples <= 0 || prm->y_samples <= 0 || prm->max_depth <= 0 ||
+      prm->max_depth > 64)
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render: bad camera or render parameters");
+  if (prm->semantics != GBRT_SEM_REFERENCE)
+    return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_render: only the reference semantics are implemented");
+  if (!(prm->termination_prob >= 0.f && prm->termination_prob <= 1.f))
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render: termination probability outside [0, 1]");
+  cudaStream_t stream = ctx->stream;
+  GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  const unsigned long long npix = (unsigned long long)cam->width * cam->height;
+  const int spp = prm->x_samples * prm->y_samples;
+  const unsigned long long total = npix * (unsigned long long)spp;
+  long long B = prm->batch_paths > 0 ? prm->batch_paths : (1ll << 22);
+  B = std::min<long long>(B, (long long)total);
+  B = std::max<long long>(B, 1);
+
+  PTParams P;
+  P.cam = make_camera(*cam);
+  P.seed = prm->seed;
+  P.xs = prm->x_samples;
+  P.ys = prm->y_samples;
+  P.spp = spp;
+  P.D = prm->max_depth;
+  P.term_p = prm->termination_prob;
+  P.rr_pdf = prm->termination_prob > 0.f ? prm->termination_prob : 1.f;
+
+  Buffers buf(stream);
+  PTState st;
+  cudaError_t e = cudaSuccess;
+  double* d_sum = d_sum_in;
+  auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
+  A(buf.alloc(&st.alpha, B)); A(buf.alloc(&st.L, B)); A(buf.alloc(&st.ctl, B));
+  A(buf.alloc(&st.pv_p, B)); A(buf.alloc(&st.pv_n, B)); A(buf.alloc(&st.pv_d, B)); A(buf.alloc(&st.pv_a, B));
+  A(buf.alloc(&st.ext[0], 2 * B)); A(buf.alloc(&st.ext[1], 2 * B));
+  A(buf.alloc(&st.ext_slot[0], B)); A(buf.alloc(&st.ext_slot[1], B));
+  A(buf.alloc(&st.hits, B));
+  A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
+  A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 4)); A(buf.alloc(&st.err, 1));
+  if (!d_sum) A(buf.alloc(&d_sum, npix * 3));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "render buffers");
+  A(cudaMemsetAsync(d_sum, 0, npix * 3 * sizeof(double), stream));
+  if (d_sumsq) A(cudaMemsetAsync(d_sumsq, 0, npix * 3 * sizeof(double), stream));
+  A(cudaMemsetAsync(st.tally, 0, 4 * sizeof(unsigned long long), stream));
+  A(cudaMemsetAsync(st.err, 0, sizeof(int), stream));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "render set-up");
+
+  static int traceGrid = 0, shadowGrid = 0;
+  if (!traceGrid) {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_extend, kTraceBlock, 0);
+    traceGrid = std::max(1, per) * ctx->num_sms;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shadow, kTraceBlock, 0);
+    shadowGrid = std::max(1, per) * ctx->num_sms;
+  }
+  const int shadeGrid = ctx->num_sms * 8;
+  cudaEvent_t ev0, ev1;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  cudaEventRecord(ev0, stream);
+  unsigned long long launches = 0;
+  gbrt_status status = GBRT_OK;
+  for (unsigned long long g0 = 0; g0 < total; g0 += (unsigned long long)B) {
+    if (stop && *stop) { status = fail(ctx, GBRT_ERR_CANCELLED, "gbrt_render: cancelled"); break; }
+    P.g0 = g0;
+    P.nb = int(std::min<unsigned long long>((unsigned long long)B, total - g0));
+    k_raygen<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
+    ++launches;
+    for (int it = 0; it < P.D; ++it) {
+      int cur = it & 1, nxt = cur ^ 1;
+      A(cudaMemsetAsync(st.counts + nxt, 0, sizeof(int), stream));
+      A(cudaMemsetAsync(st.counts + 2, 0, sizeof(int), stream));
+      A(cudaMemsetAsync(st.work, 0, 4 * sizeof(unsigned long long), stream));
+      k_extend<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
+      k_shade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
+      k_shadow<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
+      launches += 3;
+    }
+    unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
+    unsigned long long np = p1 - p0 + 1;
+    k_accumulate<<<unsigned((np + 255) / 256), 256, 0, stream>>>(P, st, d_sum, d_sumsq);
+    ++launches;
+    A(cudaGetLastError());
+    if (e != cudaSuccess) break;
+  }
+  size_t n3 = size_t(npix) * 3;
+  k_finalize<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_sum, d_film, n3, 1.0 / spp);
+  ++launches;
+  cudaEventRecord(ev1, stream);
+  A(cudaGetLastError());
+  unsigned long long tally[4] = {0, 0, 0, 0};
+  int err = 0;
+  A(cudaMemcpyAsync(tally, st.tally, sizeof tally, cudaMemcpyDeviceToHost, stream));
+  A(cudaMemcpyAsync(&err, st.err, sizeof err, cudaMemcpyDeviceToHost, stream));
+  A(cudaStreamSynchronize(stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gbrt_render");
+  if (stats) {
+    stats->paths = status == GBRT_OK ? total : 0;
+    stats->extension_rays = tally[0];
+    stats->shadow_rays = tally[1];
+    stats->nonfinite = tally[2];
+    stats->render_ms = ms;
+    stats->kernel_launches = launches;
+  }
+  if (err) return fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render: traversal stack overflow");
+  return status;
+}
+
+}  // namespace gbrt
+
+using namespace gbrt;
+
+extern "C" {
+
+gbrt_status gbrt_render_device(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render_params* prm, float* d_film,
+                               double* d_sum, double* d_sumsq, gbrt_stats* stats) {
+  if (!s) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_render_device: NULL scene");
+  clear_error(s->ctx);
+  return render_impl(s, cam, prm, d_film, d_sum, d_sumsq, nullptr, stats);
+}
+
+gbrt_status gbrt_render(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render_params* prm, float* film,
+                        double* sum, double* sumsq, const volatile int32_t* stop, gbrt_stats* stats) {
+  if (!s || !cam || !film) return fail(s ? s->ctx : nullptr, GBRT_ERR_INVALID_ARG, "gbrt_render: NULL argument");
+  gbrt_ctx* ctx = s->ctx;
+  clear_error(ctx);
+  if (cam->width <= 0 || cam->height <= 0) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render: bad resolution");
+  GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  size_t n3 = size_t(cam->width) * cam->height * 3;
+  float* d_film = nullptr;
+  double* d_sum = nullptr;
+  double* d_sq = nullptr;
+  cudaError_t e = cudaMallocAsync(&d_film, n3 * sizeof(float), ctx->stream);
+  if (e == cudaSuccess && sum) e = cudaMallocAsync(&d_sum, n3 * sizeof(double), ctx->stream);
+  if (e == cudaSuccess && sumsq) e = cudaMallocAsync(&d_sq, n3 * sizeof(double), ctx->stream);
+  gbrt_status st = e == cudaSuccess ? GBRT_OK : cuda_fail(ctx, e, "gbrt_render buffers");
+  if (st == GBRT_OK) st = render_impl(s, cam, prm, d_film, d_sum, d_sq, stop, stats);
+  if (st == GBRT_OK || st == GBRT_ERR_CANCELLED) {
+    cudaMemcpyAsync(film, d_film, n3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (sum) cudaMemcpyAsync(sum, d_sum, n3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    if (sumsq) cudaMemcpyAsync(sumsq, d_sq, n3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  }
+  if (d_film) cudaFreeAsync(d_film, ctx->stream);
+  if (d_sum) cudaFreeAsync(d_sum, ctx->stream);
+  if (d_sq) cudaFreeAsync(d_sq, ctx->stream);
+  e = cudaStreamSynchronize(ctx->stream);
+  if (st == GBRT_OK && e != cudaSuccess) st = cuda_fail(ctx, e, "gbrt_render copy-out");
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,392 @@
+// scene.cpp — context and scene objects of the C ABI: validation of the scene
+// description, flattening into leaf-ordered primitive records, the SAH BVH
+// build and the upload to HBM.
+//
+// Replaces scene_builder::getScene (src/sceneast.cpp:673-695), which wraps the
+// lights and the scene in an IntersectableList and calls createBVH
+// (src/intersectable.cpp:11-14, src/bvh.cpp:67-94). Primitive ids follow the
+// type order documented in include/gbrt.h.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bvh_build.h"
+#include "gbrt_internal.h"
+
+namespace gbrt {
+
+static std::mutex g_err_mu;
+static std::string g_last_error;
+
+gbrt_status fail(gbrt_ctx* ctx, gbrt_status st, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_last_error = msg;
+  return st;
+}
+
+gbrt_status cuda_fail(gbrt_ctx* ctx, cudaError_t e, const char* what) {
+  std::string msg = std::string("CUDA error ") + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ") in " + what;
+  return fail(ctx, e == cudaErrorMemoryAllocation ? GBRT_ERR_OOM : GBRT_ERR_CUDA, msg);
+}
+
+void clear_error(gbrt_ctx* ctx) {
+  if (ctx) ctx->last_error.clear();
+}
+
+namespace {
+
+// QVector3D-style helpers in float without contraction (the host code is built
+// with -ffp-contract=off).
+struct F3 {
+  float x, y, z;
+};
+F3 f3(const float* p) { return {p[0], p[1], p[2]}; }
+F3 sub(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+F3 cross(F3 a, F3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+bool isNull(F3 a) { return a.x == 0.f && a.y == 0.f && a.z == 0.f; }
+// QVector3D::normalized (double length, unit vectors left unchanged).
+F3 normalized(F3 a) {
+  double l = double(a.x) * a.x + double(a.y) * a.y + double(a.z) * a.z;
+  if (std::fabs(l - 1.0) <= 1e-12) return a;
+  if (std::fabs(l) > 1e-12) {
+    double s = std::sqrt(l);
+    return {float(a.x / s), float(a.y / s), float(a.z / s)};
+  }
+  return {0.f, 0.f, 0.f};
+}
+float length(F3 a) { return float(std::sqrt(double(a.x) * a.x + double(a.y) * a.y + double(a.z) * a.z)); }
+bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+float lumBGR(const float* c) { return float(.299 * c[2] + .587 * c[1] + .114 * c[0]); }
+
+struct Rec {
+  float v[12];
+  int32_t meta[4];
+};
+
+void setW(float& slot, int32_t bits) { std::memcpy(&slot, &bits, 4); }
+
+template <typename T>
+gbrt_status upload(gbrt_scene* s, const std::vector<T>& host, const T** dst) {
+  *dst = nullptr;
+  if (host.empty()) return GBRT_OK;
+  void* p = nullptr;
+  size_t bytes = host.size() * sizeof(T);
+  GBRT_CUDA_TRY(s->ctx, cudaMalloc(&p, bytes));
+  s->allocations.push_back(p);
+  GBRT_CUDA_TRY(s->ctx, cudaMemcpy(p, host.data(), bytes, cudaMemcpyHostToDevice));
+  *dst = static_cast<const T*>(p);
+  return GBRT_OK;
+}
+
+void free_scene(gbrt_scene* s) {
+  for (void* p : s->allocations) cudaFree(p);
+  s->allocations.clear();
+}
+
+}  // namespace
+}  // namespace gbrt
+
+using namespace gbrt;
+
+extern "C" {
+
+int32_t gbrt_abi_version(void) { return GBRT_ABI_VERSION; }
+
+const char* gbrt_last_error(const gbrt_ctx* ctx) {
+  if (ctx) return ctx->last_error.c_str();
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_last_error.c_str();
+}
+
+gbrt_status gbrt_ctx_create(int32_t device, gbrt_ctx** out) {
+  if (!out) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_ctx_create: out is NULL");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    return fail(nullptr, GBRT_ERR_CUDA,
+                std::string("gbrt_ctx_create: no CUDA device (") + cudaGetErrorString(e) + ")");
+  }
+  if (device < 0 || device >= n) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_ctx_create: bad device index");
+  auto* c = new (std::nothrow) gbrt_ctx();
+  if (!c) return fail(nullptr, GBRT_ERR_OOM, "gbrt_ctx_create: out of host memory");
+  c->device = device;
+  if ((e = cudaSetDevice(device)) != cudaSuccess) { delete c; return cuda_fail(nullptr, e, "cudaSetDevice"); }
+  int major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (major * 10 + minor != 103) {
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "gbrt_ctx_create: device %d is sm_%d%d; this library is built for sm_103a (GB300) only",
+                  device, major, minor);
+    delete c;
+    return fail(nullptr, GBRT_ERR_UNSUPPORTED, buf);
+  }
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    delete c;
+    return cuda_fail(nullptr, e, "cudaStreamCreate");
+  }
+  if ((e = cudaMalloc(&c->d_work, sizeof(unsigned long long))) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_err, sizeof(int))) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return cuda_fail(nullptr, e, "cudaMalloc(ctx scratch)");
+  }
+  *out = c;
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_ctx_destroy(gbrt_ctx* ctx) {
+  if (!ctx) return GBRT_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->d_work);
+  cudaFree(ctx->d_err);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scene** out) {
+  if (!ctx || !d || !out) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: NULL argument");
+  *out = nullptr;
+  clear_error(ctx);
+  auto t0 = std::chrono::steady_clock::now();
+  if (d->n_materials < 0 || d->n_tri < 0 || d->n_quads < 0 || d->n_spheres < 0 || d->n_planes < 0 ||
+      d->n_lights < 0)
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: negative count");
+  if ((d->n_materials && !d->materials) || (d->n_tri && !d->tri_pos) || (d->n_quads && !d->quads) ||
+      (d->n_spheres && !d->spheres) || (d->n_planes && !d->planes) || (d->n_lights && !d->lights))
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: NULL array with a non-zero count");
+  int envLights = 0;
+  for (int i = 0; i < d->n_lights; ++i) {
+    int ty = d->lights[i].type;
+    if (ty < GBRT_LIGHT_AREA || ty > GBRT_LIGHT_BLACK)
+      return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: unknown light type");
+    if (ty == GBRT_LIGHT_ENV) {
+      ++envLights;
+      if (!d->env || !d->env->texels || d->env->width <= 0 || d->env->height <= 0)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: environment light without an image");
+      if (d->env->mapping != GBRT_ENV_ANGULAR && d->env->mapping != GBRT_ENV_LATLONG)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: unknown environment mapping");
+    }
+  }
+  if (envLights > 1)
+    return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: at most one environment map per scene");
+  const int64_t nPrims = int64_t(d->n_lights) + d->n_tri + d->n_quads + d->n_spheres + d->n_planes;
+  if (nPrims >= (int64_t(1) << 31) - 2) return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: too many primitives");
+  const int64_t nRecs = int64_t(d->n_tri) + 2 * int64_t(d->n_quads) + d->n_spheres;
+  if (nRecs + d->n_lights >= (int64_t(1) << 27))
+    return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: more than 2^27 bounded primitives");
+
+  GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  std::vector<Rec> recs;
+  std::vector<Box> boxes;
+  recs.reserve(size_t(nRecs + d->n_lights));
+  boxes.reserve(size_t(nRecs + d->n_lights));
+  std::vector<float> nrm;  // 12 floats per smooth triangle
+  auto matIndex = [&](int32_t m) { return (m >= 0 && m < d->n_materials) ? m : -1; };
+  auto boxOf = [](std::initializer_list<F3> pts) {
+    Box b;
+    for (int k = 0; k < 3; ++k) { b.lo[k] = INFINITY; b.hi[k] = -INFINITY; }
+    for (F3 p : pts) {
+      const float c[3] = {p.x, p.y, p.z};
+      for (int k = 0; k < 3; ++k) { b.lo[k] = std::min(b.lo[k], c[k]); b.hi[k] = std::max(b.hi[k], c[k]); }
+    }
+    return b;
+  };
+  auto addTri = [&](F3 p1, F3 p2, F3 p3, int32_t prim, int32_t mat, int32_t nidx) {
+    Rec r{};
+    r.v[0] = p1.x; r.v[1] = p1.y; r.v[2] = p1.z; setW(r.v[3], kRecTriangle);
+    r.v[4] = p2.x; r.v[5] = p2.y; r.v[6] = p2.z; setW(r.v[7], 0);
+    r.v[8] = p3.x; r.v[9] = p3.y; r.v[10] = p3.z; setW(r.v[11], prim);
+    r.meta[0] = prim; r.meta[1] = mat; r.meta[2] = nidx; r.meta[3] = -1;
+    recs.push_back(r);
+    boxes.push_back(boxOf({p1, p2, p3}));
+  };
+
+  std::vector<DevLight> lights(size_t(d->n_lights));
+  int32_t pid = 0;
+  int32_t envLight = -1;
+  for (int i = 0; i < d->n_lights; ++i, ++pid) {
+    const gbrt_light& L = d->lights[i];
+    DevLight& dl = lights[i];
+    std::memset(&dl, 0, sizeof dl);
+    dl.type = L.type;
+    dl.prim = pid;
+    for (int k = 0; k < 3; ++k) {
+      dl.origin[k] = L.origin[k]; dl.u[k] = L.u[k]; dl.v[k] = L.v[k]; dl.intensity[k] = L.intensity[k];
+    }
+    if (L.type == GBRT_LIGHT_AREA) {
+      if (!finite3(L.origin) || !finite3(L.u) || !finite3(L.v))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: non-finite area light");
+      F3 o = f3(L.origin), u = f3(L.u), v = f3(L.v);
+      F3 n = cross(u, v);
+      F3 nh = normalized(n);
+      dl.normal[0] = n.x; dl.normal[1] = n.y; dl.normal[2] = n.z;
+      dl.normal_len = length(n);
+      dl.nhat[0] = nh.x; dl.nhat[1] = nh.y; dl.nhat[2] = nh.z;
+      Rec r{};
+      r.v[0] = o.x; r.v[1] = o.y; r.v[2] = o.z; setW(r.v[3], kRecParallelogram);
+      r.v[4] = u.x; r.v[5] = u.y; r.v[6] = u.z; setW(r.v[7], 0);
+      r.v[8] = v.x; r.v[9] = v.y; r.v[10] = v.z; setW(r.v[11], pid);
+      r.meta[0] = pid; r.meta[1] = -1; r.meta[2] = -1; r.meta[3] = i;
+      recs.push_back(r);
+      F3 ou = {o.x + u.x, o.y + u.y, o.z + u.z}, ov = {o.x + v.x, o.y + v.y, o.z + v.z};
+      F3 ouv = {ou.x + v.x, ou.y + v.y, ou.z + v.z};
+      boxes.push_back(boxOf({o, ou, ov, ouv}));
+    } else if (L.type == GBRT_LIGHT_POINT) {
+      if (!finite3(L.origin)) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: non-finite point light");
+    } else if (L.type == GBRT_LIGHT_ENV) {
+      envLight = i;
+    }
+  }
+  for (int64_t i = 0; i < d->n_tri; ++i, ++pid) {
+    const float* p = d->tri_pos + 9 * i;
+    if (!finite3(p) || !finite3(p + 3) || !finite3(p + 6))
+      return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: non-finite triangle vertex");
+    int32_t nidx = -1;
+    if (d->tri_nrm) {
+      const float* n = d->tri_nrm + 9 * i;
+      F3 n1 = f3(n), n2 = f3(n + 3), n3 = f3(n + 6);
+      if (!isNull(n1) && !isNull(n2) && !isNull(n3)) {
+        nidx = int32_t(nrm.size() / 12);
+        if (nidx < 0) return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: too many smooth triangles");
+        F3 m[3] = {normalized(n1), normalized(n2), normalized(n3)};
+        for (int k = 0; k < 3; ++k) { nrm.push_back(m[k].x); nrm.push_back(m[k].y); nrm.push_back(m[k].z); }
+        for (int k = 0; k < 3; ++k) nrm.push_back(0.f);
+      }
+    }
+    addTri(f3(p), f3(p + 3), f3(p + 6), pid, matIndex(d->tri_mat ? d->tri_mat[i] : 0), nidx);
+  }
+  for (int i = 0; i < d->n_quads; ++i, ++pid) {
+    const gbrt_quad& q = d->quads[i];
+    for (int k = 0; k < 4; ++k)
+      if (!finite3(q.p[k])) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: non-finite quad vertex");
+    // Quad(p1,p2,p3,p4) = Triangle(p1,p2,p4) + Triangle(p4,p2,p3), src/quad.h:32.
+    addTri(f3(q.p[0]), f3(q.p[1]), f3(q.p[3]), pid, matIndex(q.material), -1);
+    addTri(f3(q.p[3]), f3(q.p[1]), f3(q.p[2]), pid, matIndex(q.material), -1);
+  }
+  for (int i = 0; i < d->n_spheres; ++i, ++pid) {
+    const gbrt_sphere& s = d->spheres[i];
+    if (!finite3(s.center) || !std::isfinite(s.radius))
+      return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: non-finite sphere");
+    Rec r{};
+    r.v[0] = s.center[0]; r.v[1] = s.center[1]; r.v[2] = s.center[2]; setW(r.v[3], kRecSphere);
+    r.v[4] = s.radius; setW(r.v[11], pid);
+    r.meta[0] = pid; r.meta[1] = matIndex(s.material); r.meta[2] = -1; r.meta[3] = -1;
+    recs.push_back(r);
+    float ar = std::fabs(s.radius);
+    Box b;
+    for (int k = 0; k < 3; ++k) { b.lo[k] = s.center[k] - ar; b.hi[k] = s.center[k] + ar; }
+    boxes.push_back(b);
+  }
+  std::vector<float4> planes(size_t(d->n_planes));
+  std::vector<int2> planeMeta(size_t(d->n_planes));
+  for (int i = 0; i < d->n_planes; ++i, ++pid) {
+    const gbrt_plane& pl = d->planes[i];
+    planes[i] = make_float4(pl.plane[0], pl.plane[1], pl.plane[2], pl.plane[3]);
+    planeMeta[i] = make_int2(pid, matIndex(pl.material));
+  }
+
+  BuildOptions bo;
+  BuildResult br = build_bvh(boxes, bo);
+  if (br.max_depth > kMaxTreeDepth)
+    return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: BVH deeper than the traversal stack");
+  std::vector<float4> recv(recs.size() * 3);
+  std::vector<int4> meta(recs.size());
+  for (size_t k = 0; k < br.order.size(); ++k) {
+    const Rec& r = recs[br.order[k]];
+    std::memcpy(&recv[3 * k], r.v, sizeof r.v);
+    meta[k] = make_int4(r.meta[0], r.meta[1], r.meta[2], r.meta[3]);
+  }
+  std::vector<float4> nodes(br.nodes.size() * 4);
+  if (!br.nodes.empty()) std::memcpy(nodes.data(), br.nodes.data(), br.nodes.size() * sizeof(Node));
+
+  std::vector<DevMaterial> mats(size_t(d->n_materials));
+  for (int i = 0; i < d->n_materials; ++i) {
+    const gbrt_material& m = d->materials[i];
+    DevMaterial& dm = mats[i];
+    std::memset(&dm, 0, sizeof dm);
+    dm.type = (m.type >= GBRT_MAT_DARK && m.type <= GBRT_MAT_TRANSPARENT) ? m.type : GBRT_MAT_DARK;
+    for (int k = 0; k < 3; ++k) { dm.kd[k] = m.kd[k]; dm.ks[k] = m.ks[k]; }
+    dm.exponent = m.exponent;
+    dm.ior = m.ior;
+    dm.rho_d = lumBGR(m.kd);
+    dm.rho_s = lumBGR(m.ks);
+  }
+
+  auto* s = new (std::nothrow) gbrt_scene();
+  if (!s) return fail(ctx, GBRT_ERR_OOM, "gbrt_scene_create: out of host memory");
+  s->ctx = ctx;
+  DeviceScene& v = s->view;
+  gbrt_status st;
+  std::vector<float> envTex;
+  if ((st = upload(s, nodes, &v.nodes)) != GBRT_OK || (st = upload(s, recv, &v.recs)) != GBRT_OK ||
+      (st = upload(s, meta, &v.meta)) != GBRT_OK || (st = upload(s, nrm, &v.tri_nrm)) != GBRT_OK ||
+      (st = upload(s, planes, &v.planes)) != GBRT_OK || (st = upload(s, planeMeta, &v.plane_meta)) != GBRT_OK ||
+      (st = upload(s, mats, &v.materials)) != GBRT_OK || (st = upload(s, lights, &v.lights)) != GBRT_OK) {
+    free_scene(s);
+    delete s;
+    return st;
+  }
+  v.n_nodes = int64_t(br.nodes.size());
+  v.n_recs = int64_t(recs.size());
+  v.n_planes = d->n_planes;
+  v.n_materials = d->n_materials;
+  v.n_lights = d->n_lights;
+  v.env_light = -1;
+  if (envLight >= 0) {
+    const gbrt_env_map* e = d->env;
+    envTex.assign(e->texels, e->texels + size_t(e->width) * e->height * 3);
+    if ((st = upload(s, envTex, &v.env_texels)) != GBRT_OK) {
+      free_scene(s);
+      delete s;
+      return st;
+    }
+    v.env_light = envLight;
+    v.env_w = e->width;
+    v.env_h = e->height;
+    v.env_mapping = e->mapping;
+    for (int k = 0; k < 3; ++k) v.env_coef[k] = d->lights[envLight].intensity[k];
+  }
+  s->n_leaves = br.leaves;
+  s->max_depth = br.max_depth;
+  s->sah_cost = br.sah_cost;
+  s->n_prims = int32_t(nPrims);
+  s->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  *out = s;
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_scene_destroy(gbrt_scene* s) {
+  if (!s) return GBRT_OK;
+  cudaSetDevice(s->ctx->device);
+  cudaStreamSynchronize(s->ctx->stream);
+  free_scene(s);
+  delete s;
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_scene_info(const gbrt_scene* s, int64_t* n_nodes, int64_t* n_leaves, int32_t* max_depth,
+                            double* sah_cost, double* build_ms) {
+  if (!s) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_scene_info: NULL scene");
+  if (n_nodes) *n_nodes = s->view.n_nodes;
+  if (n_leaves) *n_leaves = s->n_leaves;
+  if (max_depth) *max_depth = s->max_depth;
+  if (sah_cost) *sah_cost = s->sah_cost;
+  if (build_ms) *build_ms = s->build_ms;
+  return GBRT_OK;
+}
+
+void gbrt_free(void* p) { std::free(p); }
+
+}  // extern "C"

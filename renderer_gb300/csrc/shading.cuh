@@ -1,0 +1,247 @@
+// shading.cuh — per-vertex material, light and sampling math of the renderer,
+// restated for the GPU in FP32 (reference semantics, quirks included):
+//   Sample::getCosinePowerWeightedDirection  src/sampler.cpp:48-76
+//   DiffuseMaterial / AbstractDiffuse        src/diffusematerial.cpp:25-28, src/abstractdiffusematerial.cpp:8-14
+//   MirrorMaterial                           src/mirrormaterial.cpp:31-41
+//   PhongMaterial                            src/phongmaterial.cpp:31-81
+//   BlinnMaterial                            src/blinnmaterial.cpp:34-84
+//   TransparentMaterial                      src/transparentmaterial.cpp:34-75
+//   AreaLight / PointLight intensity         src/arealight.cpp:35-59, src/pointlight.cpp:29-41
+//   EnvironmentMap::get / getIntensity       src/environmentmap.cpp:40-65
+// plus the counter-based random stream shared with the CPU oracle.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include "gbrt_scene.h"
+
+namespace gbrt {
+
+constexpr float kEps = 0.001f;  // EPSILON, src/ray.h:34
+constexpr float kInvPi = 0.318309886183790671537767526745028724f;
+
+struct V3f {
+  float x, y, z;
+};
+__device__ __forceinline__ V3f v3(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ V3f operator+(V3f a, V3f b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3f operator-(V3f a, V3f b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3f operator-(V3f a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ V3f operator*(float s, V3f a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ V3f mulc(V3f a, V3f b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ float dot(V3f a, V3f b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3f cross(V3f a, V3f b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float len2(V3f a) { return dot(a, a); }
+__device__ __forceinline__ float len(V3f a) { return sqrtf(dot(a, a)); }
+// QVector3D::normalized: the zero vector stays zero.
+__device__ __forceinline__ V3f normalize(V3f a) {
+  float l2 = dot(a, a);
+  if (!(l2 > 1e-24f)) return {0.f, 0.f, 0.f};
+  float s = rsqrtf(l2);
+  return {a.x * s, a.y * s, a.z * s};
+}
+__device__ __forceinline__ bool is_zero(V3f a) { return a.x == 0.f && a.y == 0.f && a.z == 0.f; }
+__device__ __forceinline__ int signum(float x) { return (0.f < x) - (x < 0.f); }
+__device__ __forceinline__ V3f reflect(V3f v, V3f n) { return v - (2.f * dot(v, n)) * n; }
+__device__ __forceinline__ V3f ld3(const float* p) { return {p[0], p[1], p[2]}; }
+
+// ---------------------------------------------------------------- RNG -----
+// SplitMix64 output function (Steele, Lea, Flood 2014). One camera sample
+// owns the stream key = mix64(seed ^ mix64(sample_id + c)); its d-th uniform
+// is the top 24 bits of mix64(key + d * phi). The CPU oracle defines the same
+// stream, so both can draw identical numbers.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ unsigned long long stream_key(unsigned long long seed, unsigned long long sample_id) {
+  return mix64(seed ^ mix64(sample_id + 0x632BE59BD9B4E019ull));
+}
+__device__ __forceinline__ float stream_u(unsigned long long key, unsigned dim) {
+  unsigned long long h = mix64(key + (unsigned long long)dim * 0x9E3779B97F4A7C15ull);
+  return float(h >> 40) * (1.0f / 16777216.0f);
+}
+// Dimension layout per camera sample (D = max depth):
+//   0,1 jitter | 2 path length | 3+2i, 4+2i path sample i |
+//   3+2D+3k, +1 light sample k, +2 light index k
+__device__ __forceinline__ unsigned dim_path(int i) { return 3u + 2u * unsigned(i); }
+__device__ __forceinline__ unsigned dim_light(int D, int k) { return 3u + 2u * unsigned(D) + 3u * unsigned(k); }
+
+// ----------------------------------------------------------- Sampling -----
+// Cosine-power direction about w, src/sampler.cpp:48-76 (opening angle pi/2).
+__device__ __forceinline__ V3f cosine_power_dir(V3f w, float sx, float sy, float e, float& pdf) {
+  w = normalize(w);
+  float ie = 1.f / (e + 1.f);
+  float z = powf(sx, ie);
+  float r = sqrtf(fmaxf(0.f, 1.f - powf(sx, 2.f * ie)));
+  float sn, cs;
+  sincospif(2.f * sy, &sn, &cs);
+  V3f nd = v3(cs * r, sn * r, z);
+  pdf = powf(z, e) * (e + 1.f) * (0.5f * kInvPi);
+  V3f v;
+  float ax = fabsf(w.x), ay = fabsf(w.y), az = fabsf(w.z);
+  if (ax < ay && ax < az) v = v3(0.f, w.z, -w.y);
+  else if (ay < az) v = v3(w.z, 0.f, -w.x);
+  else v = v3(w.y, -w.x, 0.f);
+  v = normalize(v);
+  V3f u = cross(v, w);
+  return normalize(nd.x * u + nd.y * v + nd.z * w);
+}
+
+// --------------------------------------------------------- Materials -----
+struct Vertex {
+  V3f p;     // hit point
+  V3f n;     // normalised surface normal (unflipped)
+  V3f d;     // direction of the ray that hit it (unnormalised)
+  int mat;   // material index, -1 = DarkMatter
+};
+
+__device__ __forceinline__ V3f phong_spec(const DevMaterial& m, const Vertex& h, V3f dir) {
+  V3f refl = reflect(dir, h.n);
+  float dp = fmaxf(dot(normalize(refl), -normalize(h.d)), 0.f);
+  float s = (m.exponent + 2.f) * (0.5f * kInvPi) * powf(dp, m.exponent);
+  return v3(s * m.ks[0], s * m.ks[1], s * m.ks[2]);
+}
+
+__device__ __forceinline__ float blinn_G(V3f wi, V3f wo, V3f n) {
+  V3f wh = normalize(wi + wo);
+  return fminf(1.f, 2.f * dot(n, wh) * fminf(dot(n, wo), dot(n, wi)) / dot(wo, wh));
+}
+
+// Material::brdf(hit, direction): direction points from the light towards the
+// surface (the renderer's convention).
+__device__ __forceinline__ V3f brdf_eval(const DevMaterial* mats, const Vertex& h, V3f dir) {
+  if (h.mat < 0) return v3(0.f, 0.f, 0.f);
+  const DevMaterial& m = mats[h.mat];
+  switch (m.type) {
+    case kMatDiffuse:
+      return v3(m.kd[0] * kInvPi, m.kd[1] * kInvPi, m.kd[2] * kInvPi);
+    case kMatPhong: {
+      V3f s = phong_spec(m, h, dir);
+      return v3(m.kd[0] * kInvPi + s.x, m.kd[1] * kInvPi + s.y, m.kd[2] * kInvPi + s.z);
+    }
+    case kMatBlinn: {
+      V3f n = h.n;
+      V3f wo = -normalize(h.d);
+      V3f wi = -normalize(dir);
+      if (signum(dot(n, wo)) != signum(dot(n, wi))) return v3(0.f, 0.f, 0.f);
+      if (dot(n, wo) < 0.f) n = -n;
+      V3f wh = normalize(wi + wo);
+      float D = (m.exponent + 2.f) * (0.5f * kInvPi) * powf(dot(wh, n), m.exponent);
+      float f = D * blinn_G(wi, wo, n) / (4.f * dot(wo, n) * dot(wi, n));
+      return v3(m.kd[0] * kInvPi + m.ks[0] * f, m.kd[1] * kInvPi + m.ks[1] * f, m.kd[2] * kInvPi + m.ks[2] * f);
+    }
+    default:
+      return v3(0.f, 0.f, 0.f);
+  }
+}
+
+__device__ __forceinline__ bool mat_specular(const DevMaterial* mats, int mat) {
+  if (mat < 0) return false;
+  int t = mats[mat].type;
+  return t == kMatMirror || t == kMatTransparent;
+}
+
+// Material::outDirection(hit, sample, pdf, brdf).
+__device__ __forceinline__ V3f out_direction(const DevMaterial* mats, const Vertex& h, float sx, float sy, float& pdf,
+                                             V3f& brdf) {
+  brdf = v3(0.f, 0.f, 0.f);
+  pdf = 0.f;
+  if (h.mat < 0) return v3(0.f, 0.f, 0.f);
+  const DevMaterial& m = mats[h.mat];
+  switch (m.type) {
+    case kMatDiffuse: {
+      V3f n = h.n;
+      if (dot(n, normalize(h.d)) > 0.f) n = -n;
+      V3f out = cosine_power_dir(n, sx, sy, 1.f, pdf);
+      brdf = v3(m.kd[0] * kInvPi, m.kd[1] * kInvPi, m.kd[2] * kInvPi);
+      return out;
+    }
+    case kMatMirror:
+      pdf = 1.f;
+      return reflect(h.d, h.n);
+    case kMatPhong: {
+      V3f n = h.n;
+      if (dot(h.d, n) > 0.f) n = -n;
+      V3f specDir = reflect(h.d, n);
+      if (sx < m.rho_d) {
+        V3f out = cosine_power_dir(n, sx / m.rho_d, sy, 1.f, pdf);
+        brdf = v3(m.kd[0] * kInvPi, m.kd[1] * kInvPi, m.kd[2] * kInvPi);
+        return out;
+      } else if (sx < m.rho_d + m.rho_s) {
+        V3f out = cosine_power_dir(specDir, (sx - m.rho_d) / m.rho_s, sy, m.exponent, pdf);
+        if (dot(out, n) < 1.f) pdf = 0.f;  // the renderer's glossy-lobe quirk
+        brdf = phong_spec(m, h, out);
+        return out;
+      }
+      return v3(0.f, 0.f, 0.f);
+    }
+    case kMatBlinn: {
+      V3f n = h.n;
+      V3f wo = -normalize(h.d);
+      if (dot(n, wo) < 0.f) n = -n;
+      V3f wh = cosine_power_dir(n, sx, sy, m.exponent, pdf);
+      if (dot(wo, wh) < 0.f) { pdf = 0.f; return v3(0.f, 0.f, 0.f); }
+      V3f out = -reflect(wo, wh);
+      pdf /= 4.f * fmaxf(dot(wo, wh), 0.0001f);
+      brdf = brdf_eval(mats, h, out);
+      return out;
+    }
+    case kMatTransparent: {
+      pdf = 1.f;
+      V3f d = normalize(h.d), n = h.n;
+      float ratio;
+      if (dot(-n, d) < 0.f) { n = -n; ratio = m.ior; } else { ratio = 1.f / m.ior; }
+      float cosI = dot(-n, d);
+      float s2 = fmaxf(0.f, 1.f - cosI * cosI);
+      float sinO = ratio * sqrtf(s2);
+      float cosO = sqrtf(fmaxf(0.f, 1.f - ratio * ratio * s2));
+      float rPerp = (cosI - ratio * cosO) / (cosI + ratio * cosO);
+      float rPara = (ratio * cosI - cosO) / (ratio * cosI + cosO);
+      float R = 0.5f * (rPerp * rPerp + rPara * rPara);
+      if (sinO > 1.f || sx < R) return reflect(d, n);
+      return ratio * d + (ratio * cosI - float(signum(cosI)) * cosO) * n;
+    }
+    default:
+      return v3(0.f, 0.f, 0.f);
+  }
+}
+
+// ------------------------------------------------------------- Lights -----
+// AreaLight::getIntensity(direction): Le * max(0, cos) * |u x v| / |d|^2.
+__device__ __forceinline__ V3f area_intensity(const DevLight& L, V3f dir) {
+  float c = dot(normalize(dir), ld3(L.nhat)) / len2(dir) * L.normal_len;
+  if (!(c >= 0.f)) c = (c < 0.f) ? 0.f : c;
+  return v3(c * L.intensity[0], c * L.intensity[1], c * L.intensity[2]);
+}
+
+// EnvironmentMap::get(direction). Angular light probe (+x at the centre) or
+// equirectangular; nearest texel, indices clamped into the image.
+__device__ __forceinline__ V3f env_get(const DeviceScene& S, V3f d) {
+  int W = S.env_w, H = S.env_h;
+  int row, col;
+  if (S.env_mapping == GBRT_ENV_LATLONG) {
+    float u = atan2f(d.x, -d.z) * (0.5f * kInvPi) + 0.5f;
+    float v = acosf(fminf(1.f, fmaxf(-1.f, d.y))) * kInvPi;
+    col = min(int(u * W), W - 1);
+    row = min(int(v * H), H - 1);
+  } else {
+    float cx = d.y, cy = -d.z;
+    float f = acosf(d.x) / (sqrtf(cx * cx + cy * cy) * CUDART_PI_F);
+    cx *= f; cy *= f;
+    int x = int((cx + 1.f) * 0.5f * float(W) - 1.f);
+    int y = int((cy + 1.f) * 0.5f * float(H) - 1.f);
+    row = min(y, W - 1);
+    col = min(x, H - 1);
+  }
+  row = min(max(row, 0), H - 1);
+  col = min(max(col, 0), W - 1);
+  const float* p = S.env_texels + (size_t(row) * W + col) * 3;
+  return v3(__ldg(p) * S.env_coef[0], __ldg(p + 1) * S.env_coef[1], __ldg(p + 2) * S.env_coef[2]);
+}
+
+}  // namespace gbrt

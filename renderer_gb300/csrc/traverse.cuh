@@ -1,0 +1,288 @@
+// traverse.cuh — closest-hit and any-hit BVH traversal for sm_103a.
+//
+// Replaces the renderer's per-ray virtual intersect chain:
+//   BVHNode::intersect                 src/bvh.cpp:135-149
+//   AxisAlignedBox::getCSGIntersection src/axisalignedbox.cpp:30-73
+//   Triangle::intersect                src/triangle.cpp:30-56
+//   Quad::intersect                    src/quad.cpp:23-34 (as two triangles)
+//   Sphere + CSGObject::intersect      src/sphere.cpp:29-56, src/csgobject.cpp:25-44
+//   Plane::intersect                   src/plane.cpp:27-40
+//   AreaLight::intersect               src/arealight.cpp:73-90
+//   EnvironmentMap::intersect          src/environmentmap.cpp:73-83 (as "no hit, tmax = inf")
+//
+// Structure: ordered (near child first) while-while traversal of a BVH2 with
+// tmax shrinking, 64-byte nodes fetched as four 128-bit non-coherent loads, and
+// a per-thread stack in shared memory laid out [depth][thread] so that a warp's
+// pushes and pops fall in distinct banks.
+//
+// Numerics. Inside/outside decisions for triangles use the watertight test of
+// Woop, Benthin and Wald (JCGT 2013): vertices are translated to the ray
+// origin, sheared so the ray runs along +z, and the three 2D edge functions are
+// evaluated without fused multiply-adds (so that the two triangles sharing an
+// edge evaluate it as exact negations of each other), with a double-precision
+// re-evaluation when one is exactly zero. The hit distance t, and the
+// barycentrics, are then computed with the renderer's own formulas and
+// operation order, again without fused multiply-adds, so that t is bit-identical
+// to the renderer's float arithmetic for the same ray and primitive. Spheres,
+// planes and parallelograms use the renderer's formulas the same way. Box tests
+// are conservative: (bound - origin) * (1/d) with the far distance enlarged by
+// 1 + 2*gamma(3) (Ize 2013, "Robust BVH Ray Traversal").
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include "gbrt_scene.h"
+
+namespace gbrt {
+
+constexpr int kStackSize = 64;   // the builder keeps tree depth <= kStackSize - 2
+constexpr int kTraceBlock = 128;
+
+// Exactly rounded, never-contracted float operations.
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fdv(float a, float b) { return __fdiv_rn(a, b); }
+// (a*b) - (c*d) with both products rounded, like the renderer's cross product.
+__device__ __forceinline__ float dmd(float a, float b, float c, float d) { return fs(fm(a, b), fm(c, d)); }
+// x1*x2 + y1*y2 + z1*z2 evaluated left to right (QVector3D::dotProduct).
+__device__ __forceinline__ float dot3x(float ax, float ay, float az, float bx, float by, float bz) {
+  return fa(fa(fm(ax, bx), fm(ay, by)), fm(az, bz));
+}
+
+struct TRay {
+  float ox, oy, oz, tmin;
+  float dx, dy, dz, tmax;
+  float ix, iy, iz;        // 1 / d
+  float sx0, sx1, sx2;     // shear row for the 2D x coordinate
+  float sy0, sy1, sy2;     // shear row for the 2D y coordinate
+};
+
+__device__ __forceinline__ TRay make_tray(float4 a, float4 b) {
+  TRay r;
+  r.ox = a.x; r.oy = a.y; r.oz = a.z; r.tmin = a.w;
+  r.dx = b.x; r.dy = b.y; r.dz = b.z; r.tmax = b.w;
+  r.ix = 1.0f / r.dx; r.iy = 1.0f / r.dy; r.iz = 1.0f / r.dz;
+  // Watertight shear: kz = dominant axis, (kx, ky) the two others in cyclic
+  // order. A vertex A (relative to the origin) maps to
+  //   (A[kx] - Sx A[kz], A[ky] - Sy A[kz]),  Sx = d[kx]/d[kz], Sy = d[ky]/d[kz].
+  // Both signs of the edge functions are accepted (two-sided), so the
+  // winding-preserving swap of kx and ky is not needed.
+  float ax = fabsf(r.dx), ay = fabsf(r.dy), az = fabsf(r.dz);
+  int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  float dkz = kz == 0 ? r.dx : (kz == 1 ? r.dy : r.dz);
+  float sx0 = 0, sx1 = 0, sx2 = 0, sy0 = 0, sy1 = 0, sy2 = 0;
+  if (kz == 0) {        // kx = 1, ky = 2
+    sx1 = 1.f; sx0 = -r.dy / dkz;
+    sy2 = 1.f; sy0 = -r.dz / dkz;
+  } else if (kz == 1) { // kx = 2, ky = 0
+    sx2 = 1.f; sx1 = -r.dz / dkz;
+    sy0 = 1.f; sy1 = -r.dx / dkz;
+  } else {              // kx = 0, ky = 1
+    sx0 = 1.f; sx2 = -r.dx / dkz;
+    sy1 = 1.f; sy2 = -r.dy / dkz;
+  }
+  r.sx0 = sx0; r.sx1 = sx1; r.sx2 = sx2;
+  r.sy0 = sy0; r.sy1 = sy1; r.sy2 = sy2;
+  return r;
+}
+
+// Conservative slab test of one child box against [tmin, tcur].
+__device__ __forceinline__ bool box_hit(const TRay& r, float lox, float hix, float loy, float hiy, float loz,
+                                        float hiz, float tcur, float& tnear) {
+  float tx0 = (lox - r.ox) * r.ix, tx1 = (hix - r.ox) * r.ix;
+  float ty0 = (loy - r.oy) * r.iy, ty1 = (hiy - r.oy) * r.iy;
+  float tz0 = (loz - r.oz) * r.iz, tz1 = (hiz - r.oz) * r.iz;
+  float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), r.tmin));
+  float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1)) * 1.0000004f;
+  tf = fminf(tf, tcur);
+  tnear = tn;
+  return tn <= tf;
+}
+
+// Accepts t against the current best: inclusive of tmax for the first hit
+// (the renderer's Ray::inRange), strictly closer afterwards.
+__device__ __forceinline__ bool accept_t(float t, float tmin, float tcur, bool found) {
+  return t >= tmin && (found ? t < tcur : t <= tcur);
+}
+
+// Triangle p1 p2 p3. Returns true and t/u/v when the ray hits it in range.
+__device__ __forceinline__ bool tri_test(const TRay& r, float4 v0, float4 v1, float4 v2, float tcur, bool found,
+                                         float& t_out, float& u_out, float& v_out) {
+  // Watertight inside test.
+  float Ax = v0.x - r.ox, Ay = v0.y - r.oy, Az = v0.z - r.oz;
+  float Bx = v1.x - r.ox, By = v1.y - r.oy, Bz = v1.z - r.oz;
+  float Cx = v2.x - r.ox, Cy = v2.y - r.oy, Cz = v2.z - r.oz;
+  float ax = fmaf(r.sx2, Az, fmaf(r.sx1, Ay, r.sx0 * Ax));
+  float ay = fmaf(r.sy2, Az, fmaf(r.sy1, Ay, r.sy0 * Ax));
+  float bx = fmaf(r.sx2, Bz, fmaf(r.sx1, By, r.sx0 * Bx));
+  float by = fmaf(r.sy2, Bz, fmaf(r.sy1, By, r.sy0 * Bx));
+  float cx = fmaf(r.sx2, Cz, fmaf(r.sx1, Cy, r.sx0 * Cx));
+  float cy = fmaf(r.sy2, Cz, fmaf(r.sy1, Cy, r.sy0 * Cx));
+  float U = dmd(cx, by, cy, bx);
+  float V = dmd(ax, cy, ay, cx);
+  float W = dmd(bx, ay, by, ax);
+  if (U == 0.f || V == 0.f || W == 0.f) {
+    U = float(double(cx) * double(by) - double(cy) * double(bx));
+    V = float(double(ax) * double(cy) - double(ay) * double(cx));
+    W = float(double(bx) * double(ay) - double(by) * double(ax));
+  }
+  if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
+  if (U + V + W == 0.f) return false;
+  // t by the renderer's formula (src/triangle.cpp:32-37).
+  float e1x = fs(v1.x, v0.x), e1y = fs(v1.y, v0.y), e1z = fs(v1.z, v0.z);
+  float e2x = fs(v2.x, v0.x), e2y = fs(v2.y, v0.y), e2z = fs(v2.z, v0.z);
+  float nx = dmd(e1y, e2z, e1z, e2y);
+  float ny = dmd(e1z, e2x, e1x, e2z);
+  float nz = dmd(e1x, e2y, e1y, e2x);
+  float w = -dot3x(nx, ny, nz, r.dx, r.dy, r.dz);
+  if (w == 0.f) return false;
+  float adx = fs(r.ox, v0.x), ady = fs(r.oy, v0.y), adz = fs(r.oz, v0.z);
+  float t = fdv(dot3x(nx, ny, nz, adx, ady, adz), w);
+  if (!accept_t(t, r.tmin, tcur, found)) return false;
+  // Barycentrics by the renderer's formula (src/triangle.cpp:40-43).
+  float qx = dmd(ady, r.dz, adz, r.dy);
+  float qy = dmd(adz, r.dx, adx, r.dz);
+  float qz = dmd(adx, r.dy, ady, r.dx);
+  u_out = fdv(dot3x(qx, qy, qz, e2x, e2y, e2z), w);
+  v_out = -fdv(dot3x(qx, qy, qz, e1x, e1y, e1z), w);
+  t_out = t;
+  return true;
+}
+
+// Parallelogram origin + a u + b v, a, b in [0, 1] (AreaLight::intersect).
+__device__ __forceinline__ bool pgram_test(const TRay& r, float4 o, float4 eu, float4 ev, float tcur, bool found,
+                                           float& t_out, float& u_out, float& v_out) {
+  float nx = dmd(eu.y, ev.z, eu.z, ev.y);
+  float ny = dmd(eu.z, ev.x, eu.x, ev.z);
+  float nz = dmd(eu.x, ev.y, eu.y, ev.x);
+  float w = -dot3x(nx, ny, nz, r.dx, r.dy, r.dz);
+  if (w == 0.f) return false;
+  float adx = fs(r.ox, o.x), ady = fs(r.oy, o.y), adz = fs(r.oz, o.z);
+  float t = fdv(dot3x(nx, ny, nz, adx, ady, adz), w);
+  if (!(t >= r.tmin && t <= r.tmax)) return false;
+  float qx = dmd(ady, r.dz, adz, r.dy);
+  float qy = dmd(adz, r.dx, adx, r.dz);
+  float qz = dmd(adx, r.dy, ady, r.dx);
+  float u = fdv(dot3x(qx, qy, qz, ev.x, ev.y, ev.z), w);
+  if (u < 0.f || u > 1.f) return false;
+  float v = -fdv(dot3x(qx, qy, qz, eu.x, eu.y, eu.z), w);
+  if (v < 0.f || v > 1.f) return false;
+  if (!accept_t(t, r.tmin, tcur, found)) return false;
+  t_out = t; u_out = u; v_out = v;
+  return true;
+}
+
+// Sphere, first intersection parameter at or beyond tmin (CSGObject rule).
+__device__ __forceinline__ bool sphere_test(const TRay& r, float4 c, float rad, float tcur, bool found,
+                                            float& t_out) {
+  float dfx = fs(r.ox, c.x), dfy = fs(r.oy, c.y), dfz = fs(r.oz, c.z);
+  float r2 = fm(rad, rad);
+  float a = dot3x(r.dx, r.dy, r.dz, r.dx, r.dy, r.dz);
+  float b = fm(2.f, dot3x(r.dx, r.dy, r.dz, dfx, dfy, dfz));
+  float cc = fs(dot3x(dfx, dfy, dfz, dfx, dfy, dfz), r2);
+  float disc = fs(fm(b, b), fm(fm(4.f, a), cc));
+  if (!(disc >= 0.f)) return false;
+  float rd = __fsqrt_rn(disc);
+  float a2 = fm(2.f, a);
+  float t1 = fdv(fs(-b, rd), a2);
+  float t2 = fdv(fa(-b, rd), a2);
+  if (r.tmin > t2) return false;
+  float t = (t1 >= r.tmin) ? t1 : t2;
+  if (!(t >= r.tmin)) return false;  // NaN guard
+  if (t > r.tmax) return false;
+  if (!accept_t(t, r.tmin, tcur, found)) return false;
+  t_out = t;
+  return true;
+}
+
+// Plane (src/plane.cpp:29-31): t = dot((o,1), P) / -dot(d, P.xyz).
+__device__ __forceinline__ float plane_t(const TRay& r, float4 P) {
+  float d = -dot3x(r.dx, r.dy, r.dz, P.x, P.y, P.z);
+  float u = fa(dot3x(r.ox, r.oy, r.oz, P.x, P.y, P.z), P.w);
+  return fdv(u, d);
+}
+
+struct TraceCounters {
+  unsigned long long nodes, prims;
+};
+
+// Traverses the scene. ANY: stop at the first accepted hit and skip records
+// (and planes) whose prim id equals ignore_prim. Returns the internal hit
+// encoding (RawHit::rec) and fills t/u/v. stack is this thread's column of the
+// block's shared stack (stride kTraceBlock).
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ int32_t trace_ray(const DeviceScene& S, const TRay& r, int ignore_prim, int* stack,
+                                             float& t_best, float& u_best, float& v_best, int* err,
+                                             TraceCounters* cnt) {
+  float tcur = r.tmax;
+  bool found = false;
+  int32_t best = -1;
+  float bu = 0.f, bv = 0.f;
+  // Planes: unbounded, tested first to give the BVH a tighter tmax.
+  for (int k = 0; k < S.n_planes; ++k) {
+    if (ANY && S.plane_meta[k].x == ignore_prim) continue;
+    float t = plane_t(r, __ldg(&S.planes[k]));
+    if (t >= r.tmin && t <= r.tmax && accept_t(t, r.tmin, tcur, found)) {
+      tcur = t; found = true; best = -2 - k; bu = 0.f; bv = 0.f;
+      if (ANY) { t_best = t; return best; }
+    }
+  }
+  if (S.n_nodes > 0) {
+    int sp = 0;
+    stack[0] = 0x7fffffff;  // sentinel
+    int32_t node = 0;
+    while (node != 0x7fffffff) {
+      if (node >= 0) {
+        const float4* np = S.nodes + 4 * int64_t(node);
+        float4 n0 = __ldg(np + 0), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
+        int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+        if (COUNT) cnt->nodes++;
+        float tn0, tn1;
+        bool h0 = box_hit(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, tcur, tn0);
+        bool h1 = box_hit(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, tcur, tn1);
+        if (h0 && h1) {
+          int32_t nearRef = n3.x, farRef = n3.y;
+          if (tn1 < tn0) { nearRef = n3.y; farRef = n3.x; }
+          if (sp + 1 >= kStackSize) { *err = 1; break; }
+          stack[(++sp) * kTraceBlock] = farRef;
+          node = nearRef;
+        } else if (h0) {
+          node = n3.x;
+        } else if (h1) {
+          node = n3.y;
+        } else {
+          node = stack[(sp--) * kTraceBlock];
+        }
+        continue;
+      }
+      // Leaf.
+      uint32_t lv = ~uint32_t(node);
+      int64_t first = int64_t(lv >> 4), count = int64_t(lv & 15u) + 1;
+      for (int64_t k = first; k < first + count; ++k) {
+        const float4* rp = S.recs + 3 * k;
+        float4 a = __ldg(rp + 0), b = __ldg(rp + 1), c = __ldg(rp + 2);
+        if (COUNT) cnt->prims++;
+        int kind = __float_as_int(a.w);
+        if (ANY && __float_as_int(c.w) == ignore_prim) continue;
+        float t, u = 0.f, v = 0.f;
+        bool hit;
+        if (kind == kRecTriangle) hit = tri_test(r, a, b, c, tcur, found, t, u, v);
+        else if (kind == kRecSphere) hit = sphere_test(r, a, b.x, tcur, found, t);
+        else hit = pgram_test(r, a, b, c, tcur, found, t, u, v);
+        if (hit) {
+          tcur = t; found = true; best = int32_t(k); bu = u; bv = v;
+          if (ANY) break;
+        }
+      }
+      if (ANY && found) break;
+      node = stack[(sp--) * kTraceBlock];
+    }
+  }
+  t_best = found ? tcur : CUDART_NAN_F;
+  u_best = bu; v_best = bv;
+  return best;
+}
+
+}  // namespace gbrt

@@ -1,0 +1,132 @@
+"""Scene description held in numpy arrays, and its gbrt_scene_desc view.
+
+A SceneData mirrors what the renderer's scene builder produces
+(src/sceneast.cpp:673-695): materials, geometry (triangles, quads, spheres,
+planes), the ordered light list and at most one environment image. Spectra are
+BGR, as in the renderer's cv::Vec3f.
+"""
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import _abi
+
+
+def _f3(v):
+    return _abi.F3(*[float(x) for x in v])
+
+
+@dataclass
+class SceneData:
+    materials: List[dict] = field(default_factory=list)
+    tri_pos: Optional[np.ndarray] = None   # (N, 9) float32
+    tri_nrm: Optional[np.ndarray] = None   # (N, 9) float32 or None
+    tri_mat: Optional[np.ndarray] = None   # (N,) int32 or None (all material 0)
+    quads: List[tuple] = field(default_factory=list)     # (p1, p2, p3, p4, material)
+    spheres: List[tuple] = field(default_factory=list)   # (center, radius, material)
+    planes: List[tuple] = field(default_factory=list)    # (plane4, material)
+    lights: List[dict] = field(default_factory=list)     # {"type", "origin", "u", "v", "intensity"}
+    env: Optional[np.ndarray] = None       # (H, W, 3) float32 BGR
+    env_mapping: int = _abi.ENV_ANGULAR
+    camera: Optional[dict] = None          # {"eye", "look_at", "up", "fov", "width", "height"}
+
+    # ------------------------------------------------------------ building
+    def add_material(self, type, kd=(0, 0, 0), ks=(0, 0, 0), exponent=0.0, ior=1.0, coefficient=1.0):
+        self.materials.append(dict(type=type, kd=tuple(kd), ks=tuple(ks), exponent=float(exponent),
+                                   ior=float(ior), coefficient=float(coefficient)))
+        return len(self.materials) - 1
+
+    def n_tri(self):
+        return 0 if self.tri_pos is None else int(self.tri_pos.shape[0])
+
+    def n_prims(self):
+        return len(self.lights) + self.n_tri() + len(self.quads) + len(self.spheres) + len(self.planes)
+
+    def prim_offsets(self):
+        """First primitive id of each type, in the order of include/gbrt.h."""
+        o = {"lights": 0}
+        o["tri"] = len(self.lights)
+        o["quads"] = o["tri"] + self.n_tri()
+        o["spheres"] = o["quads"] + len(self.quads)
+        o["planes"] = o["spheres"] + len(self.spheres)
+        return o
+
+    # ------------------------------------------------------------ C view
+    def to_desc(self):
+        """Returns (gbrt_scene_desc, keepalive). keepalive must outlive every use."""
+        keep = []
+        d = _abi.SceneDesc()
+        if self.materials:
+            arr = (_abi.Material * len(self.materials))()
+            for i, m in enumerate(self.materials):
+                arr[i] = _abi.Material(m["type"], _f3(m["kd"]), _f3(m["ks"]), m["exponent"], m["ior"],
+                                       m["coefficient"])
+            keep.append(arr)
+            d.materials = arr
+            d.n_materials = len(self.materials)
+        if self.n_tri():
+            pos = np.ascontiguousarray(self.tri_pos, dtype=np.float32)
+            keep.append(pos)
+            d.tri_pos = pos.ctypes.data_as(C.POINTER(C.c_float))
+            if self.tri_nrm is not None:
+                nrm = np.ascontiguousarray(self.tri_nrm, dtype=np.float32)
+                keep.append(nrm)
+                d.tri_nrm = nrm.ctypes.data_as(C.POINTER(C.c_float))
+            if self.tri_mat is not None:
+                mat = np.ascontiguousarray(self.tri_mat, dtype=np.int32)
+                keep.append(mat)
+                d.tri_mat = mat.ctypes.data_as(C.POINTER(C.c_int32))
+            d.n_tri = self.n_tri()
+        if self.quads:
+            arr = (_abi.Quad * len(self.quads))()
+            for i, q in enumerate(self.quads):
+                arr[i].p = (_abi.F3 * 4)(*[_f3(p) for p in q[:4]])
+                arr[i].material = int(q[4])
+            keep.append(arr)
+            d.quads = arr
+            d.n_quads = len(self.quads)
+        if self.spheres:
+            arr = (_abi.Sphere * len(self.spheres))()
+            for i, s in enumerate(self.spheres):
+                arr[i] = _abi.Sphere(_f3(s[0]), float(s[1]), int(s[2]))
+            keep.append(arr)
+            d.spheres = arr
+            d.n_spheres = len(self.spheres)
+        if self.planes:
+            arr = (_abi.Plane * len(self.planes))()
+            for i, p in enumerate(self.planes):
+                arr[i] = _abi.Plane((C.c_float * 4)(*[float(x) for x in p[0]]), int(p[1]))
+            keep.append(arr)
+            d.planes = arr
+            d.n_planes = len(self.planes)
+        if self.lights:
+            arr = (_abi.Light * len(self.lights))()
+            for i, L in enumerate(self.lights):
+                arr[i] = _abi.Light(L["type"], _f3(L.get("origin", (0, 0, 0))), _f3(L.get("u", (0, 0, 0))),
+                                    _f3(L.get("v", (0, 0, 0))), _f3(L.get("intensity", (0, 0, 0))))
+            keep.append(arr)
+            d.lights = arr
+            d.n_lights = len(self.lights)
+        if self.env is not None:
+            tex = np.ascontiguousarray(self.env, dtype=np.float32)
+            keep.append(tex)
+            e = _abi.EnvMap(tex.shape[1], tex.shape[0], self.env_mapping,
+                            tex.ctypes.data_as(C.POINTER(C.c_float)))
+            keep.append(e)
+            d.env = C.pointer(e)
+        return d, keep
+
+    def camera_struct(self, width=None, height=None):
+        c = self.camera
+        return _abi.Camera(_f3(c["eye"]), _f3(c["look_at"]), _f3(c["up"]), float(c["fov"]),
+                           int(width or c["width"]), int(height or c["height"]))
+
+
+def render_params(x_samples=4, y_samples=4, termination_prob=0.5, max_depth=5, seed=0,
+                  semantics=_abi.SEM_REFERENCE, batch_paths=0):
+    """gbrt_render_params with PerPixelRenderer's defaults (src/perpixelrenderer.cpp:103-112)
+    and the renderer's MAX_DEPTH of 5 (src/renderer.h:38)."""
+    return _abi.RenderParams(int(x_samples), int(y_samples), float(termination_prob), int(max_depth),
+                             int(seed), int(semantics), int(batch_paths))

@@ -1,0 +1,206 @@
+"""Deterministic synthetic workloads (seeded; no external data).
+
+cornell_box()      256x256, 4x4 jittered spp, max depth 8, Russian roulette
+                   from depth 3: five diffuse quads (2x2x2 room, white 0.73,
+                   red and green side walls), a 0.5x0.5 ceiling area light of
+                   radiance 15, a mirror and a glass (IOR 1.5) sphere, r=0.35,
+                   pinhole camera with a 40 degree vertical field of view.
+icosphere_scene()  an icosahedron subdivided 8 times (1,310,720 triangles)
+                   displaced radially by 4-octave value noise of amplitude 0.1
+                   (Phong kd 0.5, ks 0.3, exponent 50), a diffuse ground plane
+                   of albedo 0.6, a 1024x512 lat-long sky (seeded gradient and a
+                   0.5 degree sun disc of radiance 5e4) and one area light;
+                   1024x1024, 8x8 spp, max depth 12.
+Spectra are BGR. Values given in RGB below are swapped on the way in.
+"""
+import numpy as np
+
+from . import _abi
+from .scene import SceneData, render_params
+
+FOV_40 = 0.6981317  # 40 degrees in radians (the renderer's camera takes radians)
+
+
+def bgr(rgb):
+    return (float(rgb[2]), float(rgb[1]), float(rgb[0]))
+
+
+# ---------------------------------------------------------------- Cornell box
+def cornell_box(width=256, height=256):
+    s = SceneData()
+    white = s.add_material(_abi.MAT_DIFFUSE, kd=bgr((0.73, 0.73, 0.73)))
+    red = s.add_material(_abi.MAT_DIFFUSE, kd=bgr((0.63, 0.065, 0.05)))
+    green = s.add_material(_abi.MAT_DIFFUSE, kd=bgr((0.14, 0.45, 0.09)))
+    mirror = s.add_material(_abi.MAT_MIRROR, coefficient=1.0)
+    glass = s.add_material(_abi.MAT_TRANSPARENT, ior=1.5)
+    s.quads = [
+        ((-1, 0, -1), (1, 0, -1), (1, 0, 1), (-1, 0, 1), white),      # floor
+        ((-1, 2, -1), (-1, 2, 1), (1, 2, 1), (1, 2, -1), white),      # ceiling
+        ((-1, 0, -1), (-1, 2, -1), (1, 2, -1), (1, 0, -1), white),    # back
+        ((-1, 0, -1), (-1, 0, 1), (-1, 2, 1), (-1, 2, -1), red),      # left
+        ((1, 0, -1), (1, 2, -1), (1, 2, 1), (1, 0, 1), green),        # right
+    ]
+    s.spheres = [((-0.45, 0.35, -0.3), 0.35, mirror), ((0.45, 0.35, 0.25), 0.35, glass)]
+    # u x v = (0, -0.25, 0): the light faces down.
+    s.lights = [dict(type=_abi.LIGHT_AREA, origin=(-0.25, 1.98, -0.25), u=(0.5, 0, 0), v=(0, 0, 0.5),
+                     intensity=(15.0, 15.0, 15.0))]
+    s.camera = dict(eye=(0, 1, 3.4), look_at=(0, 1, 0), up=(0, 1, 0), fov=FOV_40, width=width, height=height)
+    return s
+
+
+def cornell_params(max_depth=8, seed=0, x_samples=4, y_samples=4):
+    return render_params(x_samples, y_samples, 0.5, max_depth, seed)
+
+
+# ------------------------------------------------------------------ icosphere
+_ICO_T = (1.0 + 5.0 ** 0.5) / 2.0
+_ICO_V = np.array([(-1, _ICO_T, 0), (1, _ICO_T, 0), (-1, -_ICO_T, 0), (1, -_ICO_T, 0),
+                   (0, -1, _ICO_T), (0, 1, _ICO_T), (0, -1, -_ICO_T), (0, 1, -_ICO_T),
+                   (_ICO_T, 0, -1), (_ICO_T, 0, 1), (-_ICO_T, 0, -1), (-_ICO_T, 0, 1)], np.float64)
+_ICO_F = np.array([(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+                   (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8),
+                   (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)], np.int64)
+
+
+def icosphere(levels):
+    """Unit icosphere: 20 * 4^levels triangles, 10 * 4^levels + 2 vertices."""
+    V = _ICO_V / np.linalg.norm(_ICO_V, axis=1, keepdims=True)
+    F = _ICO_F.copy()
+    for _ in range(levels):
+        nv = len(V)
+        e = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]])
+        e.sort(axis=1)
+        key = e[:, 0] * nv + e[:, 1]
+        uniq, inv = np.unique(key, return_inverse=True)
+        a, b = uniq // nv, uniq % nv
+        mid = V[a] + V[b]
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        m = nv + inv.reshape(-1)
+        nf = len(F)
+        m01, m12, m20 = m[:nf], m[nf:2 * nf], m[2 * nf:]
+        F = np.concatenate([np.stack([F[:, 0], m01, m20], 1), np.stack([F[:, 1], m12, m01], 1),
+                            np.stack([F[:, 2], m20, m12], 1), np.stack([m01, m12, m20], 1)])
+        V = np.concatenate([V, mid])
+    return V, F
+
+
+def _splitmix64(z):
+    z = z + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def _lattice(seed, i, j, k):
+    h = (np.uint64(seed) ^ (i.astype(np.uint64) * np.uint64(0x8CB92BA72F3D8DD7))
+         ^ (j.astype(np.uint64) * np.uint64(0xABC98388FB8FAC03))
+         ^ (k.astype(np.uint64) * np.uint64(0xD6E8FEB86659FD93)))
+    h = _splitmix64(h)
+    return (h >> np.uint64(11)).astype(np.float64) * (2.0 / 9007199254740992.0) - 1.0
+
+
+def value_noise(p, seed):
+    """Trilinear value noise with smoothstep weights; lattice values in [-1, 1]
+    from SplitMix64 of the integer coordinates."""
+    f = np.floor(p)
+    t = p - f
+    w = t * t * (3.0 - 2.0 * t)
+    i = f.astype(np.int64)
+    out = np.zeros(len(p))
+    for dx in (0, 1):
+        wx = w[:, 0] if dx else 1.0 - w[:, 0]
+        for dy in (0, 1):
+            wy = w[:, 1] if dy else 1.0 - w[:, 1]
+            for dz in (0, 1):
+                wz = w[:, 2] if dz else 1.0 - w[:, 2]
+                out += wx * wy * wz * _lattice(seed, i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz)
+    return out
+
+
+def fbm(p, seed, octaves=4, base_freq=2.0, lacunarity=2.0, gain=0.5):
+    """Fractal sum of value noise, normalised by the amplitude sum to [-1, 1]."""
+    total, amp, norm, freq = np.zeros(len(p)), 1.0, 0.0, base_freq
+    with np.errstate(over="ignore"):
+        for o in range(octaves):
+            total += amp * value_noise(p * freq, seed + 0x1000193 * o)
+            norm += amp
+            amp *= gain
+            freq *= lacunarity
+    return total / norm
+
+
+def displaced_icosphere(levels=8, seed=0, amplitude=0.1, smooth_normals=True):
+    """(tri_pos (N,9) float32, tri_nrm (N,9) float32 or None)."""
+    V, F = icosphere(levels)
+    r = 1.0 + amplitude * fbm(V, seed)
+    P = V * r[:, None]
+    tri = P[F]                                     # (N, 3, 3)
+    pos = tri.reshape(-1, 9).astype(np.float32)
+    if not smooth_normals:
+        return pos, None
+    fn = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])   # area-weighted
+    N = np.zeros_like(P)
+    for c in range(3):
+        for k in range(3):
+            N[:, c] += np.bincount(F[:, k], weights=fn[:, c], minlength=len(P))
+    N /= np.linalg.norm(N, axis=1, keepdims=True)
+    nrm = N[F].reshape(-1, 9).astype(np.float32)
+    return pos, nrm
+
+
+def latlong_dir(H, W):
+    """Unit direction of each texel centre of a lat-long map: u = atan2(x, -z)
+    / 2pi + 1/2 across, v = acos(y) / pi down (the library's lat-long lookup)."""
+    v = (np.arange(H) + 0.5) / H
+    u = (np.arange(W) + 0.5) / W
+    theta = v[:, None] * np.pi
+    phi = (u[None, :] - 0.5) * 2.0 * np.pi
+    st = np.sin(theta)
+    return np.stack([st * np.sin(phi), np.cos(theta) * np.ones_like(phi), -st * np.cos(phi)], -1)
+
+
+def synthetic_sky(width=1024, height=512, seed=0, sun_radiance=5e4, sun_diameter_deg=0.5):
+    """Lat-long HDR sky (H, W, 3) float32 BGR: zenith-to-horizon gradient, a
+    darker ground, and a sun disc."""
+    rng = np.random.default_rng(seed)
+    d = latlong_dir(height, width)
+    zen = np.array([0.25, 0.45, 1.0]) * rng.uniform(0.8, 1.2)
+    hor = np.array([0.9, 0.9, 1.0]) * rng.uniform(0.8, 1.2)
+    gnd = np.array([0.2, 0.18, 0.15])
+    y = d[..., 1:2]
+    sky = np.where(y >= 0, hor + (zen - hor) * np.sqrt(np.clip(y, 0, 1)), gnd)
+    el = np.deg2rad(rng.uniform(25, 50))
+    az = rng.uniform(0, 2 * np.pi)
+    sun = np.array([np.cos(el) * np.sin(az), np.sin(el), -np.cos(el) * np.cos(az)])
+    cosang = d @ sun
+    disc = cosang >= np.cos(np.deg2rad(sun_diameter_deg / 2))
+    # The texel containing the sun centre always carries it.
+    row = min(int(np.arccos(sun[1]) / np.pi * height), height - 1)
+    col = min(int((np.arctan2(sun[0], -sun[2]) / (2 * np.pi) + 0.5) * width), width - 1)
+    disc[row, col] = True
+    sky = np.where(disc[..., None], np.array([1.0, 0.95, 0.9]) * sun_radiance, sky)
+    return sky[..., ::-1].astype(np.float32).copy(), sun   # RGB -> BGR
+
+
+def icosphere_scene(levels=8, seed=0, width=1024, height=1024, env_size=(1024, 512), smooth_normals=True):
+    s = SceneData()
+    phong = s.add_material(_abi.MAT_PHONG, kd=bgr((0.5, 0.5, 0.5)), ks=bgr((0.3, 0.3, 0.3)), exponent=50.0)
+    ground = s.add_material(_abi.MAT_DIFFUSE, kd=bgr((0.6, 0.6, 0.6)))
+    pos, nrm = displaced_icosphere(levels, seed, 0.1, smooth_normals)
+    s.tri_pos = pos
+    s.tri_nrm = nrm
+    s.tri_mat = np.full(len(pos), phong, np.int32)
+    s.planes = [((0.0, 1.0, 0.0, 1.1), ground)]      # the plane y = -1.1
+    sky, _ = synthetic_sky(env_size[0], env_size[1], seed)
+    s.env = sky
+    s.env_mapping = _abi.ENV_LATLONG
+    s.lights = [dict(type=_abi.LIGHT_AREA, origin=(-0.5, 2.5, -0.5), u=(1, 0, 0), v=(0, 0, 1),
+                     intensity=(10.0, 10.0, 10.0)),
+                dict(type=_abi.LIGHT_ENV, intensity=(1.0, 1.0, 1.0))]
+    s.camera = dict(eye=(0, 0.4, 3.2), look_at=(0, -0.1, 0), up=(0, 1, 0), fov=FOV_40, width=width,
+                    height=height)
+    return s
+
+
+def icosphere_params(seed=0):
+    return render_params(8, 8, 0.5, 12, seed)
