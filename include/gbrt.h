@@ -134,7 +134,17 @@ typedef struct gbrt_scene_desc {
   const gbrt_plane* planes; int32_t n_planes;
   const gbrt_light* lights; int32_t n_lights;
   const gbrt_env_map* env;  /* NULL if no environment map */
+  int32_t flags;            /* gbrt_scene_flags */
 } gbrt_scene_desc;
+
+typedef enum gbrt_scene_flags {
+  /* Triangle inside/outside decisions by the watertight test of Woop, Benthin
+   * and Wald (JCGT 2013) instead of the renderer's own float test
+   * (src/triangle.cpp:30-56). The renderer's test leaves cracks and overlaps
+   * along shared edges; with this flag no ray slips through a closed mesh, at
+   * the price of decisions that differ from the renderer's near edges. */
+  GBRT_SCENE_WATERTIGHT = 1
+} gbrt_scene_flags;
 
 /* Camera(cop, lookAt, up, fov[radians, full vertical], resolution),
  * src/camera.cpp:34-58. */
@@ -162,7 +172,17 @@ typedef struct gbrt_render_params {
   uint64_t seed;            /* --seed                                      */
   int32_t semantics;        /* gbrt_semantics                              */
   int32_t batch_paths;      /* paths in flight per wavefront; 0 = auto     */
+  int32_t flags;            /* gbrt_render_flags                           */
 } gbrt_render_params;
+
+typedef enum gbrt_render_flags {
+  /* Time every extend / shade / shadow kernel with CUDA events on the
+   * render stream (gbrt_stats *_ms fields). */
+  GBRT_RENDER_TIME_KERNELS = 1,
+  /* Count BVH nodes visited and primitives tested (gbrt_stats counters);
+   * slower, for measurement only. */
+  GBRT_RENDER_COUNT_TRAVERSAL = 2
+} gbrt_render_flags;
 
 typedef struct gbrt_stats {
   uint64_t paths;           /* camera samples traced to termination        */
@@ -171,6 +191,11 @@ typedef struct gbrt_stats {
   uint64_t nonfinite;       /* samples whose radiance was NaN/inf (dropped)*/
   double render_ms;         /* device time of the render loop              */
   uint64_t kernel_launches; /* kernels launched by the render loop         */
+  /* with GBRT_RENDER_TIME_KERNELS: summed kernel times and launch counts */
+  double extend_ms, shade_ms, shadow_ms;
+  uint64_t extend_launches, shade_launches, shadow_launches;
+  /* with GBRT_RENDER_COUNT_TRAVERSAL: traversal work of all rays */
+  uint64_t nodes_closest, prims_closest, nodes_any, prims_any;
 } gbrt_stats;
 
 /* Ray(origin, direction, from, to), src/ray.h:36-57. 32 bytes. */
@@ -206,6 +231,7 @@ gbrt_status gbrt_ctx_destroy(gbrt_ctx* ctx);
  *      BVH. ------------------------------------------------------------- */
 gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* desc,
                               gbrt_scene** out);
+/* A scene must be destroyed before the context it was created on. */
 gbrt_status gbrt_scene_destroy(gbrt_scene* scene);
 /* BVH statistics: nodes, leaves, max depth, SAH cost, build milliseconds. */
 gbrt_status gbrt_scene_info(const gbrt_scene* scene, int64_t* n_nodes,

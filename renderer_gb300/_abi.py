@@ -43,7 +43,7 @@ class SceneDesc(C.Structure):
                 ("spheres", C.POINTER(Sphere)), ("n_spheres", C.c_int32),
                 ("planes", C.POINTER(Plane)), ("n_planes", C.c_int32),
                 ("lights", C.POINTER(Light)), ("n_lights", C.c_int32),
-                ("env", C.POINTER(EnvMap))]
+                ("env", C.POINTER(EnvMap)), ("flags", C.c_int32)]
 
 
 class Camera(C.Structure):
@@ -54,13 +54,19 @@ class Camera(C.Structure):
 class RenderParams(C.Structure):
     _fields_ = [("x_samples", C.c_int32), ("y_samples", C.c_int32),
                 ("termination_prob", C.c_float), ("max_depth", C.c_int32),
-                ("seed", C.c_uint64), ("semantics", C.c_int32), ("batch_paths", C.c_int32)]
+                ("seed", C.c_uint64), ("semantics", C.c_int32), ("batch_paths", C.c_int32),
+                ("flags", C.c_int32)]
 
 
 class Stats(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("extension_rays", C.c_uint64),
                 ("shadow_rays", C.c_uint64), ("nonfinite", C.c_uint64),
-                ("render_ms", C.c_double), ("kernel_launches", C.c_uint64)]
+                ("render_ms", C.c_double), ("kernel_launches", C.c_uint64),
+                ("extend_ms", C.c_double), ("shade_ms", C.c_double), ("shadow_ms", C.c_double),
+                ("extend_launches", C.c_uint64), ("shade_launches", C.c_uint64),
+                ("shadow_launches", C.c_uint64),
+                ("nodes_closest", C.c_uint64), ("prims_closest", C.c_uint64),
+                ("nodes_any", C.c_uint64), ("prims_any", C.c_uint64)]
 
 
 class Ray(C.Structure):
@@ -85,6 +91,9 @@ LIGHT_AREA, LIGHT_POINT, LIGHT_ENV, LIGHT_BLACK = range(4)
 ENV_ANGULAR, ENV_LATLONG = range(2)
 # gbrt_semantics
 SEM_REFERENCE, SEM_PHYSICAL = range(2)
+# gbrt_scene_flags / gbrt_render_flags
+SCENE_WATERTIGHT = 1
+RENDER_TIME_KERNELS, RENDER_COUNT_TRAVERSAL = 1, 2
 
 P = C.c_void_p
 

@@ -22,6 +22,8 @@ struct gbrt_ctx {
 
 struct gbrt_scene {
   gbrt_ctx* ctx = nullptr;
+  int device = 0;
+  bool watertight = false;  // GBRT_SCENE_WATERTIGHT
   gbrt::DeviceScene view{};
   std::vector<void*> allocations;
   int64_t n_leaves = 0;

@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "gbrt_internal.h"
@@ -127,7 +128,21 @@ __global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
   st.ext_slot[0][slot] = slot;
 }
 
+// Adds a warp's traversal counters to two global totals (all lanes call it).
+__device__ __forceinline__ void warp_add_counters(TraceCounters c, unsigned long long* nodes,
+                                                  unsigned long long* prims) {
+  for (int o = 16; o > 0; o >>= 1) {
+    c.nodes += __shfl_xor_sync(0xffffffffu, c.nodes, o);
+    c.prims += __shfl_xor_sync(0xffffffffu, c.prims, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(nodes, c.nodes);
+    atomicAdd(prims, c.prims);
+  }
+}
+
 // ------------------------------------------------------------- extend ----
+template <bool COUNT, bool WT>
 __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState st, int cur) {
   __shared__ int s_stack[kStackSize * kTraceBlock];
   int* stack = s_stack + threadIdx.x;
@@ -136,6 +151,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState s
   const float4* rays = st.ext[cur];
   unsigned long long* work = st.work + cur;
   const int lane = threadIdx.x & 31;
+  TraceCounters cnt{0, 0};
   for (;;) {
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(work, 32ull);
@@ -145,12 +161,14 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState s
     if (i >= n) continue;
     TRay r = make_tray(rays[2 * i], rays[2 * i + 1]);
     RawHit h;
-    h.rec = trace_ray<false, false>(S, r, -1, stack, h.t, h.u, h.v, st.err, nullptr);
+    h.rec = trace_ray<false, COUNT, WT>(S, r, -1, stack, h.t, h.u, h.v, st.err, &cnt);
     st.hits[i] = h;
   }
+  if (COUNT) warp_add_counters(cnt, &st.tally[3], &st.tally[4]);
 }
 
 // ------------------------------------------------------------- shadow ----
+template <bool COUNT, bool WT>
 __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState st) {
   __shared__ int s_stack[kStackSize * kTraceBlock];
   int* stack = s_stack + threadIdx.x;
@@ -158,6 +176,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState s
   if (blockIdx.x == 0 && threadIdx.x == 0) st.tally[1] += (unsigned long long)n;
   unsigned long long* work = st.work + 2;
   const int lane = threadIdx.x & 31;
+  TraceCounters cnt{0, 0};
   for (;;) {
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(work, 32ull);
@@ -168,7 +187,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState s
     float4 c = st.sh_c[i];
     TRay r = make_tray(st.sh_ray[2 * i], st.sh_ray[2 * i + 1]);
     float t, u, v;
-    int32_t rec = trace_ray<true, false>(S, r, __float_as_int(c.w), stack, t, u, v, st.err, nullptr);
+    int32_t rec = trace_ray<true, COUNT, WT>(S, r, __float_as_int(c.w), stack, t, u, v, st.err, &cnt);
     if (rec == -1) {
       float4* L = st.L + st.sh_slot[i];
       atomicAdd(&L->x, c.x);
@@ -176,6 +195,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState s
       atomicAdd(&L->z, c.z);
     }
   }
+  if (COUNT) warp_add_counters(cnt, &st.tally[5], &st.tally[6]);
 }
 
 // -------------------------------------------------------------- shade ----
@@ -542,27 +562,40 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   A(buf.alloc(&st.ext_slot[0], B)); A(buf.alloc(&st.ext_slot[1], B));
   A(buf.alloc(&st.hits, B));
   A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
-  A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 4)); A(buf.alloc(&st.err, 1));
+  A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
   if (!d_sum) A(buf.alloc(&d_sum, npix * 3));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "render buffers");
   A(cudaMemsetAsync(d_sum, 0, npix * 3 * sizeof(double), stream));
   if (d_sumsq) A(cudaMemsetAsync(d_sumsq, 0, npix * 3 * sizeof(double), stream));
-  A(cudaMemsetAsync(st.tally, 0, 4 * sizeof(unsigned long long), stream));
+  A(cudaMemsetAsync(st.tally, 0, 8 * sizeof(unsigned long long), stream));
   A(cudaMemsetAsync(st.err, 0, sizeof(int), stream));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "render set-up");
 
-  static int traceGrid = 0, shadowGrid = 0;
-  if (!traceGrid) {
-    int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_extend, kTraceBlock, 0);
-    traceGrid = std::max(1, per) * ctx->num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shadow, kTraceBlock, 0);
-    shadowGrid = std::max(1, per) * ctx->num_sms;
-  }
+  const bool count = (prm->flags & GBRT_RENDER_COUNT_TRAVERSAL) != 0;
+  const bool timeK = (prm->flags & GBRT_RENDER_TIME_KERNELS) != 0;
+  const bool wt = s->watertight;
+  auto kExt = count ? (wt ? k_extend<true, true> : k_extend<true, false>)
+                    : (wt ? k_extend<false, true> : k_extend<false, false>);
+  auto kSh = count ? (wt ? k_shadow<true, true> : k_shadow<true, false>)
+                   : (wt ? k_shadow<false, true> : k_shadow<false, false>);
+  // Persistent grids: every SM filled with as many blocks as fit.
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kExt, kTraceBlock, 0);
+  const int traceGrid = std::max(1, per) * ctx->num_sms;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kSh, kTraceBlock, 0);
+  const int shadowGrid = std::max(1, per) * ctx->num_sms;
   const int shadeGrid = ctx->num_sms * 8;
   cudaEvent_t ev0, ev1;
   cudaEventCreate(&ev0);
   cudaEventCreate(&ev1);
+  // Per-kernel timing: one event pair per launch of extend / shade / shadow.
+  std::vector<cudaEvent_t> kev;
+  auto mark = [&]() {
+    cudaEvent_t e2;
+    cudaEventCreate(&e2);
+    cudaEventRecord(e2, stream);
+    kev.push_back(e2);
+  };
   cudaEventRecord(ev0, stream);
   unsigned long long launches = 0;
   gbrt_status status = GBRT_OK;
@@ -577,9 +610,13 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
       A(cudaMemsetAsync(st.counts + nxt, 0, sizeof(int), stream));
       A(cudaMemsetAsync(st.counts + 2, 0, sizeof(int), stream));
       A(cudaMemsetAsync(st.work, 0, 4 * sizeof(unsigned long long), stream));
-      k_extend<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
+      if (timeK) mark();
+      kExt<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
+      if (timeK) mark();
       k_shade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
-      k_shadow<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
+      if (timeK) mark();
+      kSh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
+      if (timeK) mark();
       launches += 3;
     }
     unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
@@ -594,7 +631,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   ++launches;
   cudaEventRecord(ev1, stream);
   A(cudaGetLastError());
-  unsigned long long tally[4] = {0, 0, 0, 0};
+  unsigned long long tally[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int err = 0;
   A(cudaMemcpyAsync(tally, st.tally, sizeof tally, cudaMemcpyDeviceToHost, stream));
   A(cudaMemcpyAsync(&err, st.err, sizeof err, cudaMemcpyDeviceToHost, stream));
@@ -603,14 +640,33 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   cudaEventElapsedTime(&ms, ev0, ev1);
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
+  double kms[3] = {0, 0, 0};
+  for (size_t k = 0; k + 3 < kev.size(); k += 4) {
+    for (int j = 0; j < 3; ++j) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, kev[k + j], kev[k + j + 1]);
+      kms[j] += t;
+    }
+  }
+  for (cudaEvent_t x : kev) cudaEventDestroy(x);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "gbrt_render");
   if (stats) {
+    std::memset(stats, 0, sizeof *stats);
     stats->paths = status == GBRT_OK ? total : 0;
     stats->extension_rays = tally[0];
     stats->shadow_rays = tally[1];
     stats->nonfinite = tally[2];
     stats->render_ms = ms;
     stats->kernel_launches = launches;
+    stats->extend_ms = kms[0];
+    stats->shade_ms = kms[1];
+    stats->shadow_ms = kms[2];
+    unsigned long long nl = kev.size() / 4;
+    stats->extend_launches = stats->shade_launches = stats->shadow_launches = nl;
+    stats->nodes_closest = tally[3];
+    stats->prims_closest = tally[4];
+    stats->nodes_any = tally[5];
+    stats->prims_any = tally[6];
   }
   if (err) return fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render: traversal stack overflow");
   return status;

@@ -203,10 +203,12 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     }
     return b;
   };
-  auto addTri = [&](F3 p1, F3 p2, F3 p3, int32_t prim, int32_t mat, int32_t nidx) {
+  // quadHalf: 0 for a plain triangle, 1 / 2 for the first / second triangle
+  // of a quad (the traversal keeps Quad::intersect's first-triangle rule).
+  auto addTri = [&](F3 p1, F3 p2, F3 p3, int32_t prim, int32_t mat, int32_t nidx, int32_t quadHalf) {
     Rec r{};
     r.v[0] = p1.x; r.v[1] = p1.y; r.v[2] = p1.z; setW(r.v[3], kRecTriangle);
-    r.v[4] = p2.x; r.v[5] = p2.y; r.v[6] = p2.z; setW(r.v[7], 0);
+    r.v[4] = p2.x; r.v[5] = p2.y; r.v[6] = p2.z; setW(r.v[7], quadHalf);
     r.v[8] = p3.x; r.v[9] = p3.y; r.v[10] = p3.z; setW(r.v[11], prim);
     r.meta[0] = prim; r.meta[1] = mat; r.meta[2] = nidx; r.meta[3] = -1;
     recs.push_back(r);
@@ -265,15 +267,15 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
         for (int k = 0; k < 3; ++k) nrm.push_back(0.f);
       }
     }
-    addTri(f3(p), f3(p + 3), f3(p + 6), pid, matIndex(d->tri_mat ? d->tri_mat[i] : 0), nidx);
+    addTri(f3(p), f3(p + 3), f3(p + 6), pid, matIndex(d->tri_mat ? d->tri_mat[i] : 0), nidx, 0);
   }
   for (int i = 0; i < d->n_quads; ++i, ++pid) {
     const gbrt_quad& q = d->quads[i];
     for (int k = 0; k < 4; ++k)
       if (!finite3(q.p[k])) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: non-finite quad vertex");
     // Quad(p1,p2,p3,p4) = Triangle(p1,p2,p4) + Triangle(p4,p2,p3), src/quad.h:32.
-    addTri(f3(q.p[0]), f3(q.p[1]), f3(q.p[3]), pid, matIndex(q.material), -1);
-    addTri(f3(q.p[3]), f3(q.p[1]), f3(q.p[2]), pid, matIndex(q.material), -1);
+    addTri(f3(q.p[0]), f3(q.p[1]), f3(q.p[3]), pid, matIndex(q.material), -1, 1);
+    addTri(f3(q.p[3]), f3(q.p[1]), f3(q.p[2]), pid, matIndex(q.material), -1, 2);
   }
   for (int i = 0; i < d->n_spheres; ++i, ++pid) {
     const gbrt_sphere& s = d->spheres[i];
@@ -327,6 +329,8 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   auto* s = new (std::nothrow) gbrt_scene();
   if (!s) return fail(ctx, GBRT_ERR_OOM, "gbrt_scene_create: out of host memory");
   s->ctx = ctx;
+  s->device = ctx->device;
+  s->watertight = (d->flags & GBRT_SCENE_WATERTIGHT) != 0;
   DeviceScene& v = s->view;
   gbrt_status st;
   std::vector<float> envTex;
@@ -369,9 +373,9 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
 
 gbrt_status gbrt_scene_destroy(gbrt_scene* s) {
   if (!s) return GBRT_OK;
-  cudaSetDevice(s->ctx->device);
-  cudaStreamSynchronize(s->ctx->stream);
-  free_scene(s);
+  // Touches no context state, so it stays safe in any destruction order.
+  cudaSetDevice(s->device);
+  free_scene(s);  // cudaFree waits for work using the memory
   delete s;
   return GBRT_OK;
 }

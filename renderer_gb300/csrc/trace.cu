@@ -16,7 +16,7 @@
 
 namespace gbrt {
 
-template <bool ANY>
+template <bool ANY, bool WT>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_api(DeviceScene S, const float4* __restrict__ rays, int64_t n, const int32_t* __restrict__ ignore,
                 gbrt_hit* __restrict__ hits, uint8_t* __restrict__ occluded, unsigned long long* work, int* err) {
@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(kTraceBlock)
     TRay r = make_tray(a, b);
     float t, u, v;
     int ign = (ANY && ignore) ? ignore[i] : -1;
-    int32_t rec = trace_ray<ANY, false>(S, r, ign, stack, t, u, v, err, nullptr);
+    int32_t rec = trace_ray<ANY, false, WT>(S, r, ign, stack, t, u, v, err, nullptr);
     if (ANY) {
       occluded[i] = rec != -1 ? 1 : 0;
     } else {
@@ -63,16 +63,16 @@ static gbrt_status launch_api(gbrt_scene* s, bool any, const gbrt_ray* d_rays, c
   gbrt_ctx* ctx = s->ctx;
   GBRT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long), st));
   const float4* rays = reinterpret_cast<const float4*>(d_rays);
+  // One grid size serves every instantiation (same block size and shared
+  // memory; registers checked by -Xptxas -v).
+  static int grid = 0;
+  if (!grid) grid = trace_grid(ctx, (const void*)k_trace_api<false, false>);
   if (any) {
-    static int grid = 0;
-    if (!grid) grid = trace_grid(ctx, (const void*)k_trace_api<true>);
-    k_trace_api<true><<<grid, kTraceBlock, 0, st>>>(s->view, rays, n, d_ignore, nullptr, d_occ, ctx->d_work,
-                                                    ctx->d_err);
+    auto k = s->watertight ? k_trace_api<true, true> : k_trace_api<true, false>;
+    k<<<grid, kTraceBlock, 0, st>>>(s->view, rays, n, d_ignore, nullptr, d_occ, ctx->d_work, ctx->d_err);
   } else {
-    static int grid = 0;
-    if (!grid) grid = trace_grid(ctx, (const void*)k_trace_api<false>);
-    k_trace_api<false><<<grid, kTraceBlock, 0, st>>>(s->view, rays, n, nullptr, d_hits, nullptr, ctx->d_work,
-                                                     ctx->d_err);
+    auto k = s->watertight ? k_trace_api<false, true> : k_trace_api<false, false>;
+    k<<<grid, kTraceBlock, 0, st>>>(s->view, rays, n, nullptr, d_hits, nullptr, ctx->d_work, ctx->d_err);
   }
   GBRT_CUDA_TRY(ctx, cudaGetLastError());
   return GBRT_OK;

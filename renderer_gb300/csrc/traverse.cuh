@@ -15,16 +15,21 @@
 // a per-thread stack in shared memory laid out [depth][thread] so that a warp's
 // pushes and pops fall in distinct banks.
 //
-// Numerics. Inside/outside decisions for triangles use the watertight test of
-// Woop, Benthin and Wald (JCGT 2013): vertices are translated to the ray
-// origin, sheared so the ray runs along +z, and the three 2D edge functions are
-// evaluated without fused multiply-adds (so that the two triangles sharing an
-// edge evaluate it as exact negations of each other), with a double-precision
-// re-evaluation when one is exactly zero. The hit distance t, and the
-// barycentrics, are then computed with the renderer's own formulas and
-// operation order, again without fused multiply-adds, so that t is bit-identical
-// to the renderer's float arithmetic for the same ray and primitive. Spheres,
-// planes and parallelograms use the renderer's formulas the same way. Box tests
+// Numerics. By default a triangle is tested with the renderer's own formulas
+// (src/triangle.cpp:32-44: Cramer's rule, t first, then u in [0,1], v >= 0,
+// u + v <= 1) evaluated in the renderer's operation order with every product,
+// sum and quotient rounded separately (no fused multiply-adds), so the hit
+// decision and t are bit-identical to the renderer's float arithmetic for the
+// same ray. That test is not watertight: its barycentrics carry a rounding
+// error of about eps * |origin - vertex| / |edge|, so near a shared edge a ray
+// can miss both triangles or hit both. With GBRT_SCENE_WATERTIGHT the inside
+// decision instead uses the watertight test of Woop, Benthin and Wald (JCGT
+// 2013): vertices are translated to the ray origin and sheared so the ray runs
+// along +z, and the three 2D edge functions are evaluated without fused
+// multiply-adds (the two triangles sharing an edge then evaluate it as exact
+// negations of each other), with a double-precision re-evaluation when one is
+// exactly zero; t still comes from the renderer's formula. Spheres, planes and
+// parallelograms always use the renderer's formulas the same way. Box tests
 // are conservative: (bound - origin) * (1/d) with the far distance enlarged by
 // 1 + 2*gamma(3) (Ize 2013, "Robust BVH Ray Traversal").
 #pragma once
@@ -107,9 +112,35 @@ __device__ __forceinline__ bool accept_t(float t, float tmin, float tcur, bool f
   return t >= tmin && (found ? t < tcur : t <= tcur);
 }
 
-// Triangle p1 p2 p3. Returns true and t/u/v when the ray hits it in range.
-__device__ __forceinline__ bool tri_test(const TRay& r, float4 v0, float4 v1, float4 v2, float tcur, bool found,
-                                         float& t_out, float& u_out, float& v_out) {
+// Triangle p1 p2 p3, the renderer's test (src/triangle.cpp:30-56). Returns
+// true and t/u/v when the ray hits it inside [tmin, tlim].
+__device__ __forceinline__ bool tri_test_ref(const TRay& r, float4 v0, float4 v1, float4 v2, float tlim,
+                                             float& t_out, float& u_out, float& v_out) {
+  float e1x = fs(v1.x, v0.x), e1y = fs(v1.y, v0.y), e1z = fs(v1.z, v0.z);
+  float e2x = fs(v2.x, v0.x), e2y = fs(v2.y, v0.y), e2z = fs(v2.z, v0.z);
+  float nx = dmd(e1y, e2z, e1z, e2y);
+  float ny = dmd(e1z, e2x, e1x, e2z);
+  float nz = dmd(e1x, e2y, e1y, e2x);
+  float w = -dot3x(nx, ny, nz, r.dx, r.dy, r.dz);
+  if (w == 0.f) return false;
+  float adx = fs(r.ox, v0.x), ady = fs(r.oy, v0.y), adz = fs(r.oz, v0.z);
+  float t = fdv(dot3x(nx, ny, nz, adx, ady, adz), w);
+  if (!(t >= r.tmin && t <= tlim)) return false;
+  float qx = dmd(ady, r.dz, adz, r.dy);
+  float qy = dmd(adz, r.dx, adx, r.dz);
+  float qz = dmd(adx, r.dy, ady, r.dx);
+  float u = fdv(dot3x(qx, qy, qz, e2x, e2y, e2z), w);
+  if (u < 0.f || u > 1.f) return false;
+  float v = fdv(-dot3x(qx, qy, qz, e1x, e1y, e1z), w);
+  if (v < 0.f || fa(u, v) > 1.f) return false;
+  t_out = t; u_out = u; v_out = v;
+  return true;
+}
+
+// Triangle p1 p2 p3 with the watertight inside test; t and the barycentrics by
+// the renderer's formulas. Returns true when the ray hits it inside [tmin, tlim].
+__device__ __forceinline__ bool tri_test_wt(const TRay& r, float4 v0, float4 v1, float4 v2, float tlim,
+                                            float& t_out, float& u_out, float& v_out) {
   // Watertight inside test.
   float Ax = v0.x - r.ox, Ay = v0.y - r.oy, Az = v0.z - r.oz;
   float Bx = v1.x - r.ox, By = v1.y - r.oy, Bz = v1.z - r.oz;
@@ -140,19 +171,19 @@ __device__ __forceinline__ bool tri_test(const TRay& r, float4 v0, float4 v1, fl
   if (w == 0.f) return false;
   float adx = fs(r.ox, v0.x), ady = fs(r.oy, v0.y), adz = fs(r.oz, v0.z);
   float t = fdv(dot3x(nx, ny, nz, adx, ady, adz), w);
-  if (!accept_t(t, r.tmin, tcur, found)) return false;
+  if (!(t >= r.tmin && t <= tlim)) return false;
   // Barycentrics by the renderer's formula (src/triangle.cpp:40-43).
   float qx = dmd(ady, r.dz, adz, r.dy);
   float qy = dmd(adz, r.dx, adx, r.dz);
   float qz = dmd(adx, r.dy, ady, r.dx);
   u_out = fdv(dot3x(qx, qy, qz, e2x, e2y, e2z), w);
-  v_out = -fdv(dot3x(qx, qy, qz, e1x, e1y, e1z), w);
+  v_out = fdv(-dot3x(qx, qy, qz, e1x, e1y, e1z), w);
   t_out = t;
   return true;
 }
 
 // Parallelogram origin + a u + b v, a, b in [0, 1] (AreaLight::intersect).
-__device__ __forceinline__ bool pgram_test(const TRay& r, float4 o, float4 eu, float4 ev, float tcur, bool found,
+__device__ __forceinline__ bool pgram_test(const TRay& r, float4 o, float4 eu, float4 ev, float tlim,
                                            float& t_out, float& u_out, float& v_out) {
   float nx = dmd(eu.y, ev.z, eu.z, ev.y);
   float ny = dmd(eu.z, ev.x, eu.x, ev.z);
@@ -167,16 +198,15 @@ __device__ __forceinline__ bool pgram_test(const TRay& r, float4 o, float4 eu, f
   float qz = dmd(adx, r.dy, ady, r.dx);
   float u = fdv(dot3x(qx, qy, qz, ev.x, ev.y, ev.z), w);
   if (u < 0.f || u > 1.f) return false;
-  float v = -fdv(dot3x(qx, qy, qz, eu.x, eu.y, eu.z), w);
+  float v = fdv(-dot3x(qx, qy, qz, eu.x, eu.y, eu.z), w);
   if (v < 0.f || v > 1.f) return false;
-  if (!accept_t(t, r.tmin, tcur, found)) return false;
+  if (!(t <= tlim)) return false;
   t_out = t; u_out = u; v_out = v;
   return true;
 }
 
 // Sphere, first intersection parameter at or beyond tmin (CSGObject rule).
-__device__ __forceinline__ bool sphere_test(const TRay& r, float4 c, float rad, float tcur, bool found,
-                                            float& t_out) {
+__device__ __forceinline__ bool sphere_test(const TRay& r, float4 c, float rad, float tlim, float& t_out) {
   float dfx = fs(r.ox, c.x), dfy = fs(r.oy, c.y), dfz = fs(r.oz, c.z);
   float r2 = fm(rad, rad);
   float a = dot3x(r.dx, r.dy, r.dz, r.dx, r.dy, r.dz);
@@ -192,7 +222,7 @@ __device__ __forceinline__ bool sphere_test(const TRay& r, float4 c, float rad, 
   float t = (t1 >= r.tmin) ? t1 : t2;
   if (!(t >= r.tmin)) return false;  // NaN guard
   if (t > r.tmax) return false;
-  if (!accept_t(t, r.tmin, tcur, found)) return false;
+  if (!(t <= tlim)) return false;
   t_out = t;
   return true;
 }
@@ -209,16 +239,25 @@ struct TraceCounters {
 };
 
 // Traverses the scene. ANY: stop at the first accepted hit and skip records
-// (and planes) whose prim id equals ignore_prim. Returns the internal hit
-// encoding (RawHit::rec) and fills t/u/v. stack is this thread's column of the
-// block's shared stack (stride kTraceBlock).
-template <bool ANY, bool COUNT>
+// (and planes) whose prim id equals ignore_prim. WT: watertight triangle test.
+// Returns the internal hit encoding (RawHit::rec) and fills t/u/v. stack is
+// this thread's column of the block's shared stack (stride kTraceBlock).
+//
+// Acceptance: the first hit may lie anywhere in [tmin, tmax] (Ray::inRange is
+// inclusive); later hits must be strictly closer. One exception keeps
+// Quad::intersect's rule (src/quad.cpp:23-34) that the first triangle of a
+// quad wins over the second whenever it is hit: the first half replaces a
+// current best that is the same quad's second half even at a larger t, and the
+// second half never replaces the first.
+template <bool ANY, bool COUNT, bool WT>
 __device__ __forceinline__ int32_t trace_ray(const DeviceScene& S, const TRay& r, int ignore_prim, int* stack,
                                              float& t_best, float& u_best, float& v_best, int* err,
                                              TraceCounters* cnt) {
   float tcur = r.tmax;
   bool found = false;
   int32_t best = -1;
+  int32_t bestPrim = -1;
+  int32_t bestQuad = 0;  // 0: not a quad half, 1: first half, 2: second half
   float bu = 0.f, bv = 0.f;
   // Planes: unbounded, tested first to give the BVH a tighter tmax.
   for (int k = 0; k < S.n_planes; ++k) {
@@ -265,14 +304,29 @@ __device__ __forceinline__ int32_t trace_ray(const DeviceScene& S, const TRay& r
         float4 a = __ldg(rp + 0), b = __ldg(rp + 1), c = __ldg(rp + 2);
         if (COUNT) cnt->prims++;
         int kind = __float_as_int(a.w);
-        if (ANY && __float_as_int(c.w) == ignore_prim) continue;
+        int prim = __float_as_int(c.w);
+        if (ANY && prim == ignore_prim) continue;
+        int quad = kind == kRecTriangle ? __float_as_int(b.w) : 0;
+        // The first half of a quad may displace its own second half at any t.
+        bool displace = !ANY && quad == 1 && found && bestPrim == prim && bestQuad == 2;
+        float tlim = displace ? r.tmax : tcur;
         float t, u = 0.f, v = 0.f;
         bool hit;
-        if (kind == kRecTriangle) hit = tri_test(r, a, b, c, tcur, found, t, u, v);
-        else if (kind == kRecSphere) hit = sphere_test(r, a, b.x, tcur, found, t);
-        else hit = pgram_test(r, a, b, c, tcur, found, t, u, v);
+        if (kind == kRecTriangle) {
+          if (WT) hit = tri_test_wt(r, a, b, c, tlim, t, u, v);
+          else hit = tri_test_ref(r, a, b, c, tlim, t, u, v);
+        } else if (kind == kRecSphere) {
+          hit = sphere_test(r, a, b.x, tlim, t);
+        } else {
+          hit = pgram_test(r, a, b, c, tlim, t, u, v);
+        }
+        if (hit && found && !displace) {
+          // strictly closer, and a second half never displaces its first half
+          hit = t < tcur && !(quad == 2 && bestPrim == prim && bestQuad == 1);
+        }
         if (hit) {
           tcur = t; found = true; best = int32_t(k); bu = u; bv = v;
+          bestPrim = prim; bestQuad = quad;
           if (ANY) break;
         }
       }

@@ -7,6 +7,7 @@
   PerPixelRenderer            render() of the image loop (src/perpixelrenderer.cpp:43-114)
 """
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -35,12 +36,19 @@ def _ptr(a):
 
 
 class Context:
+    """A device context. Closing it first closes the scenes created on it (a
+    scene must not outlive its context)."""
+
     def __init__(self, device=0):
         h = C.c_void_p()
+        self.handle = None
+        self._scenes = weakref.WeakSet()
         check(lib().gbrt_ctx_create(int(device), C.byref(h)))
         self.handle = h
 
     def close(self):
+        for sc in list(self._scenes):
+            sc.close()
         if self.handle:
             lib().gbrt_ctx_destroy(self.handle)
             self.handle = None
@@ -64,10 +72,12 @@ class GpuScene:
     def __init__(self, ctx: Context, data: SceneData):
         self.ctx = ctx
         self.data = data
+        self.handle = None
         desc, keep = data.to_desc()
         h = C.c_void_p()
         check(lib().gbrt_scene_create(ctx.handle, C.byref(desc), C.byref(h)), ctx.handle)
         self.handle = h
+        ctx._scenes.add(self)
 
     def info(self):
         nn, nl = C.c_int64(), C.c_int64()

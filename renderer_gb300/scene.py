@@ -31,6 +31,7 @@ class SceneData:
     env: Optional[np.ndarray] = None       # (H, W, 3) float32 BGR
     env_mapping: int = _abi.ENV_ANGULAR
     camera: Optional[dict] = None          # {"eye", "look_at", "up", "fov", "width", "height"}
+    flags: int = 0                         # gbrt_scene_flags
 
     # ------------------------------------------------------------ building
     def add_material(self, type, kd=(0, 0, 0), ks=(0, 0, 0), exponent=0.0, ior=1.0, coefficient=1.0):
@@ -116,6 +117,7 @@ class SceneData:
                             tex.ctypes.data_as(C.POINTER(C.c_float)))
             keep.append(e)
             d.env = C.pointer(e)
+        d.flags = int(self.flags)
         return d, keep
 
     def camera_struct(self, width=None, height=None):
@@ -125,8 +127,8 @@ class SceneData:
 
 
 def render_params(x_samples=4, y_samples=4, termination_prob=0.5, max_depth=5, seed=0,
-                  semantics=_abi.SEM_REFERENCE, batch_paths=0):
+                  semantics=_abi.SEM_REFERENCE, batch_paths=0, flags=0):
     """gbrt_render_params with PerPixelRenderer's defaults (src/perpixelrenderer.cpp:103-112)
     and the renderer's MAX_DEPTH of 5 (src/renderer.h:38)."""
     return _abi.RenderParams(int(x_samples), int(y_samples), float(termination_prob), int(max_depth),
-                             int(seed), int(semantics), int(batch_paths))
+                             int(seed), int(semantics), int(batch_paths), int(flags))

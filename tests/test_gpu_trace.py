@@ -61,7 +61,7 @@ def box_rays(s, rng, n):
     return make_rays(rng.uniform(lo, hi, (n, 3)), rng.normal(size=(n, 3)))
 
 
-def compare(g, o, tag):
+def compare(g, o, tag, min_frac=0.99999):
     same = g["prim"] == o["prim"]
     n = len(g)
     frac = same.mean()
@@ -79,11 +79,11 @@ def compare(g, o, tag):
         unexplained = ~(tie | edge | gedge)
         assert not unexplained.any(), (tag, np.nonzero(bad)[0][unexplained][:10], g[bad][unexplained][:5],
                                        o[bad][unexplained][:5])
-    assert frac >= 0.99999 or (n - same.sum()) <= 1, (tag, frac, n - same.sum())
+    assert frac >= min_frac or (n - same.sum()) <= 1, (tag, frac, n - same.sum())
     return frac
 
 
-def run_parity(ctx, s, rng, n_box=200000, n_per_pixel=1, cam_size=None):
+def run_parity(ctx, s, rng, n_box=200000, n_per_pixel=1, cam_size=None, min_frac=0.99999):
     gs = GpuScene(ctx, s)
     orc = OracleScene(s)
     sets = {"camera": camera_rays(s, rng, n_per_pixel, *(cam_size or (None, None)))}
@@ -96,7 +96,7 @@ def run_parity(ctx, s, rng, n_box=200000, n_per_pixel=1, cam_size=None):
     sets["box"] = box_rays(s, rng, n_box)
     res = {}
     for k, rays in sets.items():
-        res[k] = compare(gs.intersect(rays), orc.intersect(rays, threads=0), k)
+        res[k] = compare(gs.intersect(rays), orc.intersect(rays, threads=0), k, min_frac)
     return gs, orc, sets, res
 
 
@@ -120,6 +120,18 @@ def test_parity_icosphere_full_mesh(ctx):
     gs, orc, sets, res = run_parity(ctx, s, rng, n_box=100000, n_per_pixel=1)
     info = gs.info()
     assert info["max_depth"] <= 62 and info["nodes"] > 0
+
+
+def test_watertight_mode_differs_only_at_edges(ctx):
+    """GBRT_SCENE_WATERTIGHT: no cracks, so decisions near shared edges may
+    differ from the renderer's float test; every difference must be an edge or
+    a near-tie, and they stay rare."""
+    from renderer_gb300 import _abi
+    rng = np.random.default_rng(5)
+    s = workloads.icosphere_scene(levels=6, width=256, height=256, env_size=(64, 32))
+    s.flags = _abi.SCENE_WATERTIGHT
+    gs, orc, sets, res = run_parity(ctx, s, rng, n_box=100000, min_frac=0.999)
+    print("watertight agreement:", res)
 
 
 def test_any_hit_matches_oracle(ctx):
