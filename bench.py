@@ -1,0 +1,332 @@
+"""Benchmark of the GB300 path-tracing hot path (one JSON line on stdout).
+
+Workload (the headline configuration): the 1,310,720-triangle displaced
+icosphere with a diffuse ground plane, a 1024x512 lat-long sky with a sun
+disc and one area light; 1024x1024 pixels, 8x8 jittered samples per pixel
+(67,108,864 camera samples per frame), maximum path length 12, Russian
+roulette with termination probability 0.5, the renderer's estimator
+("reference semantics"). Synthetic, seeded data; no files are read.
+
+A step is one full frame. value = camera samples (paths) per second over the
+K timed frames, inputs resident in HBM (gbrt_render_device); e2e = the same
+metric through the C ABI with host buffers (gbrt_render: film copied back to
+the host every frame). The roofline entry covers the dominant kernel, the
+closest-hit traversal (k_extend), timed with CUDA events on its own stream.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the renderer's own
+PerPixelRenderer path (the oracle, built from oracle/) on all host cores, on a
+bounded sample of rows of the same workload per step. With torchrun (N > 1)
+every rank renders its own frame (replicas; the path needs no exchange).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = ("icosphere-1.31M-tri, 1024x1024, 8x8 spp, max depth 12, RR p=0.5, lat-long sky 1024x512 "
+            "+ sun + area light, reference semantics")
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return ws, rank, local, dist
+    return 1, 0, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(x, dist):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)])
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_ray():
+    """DRAM bytes per closest-hit ray from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_extend_icosphere.md")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"dram_bytes_per_ray\s*[:=]\s*([0-9.eE+-]+)", open(p).read())
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(scene, cam, params, rows, threads=0):
+    """The oracle (CPU restatement of the renderer's PerPixelRenderer path,
+    reference semantics, per-row generators) on a bounded, evenly spread
+    sample of rows. Returns (paths/s, paths, seconds, threads)."""
+    from oracle.binding import OracleScene
+    H = cam.height
+    step = max(1, H // rows)
+    o = scene if hasattr(scene, "render") else OracleScene(scene)
+    t = time.perf_counter()
+    r = o.render(cam, params, rng_mode=0, rows=(step // 2, H), row_step=step, threads=threads)
+    dt = time.perf_counter() - t
+    return r["paths"] / dt, r["paths"], dt, (threads or os.cpu_count())
+
+
+def run_reference(args, ws, rank, dist):
+    if rank != 0:
+        return
+    from oracle.binding import OracleScene
+    from renderer_gb300 import workloads
+    s = workloads.icosphere_scene(levels=8)
+    cam = s.camera_struct()
+    params = workloads.icosphere_params()
+    t = time.perf_counter()
+    o = OracleScene(s)
+    build_s = time.perf_counter() - t
+    rows = args.reference_rows
+    for _ in range(args.warmup):
+        cpu_baseline(o, cam, params, rows)
+    rates, paths, secs = [], 0, 0.0
+    for _ in range(args.steps):
+        rate, n, dt, cores = cpu_baseline(o, cam, params, rows)
+        rates.append(rate)
+        paths += n
+        secs += dt
+    value = paths / secs
+    sample = "%d evenly spaced rows of 1024 (x 1024 px x 64 spp = %d paths) per step" % (rows, paths // args.steps)
+    line = {"impl": "reference", "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "scene_build_s": build_s},
+            "cpu_baseline": {"value": value, "unit": "paths/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-rows", type=int, default=64, help="rows in the CPU-baseline sample")
+    ap.add_argument("--reference-rows", type=int, default=32, help="rows per step of --impl reference")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-paths", type=int, default=0)
+    ap.add_argument("--profile", action="store_true",
+                    help="for ncu: one untimed frame, then one frame, nothing else")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank, dist)
+        return
+
+    import numpy as np
+    import torch
+
+    import renderer_gb300 as rg
+    from renderer_gb300 import _abi, workloads
+    from renderer_gb300.runtime import Context, GpuScene
+
+    torch.cuda.set_device(local)
+    s = workloads.icosphere_scene(levels=8, seed=0)
+    cam = s.camera_struct()
+    H, W = cam.height, cam.width
+    ctx = Context(local)
+    gs = GpuScene(ctx, s)
+    info = gs.info()
+    lib = rg.lib()
+
+    film = torch.empty(H * W * 3, dtype=torch.float32, device="cuda")
+    fsum = torch.empty(H * W * 3, dtype=torch.float64, device="cuda")
+    ptr = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+
+    def render_dev(flags, stats):
+        p = workloads.icosphere_params()
+        p.flags = flags
+        p.batch_paths = args.batch_paths
+        rg.check(lib.gbrt_render_device(gs.handle, C.byref(cam), C.byref(p), ptr(film), ptr(fsum), None,
+                                        C.byref(stats)), ctx.handle)
+
+    if args.profile:
+        for _ in range(2):
+            st = _abi.Stats()
+            render_dev(0, st)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_frames": 2, "paths": st.paths, "render_ms": st.render_ms,
+                          "launches_per_frame": st.kernel_launches}))
+        return
+
+    # Traversal work of this workload (untimed pass with counters).
+    cs = _abi.Stats()
+    render_dev(_abi.RENDER_COUNT_TRAVERSAL, cs)
+    n_node = cs.nodes_closest / max(cs.extension_rays, 1)
+    n_prim = cs.prims_closest / max(cs.extension_rays, 1)
+    bytes_per_ray = 32 + 16 + 64 * n_node + 48 * n_prim
+
+    for _ in range(args.warmup):
+        render_dev(0, _abi.Stats())
+    clocks = ClockSampler(local)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    tot = dict(ms=0.0, ext_ms=0.0, shade_ms=0.0, shadow_ms=0.0, ext_launch=0, ext_rays=0, sh_rays=0, paths=0,
+               launches=0)
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = _abi.Stats()
+        render_dev(_abi.RENDER_TIME_KERNELS, st)
+        tot["ms"] += st.render_ms
+        tot["ext_ms"] += st.extend_ms
+        tot["shade_ms"] += st.shade_ms
+        tot["shadow_ms"] += st.shadow_ms
+        tot["ext_launch"] += st.extend_launches
+        tot["ext_rays"] += st.extension_rays
+        tot["sh_rays"] += st.shadow_rays
+        tot["paths"] += st.paths
+        tot["launches"] += st.kernel_launches
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    barrier(dist)
+    clk = clocks.stop()
+    ms = max_over_ranks(tot["ms"], dist)
+    value = tot["paths"] * ws / (ms / 1000.0)
+
+    # End to end through the C ABI with host buffers (film back every frame).
+    hfilm = np.zeros((H, W, 3), np.float32)
+    p = workloads.icosphere_params()
+    p.batch_paths = args.batch_paths
+    e2e_s = 0.0
+    e2e_paths = 0
+    for i in range(args.warmup + args.steps):
+        st = _abi.Stats()
+        barrier(dist)
+        t0 = time.perf_counter()
+        rg.check(lib.gbrt_render(gs.handle, C.byref(cam), C.byref(p), hfilm.ctypes.data_as(C.c_void_p), None, None,
+                                 None, C.byref(st)), ctx.handle)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e_s += dt
+            e2e_paths += st.paths
+    e2e_s = max_over_ranks(e2e_s, dist)
+    e2e = e2e_paths * ws / e2e_s
+
+    peak, peak_kind = measured_peaks()
+    achieved = tot["ext_rays"] * bytes_per_ray / (tot["ext_ms"] / 1000.0) / 1e9
+    tpr = traffic_per_ray()
+    rays_per_launch = tot["ext_rays"] / max(tot["ext_launch"], 1)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": peak_kind,
+                "traffic": None if tpr is None else tpr * rays_per_launch,
+                "kernel": "k_extend (closest-hit BVH traversal)",
+                "bytes_per_ray": bytes_per_ray, "nodes_per_ray": n_node, "prims_per_ray": n_prim,
+                "launches": tot["ext_launch"], "avg_launch_ms": tot["ext_ms"] / max(tot["ext_launch"], 1),
+                "share_of_render": tot["ext_ms"] / max(tot["ms"], 1e-9)}
+
+    line = {"metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "paths_per_step": tot["paths"] // args.steps,
+                       "l2": "inputs larger than L2 (scene ~240 MB, path state ~1.2 GB per wavefront)",
+                       "scene_build_ms": info["build_ms"], "bvh_nodes": info["nodes"],
+                       "bvh_max_depth": info["max_depth"], "wall_s_timed": wall,
+                       "rays_per_s": (tot["ext_rays"] + tot["sh_rays"]) * ws / (ms / 1000.0),
+                       "kernel_ms_per_step": {"extend": tot["ext_ms"] / args.steps,
+                                              "shade": tot["shade_ms"] / args.steps,
+                                              "shadow": tot["shadow_ms"] / args.steps},
+                       "extension_rays_per_path": tot["ext_rays"] / max(tot["paths"], 1),
+                       "shadow_rays_per_path": tot["sh_rays"] / max(tot["paths"], 1)},
+            "roofline": roofline,
+            "e2e": {"value": e2e, "unit": "paths/s", "h2d_bytes_per_step": C.sizeof(_abi.Camera) +
+                    C.sizeof(_abi.RenderParams), "d2h_bytes_per_step": H * W * 3 * 4},
+            "gpu_launches": tot["launches"], "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        del gs
+        ctx.close()
+        rate, n, dt, cores = cpu_baseline(s, cam, workloads.icosphere_params(), args.cpu_rows)
+        line["cpu_baseline"] = {"value": rate, "unit": "paths/s", "cores": cores, "kind": "port",
+                                "sample": "%d evenly spaced rows (%d paths, %.1f s) of the same frame"
+                                % (args.cpu_rows, n, dt)}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -37,7 +37,7 @@ def lib():
         L.orc_trace_any.argtypes = [P, P, P, C.c_int64, P, C.c_int]
         L.orc_render.restype = C.c_int
         L.orc_render.argtypes = [P, C.POINTER(_abi.Camera), C.POINTER(_abi.RenderParams), C.c_int, C.c_int, C.c_int,
-                                 P, P, P, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                 C.c_int, P, P, P, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                  C.POINTER(C.c_uint64)]
         L.orc_camera_ray.argtypes = [C.POINTER(_abi.Camera), C.c_double, C.c_double, P]
         L.orc_stream_u.restype = C.c_float
@@ -74,16 +74,16 @@ class OracleScene:
         lib().orc_trace_any(self.handle, _ptr(rays), _ptr(ign), len(rays), _ptr(occ), threads)
         return occ.astype(bool)
 
-    def render(self, camera, params, rng_mode=0, rows=None, threads=0):
+    def render(self, camera, params, rng_mode=0, rows=None, threads=0, row_step=1):
         """Returns dict(film, sum, sumsq, paths, rays, shadow_rays) for rows
-        [r0, r1) (all rows by default)."""
+        r0, r0 + row_step, ... < r1 (all rows by default)."""
         H, W = camera.height, camera.width
         r0, r1 = rows if rows is not None else (0, H)
         film = np.zeros((H, W, 3), np.float32)
         s = np.zeros((H, W, 3), np.float64)
         q = np.zeros((H, W, 3), np.float64)
         paths, rays, sh = C.c_uint64(), C.c_uint64(), C.c_uint64()
-        rc = lib().orc_render(self.handle, C.byref(camera), C.byref(params), rng_mode, r0, r1, _ptr(film), _ptr(s),
+        rc = lib().orc_render(self.handle, C.byref(camera), C.byref(params), rng_mode, r0, r1, row_step, _ptr(film), _ptr(s),
                               _ptr(q), threads, C.byref(paths), C.byref(rays), C.byref(sh))
         if rc != 0:
             raise RuntimeError("orc_render failed")

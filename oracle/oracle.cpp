@@ -984,8 +984,8 @@ void orc_trace_any(void* sp, const gbrt_ray* rays, const int32_t* ignore, int64_
  * height * seed + row; rng_mode 1: the counter-based stream shared with the
  * CUDA path. Returns 0 on success. */
 int orc_render(void* sp, const gbrt_camera* cam, const gbrt_render_params* prm, int rng_mode, int row_begin,
-               int row_end, float* film, double* sum, double* sumsq, int threads, uint64_t* out_paths,
-               uint64_t* out_rays, uint64_t* out_shadow) {
+               int row_end, int row_step, float* film, double* sum, double* sumsq, int threads,
+               uint64_t* out_paths, uint64_t* out_rays, uint64_t* out_shadow) {
   Scene* s = static_cast<Scene*>(sp);
   if (!s || !cam || !prm) return 1;
   Camera camera;
@@ -998,12 +998,15 @@ int orc_render(void* sp, const gbrt_camera* cam, const gbrt_render_params* prm, 
   const int rrStart = 3;
   if (row_begin < 0) row_begin = 0;
   if (row_end > H || row_end < 0) row_end = H;
+  if (row_step < 1) row_step = 1;
+  const int nRows = row_end > row_begin ? (row_end - row_begin + row_step - 1) / row_step : 0;
   uint64_t totRays = 0, totShadow = 0, totPaths = 0;
 #ifdef _OPENMP
   if (threads > 0) omp_set_num_threads(threads);
 #pragma omp parallel for schedule(dynamic) reduction(+ : totRays, totShadow, totPaths)
 #endif
-  for (int i = row_begin; i < row_end; ++i) {
+  for (int ri = 0; ri < nRows; ++ri) {
+    const int i = row_begin + ri * row_step;
     std::unique_ptr<TausRng> rng;
     if (rng_mode == 0) rng.reset(new TausRng(uint64_t(H) * prm->seed + uint64_t(i)));
     Draws dr;

@@ -93,14 +93,22 @@ __device__ __forceinline__ TRay make_tray(float4 a, float4 b) {
   return r;
 }
 
-// Conservative slab test of one child box against [tmin, tcur].
+// Conservative slab test of one child box against [tmin, tcur]. As in
+// AxisAlignedBox::getCSGIntersection (src/axisalignedbox.cpp:41-66) the near
+// and far planes of each slab are chosen by the sign of 1/d, and a slab whose
+// distance is NaN (a zero direction component with the origin on that slab's
+// plane: 0 * inf) constrains nothing, because fmaxf / fminf ignore NaN.
 __device__ __forceinline__ bool box_hit(const TRay& r, float lox, float hix, float loy, float hiy, float loz,
                                         float hiz, float tcur, float& tnear) {
   float tx0 = (lox - r.ox) * r.ix, tx1 = (hix - r.ox) * r.ix;
   float ty0 = (loy - r.oy) * r.iy, ty1 = (hiy - r.oy) * r.iy;
   float tz0 = (loz - r.oz) * r.iz, tz1 = (hiz - r.oz) * r.iz;
-  float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), r.tmin));
-  float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1)) * 1.0000004f;
+  const bool px = r.ix >= 0.f, py = r.iy >= 0.f, pz = r.iz >= 0.f;
+  float nx = px ? tx0 : tx1, fx = px ? tx1 : tx0;
+  float ny = py ? ty0 : ty1, fy = py ? ty1 : ty0;
+  float nz = pz ? tz0 : tz1, fz = pz ? tz1 : tz0;
+  float tn = fmaxf(fmaxf(nx, ny), fmaxf(nz, r.tmin));
+  float tf = fminf(fminf(fx, fy), fz) * 1.0000004f;
   tf = fminf(tf, tcur);
   tnear = tn;
   return tn <= tf;
