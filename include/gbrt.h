@@ -277,6 +277,29 @@ gbrt_status gbrt_render_device(gbrt_scene* scene, const gbrt_camera* camera,
                                const gbrt_render_params* params,
                                float* d_film_bgr, double* d_sum,
                                double* d_sumsq, gbrt_stats* stats);
+/* No counterpart in the renderer. The same render as gbrt_render_device,
+ * for callers that cannot call cudaMalloc during a render: an application
+ * whose device memory is owned by its own pool or held to a fixed budget, or a
+ * frame loop that cannot take the device-wide synchronisation cudaMalloc and
+ * cudaFree may imply. It allocates nothing: the wavefront state lives in one
+ * fixed 20 MiB array in device memory (a batch of at most
+ * GBRT_NOALLOC_MAX_BATCH paths), which every GPU that loads this library
+ * holds until the process exits. The caller passes every buffer that scales
+ * with the image: d_film_bgr (float) and d_sum (double, required here) and
+ * the optional d_sumsq, each H x W x 3 on the device. params->batch_paths = 0
+ * means GBRT_NOALLOC_MAX_BATCH; a larger value is rejected with
+ * GBRT_ERR_INVALID_ARG. The first call on a device looks up the array's
+ * device address; make that first call before any stream capture. All calls
+ * in the process share the one array and leave their state in it (each call
+ * clears what must start at zero), so calls that overlap on the GPU race:
+ * issue them one at a time. GBRT_RENDER_TIME_KERNELS is ignored (stats get
+ * host-timed render_ms only). Synchronous. */
+#define GBRT_NOALLOC_MAX_BATCH 65536
+gbrt_status gbrt_render_device_noalloc(gbrt_scene* scene,
+                                       const gbrt_camera* camera,
+                                       const gbrt_render_params* params,
+                                       float* d_film_bgr, double* d_sum,
+                                       double* d_sumsq, gbrt_stats* stats);
 
 /* ---- scene files (SceneGrammar::parse + resolveVars + buildScene,
  *      src/sceneparser.cpp:36-156, src/sceneast.cpp:673-747,

@@ -94,6 +94,7 @@ SEM_REFERENCE, SEM_PHYSICAL = range(2)
 # gbrt_scene_flags / gbrt_render_flags
 SCENE_WATERTIGHT = 1
 RENDER_TIME_KERNELS, RENDER_COUNT_TRAVERSAL = 1, 2
+NOALLOC_MAX_BATCH = 65536
 
 P = C.c_void_p
 
@@ -115,6 +116,8 @@ SIGNATURES = [
                               C.POINTER(Stats)]),
     ("gbrt_render_device", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), P, P, P,
                                      C.POINTER(Stats)]),
+    ("gbrt_render_device_noalloc", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), P, P, P,
+                                             C.POINTER(Stats)]),
     ("gbrt_parse_scene_file", C.c_int, [C.c_char_p, C.POINTER(P), C.c_char_p, C.c_int32]),
     ("gbrt_parse_scene_string", C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(P), C.c_char_p, C.c_int32]),
     ("gbrt_parsed_scene_desc", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(Camera),

@@ -30,6 +30,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "gbrt_internal.h"
@@ -672,6 +673,197 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   return status;
 }
 
+// ------------------------------------------- render without allocation ----
+// gbrt_render_device_noalloc keeps its wavefront state in one file-scope
+// device array instead of allocating it. Its layout, per path of a batch of
+// at most kNoAllocBatch paths, mirrors PTState; every sub-array starts on a
+// 256-byte boundary.
+constexpr long long kNoAllocBatch = GBRT_NOALLOC_MAX_BATCH;
+
+struct NoAllocLayout {
+  size_t off[19];
+  size_t bytes;
+};
+
+constexpr size_t noalloc_align(size_t x) { return (x + 255) & ~size_t(255); }
+
+static NoAllocLayout noalloc_layout() {
+  const size_t B = size_t(kNoAllocBatch);
+  const size_t sizes[19] = {
+      B * sizeof(float4), B * sizeof(float4), B * sizeof(int4),                          // alpha, L, ctl
+      B * sizeof(float4), B * sizeof(float4), B * sizeof(float4), B * sizeof(float4),    // pending vertex
+      2 * B * sizeof(float4), 2 * B * sizeof(float4),                                    // ext[0], ext[1]
+      B * sizeof(int), B * sizeof(int),                                                  // ext_slot[0], [1]
+      B * sizeof(RawHit),                                                                // hits
+      4 * B * sizeof(float4), 2 * B * sizeof(float4), 2 * B * sizeof(int),               // shadow queue
+      4 * sizeof(int), 4 * sizeof(unsigned long long), 8 * sizeof(unsigned long long),   // counts, work, tally
+      sizeof(int)};                                                                      // err
+  NoAllocLayout L{};
+  size_t o = 0;
+  for (int i = 0; i < 19; ++i) {
+    L.off[i] = o;
+    o += noalloc_align(sizes[i]);
+  }
+  L.bytes = o;
+  return L;
+}
+
+// 65,536 paths x 304 bytes + counters, rounded up: 20 MiB.
+constexpr size_t kNoAllocScratchBytes = size_t(20) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch per device, looked up once per device
+// with that device current (the array's host-side name is not a device
+// address).
+static std::mutex g_noalloc_mu;
+static unsigned char* g_noalloc_ptr[64] = {nullptr};
+
+static gbrt_status noalloc_scratch(gbrt_ctx* ctx, unsigned char** out) {
+  if (ctx->device < 0 || ctx->device >= 64) return fail(ctx, GBRT_ERR_UNSUPPORTED, "device index beyond 63");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[ctx->device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_ptr[ctx->device] = static_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_ptr[ctx->device];
+  return GBRT_OK;
+}
+
+static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render_params* prm,
+                                       float* d_film, double* d_sum, double* d_sumsq, gbrt_stats* stats) {
+  gbrt_ctx* ctx = s->ctx;
+  if (!cam || !prm || !d_film || !d_sum)
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_device_noalloc: NULL camera, params, film or sum");
+  if (cam->width <= 0 || cam->height <= 0 || prm->x_samples <= 0 || prm->y_samples <= 0 || prm->max_depth <= 0 ||
+      prm->max_depth > 64)
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_device_noalloc: bad camera or render parameters");
+  if (prm->batch_paths < 0 || prm->batch_paths > kNoAllocBatch)
+    return fail(ctx, GBRT_ERR_INVALID_ARG,
+                "gbrt_render_device_noalloc: batch_paths exceeds the 65536-path (GBRT_NOALLOC_MAX_BATCH) "
+                "scratch of the no-allocation entry point");
+  if (prm->semantics != GBRT_SEM_REFERENCE)
+    return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_render_device_noalloc: only the reference semantics are implemented");
+  if (!(prm->termination_prob >= 0.f && prm->termination_prob <= 1.f))
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_device_noalloc: termination probability outside [0, 1]");
+  const NoAllocLayout Lay = noalloc_layout();
+  if (Lay.bytes > kNoAllocScratchBytes)
+    return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_render_device_noalloc: scratch layout exceeds the array");
+  GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  unsigned char* base = nullptr;
+  gbrt_status gs = noalloc_scratch(ctx, &base);
+  if (gs != GBRT_OK) return gs;
+  cudaStream_t stream = ctx->stream;
+  auto at = [&](int i) { return static_cast<void*>(base + Lay.off[i]); };
+  PTState st;
+  st.alpha = static_cast<float4*>(at(0));
+  st.L = static_cast<float4*>(at(1));
+  st.ctl = static_cast<int4*>(at(2));
+  st.pv_p = static_cast<float4*>(at(3));
+  st.pv_n = static_cast<float4*>(at(4));
+  st.pv_d = static_cast<float4*>(at(5));
+  st.pv_a = static_cast<float4*>(at(6));
+  st.ext[0] = static_cast<float4*>(at(7));
+  st.ext[1] = static_cast<float4*>(at(8));
+  st.ext_slot[0] = static_cast<int*>(at(9));
+  st.ext_slot[1] = static_cast<int*>(at(10));
+  st.hits = static_cast<RawHit*>(at(11));
+  st.sh_ray = static_cast<float4*>(at(12));
+  st.sh_c = static_cast<float4*>(at(13));
+  st.sh_slot = static_cast<int*>(at(14));
+  st.counts = static_cast<int*>(at(15));
+  st.work = static_cast<unsigned long long*>(at(16));
+  st.tally = static_cast<unsigned long long*>(at(17));
+  st.err = static_cast<int*>(at(18));
+
+  const unsigned long long npix = (unsigned long long)cam->width * cam->height;
+  const int spp = prm->x_samples * prm->y_samples;
+  const unsigned long long total = npix * (unsigned long long)spp;
+  long long B = prm->batch_paths > 0 ? prm->batch_paths : kNoAllocBatch;
+  B = std::max<long long>(1, std::min<long long>(B, (long long)total));
+  PTParams P;
+  P.cam = make_camera(*cam);
+  P.seed = prm->seed;
+  P.xs = prm->x_samples;
+  P.ys = prm->y_samples;
+  P.spp = spp;
+  P.D = prm->max_depth;
+  P.term_p = prm->termination_prob;
+  P.rr_pdf = prm->termination_prob > 0.f ? prm->termination_prob : 1.f;
+
+  // The array keeps the previous call's contents: clear what starts at zero.
+  cudaError_t e = cudaSuccess;
+  auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
+  A(cudaMemsetAsync(st.tally, 0, 8 * sizeof(unsigned long long), stream));
+  A(cudaMemsetAsync(st.err, 0, sizeof(int), stream));
+  A(cudaMemsetAsync(d_sum, 0, npix * 3 * sizeof(double), stream));
+  if (d_sumsq) A(cudaMemsetAsync(d_sumsq, 0, npix * 3 * sizeof(double), stream));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gbrt_render_device_noalloc set-up");
+
+  const bool count = (prm->flags & GBRT_RENDER_COUNT_TRAVERSAL) != 0;
+  const bool wt = s->watertight;
+  auto kExt = count ? (wt ? k_extend<true, true> : k_extend<true, false>)
+                    : (wt ? k_extend<false, true> : k_extend<false, false>);
+  auto kSh = count ? (wt ? k_shadow<true, true> : k_shadow<true, false>)
+                   : (wt ? k_shadow<false, true> : k_shadow<false, false>);
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kExt, kTraceBlock, 0);
+  const int traceGrid = std::max(1, per) * ctx->num_sms;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kSh, kTraceBlock, 0);
+  const int shadowGrid = std::max(1, per) * ctx->num_sms;
+  const int shadeGrid = ctx->num_sms * 8;
+  auto t0 = std::chrono::steady_clock::now();
+  unsigned long long launches = 0;
+  for (unsigned long long g0 = 0; g0 < total; g0 += (unsigned long long)B) {
+    P.g0 = g0;
+    P.nb = int(std::min<unsigned long long>((unsigned long long)B, total - g0));
+    k_raygen<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
+    ++launches;
+    for (int it = 0; it < P.D; ++it) {
+      int cur = it & 1, nxt = cur ^ 1;
+      A(cudaMemsetAsync(st.counts + nxt, 0, sizeof(int), stream));
+      A(cudaMemsetAsync(st.counts + 2, 0, sizeof(int), stream));
+      A(cudaMemsetAsync(st.work, 0, 4 * sizeof(unsigned long long), stream));
+      kExt<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
+      k_shade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
+      kSh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
+      launches += 3;
+    }
+    unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
+    k_accumulate<<<unsigned((p1 - p0 + 1 + 255) / 256), 256, 0, stream>>>(P, st, d_sum, d_sumsq);
+    ++launches;
+    A(cudaGetLastError());
+    if (e != cudaSuccess) break;
+  }
+  size_t n3 = size_t(npix) * 3;
+  k_finalize<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_sum, d_film, n3, 1.0 / spp);
+  ++launches;
+  A(cudaGetLastError());
+  unsigned long long tally[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int err = 0;
+  A(cudaMemcpyAsync(tally, st.tally, sizeof tally, cudaMemcpyDeviceToHost, stream));
+  A(cudaMemcpyAsync(&err, st.err, sizeof err, cudaMemcpyDeviceToHost, stream));
+  A(cudaStreamSynchronize(stream));
+  double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gbrt_render_device_noalloc");
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    stats->paths = total;
+    stats->extension_rays = tally[0];
+    stats->shadow_rays = tally[1];
+    stats->nonfinite = tally[2];
+    stats->render_ms = ms;
+    stats->kernel_launches = launches;
+    stats->nodes_closest = tally[3];
+    stats->prims_closest = tally[4];
+    stats->nodes_any = tally[5];
+    stats->prims_any = tally[6];
+  }
+  if (err) return fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render_device_noalloc: traversal stack overflow");
+  return GBRT_OK;
+}
+
 }  // namespace gbrt
 
 using namespace gbrt;
@@ -712,6 +904,13 @@ gbrt_status gbrt_render(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render
   e = cudaStreamSynchronize(ctx->stream);
   if (st == GBRT_OK && e != cudaSuccess) st = cuda_fail(ctx, e, "gbrt_render copy-out");
   return st;
+}
+
+gbrt_status gbrt_render_device_noalloc(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render_params* prm,
+                                       float* d_film, double* d_sum, double* d_sumsq, gbrt_stats* stats) {
+  if (!s) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_render_device_noalloc: NULL scene");
+  clear_error(s->ctx);
+  return render_noalloc_impl(s, cam, prm, d_film, d_sum, d_sumsq, stats);
 }
 
 }  // extern "C"
