@@ -51,10 +51,12 @@ struct PTParams {
   unsigned long long seed;
   unsigned long long g0;   // first path index of the batch
   int nb;                  // paths in the batch
+  int idx32;               // every path index of the frame fits in 32 bits
   int xs, ys, spp;
   int D;                   // maximum path length
   float rr_pdf;            // Russian-roulette compensation pdf
   float term_p;            // termination probability
+  float inv_log1mp;        // 1 / log(1 - term_p), for the geometric draw
 };
 
 // Path state, structure of arrays indexed by slot (path index - g0).
@@ -93,11 +95,21 @@ __device__ __forceinline__ int warp_push(int* counter, bool pred) {
 // ------------------------------------------------------------- raygen ----
 __global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
   int slot = blockIdx.x * blockDim.x + threadIdx.x;
-  if (slot == 0) st.counts[0] = P.nb;
+  if (slot == 0) {
+    st.counts[0] = P.nb;
+    st.work[0] = 0;  // work counter of the first extend
+  }
   if (slot >= P.nb) return;
   unsigned long long g = P.g0 + (unsigned long long)slot;
-  int pixel = int(g / unsigned(P.spp));
-  int s = int(g % unsigned(P.spp));
+  int pixel, s;
+  if (P.idx32) {
+    unsigned g32 = unsigned(g);
+    pixel = int(g32 / unsigned(P.spp));
+    s = int(g32 - unsigned(pixel) * unsigned(P.spp));
+  } else {
+    pixel = int(g / unsigned(P.spp));
+    s = int(g % unsigned(P.spp));
+  }
   int px = pixel % P.cam.W, py = pixel / P.cam.W;
   int a = s / P.ys, b = s % P.ys;  // JitteredSampler strata: x outer, y inner
   unsigned long long key = stream_key(P.seed, g);
@@ -114,10 +126,16 @@ __global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
   if (P.term_p > 0.f) {
     int k = 0;
     if (P.term_p < 1.f) {
-      // Geometric draw by inversion, in double like the CPU oracle.
-      double ul = double(stream_u(key, 2));
-      k = int(floor(log(1.0 - ul) / log(1.0 - double(P.term_p))));
-      k = max(k, 0);
+      // Geometric draw by inversion, floor(log(1 - u) / log(1 - p)). 1 - u is
+      // exact in float (u has 24 bits), so the float quotient differs from the
+      // double one the CPU oracle uses by a few ulp; only when it falls that
+      // close to an integer is it recomputed in double.
+      float ul = stream_u(key, 2);
+      float x = logf(1.f - ul) * P.inv_log1mp;
+      float fx = floorf(x);
+      if (x - fx < 1e-5f * fmaxf(1.f, x) || fx + 1.f - x < 1e-5f * fmaxf(1.f, x))
+        fx = float(floor(log(1.0 - double(ul)) / log(1.0 - double(P.term_p))));
+      k = max(int(fx), 0);
     }
     plen = min(3 + k, P.D);
   }
@@ -143,12 +161,22 @@ __device__ __forceinline__ void warp_add_counters(TraceCounters c, unsigned long
 }
 
 // ------------------------------------------------------------- extend ----
-template <bool COUNT, bool WT>
+// Queue protocol (no host-side resets inside a batch): k_raygen sets
+// counts[0] and zeroes work[0]; k_extend on queue cur zeroes, before shade and
+// shadow run, counts[cur^1] (next extension queue), counts[2] (shadow queue),
+// work[cur^1] (next extend) and work[2] (this iteration's shadow pass).
+template <bool COUNT, bool WT, int STACK>
 __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState st, int cur) {
-  __shared__ int s_stack[kStackSize * kTraceBlock];
+  __shared__ int s_stack[STACK * kTraceBlock];
   int* stack = s_stack + threadIdx.x;
   const int n = st.counts[cur];
-  if (blockIdx.x == 0 && threadIdx.x == 0) st.tally[0] += (unsigned long long)n;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st.tally[0] += (unsigned long long)n;
+    st.counts[cur ^ 1] = 0;
+    st.counts[2] = 0;
+    st.work[cur ^ 1] = 0;
+    st.work[2] = 0;
+  }
   const float4* rays = st.ext[cur];
   unsigned long long* work = st.work + cur;
   const int lane = threadIdx.x & 31;
@@ -162,16 +190,16 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState s
     if (i >= n) continue;
     TRay r = make_tray(rays[2 * i], rays[2 * i + 1]);
     RawHit h;
-    h.rec = trace_ray<false, COUNT, WT>(S, r, -1, stack, h.t, h.u, h.v, st.err, &cnt);
+    h.rec = trace_ray<false, COUNT, WT, STACK>(S, r, -1, stack, h.t, h.u, h.v, st.err, &cnt);
     st.hits[i] = h;
   }
   if (COUNT) warp_add_counters(cnt, &st.tally[3], &st.tally[4]);
 }
 
 // ------------------------------------------------------------- shadow ----
-template <bool COUNT, bool WT>
+template <bool COUNT, bool WT, int STACK>
 __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState st) {
-  __shared__ int s_stack[kStackSize * kTraceBlock];
+  __shared__ int s_stack[STACK * kTraceBlock];
   int* stack = s_stack + threadIdx.x;
   const int n = st.counts[2];
   if (blockIdx.x == 0 && threadIdx.x == 0) st.tally[1] += (unsigned long long)n;
@@ -188,7 +216,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState s
     float4 c = st.sh_c[i];
     TRay r = make_tray(st.sh_ray[2 * i], st.sh_ray[2 * i + 1]);
     float t, u, v;
-    int32_t rec = trace_ray<true, COUNT, WT>(S, r, __float_as_int(c.w), stack, t, u, v, st.err, &cnt);
+    int32_t rec = trace_ray<true, COUNT, WT, STACK>(S, r, __float_as_int(c.w), stack, t, u, v, st.err, &cnt);
     if (rec == -1) {
       float4* L = st.L + st.sh_slot[i];
       atomicAdd(&L->x, c.x);
@@ -212,8 +240,8 @@ __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, uns
   out.valid = false;
   if (S.n_lights <= 0 || vx.mat < 0) return;
   unsigned dl = dim_light(P.D, k);
-  float lx = stream_u(key, dl), ly = stream_u(key, dl + 1), lu = stream_u(key, dl + 2);
-  int li = min(int(double(lu) * double(S.n_lights)), S.n_lights - 1);  // exact floor(u * n)
+  float lx = stream_u(key, dl), ly = stream_u(key, dl + 1);
+  int li = min(stream_index(key, dl + 2, S.n_lights), S.n_lights - 1);  // floor(u * n)
   const DevLight& Lt = S.lights[li];
   V3f dir, Le;
   V3f so, sd;
@@ -505,6 +533,38 @@ static CamDev make_camera(const gbrt_camera& c) {
   return d;
 }
 
+// The extend / shadow kernels for a scene and flags: traversal counters,
+// watertight triangles, short stack when the tree is shallow enough.
+struct TraceKernels {
+  void (*ext)(DeviceScene, PTState, int);
+  void (*sh)(DeviceScene, PTState);
+};
+template <bool C, bool W>
+static TraceKernels pick_stack(bool shortStack) {
+  if (shortStack) return {k_extend<C, W, kShortStack>, k_shadow<C, W, kShortStack>};
+  return {k_extend<C, W, kStackSize>, k_shadow<C, W, kStackSize>};
+}
+static TraceKernels pick_kernels(const gbrt_scene* s, bool count) {
+  const bool shortStack = s->max_depth <= kShortStack - 2;
+  if (count) return s->watertight ? pick_stack<true, true>(shortStack) : pick_stack<true, false>(shortStack);
+  return s->watertight ? pick_stack<false, true>(shortStack) : pick_stack<false, false>(shortStack);
+}
+
+static void init_params(PTParams& P, const gbrt_camera& cam, const gbrt_render_params& prm, unsigned long long total) {
+  P.cam = make_camera(cam);
+  P.seed = prm.seed;
+  P.xs = prm.x_samples;
+  P.ys = prm.y_samples;
+  P.spp = prm.x_samples * prm.y_samples;
+  P.D = prm.max_depth;
+  P.term_p = prm.termination_prob;
+  P.rr_pdf = prm.termination_prob > 0.f ? prm.termination_prob : 1.f;
+  P.inv_log1mp = (prm.termination_prob > 0.f && prm.termination_prob < 1.f)
+                     ? float(1.0 / std::log(1.0 - double(prm.termination_prob)))
+                     : 0.f;
+  P.idx32 = total <= 0xffffffffull ? 1 : 0;
+}
+
 struct Buffers {
   std::vector<void*> ptrs;
   cudaStream_t stream;
@@ -538,19 +598,12 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   const unsigned long long npix = (unsigned long long)cam->width * cam->height;
   const int spp = prm->x_samples * prm->y_samples;
   const unsigned long long total = npix * (unsigned long long)spp;
-  long long B = prm->batch_paths > 0 ? prm->batch_paths : (1ll << 22);
+  long long B = prm->batch_paths > 0 ? prm->batch_paths : (1ll << 23);
   B = std::min<long long>(B, (long long)total);
   B = std::max<long long>(B, 1);
 
   PTParams P;
-  P.cam = make_camera(*cam);
-  P.seed = prm->seed;
-  P.xs = prm->x_samples;
-  P.ys = prm->y_samples;
-  P.spp = spp;
-  P.D = prm->max_depth;
-  P.term_p = prm->termination_prob;
-  P.rr_pdf = prm->termination_prob > 0.f ? prm->termination_prob : 1.f;
+  init_params(P, *cam, *prm, total);
 
   Buffers buf(stream);
   PTState st;
@@ -574,11 +627,9 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
 
   const bool count = (prm->flags & GBRT_RENDER_COUNT_TRAVERSAL) != 0;
   const bool timeK = (prm->flags & GBRT_RENDER_TIME_KERNELS) != 0;
-  const bool wt = s->watertight;
-  auto kExt = count ? (wt ? k_extend<true, true> : k_extend<true, false>)
-                    : (wt ? k_extend<false, true> : k_extend<false, false>);
-  auto kSh = count ? (wt ? k_shadow<true, true> : k_shadow<true, false>)
-                   : (wt ? k_shadow<false, true> : k_shadow<false, false>);
+  const TraceKernels tk = pick_kernels(s, count);
+  auto kExt = tk.ext;
+  auto kSh = tk.sh;
   // Persistent grids: every SM filled with as many blocks as fit.
   int per = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kExt, kTraceBlock, 0);
@@ -607,10 +658,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
     k_raygen<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
     ++launches;
     for (int it = 0; it < P.D; ++it) {
-      int cur = it & 1, nxt = cur ^ 1;
-      A(cudaMemsetAsync(st.counts + nxt, 0, sizeof(int), stream));
-      A(cudaMemsetAsync(st.counts + 2, 0, sizeof(int), stream));
-      A(cudaMemsetAsync(st.work, 0, 4 * sizeof(unsigned long long), stream));
+      int cur = it & 1;
       if (timeK) mark();
       kExt<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
       if (timeK) mark();
@@ -783,14 +831,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
   long long B = prm->batch_paths > 0 ? prm->batch_paths : kNoAllocBatch;
   B = std::max<long long>(1, std::min<long long>(B, (long long)total));
   PTParams P;
-  P.cam = make_camera(*cam);
-  P.seed = prm->seed;
-  P.xs = prm->x_samples;
-  P.ys = prm->y_samples;
-  P.spp = spp;
-  P.D = prm->max_depth;
-  P.term_p = prm->termination_prob;
-  P.rr_pdf = prm->termination_prob > 0.f ? prm->termination_prob : 1.f;
+  init_params(P, *cam, *prm, total);
 
   // The array keeps the previous call's contents: clear what starts at zero.
   cudaError_t e = cudaSuccess;
@@ -801,12 +842,9 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
   if (d_sumsq) A(cudaMemsetAsync(d_sumsq, 0, npix * 3 * sizeof(double), stream));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "gbrt_render_device_noalloc set-up");
 
-  const bool count = (prm->flags & GBRT_RENDER_COUNT_TRAVERSAL) != 0;
-  const bool wt = s->watertight;
-  auto kExt = count ? (wt ? k_extend<true, true> : k_extend<true, false>)
-                    : (wt ? k_extend<false, true> : k_extend<false, false>);
-  auto kSh = count ? (wt ? k_shadow<true, true> : k_shadow<true, false>)
-                   : (wt ? k_shadow<false, true> : k_shadow<false, false>);
+  const TraceKernels tk = pick_kernels(s, (prm->flags & GBRT_RENDER_COUNT_TRAVERSAL) != 0);
+  auto kExt = tk.ext;
+  auto kSh = tk.sh;
   int per = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kExt, kTraceBlock, 0);
   const int traceGrid = std::max(1, per) * ctx->num_sms;
@@ -821,10 +859,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
     k_raygen<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
     ++launches;
     for (int it = 0; it < P.D; ++it) {
-      int cur = it & 1, nxt = cur ^ 1;
-      A(cudaMemsetAsync(st.counts + nxt, 0, sizeof(int), stream));
-      A(cudaMemsetAsync(st.counts + 2, 0, sizeof(int), stream));
-      A(cudaMemsetAsync(st.work, 0, 4 * sizeof(unsigned long long), stream));
+      int cur = it & 1;
       kExt<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
       k_shade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
       kSh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);

@@ -61,9 +61,16 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
 __device__ __forceinline__ unsigned long long stream_key(unsigned long long seed, unsigned long long sample_id) {
   return mix64(seed ^ mix64(sample_id + 0x632BE59BD9B4E019ull));
 }
+// The top 24 bits of the d-th draw; stream_u is this value / 2^24.
+__device__ __forceinline__ unsigned stream_bits(unsigned long long key, unsigned dim) {
+  return unsigned(mix64(key + (unsigned long long)dim * 0x9E3779B97F4A7C15ull) >> 40);
+}
 __device__ __forceinline__ float stream_u(unsigned long long key, unsigned dim) {
-  unsigned long long h = mix64(key + (unsigned long long)dim * 0x9E3779B97F4A7C15ull);
-  return float(h >> 40) * (1.0f / 16777216.0f);
+  return float(stream_bits(key, dim)) * (1.0f / 16777216.0f);
+}
+// floor(u * n) for u = bits / 2^24, exactly, in integer arithmetic.
+__device__ __forceinline__ int stream_index(unsigned long long key, unsigned dim, int n) {
+  return int((unsigned long long)stream_bits(key, dim) * unsigned(n) >> 24);
 }
 // Dimension layout per camera sample (D = max depth):
 //   0,1 jitter | 2 path length | 3+2i, 4+2i path sample i |

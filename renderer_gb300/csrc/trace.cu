@@ -16,11 +16,11 @@
 
 namespace gbrt {
 
-template <bool ANY, bool WT>
+template <bool ANY, bool WT, int STACK>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_api(DeviceScene S, const float4* __restrict__ rays, int64_t n, const int32_t* __restrict__ ignore,
                 gbrt_hit* __restrict__ hits, uint8_t* __restrict__ occluded, unsigned long long* work, int* err) {
-  __shared__ int s_stack[kStackSize * kTraceBlock];
+  __shared__ int s_stack[STACK * kTraceBlock];
   int* stack = s_stack + threadIdx.x;
   const int lane = threadIdx.x & 31;
   for (;;) {
@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(kTraceBlock)
     TRay r = make_tray(a, b);
     float t, u, v;
     int ign = (ANY && ignore) ? ignore[i] : -1;
-    int32_t rec = trace_ray<ANY, false, WT>(S, r, ign, stack, t, u, v, err, nullptr);
+    int32_t rec = trace_ray<ANY, false, WT, STACK>(S, r, ign, stack, t, u, v, err, nullptr);
     if (ANY) {
       occluded[i] = rec != -1 ? 1 : 0;
     } else {
@@ -63,17 +63,19 @@ static gbrt_status launch_api(gbrt_scene* s, bool any, const gbrt_ray* d_rays, c
   gbrt_ctx* ctx = s->ctx;
   GBRT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long), st));
   const float4* rays = reinterpret_cast<const float4*>(d_rays);
-  // One grid size serves every instantiation (same block size and shared
-  // memory; registers checked by -Xptxas -v).
-  static int grid = 0;
-  if (!grid) grid = trace_grid(ctx, (const void*)k_trace_api<false, false>);
+  // The short shared-memory stack when the tree is shallow enough for it.
+  const bool shortStack = s->max_depth <= kShortStack - 2;
+  decltype(&k_trace_api<false, false, kStackSize>) k;
   if (any) {
-    auto k = s->watertight ? k_trace_api<true, true> : k_trace_api<true, false>;
-    k<<<grid, kTraceBlock, 0, st>>>(s->view, rays, n, d_ignore, nullptr, d_occ, ctx->d_work, ctx->d_err);
+    if (shortStack) k = s->watertight ? k_trace_api<true, true, kShortStack> : k_trace_api<true, false, kShortStack>;
+    else k = s->watertight ? k_trace_api<true, true, kStackSize> : k_trace_api<true, false, kStackSize>;
   } else {
-    auto k = s->watertight ? k_trace_api<false, true> : k_trace_api<false, false>;
-    k<<<grid, kTraceBlock, 0, st>>>(s->view, rays, n, nullptr, d_hits, nullptr, ctx->d_work, ctx->d_err);
+    if (shortStack) k = s->watertight ? k_trace_api<false, true, kShortStack> : k_trace_api<false, false, kShortStack>;
+    else k = s->watertight ? k_trace_api<false, true, kStackSize> : k_trace_api<false, false, kStackSize>;
   }
+  const int grid = trace_grid(ctx, (const void*)k);
+  k<<<grid, kTraceBlock, 0, st>>>(s->view, rays, n, any ? d_ignore : nullptr, any ? nullptr : d_hits,
+                                  any ? d_occ : nullptr, ctx->d_work, ctx->d_err);
   GBRT_CUDA_TRY(ctx, cudaGetLastError());
   return GBRT_OK;
 }

@@ -42,6 +42,7 @@
 namespace gbrt {
 
 constexpr int kStackSize = 64;   // the builder keeps tree depth <= kStackSize - 2
+constexpr int kShortStack = 32;  // enough when the tree depth is <= kShortStack - 2
 constexpr int kTraceBlock = 128;
 
 // Exactly rounded, never-contracted float operations.
@@ -249,7 +250,8 @@ struct TraceCounters {
 // Traverses the scene. ANY: stop at the first accepted hit and skip records
 // (and planes) whose prim id equals ignore_prim. WT: watertight triangle test.
 // Returns the internal hit encoding (RawHit::rec) and fills t/u/v. stack is
-// this thread's column of the block's shared stack (stride kTraceBlock).
+// this thread's column of the block's shared stack (stride kTraceBlock) of
+// STACK entries.
 //
 // Acceptance: the first hit may lie anywhere in [tmin, tmax] (Ray::inRange is
 // inclusive); later hits must be strictly closer. One exception keeps
@@ -257,7 +259,7 @@ struct TraceCounters {
 // quad wins over the second whenever it is hit: the first half replaces a
 // current best that is the same quad's second half even at a larger t, and the
 // second half never replaces the first.
-template <bool ANY, bool COUNT, bool WT>
+template <bool ANY, bool COUNT, bool WT, int STACK>
 __device__ __forceinline__ int32_t trace_ray(const DeviceScene& S, const TRay& r, int ignore_prim, int* stack,
                                              float& t_best, float& u_best, float& v_best, int* err,
                                              TraceCounters* cnt) {
@@ -292,7 +294,7 @@ __device__ __forceinline__ int32_t trace_ray(const DeviceScene& S, const TRay& r
         if (h0 && h1) {
           int32_t nearRef = n3.x, farRef = n3.y;
           if (tn1 < tn0) { nearRef = n3.y; farRef = n3.x; }
-          if (sp + 1 >= kStackSize) { *err = 1; break; }
+          if (sp + 1 >= STACK) { *err = 1; break; }
           stack[(++sp) * kTraceBlock] = farRef;
           node = nearRef;
         } else if (h0) {
