@@ -24,6 +24,7 @@
 //               shadow  (any hit; unoccluded contributions added to the path)
 //   accumulate  per-pixel FP64 sum and sum of squares
 // Queue sizes live in device memory, so launch grids never depend on them.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,6 +39,8 @@
 #include "traverse.cuh"
 
 namespace gbrt {
+
+namespace cg = cooperative_groups;
 
 struct CamDev {
   float eye[3];
@@ -79,18 +82,6 @@ struct PTState {
   unsigned long long* tally;  // [0] extension rays, [1] shadow rays, [2] non-finite samples
   int* err;
 };
-
-// Warp-aggregated queue push: all 32 lanes must call it together.
-__device__ __forceinline__ int warp_push(int* counter, bool pred) {
-  const unsigned m = __ballot_sync(0xffffffffu, pred);
-  const int lane = threadIdx.x & 31;
-  int base = 0;
-  if (m) {
-    if (lane == __ffs(m) - 1) base = atomicAdd(counter, __popc(m));
-    base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
-  }
-  return base + __popc(m & ((1u << lane) - 1u));
-}
 
 // ------------------------------------------------------------- raygen ----
 __global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
@@ -228,30 +219,50 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState s
 }
 
 // -------------------------------------------------------------- shade ----
-struct ShadowOut {
-  bool valid;
-  float4 o, d, c;
-};
+// Queue push aggregated over the threads of a warp that reach it together
+// (one atomic per converged group), so a push can sit inside divergent code
+// and its payload need not stay live until a common exit point.
+__device__ __forceinline__ int agg_push(int* counter) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(counter, int(g.size()));
+  return g.shfl(base, 0) + int(g.thread_rank());
+}
+
+__device__ __forceinline__ void push_ext(const PTState& st, int nxt, int slot, V3f p, V3f d) {
+  int e = agg_push(&st.counts[nxt]);
+  st.ext[nxt][2 * e] = make_float4(p.x, p.y, p.z, kEps);
+  st.ext[nxt][2 * e + 1] = make_float4(d.x, d.y, d.z, CUDART_INF_F);
+  st.ext_slot[nxt][e] = slot;
+}
+
+__device__ __forceinline__ void load_pending(const PTState& st, int slot, Vertex& pv, V3f& pa, int& k) {
+  float4 pp = st.pv_p[slot], pn = st.pv_n[slot], pd = st.pv_d[slot], a = st.pv_a[slot];
+  pv.p = v3(pp.x, pp.y, pp.z);
+  pv.n = v3(pn.x, pn.y, pn.z);
+  pv.d = v3(pd.x, pd.y, pd.z);
+  pv.mat = __float_as_int(pp.w);
+  pa = v3(a.x, a.y, a.z);
+  k = __float_as_int(pn.w);
+}
 
 // Next-event estimation at a stored vertex: UniDiPathTracingIntegrator lines
-// 83-99 with Light::getIntensity for light lightIndex[k].
-__device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, unsigned long long key, const Vertex& vx,
-                                    V3f alpha, int k, ShadowOut& out) {
-  out.valid = false;
+// 83-99 with Light::getIntensity for light lightIndex[k]. A non-zero
+// contribution goes to the shadow queue with its shadow ray.
+__device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, const PTState& st, int slot,
+                                    unsigned long long key, const Vertex& vx, V3f alpha, int k) {
   if (S.n_lights <= 0 || vx.mat < 0) return;
   unsigned dl = dim_light(P.D, k);
   float lx = stream_u(key, dl), ly = stream_u(key, dl + 1);
   int li = min(stream_index(key, dl + 2, S.n_lights), S.n_lights - 1);  // floor(u * n)
   const DevLight& Lt = S.lights[li];
-  V3f dir, Le;
-  V3f so, sd;
+  V3f dir, Le, sd;
   float stmax;
   int ignore = -1;
   if (Lt.type == GBRT_LIGHT_AREA) {
     V3f lp = ld3(Lt.origin) + lx * ld3(Lt.u) + ly * ld3(Lt.v);
     dir = vx.p - lp;
     Le = area_intensity(Lt, dir);
-    so = vx.p;
     sd = -normalize(dir);
     stmax = len(dir) - kEps;
     ignore = Lt.prim;
@@ -259,7 +270,6 @@ __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, uns
     dir = vx.p - ld3(Lt.origin);
     float inv = 1.f / len2(dir);
     Le = v3(Lt.intensity[0] * inv, Lt.intensity[1] * inv, Lt.intensity[2] * inv);
-    so = vx.p;
     sd = -normalize(dir);
     stmax = len(dir) - kEps;
   } else if (Lt.type == GBRT_LIGHT_ENV && S.env_light >= 0) {
@@ -270,7 +280,6 @@ __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, uns
     float ip = 1.f / pdf;
     Le = v3(e.x * ip, e.y * ip, e.z * ip);
     // Ray(at, -s, -inf, -EPSILON) of the renderer == Ray(at, s, EPSILON, inf).
-    so = vx.p;
     sd = s;
     stmax = CUDART_INF_F;
   } else {
@@ -284,189 +293,157 @@ __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, uns
   float ac = fabsf(inCos);
   V3f c = v3(alpha.x * f.x * Le.x * ac, alpha.y * f.y * Le.y * ac, alpha.z * f.z * Le.z * ac);
   if (is_zero(c)) return;
-  out.valid = true;
-  out.o = make_float4(so.x, so.y, so.z, kEps);
-  out.d = make_float4(sd.x, sd.y, sd.z, stmax);
-  out.c = make_float4(c.x, c.y, c.z, __int_as_float(ignore));
+  int e = agg_push(&st.counts[2]);
+  st.sh_ray[2 * e] = make_float4(vx.p.x, vx.p.y, vx.p.z, kEps);
+  st.sh_ray[2 * e + 1] = make_float4(sd.x, sd.y, sd.z, stmax);
+  st.sh_c[e] = make_float4(c.x, c.y, c.z, __int_as_float(ignore));
+  st.sh_slot[e] = slot;
 }
 
-__global__ void __launch_bounds__(256) k_shade(DeviceScene S, PTParams P, PTState st, int cur) {
+// Shading of the hit at the head of one path: the body of the loop of
+// Renderer::createPath (src/renderer.cpp:73-104) for one iteration, with the
+// stored-vertex bookkeeping of UniDiPathTracingIntegrator::integrate(path)
+// done in streaming form (see the file comment).
+__global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTState st, int cur) {
   const int n = st.counts[cur];
   const int nxt = cur ^ 1;
-  const int stride = gridDim.x * blockDim.x;
-  const int nround = (n + 31) & ~31;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
-    bool active = q < n;
-    bool wantExt = false;
-    float4 eo = make_float4(0, 0, 0, 0), ed = make_float4(0, 0, 0, 0);
-    ShadowOut s1, s2;
-    s1.valid = s2.valid = false;
-    int slot = 0;
-    if (active) {
-      slot = st.ext_slot[cur][q];
-      RawHit h = st.hits[q];
-      float4 ro = st.ext[cur][2 * q], rd = st.ext[cur][2 * q + 1];
-      int4 c = st.ctl[slot];
-      int i = c.x, plen = c.y, nst = c.z;
-      bool pend = c.w != 0;
-      unsigned long long key = stream_key(P.seed, P.g0 + (unsigned long long)slot);
-      V3f o = v3(ro.x, ro.y, ro.z), d = v3(rd.x, rd.y, rd.z);
-      V3f alpha = v3(st.alpha[slot].x, st.alpha[slot].y, st.alpha[slot].z);
-      bool envHit = h.rec == -1 && S.env_light >= 0 && isinf(rd.w) && rd.w > 0.f;
-      bool done = false;
-      Vertex vx;
-      vx.d = d;
-      vx.mat = -1;
-      int light = -1;  // area light hit
-      if (h.rec == -1 && !envHit) {
-        done = true;  // the path leaves the scene
-      } else if (envHit) {
-        light = S.env_light;
-        vx.p = normalize(d);  // point at infinity (w = 0)
-        vx.n = -vx.p;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int slot = st.ext_slot[cur][q];
+    const RawHit h = st.hits[q];
+    const float4 ro = st.ext[cur][2 * q], rd = st.ext[cur][2 * q + 1];
+    int4 c = st.ctl[slot];
+    int i = c.x, plen = c.y, nst = c.z;
+    bool pend = c.w != 0;
+    const unsigned long long key = stream_key(P.seed, P.g0 + (unsigned long long)slot);
+    const V3f d = v3(rd.x, rd.y, rd.z);
+    const bool envHit = h.rec == -1 && S.env_light >= 0 && isinf(rd.w) && rd.w > 0.f;
+    if (h.rec == -1 && !envHit) {
+      // The path leaves the scene: the last stored vertex gets NEE (line 85).
+      if (pend) {
+        Vertex pv; V3f pa; int k;
+        load_pending(st, slot, pv, pa, k);
+        nee(S, P, st, slot, key, pv, pa, k);
+        st.ctl[slot] = make_int4(i, plen, nst, 0);
+      }
+      continue;
+    }
+    Vertex vx;
+    vx.d = d;
+    vx.mat = -1;
+    int light = -1;
+    if (envHit) {
+      light = S.env_light;
+      vx.p = normalize(d);  // point at infinity (w = 0)
+      vx.n = -vx.p;
+    } else {
+      vx.p = v3(ro.x, ro.y, ro.z) + h.t * d;
+      if (h.rec >= 0) {
+        const int4 m = __ldg(&S.meta[h.rec]);
+        const float4* rp = S.recs + 3 * int64_t(h.rec);
+        const float4 a = __ldg(rp);
+        const int kind = __float_as_int(a.w);
+        vx.mat = m.y;
+        light = m.w;
+        if (kind == kRecTriangle) {
+          if (m.z >= 0) {
+            const float* nn = S.tri_nrm + 12 * int64_t(m.z);
+            float w0 = 1.f - h.u - h.v;
+            vx.n = normalize(w0 * ld3(nn) + h.u * ld3(nn + 3) + h.v * ld3(nn + 6));
+          } else {
+            const float4 b = __ldg(rp + 1), cc = __ldg(rp + 2);
+            V3f p1 = v3(a.x, a.y, a.z), p2 = v3(b.x, b.y, b.z), p3 = v3(cc.x, cc.y, cc.z);
+            vx.n = normalize(cross(p1 - p2, p1 - p3));
+          }
+        } else if (kind == kRecSphere) {
+          vx.n = normalize(vx.p - v3(a.x, a.y, a.z));
+        } else {
+          vx.n = ld3(S.lights[light].nhat);
+        }
       } else {
-        vx.p = o + h.t * d;
-        if (h.rec >= 0) {
-          int4 m = __ldg(&S.meta[h.rec]);
-          const float4* rp = S.recs + 3 * int64_t(h.rec);
-          float4 a = __ldg(rp), b = __ldg(rp + 1), cc = __ldg(rp + 2);
-          int kind = __float_as_int(a.w);
-          vx.mat = m.y;
-          light = m.w;
-          if (kind == kRecTriangle) {
-            if (m.z >= 0) {
-              const float* nn = S.tri_nrm + 12 * int64_t(m.z);
-              float w0 = 1.f - h.u - h.v;
-              vx.n = normalize(w0 * ld3(nn) + h.u * ld3(nn + 3) + h.v * ld3(nn + 6));
-            } else {
-              V3f p1 = v3(a.x, a.y, a.z), p2 = v3(b.x, b.y, b.z), p3 = v3(cc.x, cc.y, cc.z);
-              vx.n = normalize(cross(p1 - p2, p1 - p3));
-            }
-          } else if (kind == kRecSphere) {
-            vx.n = normalize(vx.p - v3(a.x, a.y, a.z));
-          } else {
-            vx.n = ld3(S.lights[light].nhat);
-          }
-        } else {
-          float4 pl = __ldg(&S.planes[-2 - h.rec]);
-          vx.n = normalize(v3(pl.x, pl.y, pl.z));
-          vx.mat = S.plane_meta[-2 - h.rec].y;
-        }
+        const float4 pl = __ldg(&S.planes[-2 - h.rec]);
+        vx.n = normalize(v3(pl.x, pl.y, pl.z));
+        vx.mat = S.plane_meta[-2 - h.rec].y;
       }
+    }
+    if (light >= 0) {
+      // Emitter. Its own next-event term is zero (Material::brdf of a light
+      // is zero), so only its emission matters; the path ends here.
+      V3f e = envHit ? env_get(S, vx.p) : area_intensity(S.lights[light], -d);
       float4 L4 = st.L[slot];
-      if (!done && light >= 0) {
-        // Emitter. Its own next-event term is zero (Material::brdf of a light
-        // is zero), so only its emission matters.
-        V3f e;
-        if (light == S.env_light && envHit) e = env_get(S, vx.p);
-        else e = area_intensity(S.lights[light], -d);
-        if (nst == 0) {
-          // First stored vertex is an emitter: its emission is the sample.
-          L4.x = e.x; L4.y = e.y; L4.z = e.z;
-        } else if (pend) {
-          // The pending vertex sees this emitter (lines 70-81).
-          float4 pp = st.pv_p[slot], pn = st.pv_n[slot], pd = st.pv_d[slot], pa = st.pv_a[slot];
-          Vertex pv;
-          pv.p = v3(pp.x, pp.y, pp.z); pv.n = v3(pn.x, pn.y, pn.z); pv.d = v3(pd.x, pd.y, pd.z);
-          pv.mat = __float_as_int(pp.w);
-          V3f dir = envHit ? -vx.p : pv.p - vx.p;
-          V3f f = brdf_eval(S.materials, pv, dir);
-          float inCos = dot(-normalize(dir), pv.n);
-          float outCos = dot(-normalize(pv.d), pv.n);
-          if (signum(inCos) == signum(outCos)) {
-            float ac = fabsf(inCos);
-            L4.x += pa.x * f.x * e.x * ac;
-            L4.y += pa.y * f.y * e.y * ac;
-            L4.z += pa.z * f.z * e.z * ac;
-          }
+      if (nst == 0) {
+        // The first stored vertex is an emitter: its emission is the sample.
+        L4.x = e.x; L4.y = e.y; L4.z = e.z;
+      } else if (pend) {
+        // The pending vertex sees this emitter (lines 70-81).
+        Vertex pv; V3f pa; int k;
+        load_pending(st, slot, pv, pa, k);
+        V3f dir = envHit ? -vx.p : pv.p - vx.p;
+        V3f f = brdf_eval(S.materials, pv, dir);
+        float inCos = dot(-normalize(dir), pv.n);
+        float outCos = dot(-normalize(pv.d), pv.n);
+        if (signum(inCos) == signum(outCos)) {
+          float ac = fabsf(inCos);
+          L4.x += pa.x * f.x * e.x * ac;
+          L4.y += pa.y * f.y * e.y * ac;
+          L4.z += pa.z * f.z * e.z * ac;
         }
-        st.L[slot] = L4;
-        done = true;
-        pend = false;
-      } else if (!done && mat_specular(S.materials, vx.mat)) {
-        float pdf;
-        V3f f;
-        V3f out = out_direction(S.materials, vx, stream_u(key, dim_path(i)), stream_u(key, dim_path(i) + 1), pdf, f);
-        if (i == plen - 1 && plen < P.D) plen++;
-        i++;
-        if (i < plen) {
-          wantExt = true;
-          eo = make_float4(vx.p.x, vx.p.y, vx.p.z, kEps);
-          ed = make_float4(out.x, out.y, out.z, CUDART_INF_F);
-        } else {
-          done = true;
-        }
-      } else if (!done) {
-        // Stored, non-specular vertex k = nst.
-        if (pend) {
-          float4 pp = st.pv_p[slot], pn = st.pv_n[slot], pd = st.pv_d[slot], pa = st.pv_a[slot];
-          Vertex pv;
-          pv.p = v3(pp.x, pp.y, pp.z); pv.n = v3(pn.x, pn.y, pn.z); pv.d = v3(pd.x, pd.y, pd.z);
-          pv.mat = __float_as_int(pp.w);
-          nee(S, P, key, pv, v3(pa.x, pa.y, pa.z), __float_as_int(pn.w), s1);
-        }
-        int k = nst++;
-        st.pv_p[slot] = make_float4(vx.p.x, vx.p.y, vx.p.z, __int_as_float(vx.mat));
-        st.pv_n[slot] = make_float4(vx.n.x, vx.n.y, vx.n.z, __int_as_float(k));
-        st.pv_d[slot] = make_float4(d.x, d.y, d.z, 0.f);
-        st.pv_a[slot] = make_float4(alpha.x, alpha.y, alpha.z, 0.f);
-        pend = true;
-        float pdf;
-        V3f f;
-        V3f out = out_direction(S.materials, vx, stream_u(key, dim_path(i)), stream_u(key, dim_path(i) + 1), pdf, f);
-        if (pdf == 0.f || is_zero(alpha)) {
-          done = true;
-        } else {
-          float cs = fabsf(dot(normalize(out), vx.n));
-          float sc = cs / pdf;
-          alpha = v3(alpha.x * f.x * sc, alpha.y * f.y * sc, alpha.z * f.z * sc);
-          if (i > 3) {
-            float ir = 1.f / P.rr_pdf;
-            alpha = v3(alpha.x * ir, alpha.y * ir, alpha.z * ir);
-          }
-          i++;
-          if (i < plen) {
-            wantExt = true;
-            eo = make_float4(vx.p.x, vx.p.y, vx.p.z, kEps);
-            ed = make_float4(out.x, out.y, out.z, CUDART_INF_F);
-          } else {
-            done = true;
-          }
-        }
-        st.alpha[slot] = make_float4(alpha.x, alpha.y, alpha.z, 0.f);
       }
-      if (done && pend) {
-        // The last stored vertex gets next-event estimation (line 85).
-        float4 pp = st.pv_p[slot], pn = st.pv_n[slot], pd = st.pv_d[slot], pa = st.pv_a[slot];
-        Vertex pv;
-        pv.p = v3(pp.x, pp.y, pp.z); pv.n = v3(pn.x, pn.y, pn.z); pv.d = v3(pd.x, pd.y, pd.z);
-        pv.mat = __float_as_int(pp.w);
-        ShadowOut& so = s1.valid ? s2 : s1;
-        nee(S, P, key, pv, v3(pa.x, pa.y, pa.z), __float_as_int(pn.w), so);
+      st.L[slot] = L4;
+      st.ctl[slot] = make_int4(i, plen, nst, 0);
+      continue;
+    }
+    float pdf;
+    V3f f;
+    const V3f out = out_direction(S.materials, vx, stream_u(key, dim_path(i)), stream_u(key, dim_path(i) + 1), pdf, f);
+    if (mat_specular(S.materials, vx.mat)) {
+      // Specular vertices are not stored (lines 87-91).
+      if (i == plen - 1 && plen < P.D) plen++;
+      i++;
+      if (i < plen) {
+        push_ext(st, nxt, slot, vx.p, out);
+      } else if (pend) {
+        Vertex pv; V3f pa; int k;
+        load_pending(st, slot, pv, pa, k);
+        nee(S, P, st, slot, key, pv, pa, k);
         pend = false;
       }
       st.ctl[slot] = make_int4(i, plen, nst, pend ? 1 : 0);
+      continue;
     }
-    // Converged pushes.
-    int pe = warp_push(&st.counts[nxt], wantExt);
-    if (wantExt) {
-      st.ext[nxt][2 * pe] = eo;
-      st.ext[nxt][2 * pe + 1] = ed;
-      st.ext_slot[nxt][pe] = slot;
+    // Stored, non-specular vertex k = nst (lines 92-102): the previous pending
+    // vertex is now known not to be followed by an emitter.
+    if (pend) {
+      Vertex pv; V3f pa; int k;
+      load_pending(st, slot, pv, pa, k);
+      nee(S, P, st, slot, key, pv, pa, k);
     }
-    int p1 = warp_push(&st.counts[2], s1.valid);
-    if (s1.valid) {
-      st.sh_ray[2 * p1] = s1.o;
-      st.sh_ray[2 * p1 + 1] = s1.d;
-      st.sh_c[p1] = s1.c;
-      st.sh_slot[p1] = slot;
+    const float4 a4 = st.alpha[slot];
+    const V3f alpha = v3(a4.x, a4.y, a4.z);
+    const int k = nst++;
+    bool ends = pdf == 0.f || is_zero(alpha);
+    V3f na = alpha;
+    if (!ends) {
+      float sc = fabsf(dot(normalize(out), vx.n)) / pdf;
+      na = v3(alpha.x * f.x * sc, alpha.y * f.y * sc, alpha.z * f.z * sc);
+      if (i > 3) {
+        float ir = 1.f / P.rr_pdf;
+        na = v3(na.x * ir, na.y * ir, na.z * ir);
+      }
+      i++;
+      ends = i >= plen;
     }
-    int p2 = warp_push(&st.counts[2], s2.valid);
-    if (s2.valid) {
-      st.sh_ray[2 * p2] = s2.o;
-      st.sh_ray[2 * p2 + 1] = s2.d;
-      st.sh_c[p2] = s2.c;
-      st.sh_slot[p2] = slot;
+    if (ends) {
+      // This vertex is the last stored one: next-event estimation now.
+      nee(S, P, st, slot, key, vx, alpha, k);
+      st.ctl[slot] = make_int4(i, plen, nst, 0);
+    } else {
+      st.pv_p[slot] = make_float4(vx.p.x, vx.p.y, vx.p.z, __int_as_float(vx.mat));
+      st.pv_n[slot] = make_float4(vx.n.x, vx.n.y, vx.n.z, __int_as_float(k));
+      st.pv_d[slot] = make_float4(d.x, d.y, d.z, 0.f);
+      st.pv_a[slot] = make_float4(alpha.x, alpha.y, alpha.z, 0.f);
+      st.alpha[slot] = make_float4(na.x, na.y, na.z, 0.f);
+      st.ctl[slot] = make_int4(i, plen, nst, 1);
+      push_ext(st, nxt, slot, vx.p, out);
     }
   }
 }
