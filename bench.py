@@ -238,7 +238,8 @@ def main():
     render_dev(_abi.RENDER_COUNT_TRAVERSAL, cs)
     n_node = cs.nodes_closest / max(cs.extension_rays, 1)
     n_prim = cs.prims_closest / max(cs.extension_rays, 1)
-    bytes_per_ray = 32 + 16 + 64 * n_node + 48 * n_prim
+    # per node visit the kernel fetches 7 x 16 B (six box planes + child refs)
+    bytes_per_ray = 32 + 16 + 112 * n_node + 48 * n_prim
 
     for _ in range(args.warmup):
         render_dev(0, _abi.Stats())

@@ -300,4 +300,71 @@ BuildResult build_bvh(const std::vector<Box>& boxes, const BuildOptions& optIn) 
   return res;
 }
 
+namespace {
+
+struct Child {
+  float lo[3], hi[3];
+  int32_t ref;
+  float area() const {
+    float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    return 2.f * (dx * dy + dy * dz + dz * dx);
+  }
+};
+
+Child childOf(const Node& n, int which) {
+  Child c;
+  const float* xy = which == 0 ? n.a : n.b;
+  c.lo[0] = xy[0]; c.hi[0] = xy[1]; c.lo[1] = xy[2]; c.hi[1] = xy[3];
+  c.lo[2] = n.c[which * 2]; c.hi[2] = n.c[which * 2 + 1];
+  c.ref = n.d[which];
+  return c;
+}
+
+int32_t collapseRec(const std::vector<Node>& n2, int32_t ref2, int depth, Collapsed& out) {
+  out.max_depth = std::max(out.max_depth, depth + 1);
+  Child ch[4];
+  int cnt = 0;
+  ch[cnt++] = childOf(n2[ref2], 0);
+  ch[cnt++] = childOf(n2[ref2], 1);
+  if (ch[0].ref == ch[1].ref) cnt = 1;  // a single-leaf scene: both slots name the same leaf
+  while (cnt < 4) {
+    int best = -1;
+    float bestArea = -1.f;
+    for (int i = 0; i < cnt; ++i)
+      if (ch[i].ref >= 0 && ch[i].area() > bestArea) { bestArea = ch[i].area(); best = i; }
+    if (best < 0) break;
+    const Node& nd = n2[ch[best].ref];
+    ch[best] = childOf(nd, 0);
+    ch[cnt++] = childOf(nd, 1);
+  }
+  int32_t me = int32_t(out.nodes.size());
+  out.nodes.emplace_back();
+  Node4 node;
+  for (int i = 0; i < 4; ++i) {
+    if (i < cnt) {
+      node.lox[i] = ch[i].lo[0]; node.hix[i] = ch[i].hi[0];
+      node.loy[i] = ch[i].lo[1]; node.hiy[i] = ch[i].hi[1];
+      node.loz[i] = ch[i].lo[2]; node.hiz[i] = ch[i].hi[2];
+    } else {
+      node.lox[i] = node.loy[i] = node.loz[i] = INFINITY;
+      node.hix[i] = node.hiy[i] = node.hiz[i] = -INFINITY;
+    }
+    node.ref[i] = kEmptyRef;
+    node.pad[i] = 0;
+  }
+  for (int i = 0; i < cnt; ++i) node.ref[i] = ch[i].ref >= 0 ? collapseRec(n2, ch[i].ref, depth + 1, out) : ch[i].ref;
+  out.nodes[me] = node;
+  return me;
+}
+
+}  // namespace
+
+Collapsed collapse_bvh4(const BuildResult& b2) {
+  Collapsed out;
+  if (b2.nodes.empty()) return out;
+  out.nodes.reserve(b2.nodes.size() / 2 + 1);
+  collapseRec(b2.nodes, 0, 0, out);
+  return out;
+}
+
 }  // namespace gbrt

@@ -52,7 +52,28 @@ struct BuildResult {
   double sah_cost = 0;            // SAH cost of the tree relative to the root box
 };
 
-// Builds over boxes (all finite). Always produces at least a root node.
+// Builds over boxes (all finite). Produces no node for an empty input.
 BuildResult build_bvh(const std::vector<Box>& boxes, const BuildOptions& opt);
+
+// A 4-wide node, 128 bytes: the boxes of up to four children as six float4
+// planes (lo.x of children 0..3, hi.x, lo.y, hi.y, lo.z, hi.z), then the four
+// child references (same encoding as Node; kEmptyRef for an unused slot, whose
+// box is inverted so it never intersects).
+struct alignas(16) Node4 {
+  float lox[4], hix[4], loy[4], hiy[4], loz[4], hiz[4];
+  int32_t ref[4];
+  int32_t pad[4];
+};
+constexpr int32_t kEmptyRef = 0x7fffffff;
+
+struct Collapsed {
+  std::vector<Node4> nodes;  // nodes[0] is the root
+  int max_depth = 0;         // levels of 4-wide nodes
+};
+
+// Collapses a binary tree into a 4-wide one: every 4-wide node takes the two
+// children of a binary node and keeps opening its largest inner child until it
+// holds four. Leaves (primitive ranges) are unchanged.
+Collapsed collapse_bvh4(const BuildResult& b2);
 
 }  // namespace gbrt

@@ -27,7 +27,8 @@ struct gbrt_scene {
   gbrt::DeviceScene view{};
   std::vector<void*> allocations;
   int64_t n_leaves = 0;
-  int32_t max_depth = 0;
+  int32_t max_depth = 0;   // binary tree
+  int32_t max_depth4 = 0;  // 4-wide tree traversed on the device
   double sah_cost = 0;
   double build_ms = 0;
   int32_t n_prims = 0;  // primitive ids in use

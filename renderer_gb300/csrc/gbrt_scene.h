@@ -3,7 +3,7 @@
 //
 // HBM layout (all arrays 16-byte aligned, read through the non-coherent
 // 128-bit load path):
-//   nodes  : n_nodes x 64 B   BVH2 nodes (bvh_build.h), root at 0
+//   nodes  : n_nodes x 128 B  4-wide BVH nodes (bvh_build.h Node4), root at 0
 //   recs   : n_recs x 48 B    primitive records in BVH leaf order, 3 float4:
 //              triangle      (p1, kind) (p2, -) (p3, prim)
 //              sphere        (centre, kind) (radius, 0, 0, -) (0, 0, 0, prim)

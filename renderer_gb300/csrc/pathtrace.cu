@@ -158,8 +158,6 @@ __device__ __forceinline__ void warp_add_counters(TraceCounters c, unsigned long
 // work[cur^1] (next extend) and work[2] (this iteration's shadow pass).
 template <bool COUNT, bool WT, int STACK>
 __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState st, int cur) {
-  __shared__ int s_stack[STACK * kTraceBlock];
-  int* stack = s_stack + threadIdx.x;
   const int n = st.counts[cur];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st.tally[0] += (unsigned long long)n;
@@ -181,7 +179,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState s
     if (i >= n) continue;
     TRay r = make_tray(rays[2 * i], rays[2 * i + 1]);
     RawHit h;
-    h.rec = trace_ray<false, COUNT, WT, STACK>(S, r, -1, stack, h.t, h.u, h.v, st.err, &cnt);
+    h.rec = trace_ray<false, COUNT, WT, STACK>(S, r, -1, h.t, h.u, h.v, st.err, &cnt);
     st.hits[i] = h;
   }
   if (COUNT) warp_add_counters(cnt, &st.tally[3], &st.tally[4]);
@@ -190,8 +188,6 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState s
 // ------------------------------------------------------------- shadow ----
 template <bool COUNT, bool WT, int STACK>
 __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState st) {
-  __shared__ int s_stack[STACK * kTraceBlock];
-  int* stack = s_stack + threadIdx.x;
   const int n = st.counts[2];
   if (blockIdx.x == 0 && threadIdx.x == 0) st.tally[1] += (unsigned long long)n;
   unsigned long long* work = st.work + 2;
@@ -207,7 +203,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState s
     float4 c = st.sh_c[i];
     TRay r = make_tray(st.sh_ray[2 * i], st.sh_ray[2 * i + 1]);
     float t, u, v;
-    int32_t rec = trace_ray<true, COUNT, WT, STACK>(S, r, __float_as_int(c.w), stack, t, u, v, st.err, &cnt);
+    int32_t rec = trace_ray<true, COUNT, WT, STACK>(S, r, __float_as_int(c.w), t, u, v, st.err, &cnt);
     if (rec == -1) {
       float4* L = st.L + st.sh_slot[i];
       atomicAdd(&L->x, c.x);
@@ -522,7 +518,7 @@ static TraceKernels pick_stack(bool shortStack) {
   return {k_extend<C, W, kStackSize>, k_shadow<C, W, kStackSize>};
 }
 static TraceKernels pick_kernels(const gbrt_scene* s, bool count) {
-  const bool shortStack = s->max_depth <= kShortStack - 2;
+  const bool shortStack = stack_need(s->max_depth4) <= kShortStack;
   if (count) return s->watertight ? pick_stack<true, true>(shortStack) : pick_stack<true, false>(shortStack);
   return s->watertight ? pick_stack<false, true>(shortStack) : pick_stack<false, false>(shortStack);
 }

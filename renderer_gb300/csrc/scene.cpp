@@ -310,8 +310,9 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     std::memcpy(&recv[3 * k], r.v, sizeof r.v);
     meta[k] = make_int4(r.meta[0], r.meta[1], r.meta[2], r.meta[3]);
   }
-  std::vector<float4> nodes(br.nodes.size() * 4);
-  if (!br.nodes.empty()) std::memcpy(nodes.data(), br.nodes.data(), br.nodes.size() * sizeof(Node));
+  Collapsed c4 = collapse_bvh4(br);
+  std::vector<float4> nodes(c4.nodes.size() * 8);
+  if (!c4.nodes.empty()) std::memcpy(nodes.data(), c4.nodes.data(), c4.nodes.size() * sizeof(Node4));
 
   std::vector<DevMaterial> mats(size_t(d->n_materials));
   for (int i = 0; i < d->n_materials; ++i) {
@@ -342,7 +343,7 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     delete s;
     return st;
   }
-  v.n_nodes = int64_t(br.nodes.size());
+  v.n_nodes = int64_t(c4.nodes.size());
   v.n_recs = int64_t(recs.size());
   v.n_planes = d->n_planes;
   v.n_materials = d->n_materials;
@@ -364,6 +365,7 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   }
   s->n_leaves = br.leaves;
   s->max_depth = br.max_depth;
+  s->max_depth4 = c4.max_depth;
   s->sah_cost = br.sah_cost;
   s->n_prims = int32_t(nPrims);
   s->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -20,8 +20,6 @@ template <bool ANY, bool WT, int STACK>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_api(DeviceScene S, const float4* __restrict__ rays, int64_t n, const int32_t* __restrict__ ignore,
                 gbrt_hit* __restrict__ hits, uint8_t* __restrict__ occluded, unsigned long long* work, int* err) {
-  __shared__ int s_stack[STACK * kTraceBlock];
-  int* stack = s_stack + threadIdx.x;
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long base = 0;
@@ -34,7 +32,7 @@ __global__ void __launch_bounds__(kTraceBlock)
     TRay r = make_tray(a, b);
     float t, u, v;
     int ign = (ANY && ignore) ? ignore[i] : -1;
-    int32_t rec = trace_ray<ANY, false, WT, STACK>(S, r, ign, stack, t, u, v, err, nullptr);
+    int32_t rec = trace_ray<ANY, false, WT, STACK>(S, r, ign, t, u, v, err, nullptr);
     if (ANY) {
       occluded[i] = rec != -1 ? 1 : 0;
     } else {
@@ -63,8 +61,8 @@ static gbrt_status launch_api(gbrt_scene* s, bool any, const gbrt_ray* d_rays, c
   gbrt_ctx* ctx = s->ctx;
   GBRT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long), st));
   const float4* rays = reinterpret_cast<const float4*>(d_rays);
-  // The short shared-memory stack when the tree is shallow enough for it.
-  const bool shortStack = s->max_depth <= kShortStack - 2;
+  // The short stack when the tree is shallow enough for it.
+  const bool shortStack = stack_need(s->max_depth4) <= kShortStack;
   decltype(&k_trace_api<false, false, kStackSize>) k;
   if (any) {
     if (shortStack) k = s->watertight ? k_trace_api<true, true, kShortStack> : k_trace_api<true, false, kShortStack>;

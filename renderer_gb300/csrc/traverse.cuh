@@ -10,10 +10,16 @@
 //   AreaLight::intersect               src/arealight.cpp:73-90
 //   EnvironmentMap::intersect          src/environmentmap.cpp:73-83 (as "no hit, tmax = inf")
 //
-// Structure: ordered (near child first) while-while traversal of a BVH2 with
-// tmax shrinking, 64-byte nodes fetched as four 128-bit non-coherent loads, and
-// a per-thread stack in shared memory laid out [depth][thread] so that a warp's
-// pushes and pops fall in distinct banks.
+// Structure: ordered (nearest child first) traversal of a 4-wide BVH with tmax
+// shrinking. A node is 128 bytes; a ray fetches the six box planes it needs in
+// near/far order (chosen once per ray by the signs of its direction) and the
+// child references as seven 128-bit non-coherent loads, tests the four child
+// boxes, sorts the hit children by entry distance with a 4-key sorting
+// network, descends into the nearest and pushes the others far-to-near on a
+// per-thread stack (local memory, L1-resident). A 4-wide tree halves the chain
+// of dependent node fetches of a binary one, which is what bounds traversal:
+// the nodes of a 1.3M-triangle scene sit in L1/L2, so the kernel is
+// latency-bound rather than DRAM-bound.
 //
 // Numerics. By default a triangle is tested with the renderer's own formulas
 // (src/triangle.cpp:32-44: Cramer's rule, t first, then u in [0,1], v >= 0,
@@ -41,8 +47,11 @@
 
 namespace gbrt {
 
-constexpr int kStackSize = 64;   // the builder keeps tree depth <= kStackSize - 2
-constexpr int kShortStack = 32;  // enough when the tree depth is <= kShortStack - 2
+// Stack entries: at most three pushes per level of the 4-wide tree, whose
+// depth is at most the binary tree's (<= 62, kept by the builder).
+constexpr int kStackSize = 190;  // any tree
+constexpr int kShortStack = 64;  // trees of 4-wide depth <= 21
+__host__ __device__ constexpr int stack_need(int depth4) { return 3 * depth4 + 1; }
 constexpr int kTraceBlock = 128;
 
 // Exactly rounded, never-contracted float operations.
@@ -94,25 +103,29 @@ __device__ __forceinline__ TRay make_tray(float4 a, float4 b) {
   return r;
 }
 
-// Conservative slab test of one child box against [tmin, tcur]. As in
-// AxisAlignedBox::getCSGIntersection (src/axisalignedbox.cpp:41-66) the near
-// and far planes of each slab are chosen by the sign of 1/d, and a slab whose
-// distance is NaN (a zero direction component with the origin on that slab's
-// plane: 0 * inf) constrains nothing, because fmaxf / fminf ignore NaN.
-__device__ __forceinline__ bool box_hit(const TRay& r, float lox, float hix, float loy, float hiy, float loz,
-                                        float hiz, float tcur, float& tnear) {
-  float tx0 = (lox - r.ox) * r.ix, tx1 = (hix - r.ox) * r.ix;
-  float ty0 = (loy - r.oy) * r.iy, ty1 = (hiy - r.oy) * r.iy;
-  float tz0 = (loz - r.oz) * r.iz, tz1 = (hiz - r.oz) * r.iz;
-  const bool px = r.ix >= 0.f, py = r.iy >= 0.f, pz = r.iz >= 0.f;
-  float nx = px ? tx0 : tx1, fx = px ? tx1 : tx0;
-  float ny = py ? ty0 : ty1, fy = py ? ty1 : ty0;
-  float nz = pz ? tz0 : tz1, fz = pz ? tz1 : tz0;
-  float tn = fmaxf(fmaxf(nx, ny), fmaxf(nz, r.tmin));
-  float tf = fminf(fminf(fx, fy), fz) * 1.0000004f;
+// Entry distance of one child box, or +inf when the ray misses it inside
+// [tmin, tcur]. n* / f* are the box's near and far planes for this ray (picked
+// by the signs of 1/d, as AxisAlignedBox::getCSGIntersection does,
+// src/axisalignedbox.cpp:41-66). A plane distance that is NaN (a zero
+// direction component with the origin on that plane: 0 * inf) constrains
+// nothing, because fmaxf / fminf ignore NaN. The far distance is enlarged by
+// 1 + 2*gamma(3) so rounding never loses a box (Ize 2013).
+__device__ __forceinline__ float box_entry(const TRay& r, float nx, float fx, float ny, float fy, float nz, float fz,
+                                           float tcur) {
+  float tn = fmaxf(fmaxf((nx - r.ox) * r.ix, (ny - r.oy) * r.iy), fmaxf((nz - r.oz) * r.iz, r.tmin));
+  float tf = fminf(fminf((fx - r.ox) * r.ix, (fy - r.oy) * r.iy), (fz - r.oz) * r.iz) * 1.0000004f;
   tf = fminf(tf, tcur);
-  tnear = tn;
-  return tn <= tf;
+  return tn <= tf ? tn : CUDART_INF_F;
+}
+
+__device__ __forceinline__ void cswap(float& ka, int& ra, float& kb, int& rb) {
+  bool sw = kb < ka;
+  float k = sw ? kb : ka;
+  int rr = sw ? rb : ra;
+  kb = sw ? ka : kb;
+  rb = sw ? ra : rb;
+  ka = k;
+  ra = rr;
 }
 
 // Accepts t against the current best: inclusive of tmax for the first hit
@@ -249,9 +262,8 @@ struct TraceCounters {
 
 // Traverses the scene. ANY: stop at the first accepted hit and skip records
 // (and planes) whose prim id equals ignore_prim. WT: watertight triangle test.
-// Returns the internal hit encoding (RawHit::rec) and fills t/u/v. stack is
-// this thread's column of the block's shared stack (stride kTraceBlock) of
-// STACK entries.
+// Returns the internal hit encoding (RawHit::rec) and fills t/u/v. STACK is
+// the capacity of the traversal stack (stack_need(depth of the 4-wide tree)).
 //
 // Acceptance: the first hit may lie anywhere in [tmin, tmax] (Ray::inRange is
 // inclusive); later hits must be strictly closer. One exception keeps
@@ -260,7 +272,7 @@ struct TraceCounters {
 // current best that is the same quad's second half even at a larger t, and the
 // second half never replaces the first.
 template <bool ANY, bool COUNT, bool WT, int STACK>
-__device__ __forceinline__ int32_t trace_ray(const DeviceScene& S, const TRay& r, int ignore_prim, int* stack,
+__device__ __forceinline__ int32_t trace_ray(const DeviceScene& S, const TRay& r, int ignore_prim,
                                              float& t_best, float& u_best, float& v_best, int* err,
                                              TraceCounters* cnt) {
   float tcur = r.tmax;
@@ -279,69 +291,79 @@ __device__ __forceinline__ int32_t trace_ray(const DeviceScene& S, const TRay& r
     }
   }
   if (S.n_nodes > 0) {
+    int stack[STACK];
     int sp = 0;
-    stack[0] = 0x7fffffff;  // sentinel
+    // Offsets (in float4) of the near and far planes of each axis in a node.
+    const int nxo = r.ix >= 0.f ? 0 : 1, nyo = r.iy >= 0.f ? 2 : 3, nzo = r.iz >= 0.f ? 4 : 5;
     int32_t node = 0;
-    while (node != 0x7fffffff) {
+    for (;;) {
       if (node >= 0) {
-        const float4* np = S.nodes + 4 * int64_t(node);
-        float4 n0 = __ldg(np + 0), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
-        int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+        const float4* np = S.nodes + 8 * int64_t(node);
+        const float4 nx = __ldg(np + nxo), fx = __ldg(np + (1 - nxo));
+        const float4 ny = __ldg(np + nyo), fy = __ldg(np + (5 - nyo));
+        const float4 nz = __ldg(np + nzo), fz = __ldg(np + (9 - nzo));
+        const int4 rf = __ldg(reinterpret_cast<const int4*>(np + 6));
         if (COUNT) cnt->nodes++;
-        float tn0, tn1;
-        bool h0 = box_hit(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, tcur, tn0);
-        bool h1 = box_hit(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, tcur, tn1);
-        if (h0 && h1) {
-          int32_t nearRef = n3.x, farRef = n3.y;
-          if (tn1 < tn0) { nearRef = n3.y; farRef = n3.x; }
-          if (sp + 1 >= STACK) { *err = 1; break; }
-          stack[(++sp) * kTraceBlock] = farRef;
-          node = nearRef;
-        } else if (h0) {
-          node = n3.x;
-        } else if (h1) {
-          node = n3.y;
-        } else {
-          node = stack[(sp--) * kTraceBlock];
+        float k0 = box_entry(r, nx.x, fx.x, ny.x, fy.x, nz.x, fz.x, tcur);
+        float k1 = box_entry(r, nx.y, fx.y, ny.y, fy.y, nz.y, fz.y, tcur);
+        float k2 = box_entry(r, nx.z, fx.z, ny.z, fy.z, nz.z, fz.z, tcur);
+        float k3 = box_entry(r, nx.w, fx.w, ny.w, fy.w, nz.w, fz.w, tcur);
+        int r0 = rf.x, r1 = rf.y, r2 = rf.z, r3 = rf.w;
+        // Ascending entry distance (sorting network for four keys).
+        cswap(k0, r0, k1, r1);
+        cswap(k2, r2, k3, r3);
+        cswap(k0, r0, k2, r2);
+        cswap(k1, r1, k3, r3);
+        cswap(k1, r1, k2, r2);
+        if (k1 != CUDART_INF_F) {
+          if (sp + 3 > STACK) { *err = 1; break; }
+          if (k3 != CUDART_INF_F) stack[sp++] = r3;
+          if (k2 != CUDART_INF_F) stack[sp++] = r2;
+          stack[sp++] = r1;
         }
-        continue;
+        if (k0 != CUDART_INF_F) {
+          node = r0;
+          continue;
+        }
+      } else {
+        // Leaf.
+        uint32_t lv = ~uint32_t(node);
+        int64_t first = int64_t(lv >> 4), count = int64_t(lv & 15u) + 1;
+        for (int64_t k = first; k < first + count; ++k) {
+          const float4* rp = S.recs + 3 * k;
+          float4 a = __ldg(rp + 0), b = __ldg(rp + 1), c = __ldg(rp + 2);
+          if (COUNT) cnt->prims++;
+          int kind = __float_as_int(a.w);
+          int prim = __float_as_int(c.w);
+          if (ANY && prim == ignore_prim) continue;
+          int quad = kind == kRecTriangle ? __float_as_int(b.w) : 0;
+          // The first half of a quad may displace its own second half at any t.
+          bool displace = !ANY && quad == 1 && found && bestPrim == prim && bestQuad == 2;
+          float tlim = displace ? r.tmax : tcur;
+          float t, u = 0.f, v = 0.f;
+          bool hit;
+          if (kind == kRecTriangle) {
+            if (WT) hit = tri_test_wt(r, a, b, c, tlim, t, u, v);
+            else hit = tri_test_ref(r, a, b, c, tlim, t, u, v);
+          } else if (kind == kRecSphere) {
+            hit = sphere_test(r, a, b.x, tlim, t);
+          } else {
+            hit = pgram_test(r, a, b, c, tlim, t, u, v);
+          }
+          if (hit && found && !displace) {
+            // strictly closer, and a second half never displaces its first half
+            hit = t < tcur && !(quad == 2 && bestPrim == prim && bestQuad == 1);
+          }
+          if (hit) {
+            tcur = t; found = true; best = int32_t(k); bu = u; bv = v;
+            bestPrim = prim; bestQuad = quad;
+            if (ANY) break;
+          }
+        }
+        if (ANY && found) break;
       }
-      // Leaf.
-      uint32_t lv = ~uint32_t(node);
-      int64_t first = int64_t(lv >> 4), count = int64_t(lv & 15u) + 1;
-      for (int64_t k = first; k < first + count; ++k) {
-        const float4* rp = S.recs + 3 * k;
-        float4 a = __ldg(rp + 0), b = __ldg(rp + 1), c = __ldg(rp + 2);
-        if (COUNT) cnt->prims++;
-        int kind = __float_as_int(a.w);
-        int prim = __float_as_int(c.w);
-        if (ANY && prim == ignore_prim) continue;
-        int quad = kind == kRecTriangle ? __float_as_int(b.w) : 0;
-        // The first half of a quad may displace its own second half at any t.
-        bool displace = !ANY && quad == 1 && found && bestPrim == prim && bestQuad == 2;
-        float tlim = displace ? r.tmax : tcur;
-        float t, u = 0.f, v = 0.f;
-        bool hit;
-        if (kind == kRecTriangle) {
-          if (WT) hit = tri_test_wt(r, a, b, c, tlim, t, u, v);
-          else hit = tri_test_ref(r, a, b, c, tlim, t, u, v);
-        } else if (kind == kRecSphere) {
-          hit = sphere_test(r, a, b.x, tlim, t);
-        } else {
-          hit = pgram_test(r, a, b, c, tlim, t, u, v);
-        }
-        if (hit && found && !displace) {
-          // strictly closer, and a second half never displaces its first half
-          hit = t < tcur && !(quad == 2 && bestPrim == prim && bestQuad == 1);
-        }
-        if (hit) {
-          tcur = t; found = true; best = int32_t(k); bu = u; bv = v;
-          bestPrim = prim; bestQuad = quad;
-          if (ANY) break;
-        }
-      }
-      if (ANY && found) break;
-      node = stack[(sp--) * kTraceBlock];
+      if (sp == 0) break;
+      node = stack[--sp];
     }
   }
   t_best = found ? tcur : CUDART_NAN_F;
