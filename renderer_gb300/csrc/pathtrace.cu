@@ -151,7 +151,10 @@ __device__ __forceinline__ void warp_add_counters(TraceCounters c, unsigned long
   }
 }
 
-// ------------------------------------------------------------- extend ----
+// ----------------------------------------------------- extend / shadow ----
+// Persistent traversal kernels: each warp takes 32 rays at a time from its
+// queue with one atomic and traces them to completion.
+//
 // Queue protocol (no host-side resets inside a batch): k_raygen sets
 // counts[0] and zeroes work[0]; k_extend on queue cur zeroes, before shade and
 // shadow run, counts[cur^1] (next extension queue), counts[2] (shadow queue),
@@ -185,7 +188,6 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState s
   if (COUNT) warp_add_counters(cnt, &st.tally[3], &st.tally[4]);
 }
 
-// ------------------------------------------------------------- shadow ----
 template <bool COUNT, bool WT, int STACK>
 __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState st) {
   const int n = st.counts[2];

@@ -36,8 +36,7 @@
 // negations of each other), with a double-precision re-evaluation when one is
 // exactly zero; t still comes from the renderer's formula. Spheres, planes and
 // parallelograms always use the renderer's formulas the same way. Box tests
-// are conservative: (bound - origin) * (1/d) with the far distance enlarged by
-// 1 + 2*gamma(3) (Ize 2013, "Robust BVH Ray Traversal").
+// are conservative (box_entry; Ize 2013, "Robust BVH Ray Traversal").
 #pragma once
 
 #include <cuda_runtime.h>
@@ -108,13 +107,14 @@ __device__ __forceinline__ TRay make_tray(float4 a, float4 b) {
 // by the signs of 1/d, as AxisAlignedBox::getCSGIntersection does,
 // src/axisalignedbox.cpp:41-66). A plane distance that is NaN (a zero
 // direction component with the origin on that plane: 0 * inf) constrains
-// nothing, because fmaxf / fminf ignore NaN. The far distance is enlarged by
-// 1 + 2*gamma(3) so rounding never loses a box (Ize 2013).
+// nothing, because fmaxf / fminf ignore NaN. Each distance (p - o) * (1/d) has
+// a relative error below 2^-23, so enlarging the far distance by
+// 1 + 6.7 * 2^-24 (Ize 2013, "Robust BVH Ray Traversal") never loses a box.
 __device__ __forceinline__ float box_entry(const TRay& r, float nx, float fx, float ny, float fy, float nz, float fz,
                                            float tcur) {
   float tn = fmaxf(fmaxf((nx - r.ox) * r.ix, (ny - r.oy) * r.iy), fmaxf((nz - r.oz) * r.iz, r.tmin));
-  float tf = fminf(fminf((fx - r.ox) * r.ix, (fy - r.oy) * r.iy), (fz - r.oz) * r.iz) * 1.0000004f;
-  tf = fminf(tf, tcur);
+  float tf = fminf(fminf((fx - r.ox) * r.ix, (fy - r.oy) * r.iy), (fz - r.oz) * r.iz);
+  tf = fminf(tf * 1.0000004f, tcur);
   return tn <= tf ? tn : CUDART_INF_F;
 }
 
@@ -260,10 +260,46 @@ struct TraceCounters {
   unsigned long long nodes, prims;
 };
 
-// Traverses the scene. ANY: stop at the first accepted hit and skip records
-// (and planes) whose prim id equals ignore_prim. WT: watertight triangle test.
-// Returns the internal hit encoding (RawHit::rec) and fills t/u/v. STACK is
-// the capacity of the traversal stack (stack_need(depth of the 4-wide tree)).
+// Traversal state of one ray between steps (see trace_step).
+struct TState {
+  int32_t node;      // next node or leaf to visit
+  int sp;            // stack depth
+  float tcur;        // current far limit
+  int32_t best;      // internal hit encoding of the best hit so far
+  int32_t bestPrim;
+  int32_t bestQuad;  // 0: not a quad half, 1: first half, 2: second half
+  float bu, bv;
+  bool found;
+};
+
+// Starts a ray: tests the planes (unbounded, kept out of the BVH; testing them
+// first gives the tree a tighter tmax). Returns true when the ray is already
+// finished (an any-hit ray that hit a plane, or an empty tree).
+template <bool ANY>
+__device__ __forceinline__ bool trace_init(const DeviceScene& S, const TRay& r, int ignore_prim, TState& ts) {
+  ts.tcur = r.tmax;
+  ts.found = false;
+  ts.best = -1;
+  ts.bestPrim = -1;
+  ts.bestQuad = 0;
+  ts.bu = 0.f;
+  ts.bv = 0.f;
+  ts.sp = 0;
+  ts.node = 0;
+  for (int k = 0; k < S.n_planes; ++k) {
+    if (ANY && S.plane_meta[k].x == ignore_prim) continue;
+    float t = plane_t(r, __ldg(&S.planes[k]));
+    if (t >= r.tmin && t <= r.tmax && accept_t(t, r.tmin, ts.tcur, ts.found)) {
+      ts.tcur = t; ts.found = true; ts.best = -2 - k; ts.bu = 0.f; ts.bv = 0.f;
+      if (ANY) return true;
+    }
+  }
+  return S.n_nodes <= 0;
+}
+
+// One traversal step: one 4-wide node or one leaf. ANY: stop at the first
+// accepted hit and skip records whose prim id equals ignore_prim. WT:
+// watertight triangle test. Returns true when the ray is finished.
 //
 // Acceptance: the first hit may lie anywhere in [tmin, tmax] (Ray::inRange is
 // inclusive); later hits must be strictly closer. One exception keeps
@@ -272,103 +308,98 @@ struct TraceCounters {
 // current best that is the same quad's second half even at a larger t, and the
 // second half never replaces the first.
 template <bool ANY, bool COUNT, bool WT, int STACK>
+__device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& r, int ignore_prim, TState& ts,
+                                           int* stack, int* err, TraceCounters* cnt) {
+  const int32_t node = ts.node;
+  if (node >= 0) {
+    // Offsets (in float4) of the near and far planes of each axis.
+    const int nxo = r.ix >= 0.f ? 0 : 1, nyo = r.iy >= 0.f ? 2 : 3, nzo = r.iz >= 0.f ? 4 : 5;
+    const float4* np = S.nodes + 8 * int64_t(node);
+    const float4 nx = __ldg(np + nxo), fx = __ldg(np + (1 - nxo));
+    const float4 ny = __ldg(np + nyo), fy = __ldg(np + (5 - nyo));
+    const float4 nz = __ldg(np + nzo), fz = __ldg(np + (9 - nzo));
+    const int4 rf = __ldg(reinterpret_cast<const int4*>(np + 6));
+    if (COUNT) cnt->nodes++;
+    const float tcur = ts.tcur;
+    float k0 = box_entry(r, nx.x, fx.x, ny.x, fy.x, nz.x, fz.x, tcur);
+    float k1 = box_entry(r, nx.y, fx.y, ny.y, fy.y, nz.y, fz.y, tcur);
+    float k2 = box_entry(r, nx.z, fx.z, ny.z, fy.z, nz.z, fz.z, tcur);
+    float k3 = box_entry(r, nx.w, fx.w, ny.w, fy.w, nz.w, fz.w, tcur);
+    int r0 = rf.x, r1 = rf.y, r2 = rf.z, r3 = rf.w;
+    // Ascending entry distance (sorting network for four keys).
+    cswap(k0, r0, k1, r1);
+    cswap(k2, r2, k3, r3);
+    cswap(k0, r0, k2, r2);
+    cswap(k1, r1, k3, r3);
+    cswap(k1, r1, k2, r2);
+    if (k1 != CUDART_INF_F) {
+      if (ts.sp + 3 > STACK) { *err = 1; return true; }
+      if (k3 != CUDART_INF_F) stack[ts.sp++] = r3;
+      if (k2 != CUDART_INF_F) stack[ts.sp++] = r2;
+      stack[ts.sp++] = r1;
+    }
+    if (k0 != CUDART_INF_F) {
+      ts.node = r0;
+      return false;
+    }
+  } else {
+    // Leaf.
+    uint32_t lv = ~uint32_t(node);
+    int64_t first = int64_t(lv >> 4), count = int64_t(lv & 15u) + 1;
+    for (int64_t k = first; k < first + count; ++k) {
+      const float4* rp = S.recs + 3 * k;
+      float4 a = __ldg(rp + 0), b = __ldg(rp + 1), c = __ldg(rp + 2);
+      if (COUNT) cnt->prims++;
+      int kind = __float_as_int(a.w);
+      int prim = __float_as_int(c.w);
+      if (ANY && prim == ignore_prim) continue;
+      int quad = kind == kRecTriangle ? __float_as_int(b.w) : 0;
+      // The first half of a quad may displace its own second half at any t.
+      bool displace = !ANY && quad == 1 && ts.found && ts.bestPrim == prim && ts.bestQuad == 2;
+      float tlim = displace ? r.tmax : ts.tcur;
+      float t, u = 0.f, v = 0.f;
+      bool hit;
+      if (kind == kRecTriangle) {
+        if (WT) hit = tri_test_wt(r, a, b, c, tlim, t, u, v);
+        else hit = tri_test_ref(r, a, b, c, tlim, t, u, v);
+      } else if (kind == kRecSphere) {
+        hit = sphere_test(r, a, b.x, tlim, t);
+      } else {
+        hit = pgram_test(r, a, b, c, tlim, t, u, v);
+      }
+      if (hit && ts.found && !displace) {
+        // strictly closer, and a second half never displaces its first half
+        hit = t < ts.tcur && !(quad == 2 && ts.bestPrim == prim && ts.bestQuad == 1);
+      }
+      if (hit) {
+        ts.tcur = t; ts.found = true; ts.best = int32_t(k); ts.bu = u; ts.bv = v;
+        ts.bestPrim = prim; ts.bestQuad = quad;
+        if (ANY) return true;
+      }
+    }
+  }
+  if (ts.sp == 0) return true;
+  ts.node = stack[--ts.sp];
+  return false;
+}
+
+// A whole ray in one call (the ray-query entry points). Returns the internal
+// hit encoding (RawHit::rec) and fills t/u/v. STACK is the capacity of the
+// traversal stack (stack_need(depth of the 4-wide tree)).
+template <bool ANY, bool COUNT, bool WT, int STACK>
 __device__ __forceinline__ int32_t trace_ray(const DeviceScene& S, const TRay& r, int ignore_prim,
                                              float& t_best, float& u_best, float& v_best, int* err,
                                              TraceCounters* cnt) {
-  float tcur = r.tmax;
-  bool found = false;
-  int32_t best = -1;
-  int32_t bestPrim = -1;
-  int32_t bestQuad = 0;  // 0: not a quad half, 1: first half, 2: second half
-  float bu = 0.f, bv = 0.f;
-  // Planes: unbounded, tested first to give the BVH a tighter tmax.
-  for (int k = 0; k < S.n_planes; ++k) {
-    if (ANY && S.plane_meta[k].x == ignore_prim) continue;
-    float t = plane_t(r, __ldg(&S.planes[k]));
-    if (t >= r.tmin && t <= r.tmax && accept_t(t, r.tmin, tcur, found)) {
-      tcur = t; found = true; best = -2 - k; bu = 0.f; bv = 0.f;
-      if (ANY) { t_best = t; return best; }
+  TState ts;
+  int stack[STACK];
+  if (!trace_init<ANY>(S, r, ignore_prim, ts)) {
+    while (!trace_step<ANY, COUNT, WT, STACK>(S, r, ignore_prim, ts, stack, err, cnt)) {
     }
   }
-  if (S.n_nodes > 0) {
-    int stack[STACK];
-    int sp = 0;
-    // Offsets (in float4) of the near and far planes of each axis in a node.
-    const int nxo = r.ix >= 0.f ? 0 : 1, nyo = r.iy >= 0.f ? 2 : 3, nzo = r.iz >= 0.f ? 4 : 5;
-    int32_t node = 0;
-    for (;;) {
-      if (node >= 0) {
-        const float4* np = S.nodes + 8 * int64_t(node);
-        const float4 nx = __ldg(np + nxo), fx = __ldg(np + (1 - nxo));
-        const float4 ny = __ldg(np + nyo), fy = __ldg(np + (5 - nyo));
-        const float4 nz = __ldg(np + nzo), fz = __ldg(np + (9 - nzo));
-        const int4 rf = __ldg(reinterpret_cast<const int4*>(np + 6));
-        if (COUNT) cnt->nodes++;
-        float k0 = box_entry(r, nx.x, fx.x, ny.x, fy.x, nz.x, fz.x, tcur);
-        float k1 = box_entry(r, nx.y, fx.y, ny.y, fy.y, nz.y, fz.y, tcur);
-        float k2 = box_entry(r, nx.z, fx.z, ny.z, fy.z, nz.z, fz.z, tcur);
-        float k3 = box_entry(r, nx.w, fx.w, ny.w, fy.w, nz.w, fz.w, tcur);
-        int r0 = rf.x, r1 = rf.y, r2 = rf.z, r3 = rf.w;
-        // Ascending entry distance (sorting network for four keys).
-        cswap(k0, r0, k1, r1);
-        cswap(k2, r2, k3, r3);
-        cswap(k0, r0, k2, r2);
-        cswap(k1, r1, k3, r3);
-        cswap(k1, r1, k2, r2);
-        if (k1 != CUDART_INF_F) {
-          if (sp + 3 > STACK) { *err = 1; break; }
-          if (k3 != CUDART_INF_F) stack[sp++] = r3;
-          if (k2 != CUDART_INF_F) stack[sp++] = r2;
-          stack[sp++] = r1;
-        }
-        if (k0 != CUDART_INF_F) {
-          node = r0;
-          continue;
-        }
-      } else {
-        // Leaf.
-        uint32_t lv = ~uint32_t(node);
-        int64_t first = int64_t(lv >> 4), count = int64_t(lv & 15u) + 1;
-        for (int64_t k = first; k < first + count; ++k) {
-          const float4* rp = S.recs + 3 * k;
-          float4 a = __ldg(rp + 0), b = __ldg(rp + 1), c = __ldg(rp + 2);
-          if (COUNT) cnt->prims++;
-          int kind = __float_as_int(a.w);
-          int prim = __float_as_int(c.w);
-          if (ANY && prim == ignore_prim) continue;
-          int quad = kind == kRecTriangle ? __float_as_int(b.w) : 0;
-          // The first half of a quad may displace its own second half at any t.
-          bool displace = !ANY && quad == 1 && found && bestPrim == prim && bestQuad == 2;
-          float tlim = displace ? r.tmax : tcur;
-          float t, u = 0.f, v = 0.f;
-          bool hit;
-          if (kind == kRecTriangle) {
-            if (WT) hit = tri_test_wt(r, a, b, c, tlim, t, u, v);
-            else hit = tri_test_ref(r, a, b, c, tlim, t, u, v);
-          } else if (kind == kRecSphere) {
-            hit = sphere_test(r, a, b.x, tlim, t);
-          } else {
-            hit = pgram_test(r, a, b, c, tlim, t, u, v);
-          }
-          if (hit && found && !displace) {
-            // strictly closer, and a second half never displaces its first half
-            hit = t < tcur && !(quad == 2 && bestPrim == prim && bestQuad == 1);
-          }
-          if (hit) {
-            tcur = t; found = true; best = int32_t(k); bu = u; bv = v;
-            bestPrim = prim; bestQuad = quad;
-            if (ANY) break;
-          }
-        }
-        if (ANY && found) break;
-      }
-      if (sp == 0) break;
-      node = stack[--sp];
-    }
-  }
-  t_best = found ? tcur : CUDART_NAN_F;
-  u_best = bu; v_best = bv;
-  return best;
+  t_best = ts.found ? ts.tcur : CUDART_NAN_F;
+  u_best = ts.bu;
+  v_best = ts.bv;
+  return ts.best;
 }
 
 }  // namespace gbrt
