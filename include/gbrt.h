@@ -301,6 +301,22 @@ gbrt_status gbrt_render_device_noalloc(gbrt_scene* scene,
                                        float* d_film_bgr, double* d_sum,
                                        double* d_sumsq, gbrt_stats* stats);
 
+/* ---- output (Tonemapper::map, src/tonemapper.cpp:31-56; the --save-exr,
+ *      --save-img and --save-mat writers, src/main.cpp:223-265) ---------- */
+/* rgb: width x height x 3 bytes, RGB order: clamp(255 * c^(1/gamma)) per
+ * channel of the BGR film, truncated. Host buffers. */
+gbrt_status gbrt_tonemap(const float* film_bgr, int32_t width, int32_t height,
+                         float gamma, uint8_t* rgb);
+/* Device buffers, enqueued on stream (NULL: the context stream). */
+gbrt_status gbrt_tonemap_device(gbrt_ctx* ctx, const float* d_film_bgr,
+                                int32_t width, int32_t height, float gamma,
+                                uint8_t* d_rgb, void* stream);
+/* Writes a host film by file extension: .exr (OpenEXR, uncompressed float
+ * B,G,R), .pfm, .hdr (RGBE), .m (MATLAB function), or .png/.ppm/.bmp
+ * (8-bit, tonemapped with gamma). */
+gbrt_status gbrt_write_image(const char* path, const float* film_bgr,
+                             int32_t width, int32_t height, float gamma);
+
 /* ---- scene files (SceneGrammar::parse + resolveVars + buildScene,
  *      src/sceneparser.cpp:36-156, src/sceneast.cpp:673-747,
  *      src/objreader.cpp:142-366) --------------------------------------- */

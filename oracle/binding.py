@@ -40,6 +40,7 @@ def lib():
                                  C.c_int, P, P, P, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                  C.POINTER(C.c_uint64)]
         L.orc_camera_ray.argtypes = [C.POINTER(_abi.Camera), C.c_double, C.c_double, P]
+        L.orc_tonemap.argtypes = [P, C.c_int, C.c_int, C.c_float, P]
         L.orc_stream_u.restype = C.c_float
         L.orc_stream_u.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32]
         _lib = L
@@ -109,3 +110,11 @@ def camera_ray(camera, px, py):
 
 def stream_u(seed, sample_id, dim):
     return lib().orc_stream_u(seed, sample_id, dim)
+
+
+def tonemap(film, gamma=2.2):
+    """Tonemapper::map of a (H, W, 3) BGR film -> (H, W, 3) RGB uint8."""
+    film = np.ascontiguousarray(film, np.float32)
+    out = np.zeros(film.shape, np.uint8)
+    lib().orc_tonemap(_ptr(film), film.shape[1], film.shape[0], gamma, _ptr(out))
+    return out

@@ -1071,3 +1071,19 @@ float orc_stream_u(uint64_t seed, uint64_t sample_id, uint32_t dim) {
 }
 
 }  // extern "C"
+
+/* Tonemapper::map, src/tonemapper.cpp:31-56: RGB bytes of a BGR film. */
+extern "C" void orc_tonemap(const float* film, int w, int h, float gamma, unsigned char* rgb) {
+  double ig = 1. / gamma;
+  auto ch = [&](float c) -> unsigned char {
+    float x = float(255 * std::pow(double(c), ig));
+    if (!(x > 0)) return 0;
+    if (x >= 255) return 255;
+    return (unsigned char)int(x);
+  };
+  for (size_t i = 0; i < size_t(w) * h; ++i) {
+    rgb[3 * i] = ch(film[3 * i + 2]);
+    rgb[3 * i + 1] = ch(film[3 * i + 1]);
+    rgb[3 * i + 2] = ch(film[3 * i]);
+  }
+}

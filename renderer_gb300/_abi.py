@@ -118,6 +118,9 @@ SIGNATURES = [
                                      C.POINTER(Stats)]),
     ("gbrt_render_device_noalloc", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), P, P, P,
                                              C.POINTER(Stats)]),
+    ("gbrt_tonemap", C.c_int, [P, C.c_int32, C.c_int32, C.c_float, P]),
+    ("gbrt_tonemap_device", C.c_int, [P, P, C.c_int32, C.c_int32, C.c_float, P, P]),
+    ("gbrt_write_image", C.c_int, [C.c_char_p, P, C.c_int32, C.c_int32, C.c_float]),
     ("gbrt_parse_scene_file", C.c_int, [C.c_char_p, C.POINTER(P), C.c_char_p, C.c_int32]),
     ("gbrt_parse_scene_string", C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(P), C.c_char_p, C.c_int32]),
     ("gbrt_parsed_scene_desc", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(Camera),

@@ -164,3 +164,24 @@ def test_cancellation_flag(ctx):
     with pytest.raises(GbrtError) as e:
         r.render(stop_flag=flag)
     assert e.value.status == _abi.ERR_CANCELLED
+
+
+def test_gpu_tonemap_matches_oracle(ctx):
+    import ctypes
+
+    import torch
+
+    import renderer_gb300 as rg
+    from oracle.binding import tonemap as oracle_tonemap
+    rng = np.random.default_rng(2)
+    f = rng.uniform(0, 2, (123, 77, 3)).astype(np.float32)
+    f[0, 0] = (np.nan, -3, 1e9)
+    d = torch.from_numpy(f).cuda()
+    o = torch.zeros(f.shape, dtype=torch.uint8, device="cuda")
+    rg.check(rg.lib().gbrt_tonemap_device(ctx.handle, ctypes.c_void_p(d.data_ptr()), 77, 123, 2.2,
+                                          ctypes.c_void_p(o.data_ptr()), None))
+    torch.cuda.synchronize()
+    got = o.cpu().numpy()
+    ref = oracle_tonemap(f, 2.2)
+    diff = np.abs(got.astype(int) - ref.astype(int))
+    assert diff.max() <= 1 and (diff > 0).mean() < 1e-4   # pow(double) rounding at integer boundaries
