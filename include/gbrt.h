@@ -97,15 +97,17 @@ typedef enum gbrt_light_type {
   GBRT_LIGHT_AREA = 0,   /* AreaLight(origin,u,v,Le), src/arealight.cpp:31-118 */
   GBRT_LIGHT_POINT = 1,  /* PointLight(pos,I), src/pointlight.cpp:29-70        */
   GBRT_LIGHT_ENV = 2,    /* EnvironmentMap, src/environmentmap.cpp:16-108      */
-  GBRT_LIGHT_BLACK = 3   /* BlackLight (failed env map), src/blacklight.cpp:5-24 */
+  GBRT_LIGHT_BLACK = 3,  /* BlackLight (failed env map), src/blacklight.cpp:5-24 */
+  GBRT_LIGHT_CONE = 4    /* ConeLight(pos,dir,angle,I), src/conelight.cpp:31-60 */
 } gbrt_light_type;
 
 typedef struct gbrt_light {
   int32_t type;        /* gbrt_light_type                                  */
-  float origin[3];     /* area: corner; point: position                    */
-  float u[3];          /* area: first edge                                 */
-  float v[3];          /* area: second edge                                */
-  float intensity[3];  /* BGR; area: Le; point: I; env: coefficient        */
+  float origin[3];     /* area: corner; point / cone: position             */
+  float u[3];          /* area: first edge; cone: axis direction           */
+  float v[3];          /* area: second edge; cone: v[0] = opening angle    */
+                       /* (radians, measured from the axis)                */
+  float intensity[3];  /* BGR; area: Le; point / cone: I; env: coefficient */
 } gbrt_light;
 
 typedef enum gbrt_env_mapping {

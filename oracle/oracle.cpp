@@ -16,6 +16,7 @@
  *   Sphere + CSGObject::intersect   src/sphere.cpp:29-62, src/csgobject.cpp:25-44
  *   Plane                           src/plane.cpp:27-46
  *   AreaLight / PointLight          src/arealight.cpp:31-118, src/pointlight.cpp:29-70
+ *   ConeLight                       src/conelight.cpp:31-60
  *   EnvironmentMap / BlackLight     src/environmentmap.cpp:16-108, src/blacklight.cpp:5-24
  *   Materials                       src/darkmatter.cpp, src/abstractdiffusematerial.cpp,
  *                                   src/diffusematerial.cpp, src/mirrormaterial.cpp,
@@ -635,6 +636,22 @@ struct PointLight : Light {
   AABB bbox() const override { return AABB(V3(), V3()); }
 };
 
+/* ConeLight, src/conelight.cpp:31-60: a point light limited to a cone. */
+struct ConeLight : Light {
+  V3 loc, axis; float angle; C3 I;
+  ConeLight(V3 l, V3 a, float ang, C3 i) : loc(l), axis(a), angle(ang), I(i) {}
+  C3 intensity(const Hit& hit, V3& direction, const Intersectable& scene, const Sample&) const override {
+    V3 at = hit.point.affine();
+    direction = at - loc;
+    Hit sh = scene.intersect(Ray(at, -direction.normalized(), kEpsilon, direction.length() - kEpsilon));
+    float rayAngle = float(std::acos(double(dot(direction.normalized(), axis.normalized()))));
+    if (0 <= rayAngle && rayAngle <= angle && !sh.intersects()) return I * (1 / direction.lengthSquared());
+    return C3();
+  }
+  Hit intersect(const Ray&) const override { return Hit(); }
+  AABB bbox() const override { return AABB(V3(), V3()); }
+};
+
 /* BlackLight, src/blacklight.cpp:5-24. */
 struct BlackLight : Light {
   C3 intensity(const Hit&, V3&, const Intersectable&, const Sample&) const override { return C3(); }
@@ -752,6 +769,7 @@ static Scene* buildScene(const gbrt_scene_desc* d, bool useBVH) {
     Light* l = nullptr;
     if (L.type == GBRT_LIGHT_AREA) l = new AreaLight(vec3(L.origin), vec3(L.u), vec3(L.v), spec3(L.intensity));
     else if (L.type == GBRT_LIGHT_POINT) l = new PointLight(vec3(L.origin), spec3(L.intensity));
+    else if (L.type == GBRT_LIGHT_CONE) l = new ConeLight(vec3(L.origin), vec3(L.u), L.v[0], spec3(L.intensity));
     else if (L.type == GBRT_LIGHT_ENV && d->env && d->env->texels) {
       auto* e = new EnvironmentMap();
       e->W = d->env->width; e->H = d->env->height; e->mapping = d->env->mapping;

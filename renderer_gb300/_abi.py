@@ -86,7 +86,7 @@ STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "CANCELLED", 
 # gbrt_material_type
 MAT_DARK, MAT_DIFFUSE, MAT_MIRROR, MAT_PHONG, MAT_BLINN, MAT_TRANSPARENT = range(6)
 # gbrt_light_type
-LIGHT_AREA, LIGHT_POINT, LIGHT_ENV, LIGHT_BLACK = range(4)
+LIGHT_AREA, LIGHT_POINT, LIGHT_ENV, LIGHT_BLACK, LIGHT_CONE = range(5)
 # gbrt_env_mapping
 ENV_ANGULAR, ENV_LATLONG = range(2)
 # gbrt_semantics

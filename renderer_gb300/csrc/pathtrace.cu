@@ -264,10 +264,12 @@ __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, con
     sd = -normalize(dir);
     stmax = len(dir) - kEps;
     ignore = Lt.prim;
-  } else if (Lt.type == GBRT_LIGHT_POINT) {
+  } else if (Lt.type == GBRT_LIGHT_POINT || Lt.type == GBRT_LIGHT_CONE) {
     dir = vx.p - ld3(Lt.origin);
     float inv = 1.f / len2(dir);
     Le = v3(Lt.intensity[0] * inv, Lt.intensity[1] * inv, Lt.intensity[2] * inv);
+    // ConeLight::getIntensity (src/conelight.cpp:31-45): only inside the cone.
+    if (Lt.type == GBRT_LIGHT_CONE && !(acosf(dot(normalize(dir), ld3(Lt.nhat))) <= Lt.v[0])) return;
     sd = -normalize(dir);
     stmax = len(dir) - kEps;
   } else if (Lt.type == GBRT_LIGHT_ENV && S.env_light >= 0) {

@@ -169,7 +169,7 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   int envLights = 0;
   for (int i = 0; i < d->n_lights; ++i) {
     int ty = d->lights[i].type;
-    if (ty < GBRT_LIGHT_AREA || ty > GBRT_LIGHT_BLACK)
+    if (ty < GBRT_LIGHT_AREA || ty > GBRT_LIGHT_CONE)
       return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: unknown light type");
     if (ty == GBRT_LIGHT_ENV) {
       ++envLights;
@@ -247,6 +247,11 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
       boxes.push_back(boxOf({o, ou, ov, ouv}));
     } else if (L.type == GBRT_LIGHT_POINT) {
       if (!finite3(L.origin)) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: non-finite point light");
+    } else if (L.type == GBRT_LIGHT_CONE) {
+      if (!finite3(L.origin) || !finite3(L.u) || !std::isfinite(L.v[0]))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: non-finite cone light");
+      F3 ax = normalized(f3(L.u));
+      dl.nhat[0] = ax.x; dl.nhat[1] = ax.y; dl.nhat[2] = ax.z;  // unit axis
     } else if (L.type == GBRT_LIGHT_ENV) {
       envLight = i;
     }

@@ -15,9 +15,9 @@
 // Differences, for the GPU layout: instances are flattened by transforming
 // their primitives (a sphere needs a similarity transform); a pre-built
 // b(left, right, box) node contributes its children (the BVH is rebuilt);
-// box(min, max, m) becomes six quads; CSG operations, cone lights and texture
-// images are not part of the GPU path (texture materials fall back to a
-// diffuse material of their colour coefficient); an environment map that
+// box(min, max, m) becomes six quads; CSG operations and texture images are
+// not part of the GPU path (texture materials fall back to a diffuse material
+// of their colour coefficient); an environment map that
 // fails to load becomes a BlackLight, as in the renderer
 // (src/sceneast.cpp:598-610). As an extension, environmentmap("f", c,
 // "latlong") selects an equirectangular image.
@@ -981,7 +981,10 @@ struct Builder {
         g.u[0] = L.b.x; g.u[1] = L.b.y; g.u[2] = L.b.z;
         g.v[0] = L.c.x; g.v[1] = L.c.y; g.v[2] = L.c.z;
       } else if (L.kind == 2) {
-        throw ParseError(GBRT_ERR_UNSUPPORTED, "conelight is not part of the GPU path");
+        g.type = GBRT_LIGHT_CONE;
+        g.origin[0] = L.a.x; g.origin[1] = L.a.y; g.origin[2] = L.a.z;
+        g.u[0] = L.b.x; g.u[1] = L.b.y; g.u[2] = L.b.z;
+        g.v[0] = L.angle;
       } else {
         std::vector<float> tex;
         int W = 0, H = 0;

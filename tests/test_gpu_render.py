@@ -52,6 +52,22 @@ def test_point_light_closed_form(ctx):
     assert st.paths == 81 and st.nonfinite == 0
 
 
+def test_cone_light_closed_form(ctx):
+    """A cone light on a diffuse plane: inside the cone the sample is the
+    point-light value (same per-sample random numbers as the oracle)."""
+    s = SceneData()
+    m = s.add_material(_abi.MAT_DIFFUSE, kd=(0.5,) * 3)
+    s.planes = [((0, 1, 0, 0), m)]
+    s.lights = [dict(type=_abi.LIGHT_CONE, origin=(0, 2, 0), u=(0, -1, 0), v=(0.3, 0, 0), intensity=(4.0,) * 3)]
+    s.camera = dict(eye=(0, 5, 0.001), look_at=(0, 0, 0), up=(0, 0, -1), fov=0.5, width=17, height=17)
+    params = render_params(1, 1, 0.5, 5, 0)
+    (film, _, _), _ = gpu_render(ctx, s, params)
+    ref = OracleScene(s).render(s.camera_struct(), params, rng_mode=1)["film"]
+    inside = ref[..., 0] > 0
+    assert 0 < inside.sum() < inside.size
+    np.testing.assert_allclose(film, ref, rtol=1e-4, atol=1e-7)
+
+
 def test_env_furnace(ctx):
     s = SceneData()
     kd = 0.6

@@ -214,3 +214,19 @@ def test_cornell_box_reference_render_is_stable():
     b = o.render(s.camera_struct(), workloads.cornell_params(max_depth=8, seed=5), rng_mode=0, threads=2)
     np.testing.assert_array_equal(a["film"], b["film"])   # per-row streams: thread-count independent
     assert np.all(np.isfinite(a["film"])) and a["film"].min() >= 0
+
+
+def test_cone_light_is_a_point_light_inside_its_cone():
+    """ConeLight::getIntensity (src/conelight.cpp:31-45): I / r^2 when the angle
+    between (x - position) and the axis is within the opening angle, else 0."""
+    s = point_light_plane(width=17, height=17)
+    s.lights = [dict(type=_abi.LIGHT_CONE, origin=(0, 2, 0), u=(0, -1, 0), v=(0.3, 0, 0), intensity=(4.0,) * 3)]
+    o = OracleScene(s)
+    cam = s.camera_struct()
+    r = o.render(cam, render_params(1, 1, 0.5, 5, 0), rng_mode=1)
+    f = r["film"][..., 0]
+    ref = OracleScene(point_light_plane(width=17, height=17)).render(cam, render_params(1, 1, 0.5, 5, 0),
+                                                                      rng_mode=1)["film"][..., 0]
+    inside = f > 0
+    assert 0 < inside.sum() < f.size                       # the cone cuts the lit disc
+    np.testing.assert_array_equal(f[inside], ref[inside])  # inside it is exactly the point light

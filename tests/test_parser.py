@@ -161,3 +161,10 @@ def test_reads_the_shipped_angular_probe():
 def test_missing_environment_becomes_black_light():
     s = load_scene_string('lights = lights { environmentmap("does_not_exist.hdr", [1 1 1]) };')
     assert s.lights[0]["type"] == _abi.LIGHT_BLACK and s.env is None
+
+
+def test_cone_light_parses():
+    s = load_scene_string("lights = lights { conelight([0 2 0], [0 -1 0], 0.5, [1 2 3]) };")
+    L = s.lights[0]
+    assert L["type"] == _abi.LIGHT_CONE and L["u"] == pytest.approx((0, -1, 0)) and L["v"][0] == 0.5
+    np.testing.assert_allclose(L["intensity"], (3, 2, 1))
