@@ -159,7 +159,12 @@ typedef struct gbrt_camera {
 typedef enum gbrt_semantics {
   /* the renderer's estimator with all of its quirks */
   GBRT_SEM_REFERENCE = 0,
-  /* reserved: physically based estimator */
+  /* Physically based estimator; no counterpart in the renderer. Unbiased
+   * Russian roulette (survival 1 - termination_prob from the fourth vertex
+   * on), next-event estimation with the light-count factor combined with
+   * BSDF-sampled emission by the power heuristic, normalised modified
+   * Phong / Blinn lobes sampled with their own pdfs. Same scenes, same
+   * options; every light type and material the reference path accepts. */
   GBRT_SEM_PHYSICAL = 1
 } gbrt_semantics;
 

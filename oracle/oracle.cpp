@@ -939,6 +939,215 @@ static void drawPath(Draws& dr, int maxDepth, float p, int nLights, Rng* rng, ui
   }
 }
 
+
+/* ===================================================== physical semantics ==
+ * Not part of the renderer: the physically based estimator the GPU path
+ * offers as GBRT_SEM_PHYSICAL, restated here from the same specification to
+ * check it. Unbiased Russian roulette (survival 1 - p from the fourth vertex
+ * on), emission on direct view and on BSDF-sampled hits weighted by the power
+ * heuristic against next-event estimation (light chosen uniformly, with the
+ * light-count factor), modified Phong and Blinn with their sampling pdfs, the
+ * environment looked up in the direction the light arrives from, sampled
+ * uniformly over the sphere for NEE. Directions wo / wi point away from the
+ * surface; lobes are two-sided (the normal is flipped towards wo). Random
+ * numbers per vertex i: dims 2+8i lobe, +1/+2 BSDF direction, +3 light index,
+ * +4/+5 light sample, +6 roulette (dims 0/1: pixel jitter). */
+
+struct PhysBsdf {
+  int kind = -1;  /* 0 none, 1 diffuse, 2 phong, 3 blinn, 4 mirror, 5 glass */
+  C3 kd, ks;
+  float e = 0, ior = 1, pd = 1;
+};
+
+static PhysBsdf physOf(const Material* m) {
+  PhysBsdf b;
+  if (auto* d = dynamic_cast<const DiffuseMaterial*>(m)) { b.kind = 1; b.kd = d->color; }
+  else if (auto* ph = dynamic_cast<const PhongMaterial*>(m)) { b.kind = 2; b.kd = ph->color; b.ks = ph->spec; b.e = ph->e; }
+  else if (auto* bl = dynamic_cast<const BlinnMaterial*>(m)) { b.kind = 3; b.kd = bl->kd; b.ks = bl->ks; b.e = bl->e; }
+  else if (dynamic_cast<const MirrorMaterial*>(m)) b.kind = 4;
+  else if (auto* t = dynamic_cast<const TransparentMaterial*>(m)) { b.kind = 5; b.ior = t->k; }
+  else b.kind = 0;
+  if (b.kind == 2 || b.kind == 3) {
+    float rd = lum(b.kd), rs = lum(b.ks);
+    b.pd = (rd + rs) > 0 ? rd / (rd + rs) : 1.f;
+  }
+  return b;
+}
+
+static float cosPowerPdf(float c, float e) { return c > 0 ? float((e + 1) / (2 * M_PI) * std::pow(double(c), double(e))) : 0.f; }
+
+/* f(wo, wi) and pdf(wi) of a non-specular lobe; n faces wo. */
+static C3 physEval(const PhysBsdf& b, V3 n, V3 wo, V3 wi, float& pdf) {
+  pdf = 0;
+  float ci = dot(n, wi), co = dot(n, wo);
+  if (b.kind < 1 || b.kind > 3 || ci <= 0 || co <= 0) return C3();
+  C3 diff = b.kd * float(1 / M_PI);
+  if (b.kind == 1) { pdf = float(ci / M_PI); return diff; }
+  if (b.kind == 2) {
+    V3 r = 2 * co * n - wo;
+    float ca = std::max(0.f, dot(r, wi));
+    float sp = float((b.e + 2) / (2 * M_PI) * std::pow(double(ca), double(b.e)));
+    pdf = float(b.pd * ci / M_PI) + (1 - b.pd) * cosPowerPdf(ca, b.e);
+    return diff + b.ks * sp;
+  }
+  V3 h = (wi + wo).normalized();
+  float nh = dot(n, h), oh = dot(wo, h);
+  float D = float((b.e + 2) / (2 * M_PI) * std::pow(double(std::max(nh, 0.f)), double(b.e)));
+  float G = std::min(1.f, std::min(2 * nh * co / oh, 2 * nh * ci / oh));
+  pdf = float(b.pd * ci / M_PI) + (1 - b.pd) * (oh > 0 ? cosPowerPdf(nh, b.e) / (4 * oh) : 0.f);
+  return diff + b.ks * (D * G / (4 * ci * co));
+}
+
+/* Samples wi; returns f * |cos| / pdf in weight (or 1 for specular lobes). */
+static bool physSample(const PhysBsdf& b, V3 n, V3 wo, bool exiting, float u0, float u1, float u2, V3& wi, C3& weight,
+                       float& pdf, bool& specular) {
+  specular = false;
+  pdf = 0;
+  if (b.kind == 4) {
+    wi = 2 * dot(n, wo) * n - wo;
+    specular = true; weight = C3(1, 1, 1); pdf = 1;
+    return true;
+  }
+  if (b.kind == 5) {
+    /* n faces wo; leaving the medium the geometric normal points along the
+     * ray (TransparentMaterial's test, src/transparentmaterial.cpp:43-51). */
+    V3 d = -wo;
+    float ratio = exiting ? b.ior : 1 / b.ior;
+    float cosI = dot(-n, d);
+    float cc = cosI * cosI;
+    float sinO = float(ratio * std::sqrt(std::max(0., 1. - cc)));
+    float cosO = float(std::sqrt(std::max(0., 1 - (ratio * ratio) * std::max(0., 1. - cc))));
+    float rPerp = (cosI - ratio * cosO) / (cosI + ratio * cosO);
+    float rPara = (ratio * cosI - cosO) / (ratio * cosI + cosO);
+    float R = float(0.5 * (rPerp * rPerp + rPara * rPara));
+    if (sinO > 1 || u0 < R) wi = reflect(d, n);
+    else wi = ratio * d + (ratio * cosI - signum(cosI) * cosO) * n;
+    specular = true; weight = C3(1, 1, 1); pdf = 1;
+    return true;
+  }
+  if (b.kind < 1) return false;
+  Sample s(u1, u2);
+  float tmp;
+  if (b.kind == 1 || u0 < b.pd) {
+    wi = s.cosineDirection(n, tmp);
+  } else if (b.kind == 2) {
+    wi = s.cosinePowerDirection(2 * dot(n, wo) * n - wo, tmp, b.e);
+  } else {
+    V3 h = s.cosinePowerDirection(n, tmp, b.e);
+    wi = 2 * dot(wo, h) * h - wo;
+  }
+  C3 f = physEval(b, n, wo, wi, pdf);
+  if (!(pdf > 0)) return false;
+  weight = f * (dot(n, wi) / pdf);
+  return true;
+}
+
+static float powerHeuristic(float a, float b) { return a * a / (a * a + b * b); }
+
+struct PhysStats { uint64_t rays = 0, shadow = 0; };
+
+/* One camera sample under the physical estimator. u(dim) draws the numbers. */
+template <typename U>
+static C3 physRadiance(const Scene& s, const Ray& primary, int D, float p, U&& u, PhysStats& st) {
+  C3 Lsum, alpha(1, 1, 1);
+  Ray ray = primary;
+  float prevPdf = 0;
+  bool prevSpec = true;
+  const int nL = int(s.lights.size());
+  const float pChoose = nL > 0 ? 1.f / nL : 0.f;
+  for (int i = 0; i < D; ++i) {
+    Hit h = s.root->intersect(ray);
+    ++st.rays;
+    if (!h.intersects()) break;
+    const uint32_t base = 2 + 8 * uint32_t(i);
+    if (auto* al = dynamic_cast<const AreaLight*>(h.mat)) {
+      V3 dn = ray.d.normalized();
+      float cl = dot(-dn, al->normal.normalized());
+      if (cl > 0) {
+        float w = 1;
+        if (!prevSpec) {
+          float dist = h.t * ray.d.length();
+          float pl = pChoose * dist * dist / (cl * al->normal.length());
+          w = powerHeuristic(prevPdf, pl);
+        }
+        Lsum = Lsum + mul(alpha, al->Le) * w;
+      }
+      break;
+    }
+    if (auto* em = dynamic_cast<const EnvironmentMap*>(h.mat)) {
+      V3 dn = ray.d.normalized();
+      float w = prevSpec ? 1.f : powerHeuristic(prevPdf, float(pChoose / (4 * M_PI)));
+      Lsum = Lsum + mul(alpha, em->get(dn)) * w;
+      break;
+    }
+    PhysBsdf b = physOf(h.mat);
+    if (b.kind <= 0) break;
+    V3 x = h.point.affine();
+    V3 wo = -ray.d.normalized();
+    V3 n = h.normal.normalized();
+    bool flipped = dot(n, wo) < 0;
+    if (flipped) n = -n;
+    /* next-event estimation at non-specular vertices */
+    if (b.kind <= 3 && nL > 0) {
+      int li = std::min(int(double(u(base + 3)) * nL), nL - 1);
+      const Light* L = s.lights[li];
+      float lx = u(base + 4), ly = u(base + 5);
+      V3 wi; float dist = 0, pl = 0; C3 Le; bool delta = false; int ignore = -1;
+      bool ok = true;
+      if (auto* a = dynamic_cast<const AreaLight*>(L)) {
+        V3 y = a->origin + lx * a->u + ly * a->v;
+        V3 d = y - x;
+        dist = d.length();
+        wi = d.normalized();
+        float cl = dot(-wi, a->normal.normalized());
+        if (cl > 0) { Le = a->Le; pl = pChoose * dist * dist / (cl * a->normal.length()); }
+        else ok = false;
+        ignore = a->prim;
+      } else if (auto* pt = dynamic_cast<const PointLight*>(L)) {
+        V3 d = pt->loc - x; dist = d.length(); wi = d.normalized();
+        Le = pt->I * (1 / d.lengthSquared()); pl = pChoose; delta = true;
+      } else if (auto* cn = dynamic_cast<const ConeLight*>(L)) {
+        V3 d = cn->loc - x; dist = d.length(); wi = d.normalized();
+        float ang = float(std::acos(double(dot(-wi, cn->axis.normalized()))));
+        if (ang <= cn->angle) { Le = cn->I * (1 / d.lengthSquared()); pl = pChoose; delta = true; }
+        else ok = false;
+      } else if (auto* em = dynamic_cast<const EnvironmentMap*>(L)) {
+        wi = Sample(lx, ly).uniformSphere();
+        dist = kInf;
+        Le = em->get(wi);
+        pl = float(pChoose / (4 * M_PI));
+      } else ok = false;
+      if (ok && !Le.isZero()) {
+        float pb;
+        C3 f = physEval(b, n, wo, wi, pb);
+        float ci = std::fabs(dot(n, wi));
+        if (!f.isZero()) {
+          float w = delta ? 1.f : powerHeuristic(pl, pb);
+          C3 c = mul(mul(alpha, f), Le) * (ci * w / pl);
+          ++st.shadow;
+          Ray sr(x, wi, kEpsilon, std::isinf(dist) ? kInf : dist - kEpsilon);
+          tIgnorePrim = ignore;
+          Hit sh = s.root->intersect(sr);
+          tIgnorePrim = -1;
+          bool occluded = sh.intersects() && !std::isinf(sh.t);
+          if (!occluded) Lsum = Lsum + c;
+        }
+      }
+    }
+    /* continue the path */
+    V3 wi; C3 wgt; float pdf; bool spec;
+    if (!physSample(b, n, wo, flipped, u(base + 0), u(base + 1), u(base + 2), wi, wgt, pdf, spec)) break;
+    alpha = mul(alpha, wgt);
+    if (i + 1 >= 3 && p > 0) {
+      if (u(base + 6) < p) break;
+      alpha = alpha * (1 / (1 - p));
+    }
+    prevPdf = pdf;
+    prevSpec = spec;
+    ray = Ray(x, wi);
+  }
+  return Lsum;
+}
 }  // namespace orc
 
 /* ================================================================ C API == */
@@ -1050,10 +1259,21 @@ int orc_render(void* sp, const gbrt_camera* cam, const gbrt_render_params* prm, 
       int sidx = 0;
       for (auto& smp : samples) {
         Ray ray = camera.getRay(double(j) + smp.x, double(i) + smp.y);
-        drawPath(dr, D, p, int(s->lights.size()), rng.get(), rng ? 0 : keys[sidx]);
         uint64_t r = 0, sh = 0;
-        Path path = createPath(ray, *s->root, dr, D, rrPdf, rrStart, &r);
-        C3 c = integratePath(path, *s->root, s->lights, dr, &sh);
+        C3 c;
+        if (prm->semantics == GBRT_SEM_PHYSICAL) {
+          PhysStats ps;
+          uint64_t key = rng ? 0 : keys[sidx];
+          TausRng* tr = rng.get();
+          c = physRadiance(*s, ray, D, p, [&](uint32_t dim) -> float {
+            return tr ? float(tr->uniform()) : streamU(key, dim);
+          }, ps);
+          r = ps.rays; sh = ps.shadow;
+        } else {
+          drawPath(dr, D, p, int(s->lights.size()), rng.get(), rng ? 0 : keys[sidx]);
+          Path path = createPath(ray, *s->root, dr, D, rrPdf, rrStart, &r);
+          c = integratePath(path, *s->root, s->lights, dr, &sh);
+        }
         totRays += r; totShadow += sh; totPaths += 1;
         float inv = 1.f / spp;
         fB += c.b * inv; fG += c.g * inv; fR += c.r * inv;

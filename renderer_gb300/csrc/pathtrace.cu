@@ -60,6 +60,7 @@ struct PTParams {
   float rr_pdf;            // Russian-roulette compensation pdf
   float term_p;            // termination probability
   float inv_log1mp;        // 1 / log(1 - term_p), for the geometric draw
+  int physical;            // GBRT_SEM_PHYSICAL
 };
 
 // Path state, structure of arrays indexed by slot (path index - g0).
@@ -112,9 +113,10 @@ __global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
   float dx = x * P.cam.u[0] + y * P.cam.v[0] - P.cam.w[0];
   float dy = x * P.cam.u[1] + y * P.cam.v[1] - P.cam.w[1];
   float dz = x * P.cam.u[2] + y * P.cam.v[2] - P.cam.w[2];
-  // Path length: min(3 + Geometric(p), D) (src/renderer.cpp:52-61).
+  // Path length: min(3 + Geometric(p), D) (src/renderer.cpp:52-61). The
+  // physical estimator plays Russian roulette per vertex instead.
   int plen = P.D;
-  if (P.term_p > 0.f) {
+  if (P.term_p > 0.f && !P.physical) {
     int k = 0;
     if (P.term_p < 1.f) {
       // Geometric draw by inversion, floor(log(1 - u) / log(1 - p)). 1 - u is
@@ -132,7 +134,9 @@ __global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
   }
   st.alpha[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
   st.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-  st.ctl[slot] = make_int4(0, plen, 0, 0);
+  // ctl.w: reference semantics, "a stored vertex is pending"; physical
+  // semantics, "the previous vertex was specular (or the camera)".
+  st.ctl[slot] = make_int4(0, plen, 0, P.physical ? 1 : 0);
   st.ext[0][2 * slot] = make_float4(P.cam.eye[0], P.cam.eye[1], P.cam.eye[2], kEps);
   st.ext[0][2 * slot + 1] = make_float4(dx, dy, dz, CUDART_INF_F);
   st.ext_slot[0][slot] = slot;
@@ -448,6 +452,163 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
   }
 }
 
+// ------------------------------------------------------ shade, physical ----
+// GBRT_SEM_PHYSICAL: next-event estimation with one uniformly chosen light
+// (weighted by the light count), emission on BSDF-sampled hits, both combined
+// by the power heuristic; Russian roulette with survival 1 - p from the
+// fourth vertex on. Path state: alpha.xyz throughput, alpha.w the pdf of the
+// last BSDF sample, ctl = (vertex index, -, -, last vertex specular).
+__device__ __forceinline__ void nee_phys(const DeviceScene& S, const PTState& st, int slot, unsigned long long key,
+                                         unsigned base, const PhysBsdf& b, V3f x, V3f n, V3f wo, V3f alpha) {
+  const int nL = S.n_lights;
+  const float pChoose = 1.f / float(nL);
+  const int li = min(stream_index(key, base + 3, nL), nL - 1);
+  const DevLight& Lt = S.lights[li];
+  const float lx = stream_u(key, base + 4), ly = stream_u(key, base + 5);
+  V3f wi, Le;
+  float dist, pl;
+  bool delta = false;
+  int ignore = -1;
+  if (Lt.type == GBRT_LIGHT_AREA) {
+    V3f y = ld3(Lt.origin) + lx * ld3(Lt.u) + ly * ld3(Lt.v);
+    V3f d = y - x;
+    dist = len(d);
+    wi = normalize(d);
+    float cl = dot(-wi, ld3(Lt.nhat));
+    if (!(cl > 0.f)) return;
+    Le = ld3(Lt.intensity);
+    pl = pChoose * dist * dist / (cl * Lt.normal_len);
+    ignore = Lt.prim;
+  } else if (Lt.type == GBRT_LIGHT_POINT || Lt.type == GBRT_LIGHT_CONE) {
+    V3f d = ld3(Lt.origin) - x;
+    dist = len(d);
+    wi = normalize(d);
+    if (Lt.type == GBRT_LIGHT_CONE && !(acosf(dot(-wi, ld3(Lt.nhat))) <= Lt.v[0])) return;
+    float inv = 1.f / len2(d);
+    Le = inv * ld3(Lt.intensity);
+    pl = pChoose;
+    delta = true;
+  } else if (Lt.type == GBRT_LIGHT_ENV && S.env_light >= 0) {
+    wi = uniform_sphere(lx, ly);
+    dist = CUDART_INF_F;
+    Le = env_get(S, wi);
+    pl = pChoose * (0.25f * kInvPi);
+  } else {
+    return;
+  }
+  if (is_zero(Le)) return;
+  float pb;
+  V3f f = phys_eval(b, n, wo, wi, pb);
+  if (is_zero(f)) return;
+  float w = delta ? 1.f : power_heuristic(pl, pb);
+  float sc = fabsf(dot(n, wi)) * w / pl;
+  V3f c = v3(alpha.x * f.x * Le.x * sc, alpha.y * f.y * Le.y * sc, alpha.z * f.z * Le.z * sc);
+  if (is_zero(c)) return;
+  int e = agg_push(&st.counts[2]);
+  st.sh_ray[2 * e] = make_float4(x.x, x.y, x.z, kEps);
+  st.sh_ray[2 * e + 1] = make_float4(wi.x, wi.y, wi.z, isinf(dist) ? CUDART_INF_F : dist - kEps);
+  st.sh_c[e] = make_float4(c.x, c.y, c.z, __int_as_float(ignore));
+  st.sh_slot[e] = slot;
+}
+
+__global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P, PTState st, int cur) {
+  const int n = st.counts[cur];
+  const int nxt = cur ^ 1;
+  const float pChoose = S.n_lights > 0 ? 1.f / float(S.n_lights) : 0.f;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int slot = st.ext_slot[cur][q];
+    const RawHit h = st.hits[q];
+    const float4 ro = st.ext[cur][2 * q], rd = st.ext[cur][2 * q + 1];
+    const int4 c = st.ctl[slot];
+    const int i = c.x;
+    const bool prevSpec = c.w != 0;
+    const float4 a4 = st.alpha[slot];
+    const V3f alpha = v3(a4.x, a4.y, a4.z);
+    const float prevPdf = a4.w;
+    const V3f d = v3(rd.x, rd.y, rd.z);
+    const bool envHit = h.rec == -1 && S.env_light >= 0 && isinf(rd.w) && rd.w > 0.f;
+    if (h.rec == -1 && !envHit) continue;
+    if (envHit) {
+      V3f dn = normalize(d);
+      V3f Le = env_get(S, dn);
+      float w = prevSpec ? 1.f : power_heuristic(prevPdf, pChoose * (0.25f * kInvPi));
+      float4 L4 = st.L[slot];
+      L4.x += alpha.x * Le.x * w; L4.y += alpha.y * Le.y * w; L4.z += alpha.z * Le.z * w;
+      st.L[slot] = L4;
+      continue;
+    }
+    const V3f x = v3(ro.x, ro.y, ro.z) + h.t * d;
+    V3f nrm;
+    int mat = -1;
+    if (h.rec >= 0) {
+      const int4 m = __ldg(&S.meta[h.rec]);
+      const float4* rp = S.recs + 3 * int64_t(h.rec);
+      const float4 a = __ldg(rp);
+      const int kind = __float_as_int(a.w);
+      if (m.w >= 0) {
+        // An area light: emission on its front side (AreaLight is one-sided).
+        const DevLight& Lt = S.lights[m.w];
+        float dl = len(d);
+        float cl = dot(-(1.f / dl) * d, ld3(Lt.nhat));
+        if (cl > 0.f) {
+          float w = 1.f;
+          if (!prevSpec) {
+            float dist = h.t * dl;
+            w = power_heuristic(prevPdf, pChoose * dist * dist / (cl * Lt.normal_len));
+          }
+          float4 L4 = st.L[slot];
+          L4.x += alpha.x * Lt.intensity[0] * w;
+          L4.y += alpha.y * Lt.intensity[1] * w;
+          L4.z += alpha.z * Lt.intensity[2] * w;
+          st.L[slot] = L4;
+        }
+        continue;
+      }
+      mat = m.y;
+      if (kind == kRecTriangle) {
+        if (m.z >= 0) {
+          const float* nn = S.tri_nrm + 12 * int64_t(m.z);
+          float w0 = 1.f - h.u - h.v;
+          nrm = normalize(w0 * ld3(nn) + h.u * ld3(nn + 3) + h.v * ld3(nn + 6));
+        } else {
+          const float4 b = __ldg(rp + 1), cc = __ldg(rp + 2);
+          V3f p1 = v3(a.x, a.y, a.z), p2 = v3(b.x, b.y, b.z), p3 = v3(cc.x, cc.y, cc.z);
+          nrm = normalize(cross(p1 - p2, p1 - p3));
+        }
+      } else {
+        nrm = normalize(x - v3(a.x, a.y, a.z));  // sphere
+      }
+    } else {
+      const float4 pl = __ldg(&S.planes[-2 - h.rec]);
+      nrm = normalize(v3(pl.x, pl.y, pl.z));
+      mat = S.plane_meta[-2 - h.rec].y;
+    }
+    const PhysBsdf b = phys_bsdf(S.materials, mat);
+    if (b.kind <= 0) continue;
+    const unsigned long long key = stream_key(P.seed, P.g0 + (unsigned long long)slot);
+    const unsigned base = dim_phys(i);
+    const V3f wo = -normalize(d);
+    const bool flipped = dot(nrm, wo) < 0.f;
+    if (flipped) nrm = -nrm;
+    if (b.kind <= 3 && S.n_lights > 0) nee_phys(S, st, slot, key, base, b, x, nrm, wo, alpha);
+    V3f wi, wgt;
+    float pdf;
+    bool spec;
+    if (!phys_sample(b, nrm, wo, flipped, stream_u(key, base), stream_u(key, base + 1), stream_u(key, base + 2), wi,
+                     wgt, pdf, spec))
+      continue;
+    V3f na = mulc(alpha, wgt);
+    if (i + 1 >= 3 && P.term_p > 0.f) {
+      if (stream_u(key, base + 6) < P.term_p) continue;
+      na = (1.f / (1.f - P.term_p)) * na;
+    }
+    if (i + 1 >= P.D) continue;
+    st.alpha[slot] = make_float4(na.x, na.y, na.z, pdf);
+    st.ctl[slot] = make_int4(i + 1, c.y, 0, spec ? 1 : 0);
+    push_ext(st, nxt, slot, x, wi);
+  }
+}
+
 // --------------------------------------------------------- accumulate ----
 // One thread per pixel touched by the batch; samples of a pixel are
 // contiguous slots. FP64 sums; non-finite samples are counted and dropped.
@@ -540,6 +701,7 @@ static void init_params(PTParams& P, const gbrt_camera& cam, const gbrt_render_p
                      ? float(1.0 / std::log(1.0 - double(prm.termination_prob)))
                      : 0.f;
   P.idx32 = total <= 0xffffffffull ? 1 : 0;
+  P.physical = prm.semantics == GBRT_SEM_PHYSICAL ? 1 : 0;
 }
 
 struct Buffers {
@@ -566,8 +728,8 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   if (cam->width <= 0 || cam->height <= 0 || prm->x_samples <= 0 || prm->y_samples <= 0 || prm->max_depth <= 0 ||
       prm->max_depth > 64)
     return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render: bad camera or render parameters");
-  if (prm->semantics != GBRT_SEM_REFERENCE)
-    return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_render: only the reference semantics are implemented");
+  if (prm->semantics != GBRT_SEM_REFERENCE && prm->semantics != GBRT_SEM_PHYSICAL)
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render: unknown semantics");
   if (!(prm->termination_prob >= 0.f && prm->termination_prob <= 1.f))
     return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render: termination probability outside [0, 1]");
   cudaStream_t stream = ctx->stream;
@@ -614,6 +776,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kSh, kTraceBlock, 0);
   const int shadowGrid = std::max(1, per) * ctx->num_sms;
   const int shadeGrid = ctx->num_sms * 8;
+  auto kShade = P.physical ? k_shade_phys : k_shade;
   cudaEvent_t ev0, ev1;
   cudaEventCreate(&ev0);
   cudaEventCreate(&ev1);
@@ -639,7 +802,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
       if (timeK) mark();
       kExt<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
       if (timeK) mark();
-      k_shade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
+      kShade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
       if (timeK) mark();
       kSh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
       if (timeK) mark();
@@ -768,8 +931,8 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
     return fail(ctx, GBRT_ERR_INVALID_ARG,
                 "gbrt_render_device_noalloc: batch_paths exceeds the 65536-path (GBRT_NOALLOC_MAX_BATCH) "
                 "scratch of the no-allocation entry point");
-  if (prm->semantics != GBRT_SEM_REFERENCE)
-    return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_render_device_noalloc: only the reference semantics are implemented");
+  if (prm->semantics != GBRT_SEM_REFERENCE && prm->semantics != GBRT_SEM_PHYSICAL)
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_device_noalloc: unknown semantics");
   if (!(prm->termination_prob >= 0.f && prm->termination_prob <= 1.f))
     return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_device_noalloc: termination probability outside [0, 1]");
   const NoAllocLayout Lay = noalloc_layout();
@@ -828,6 +991,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kSh, kTraceBlock, 0);
   const int shadowGrid = std::max(1, per) * ctx->num_sms;
   const int shadeGrid = ctx->num_sms * 8;
+  auto kShade = P.physical ? k_shade_phys : k_shade;
   auto t0 = std::chrono::steady_clock::now();
   unsigned long long launches = 0;
   for (unsigned long long g0 = 0; g0 < total; g0 += (unsigned long long)B) {
@@ -838,7 +1002,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
     for (int it = 0; it < P.D; ++it) {
       int cur = it & 1;
       kExt<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
-      k_shade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
+      kShade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
       kSh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
       launches += 3;
     }

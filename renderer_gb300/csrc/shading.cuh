@@ -251,4 +251,125 @@ __device__ __forceinline__ V3f env_get(const DeviceScene& S, V3f d) {
   return v3(__ldg(p) * S.env_coef[0], __ldg(p + 1) * S.env_coef[1], __ldg(p + 2) * S.env_coef[2]);
 }
 
+// ------------------------------------------------ physical semantics -----
+// GBRT_SEM_PHYSICAL (not part of the renderer): modified Phong and Blinn with
+// their sampling pdfs, perfect mirror and Fresnel-weighted glass. wo / wi
+// point away from the surface, n faces wo (lobes are two-sided).
+struct PhysBsdf {
+  int kind;  // 0 none, 1 diffuse, 2 phong, 3 blinn, 4 mirror, 5 glass
+  V3f kd, ks;
+  float e, ior, pd;
+};
+
+__device__ __forceinline__ PhysBsdf phys_bsdf(const DevMaterial* mats, int mat) {
+  PhysBsdf b;
+  b.kind = 0; b.e = 0.f; b.ior = 1.f; b.pd = 1.f;
+  b.kd = v3(0.f, 0.f, 0.f); b.ks = v3(0.f, 0.f, 0.f);
+  if (mat < 0) return b;
+  const DevMaterial& m = mats[mat];
+  b.kd = ld3(m.kd); b.ks = ld3(m.ks); b.e = m.exponent; b.ior = m.ior;
+  switch (m.type) {
+    case kMatDiffuse: b.kind = 1; break;
+    case kMatPhong: b.kind = 2; break;
+    case kMatBlinn: b.kind = 3; break;
+    case kMatMirror: b.kind = 4; break;
+    case kMatTransparent: b.kind = 5; break;
+    default: b.kind = 0;
+  }
+  if (b.kind == 2 || b.kind == 3) {
+    float s = m.rho_d + m.rho_s;
+    b.pd = s > 0.f ? m.rho_d / s : 1.f;
+  }
+  return b;
+}
+
+__device__ __forceinline__ float cos_power_pdf(float c, float e) {
+  return c > 0.f ? (e + 1.f) * (0.5f * kInvPi) * powf(c, e) : 0.f;
+}
+
+// f(wo, wi) and the pdf of sampling wi, for the non-specular kinds.
+__device__ __forceinline__ V3f phys_eval(const PhysBsdf& b, V3f n, V3f wo, V3f wi, float& pdf) {
+  pdf = 0.f;
+  float ci = dot(n, wi), co = dot(n, wo);
+  if (b.kind < 1 || b.kind > 3 || ci <= 0.f || co <= 0.f) return v3(0.f, 0.f, 0.f);
+  V3f diff = kInvPi * b.kd;
+  if (b.kind == 1) {
+    pdf = ci * kInvPi;
+    return diff;
+  }
+  if (b.kind == 2) {
+    V3f r = (2.f * co) * n - wo;
+    float ca = fmaxf(0.f, dot(r, wi));
+    float sp = (b.e + 2.f) * (0.5f * kInvPi) * powf(ca, b.e);
+    pdf = b.pd * ci * kInvPi + (1.f - b.pd) * cos_power_pdf(ca, b.e);
+    return diff + sp * b.ks;
+  }
+  V3f h = normalize(wi + wo);
+  float nh = dot(n, h), oh = dot(wo, h);
+  float D = (b.e + 2.f) * (0.5f * kInvPi) * powf(fmaxf(nh, 0.f), b.e);
+  float G = fminf(1.f, fminf(2.f * nh * co / oh, 2.f * nh * ci / oh));
+  pdf = b.pd * ci * kInvPi + (1.f - b.pd) * (oh > 0.f ? cos_power_pdf(nh, b.e) / (4.f * oh) : 0.f);
+  return diff + (D * G / (4.f * ci * co)) * b.ks;
+}
+
+// Samples wi; weight = f * |cos| / pdf (1 for the specular kinds).
+__device__ __forceinline__ bool phys_sample(const PhysBsdf& b, V3f n, V3f wo, bool exiting, float u0, float u1,
+                                            float u2, V3f& wi, V3f& weight, float& pdf, bool& specular) {
+  specular = false;
+  pdf = 0.f;
+  if (b.kind == 4) {
+    wi = (2.f * dot(n, wo)) * n - wo;
+    specular = true; weight = v3(1.f, 1.f, 1.f); pdf = 1.f;
+    return true;
+  }
+  if (b.kind == 5) {
+    // Leaving the medium the geometric normal points along the ray
+    // (TransparentMaterial's test, src/transparentmaterial.cpp:43-51).
+    V3f d = -wo;
+    float ratio = exiting ? b.ior : 1.f / b.ior;
+    float cosI = dot(-n, d);
+    float s2 = fmaxf(0.f, 1.f - cosI * cosI);
+    float sinO = ratio * sqrtf(s2);
+    float cosO = sqrtf(fmaxf(0.f, 1.f - ratio * ratio * s2));
+    float rPerp = (cosI - ratio * cosO) / (cosI + ratio * cosO);
+    float rPara = (ratio * cosI - cosO) / (ratio * cosI + cosO);
+    float R = 0.5f * (rPerp * rPerp + rPara * rPara);
+    if (sinO > 1.f || u0 < R) wi = reflect(d, n);
+    else wi = ratio * d + (ratio * cosI - float(signum(cosI)) * cosO) * n;
+    specular = true; weight = v3(1.f, 1.f, 1.f); pdf = 1.f;
+    return true;
+  }
+  if (b.kind < 1) return false;
+  float tmp;
+  if (b.kind == 1 || u0 < b.pd) {
+    wi = cosine_power_dir(n, u1, u2, 1.f, tmp);
+  } else if (b.kind == 2) {
+    wi = cosine_power_dir((2.f * dot(n, wo)) * n - wo, u1, u2, b.e, tmp);
+  } else {
+    V3f h = cosine_power_dir(n, u1, u2, b.e, tmp);
+    wi = (2.f * dot(wo, h)) * h - wo;
+  }
+  V3f f = phys_eval(b, n, wo, wi, pdf);
+  if (!(pdf > 0.f)) return false;
+  weight = (dot(n, wi) / pdf) * f;
+  return true;
+}
+
+__device__ __forceinline__ float power_heuristic(float a, float b) { return a * a / (a * a + b * b); }
+
+// Uniform direction on the sphere (Sample::getUniformSphereDirection,
+// src/sampler.cpp:78-86).
+__device__ __forceinline__ V3f uniform_sphere(float ux, float uy) {
+  float z = 2.f * ux - 1.f;
+  float f = sqrtf(fmaxf(0.f, 1.f - z * z));
+  float sn, cs;
+  sincospif(2.f * uy, &sn, &cs);
+  return v3(f * cs, f * sn, z);
+}
+
+// Dimension layout of the physical estimator: per vertex i, base 2 + 8i:
+// +0 lobe, +1/+2 BSDF direction, +3 light index, +4/+5 light sample, +6
+// roulette (dims 0/1: pixel jitter).
+__device__ __forceinline__ unsigned dim_phys(int i) { return 2u + 8u * unsigned(i); }
+
 }  // namespace gbrt

@@ -201,3 +201,65 @@ def test_gpu_tonemap_matches_oracle(ctx):
     ref = oracle_tonemap(f, 2.2)
     diff = np.abs(got.astype(int) - ref.astype(int))
     assert diff.max() <= 1 and (diff > 0).mean() < 1e-4   # pow(double) rounding at integer boundaries
+
+
+# ------------------------------------------------------- physical semantics
+def phys(x=8, y=8, D=8, seed=0, p=0.5):
+    return render_params(x, y, p, D, seed, semantics=_abi.SEM_PHYSICAL)
+
+
+def test_physical_closed_forms(ctx):
+    from tests.test_oracle import area_light_scene, footprint_lambert
+    s = area_light_scene()
+    (film, _, _), st = gpu_render(ctx, s, phys(32, 32, 4, 1))
+    assert film.mean() == pytest.approx(footprint_lambert(s), rel=0.01)
+    s = SceneData()
+    m = s.add_material(_abi.MAT_DIFFUSE, kd=(0.6,) * 3)
+    s.planes = [((0, 1, 0, 0), m)]
+    s.env = np.ones((16, 16, 3), np.float32)
+    s.lights = [dict(type=_abi.LIGHT_ENV, intensity=(1, 1, 1))]
+    s.camera = dict(eye=(0, 5, 0.001), look_at=(0, 0, 0), up=(0, 0, -1), fov=0.5, width=64, height=64)
+    (film, _, _), _ = gpu_render(ctx, s, phys(8, 8, 8, 5))
+    assert film.mean() == pytest.approx(0.6, rel=0.005)
+
+
+def test_physical_path_level_parity(ctx):
+    s = workloads.cornell_box(48, 48)
+    path_level(ctx, s, phys(4, 4, 8, 2), min_frac=0.97)
+
+
+def test_physical_path_level_parity_materials(ctx):
+    s = SceneData()
+    floor = s.add_material(_abi.MAT_DIFFUSE, kd=(0.4, 0.5, 0.6))
+    blinn = s.add_material(_abi.MAT_BLINN, kd=(0.3, 0.2, 0.1), ks=(0.4, 0.4, 0.4), exponent=60)
+    phong = s.add_material(_abi.MAT_PHONG, kd=(0.2, 0.5, 0.2), ks=(0.3, 0.3, 0.3), exponent=20)
+    mirror = s.add_material(_abi.MAT_MIRROR)
+    glass = s.add_material(_abi.MAT_TRANSPARENT, ior=1.5)
+    s.planes = [((0, 1, 0, 0), floor)]
+    s.spheres = [((-1.5, 0.5, 0), 0.5, blinn), ((-0.5, 0.5, 0), 0.5, phong), ((0.5, 0.5, 0), 0.5, mirror),
+                 ((1.5, 0.5, 0), 0.5, glass)]
+    rng = np.random.default_rng(4)
+    s.env = rng.uniform(0.2, 1.0, (32, 32, 3)).astype(np.float32)
+    s.lights = [dict(type=_abi.LIGHT_ENV, intensity=(1, 1, 1)),
+                dict(type=_abi.LIGHT_POINT, origin=(0, 3, 2), intensity=(5, 5, 5)),
+                dict(type=_abi.LIGHT_AREA, origin=(-1, 3, -1), u=(2, 0, 0), v=(0, 0, 2), intensity=(4, 4, 4))]
+    s.camera = dict(eye=(0, 1.5, 5), look_at=(0, 0.5, 0), up=(0, 1, 0), fov=0.8, width=64, height=48)
+    path_level(ctx, s, phys(4, 4, 8, 9), min_frac=0.97)
+
+
+def test_physical_statistical_parity(ctx):
+    s = workloads.cornell_box(48, 48)
+    params = phys(8, 8, 8, 3)
+    (film, gs, gq), _ = gpu_render(ctx, s, params)
+    o = OracleScene(s).render(s.camera_struct(), params, rng_mode=0)
+    N = 64
+    ma, mb = gs / N, o["sum"] / N
+    va = np.maximum(gq / N - ma ** 2, 0) * N / (N - 1)
+    vb = np.maximum(o["sumsq"] / N - mb ** 2, 0) * N / (N - 1)
+    se = np.sqrt(va / N + vb / N)
+    ok = se > 0
+    z = (ma - mb)[ok] / se[ok]
+    bound = sst.binom.ppf(1 - 1e-6, z.size, 2 * sst.norm.sf(4.0)) + 5
+    assert (np.abs(z) > 4).sum() <= bound
+    assert abs(z.mean()) < 0.05
+    assert abs(ma.mean() - mb.mean()) / mb.mean() < 0.01

@@ -230,3 +230,71 @@ def test_cone_light_is_a_point_light_inside_its_cone():
     inside = f > 0
     assert 0 < inside.sum() < f.size                       # the cone cuts the lit disc
     np.testing.assert_array_equal(f[inside], ref[inside])  # inside it is exactly the point light
+
+
+# ------------------------------------------------------- physical semantics
+def phys(x=8, y=8, D=8, seed=0, p=0.5):
+    return render_params(x, y, p, D, seed, semantics=_abi.SEM_PHYSICAL)
+
+
+def lambert_irradiance(x, n, verts, Le):
+    """Irradiance at x (normal n) from a uniform polygonal emitter (Lambert)."""
+    E = 0.0
+    v = [(np.asarray(p, float) - x) / np.linalg.norm(np.asarray(p, float) - x) for p in verts]
+    for i in range(len(v)):
+        a, b = v[i], v[(i + 1) % len(v)]
+        c = np.cross(a, b)
+        E += math.acos(np.clip(a @ b, -1, 1)) * (n @ c) / np.linalg.norm(c)
+    return abs(E) * Le / 2
+
+
+def area_light_scene(kd=0.5, Le=3.0, width=4, fov=0.02):
+    s = SceneData()
+    m = s.add_material(_abi.MAT_DIFFUSE, kd=(kd,) * 3)
+    s.planes = [((0, 1, 0, 0), m)]
+    s.lights = [dict(type=_abi.LIGHT_AREA, origin=(-0.5, 1, -0.5), u=(1, 0, 0), v=(0, 0, 1), intensity=(Le,) * 3)]
+    s.camera = dict(eye=(0, 0.5, 3), look_at=(0.2, 0, 0.1), up=(0, 1, 0), fov=fov, width=width, height=width)
+    return s
+
+
+def test_physical_furnace():
+    s = SceneData()
+    m = s.add_material(_abi.MAT_DIFFUSE, kd=(0.6,) * 3)
+    s.planes = [((0, 1, 0, 0), m)]
+    s.env = np.ones((16, 16, 3), np.float32)
+    s.lights = [dict(type=_abi.LIGHT_ENV, intensity=(1, 1, 1))]
+    s.camera = dict(eye=(0, 5, 0.001), look_at=(0, 0, 0), up=(0, 0, -1), fov=0.5, width=32, height=32)
+    r = OracleScene(s).render(s.camera_struct(), phys(8, 8, 8, 3), rng_mode=0)
+    assert r["film"].mean() == pytest.approx(0.6, rel=0.01)
+
+
+def test_physical_area_light_matches_lambert_formula():
+    s = area_light_scene()
+    r = OracleScene(s).render(s.camera_struct(), phys(32, 32, 4, 1), rng_mode=0)
+    assert r["film"].mean() == pytest.approx(footprint_lambert(s), rel=0.01)
+
+
+def footprint_lambert(s, kd=0.5, Le=3.0, per_pixel=10):
+    """Image mean of the area-light scene: kd/pi * E averaged over the points
+    of the floor the camera's rays reach (the view is grazing, so a pixel
+    covers a strip of the floor over which E changes by several percent)."""
+    from oracle.binding import camera_ray
+    cam = s.camera_struct()
+    verts = [(-0.5, 1, -0.5), (0.5, 1, -0.5), (0.5, 1, 0.5), (-0.5, 1, 0.5)]
+    w = s.camera["width"]
+    grid = (np.arange(w * per_pixel) + 0.5) / per_pixel
+    vals = []
+    for py in grid:
+        for px in grid:
+            ray = camera_ray(cam, px, py)
+            o, d = np.array(ray["org"], float), np.array(ray["dir"], float)
+            vals.append(lambert_irradiance(o - o[1] / d[1] * d, np.array([0, 1.0, 0]), verts, Le))
+    return kd / math.pi * float(np.mean(vals))
+
+
+def test_physical_direct_view_of_area_light_is_Le():
+    s = SceneData()
+    s.lights = [dict(type=_abi.LIGHT_AREA, origin=(-1, -1, 0), u=(2, 0, 0), v=(0, 2, 0), intensity=(3, 2, 1))]
+    s.camera = dict(eye=(0, 0, 1), look_at=(0, 0, 0), up=(0, 1, 0), fov=0.1, width=3, height=3)
+    r = OracleScene(s).render(s.camera_struct(), phys(1, 1), rng_mode=1)
+    np.testing.assert_allclose(r["film"].reshape(-1, 3), np.tile([3, 2, 1], (9, 1)), rtol=1e-6)
