@@ -244,6 +244,9 @@ gbrt_status gbrt_scene_destroy(gbrt_scene* scene);
 gbrt_status gbrt_scene_info(const gbrt_scene* scene, int64_t* n_nodes,
                             int64_t* n_leaves, int32_t* max_depth,
                             double* sah_cost, double* build_ms);
+/* Box of the scene's bounded primitives (planes excluded): lo.xyz, hi.xyz.
+ * (No counterpart in the renderer; the guide normalises positions by it.) */
+gbrt_status gbrt_scene_bounds(const gbrt_scene* scene, float bounds[6]);
 
 /* ---- ray queries (batched Intersectable::intersect, src/intersectable.h:40;
  *      BVHNode::intersect, src/bvh.cpp:135-149) ------------------------- */
@@ -323,6 +326,86 @@ gbrt_status gbrt_tonemap_device(gbrt_ctx* ctx, const float* d_film_bgr,
  * (8-bit, tonemapped with gamma). */
 gbrt_status gbrt_write_image(const char* path, const float* film_bgr,
                              int32_t width, int32_t height, float gamma);
+
+/* ---- neural path guiding. No counterpart in the renderer, whose
+ *      integrators sample the BSDF only (src/unidipathtracingintegrator.cpp:
+ *      34-46); used with the physical estimator. ---------------------------
+ * The guide is an MLP 208 -> 64 -> 64 -> 64 -> 40 (ReLU, no biases) on a
+ * frequency encoding of the position (normalised by bounds) and normal and a
+ * one-blob encoding of the outgoing direction; its output is a mixture of 8
+ * von Mises-Fisher lobes. Products run in BF16 on the tensor cores with FP32
+ * accumulation; FP32 master weights and Adam state live on the device. */
+typedef struct gbrt_guide gbrt_guide;
+/* Parameters: row-major [out][in] matrices W1 64x208, W2 64x64, W3 64x64,
+ * W4 40x64, concatenated. */
+#define GBRT_GUIDE_PARAMS 24064
+/* One network input: point, normal facing the viewer, outgoing direction. */
+#define GBRT_GUIDE_INPUT 9
+/* One mixture: lobe weights [8], then (mean x, y, z, kappa) for each lobe. */
+#define GBRT_GUIDE_OUTPUT 40
+/* One training sample: point, normal, outgoing direction, sampled incident
+ * direction, weight = target / pdf (loss = -mean(weight * log q(direction))). */
+#define GBRT_GUIDE_SAMPLE 13
+
+gbrt_status gbrt_guide_create(gbrt_ctx* ctx, const float bounds[6],
+                              uint64_t seed, gbrt_guide** out);
+gbrt_status gbrt_guide_destroy(gbrt_guide* guide);
+gbrt_status gbrt_guide_get_weights(gbrt_guide* guide, float* weights,
+                                   size_t n);
+/* Also resets the optimizer state and marks the guide usable by renders. */
+gbrt_status gbrt_guide_set_weights(gbrt_guide* guide, const float* weights,
+                                   size_t n);
+/* Host arrays: inputs n x GBRT_GUIDE_INPUT -> mixtures n x GBRT_GUIDE_OUTPUT. */
+gbrt_status gbrt_guide_eval(gbrt_guide* guide, const float* inputs, size_t n,
+                            float* mixtures);
+/* Gradient of the loss over n host samples (n x GBRT_GUIDE_SAMPLE) into grad
+ * (GBRT_GUIDE_PARAMS floats); the weights are not changed. */
+gbrt_status gbrt_guide_gradient(gbrt_guide* guide, const float* samples,
+                                size_t n, float* grad, float* loss);
+/* One Adam step (beta 0.9 / 0.999) on n host samples. */
+gbrt_status gbrt_guide_train_step(gbrt_guide* guide, const float* samples,
+                                  size_t n, float learning_rate, float* loss);
+
+typedef struct gbrt_guide_params {
+  float guide_fraction;   /* probability of sampling the guide at a
+                             non-specular vertex (one-sample MIS), e.g. 0.5 */
+  int32_t passes;         /* passes of x_samples * y_samples per pixel;
+                             0 = until time_budget_ms is spent */
+  int32_t train_passes;   /* the first train_passes passes record samples and
+                             are each followed by steps_per_pass Adam steps */
+  int32_t steps_per_pass;
+  int32_t batch_samples;  /* training samples per step, e.g. 2^18 */
+  float learning_rate;    /* e.g. 1e-2 */
+  float time_budget_ms;   /* > 0 with passes = 0: equal-time rendering */
+  int32_t flags;          /* 0 */
+} gbrt_guide_params;
+
+typedef struct gbrt_guide_stats {
+  int32_t passes;
+  int32_t train_steps;
+  uint64_t paths;
+  uint64_t train_samples;
+  uint64_t extension_rays;
+  uint64_t shadow_rays;
+  uint64_t nonfinite;
+  double total_ms;        /* device time of the whole call, training included */
+  double train_ms;
+  float last_loss;
+  int32_t pad;
+} gbrt_guide_stats;
+
+/* Renders with the physical estimator (params->semantics must be
+ * GBRT_SEM_PHYSICAL) in passes, the film (host, H x W x 3 BGR) being the
+ * mean over the passes. A non-specular vertex samples the guide with
+ * probability guide_fraction once the guide is trained or given weights, and
+ * the BSDF otherwise; both densities enter the path weight and the MIS
+ * weights of emission and next-event estimation, so the estimator stays
+ * unbiased whatever the network predicts. guide = NULL (or guide_fraction 0)
+ * renders the same passes with BSDF sampling only. */
+gbrt_status gbrt_render_guided(gbrt_scene* scene, const gbrt_camera* camera,
+                               const gbrt_render_params* params,
+                               gbrt_guide* guide, const gbrt_guide_params* gp,
+                               float* film_bgr, gbrt_guide_stats* stats);
 
 /* ---- scene files (SceneGrammar::parse + resolveVars + buildScene,
  *      src/sceneparser.cpp:36-156, src/sceneast.cpp:673-747,

@@ -69,6 +69,19 @@ class Stats(C.Structure):
                 ("nodes_any", C.c_uint64), ("prims_any", C.c_uint64)]
 
 
+class GuideParams(C.Structure):
+    _fields_ = [("guide_fraction", C.c_float), ("passes", C.c_int32), ("train_passes", C.c_int32),
+                ("steps_per_pass", C.c_int32), ("batch_samples", C.c_int32), ("learning_rate", C.c_float),
+                ("time_budget_ms", C.c_float), ("flags", C.c_int32)]
+
+
+class GuideStats(C.Structure):
+    _fields_ = [("passes", C.c_int32), ("train_steps", C.c_int32), ("paths", C.c_uint64),
+                ("train_samples", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("nonfinite", C.c_uint64), ("total_ms", C.c_double), ("train_ms", C.c_double),
+                ("last_loss", C.c_float), ("pad", C.c_int32)]
+
+
 class Ray(C.Structure):
     _fields_ = [("org", F3), ("tmin", C.c_float), ("dir", F3), ("tmax", C.c_float)]
 
@@ -95,6 +108,7 @@ SEM_REFERENCE, SEM_PHYSICAL = range(2)
 SCENE_WATERTIGHT = 1
 RENDER_TIME_KERNELS, RENDER_COUNT_TRAVERSAL = 1, 2
 NOALLOC_MAX_BATCH = 65536
+GUIDE_PARAMS, GUIDE_INPUT, GUIDE_OUTPUT, GUIDE_SAMPLE = 24064, 9, 40, 13
 
 P = C.c_void_p
 
@@ -108,6 +122,7 @@ SIGNATURES = [
     ("gbrt_scene_destroy", C.c_int, [P]),
     ("gbrt_scene_info", C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                   C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("gbrt_scene_bounds", C.c_int, [P, C.POINTER(C.c_float)]),
     ("gbrt_trace_closest", C.c_int, [P, P, C.c_int64, P]),
     ("gbrt_trace_any", C.c_int, [P, P, P, C.c_int64, P]),
     ("gbrt_trace_closest_device", C.c_int, [P, P, C.c_int64, P, P]),
@@ -121,6 +136,15 @@ SIGNATURES = [
     ("gbrt_tonemap", C.c_int, [P, C.c_int32, C.c_int32, C.c_float, P]),
     ("gbrt_tonemap_device", C.c_int, [P, P, C.c_int32, C.c_int32, C.c_float, P, P]),
     ("gbrt_write_image", C.c_int, [C.c_char_p, P, C.c_int32, C.c_int32, C.c_float]),
+    ("gbrt_guide_create", C.c_int, [P, C.POINTER(C.c_float), C.c_uint64, C.POINTER(P)]),
+    ("gbrt_guide_destroy", C.c_int, [P]),
+    ("gbrt_guide_get_weights", C.c_int, [P, P, C.c_size_t]),
+    ("gbrt_guide_set_weights", C.c_int, [P, P, C.c_size_t]),
+    ("gbrt_guide_eval", C.c_int, [P, P, C.c_size_t, P]),
+    ("gbrt_guide_gradient", C.c_int, [P, P, C.c_size_t, P, C.POINTER(C.c_float)]),
+    ("gbrt_guide_train_step", C.c_int, [P, P, C.c_size_t, C.c_float, C.POINTER(C.c_float)]),
+    ("gbrt_render_guided", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), P, C.POINTER(GuideParams),
+                                     P, C.POINTER(GuideStats)]),
     ("gbrt_parse_scene_file", C.c_int, [C.c_char_p, C.POINTER(P), C.c_char_p, C.c_int32]),
     ("gbrt_parse_scene_string", C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(P), C.c_char_p, C.c_int32]),
     ("gbrt_parsed_scene_desc", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(Camera),

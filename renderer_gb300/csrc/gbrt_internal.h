@@ -32,6 +32,7 @@ struct gbrt_scene {
   double sah_cost = 0;
   double build_ms = 0;
   int32_t n_prims = 0;  // primitive ids in use
+  float bounds[6] = {0, 0, 0, 0, 0, 0};  // box of the bounded primitives: lo.xyz, hi.xyz
 };
 
 namespace gbrt {

@@ -1,0 +1,697 @@
+// guide.cu — neural path guiding: fused tcgen05 kernels for the network's
+// inference and training, Adam, and the gbrt_guide_* entry points.
+//
+// No counterpart in the renderer (its integrators sample the BSDF only,
+// src/unidipathtracingintegrator.cpp:34-46); the network and its loss are
+// those of neural path guiding: a small MLP maps (position, normal,
+// outgoing direction) to a mixture of von Mises-Fisher lobes, trained online
+// by minimising the KL divergence from the incident-radiance distribution,
+// estimated by the tracer's own radiance samples:
+//   loss = -(1/N) sum_s w_s log q(wi_s),   w_s = target_s / pdf_s.
+//
+// Both kernels process tiles of 128 rows, one row per thread of a 128-thread
+// block. Per layer: the threads write the layer input (BF16) into shared
+// memory; one thread issues the tcgen05.mma chain (M = 128, N = layer width,
+// K in steps of 16) into TMEM and commits it to an mbarrier; after the wait
+// every warp reads its 32 TMEM lanes back (tcgen05.ld 32x32b), applies the
+// activation and writes the next layer's input.
+//
+// Training keeps, for the backward pass, the hidden activations both row-wise
+// (for the next layer's product) and transposed (batch-contiguous, for the
+// weight gradients), and computes every product as a K-major A times a
+// K-major B^T:
+//   dX_l   = delta_{l+1} W_{l+1}           A = delta rows, B = W^T
+//   dW_l^T += X_{l-1}^T delta_l            A = X^T (features padded to 128
+//                                          rows), B = delta^T (batch-contiguous)
+// The weight-gradient accumulators stay in TMEM across all tiles of a block
+// and are added to global memory once at the end.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "guide_internal.h"
+
+namespace gbrt {
+namespace guide {
+
+// ------------------------------------------------------------ layouts ----
+// Inference: weights (49,152 B) and one activation tile [128][208] (53,248
+// B) reused for every layer; two blocks fit on an SM.
+constexpr int kSW1 = 0, kSW2 = 26624, kSW3 = 34816, kSW4 = 43008, kSWEnd = 49152;
+constexpr int kInferX = kSWEnd, kInferMisc = kInferX + 53248, kInferSmem = kInferMisc + 64;
+constexpr uint32_t kInferCols = 64;
+
+// Training: weights, transposed weights for dX, three activation tiles, the
+// region R (X0 rows in the forward pass, then the transposed X1..X3 at
+// offsets 0, 16 KB, 32 KB and finally the transposed X0), delta rows and
+// delta^T.
+constexpr int kTW2T = 49152, kTW3T = 57344, kTW4T = 65536;
+constexpr int kTX1 = 71680, kTX2 = 88064, kTX3 = 104448, kTR = 120832, kTDR = 186368, kTDT = 202752;
+constexpr int kTMisc = 219136, kTrainSmem = kTMisc + 64;
+constexpr uint32_t kTrainCols = 512;
+// TMEM columns of the training kernel.
+constexpr uint32_t kColScratch = 0, kColW1lo = 64, kColW1hi = 128, kColW2 = 192, kColW3 = 256, kColW4 = 320;
+
+static_assert(kTrainSmem <= 232448, "training tile exceeds the shared memory of a block");
+static_assert(2 * kInferSmem <= 233472, "two inference blocks must fit on an SM");
+
+// Layer input ReLU(TMEM columns [0, 64)) of row r into an interleaved
+// [128][64] tile at s; also returns the values (for the transposed copy).
+__device__ __forceinline__ void hidden_to_smem(uint32_t lane_taddr, uint32_t s, int r, float* h) {
+#pragma unroll
+  for (int c = 0; c < kHid; c += 16) {
+    float v[16];
+    tmem_ld16(lane_taddr + c, v);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.f);
+    st_shared_v4(s + ik_off(r, c, kHid), pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                 pack_bf16(v[6], v[7]));
+    st_shared_v4(s + ik_off(r, c + 8, kHid), pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]),
+                 pack_bf16(v[12], v[13]), pack_bf16(v[14], v[15]));
+    if (h) {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) h[c + i] = v[i];
+    }
+  }
+}
+
+// Block-wide hand-over between the threads' shared-memory writes / TMEM
+// reads and the next tcgen05 operation.
+__device__ __forceinline__ void handoff() {
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+}
+
+// ------------------------------------------------------------ inference ----
+__global__ void __launch_bounds__(128) k_guide_infer(GuideNet net, const float4* __restrict__ in,
+                                                     const int* __restrict__ count, int n_rows,
+                                                     float4* __restrict__ mix, int* err) {
+  extern __shared__ __align__(1024) uint8_t sm[];
+  const int t = threadIdx.x, warp = t >> 5;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kInferMisc);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + kInferMisc + 8);
+  const uint32_t sW1 = smem_u32(sm + kSW1), sW2 = smem_u32(sm + kSW2), sW3 = smem_u32(sm + kSW3),
+                 sW4 = smem_u32(sm + kSW4), sX = smem_u32(sm + kInferX), bar = smem_u32(mbar);
+  load_weights(sm + kSW1, net.w + kOffW1, kHid, kIn, kHid, false);
+  load_weights(sm + kSW2, net.w + kOffW2, kHid, kHid, kHid, false);
+  load_weights(sm + kSW3, net.w + kOffW3, kHid, kHid, kHid, false);
+  load_weights(sm + kSW4, net.w + kOffW4, kOut, kHid, kOutPad, false);
+  if (t == 0) mbar_init(bar, 1);
+  if (warp == 0) tmem_alloc(smem_u32(tslot), kInferCols);
+  handoff();
+  const uint32_t tmem = *tslot;
+  const uint32_t lane = tmem + (uint32_t(warp * 32) << 16);
+  const int n = count ? *count : n_rows;
+  const int ntiles = (n + kRows - 1) / kRows;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int r = tile * kRows + t;
+    EncIn e;
+    if (r < n) {
+      float4 a = in[3 * size_t(r)], b = in[3 * size_t(r) + 1], c = in[3 * size_t(r) + 2];
+      e = make_enc(net, a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z);
+    } else {
+      e = make_enc(net, net.lo[0], net.lo[1], net.lo[2], 0.f, 0.f, 1.f, 0.f, 0.f, 1.f);
+    }
+    write_enc_row(sX, t, e);
+    // Three hidden layers, then the output layer (N = 48, 40 used).
+    for (int layer = 0; layer < 4; ++layer) {
+      handoff();
+      if (t == 0) {
+        if (layer == 0) gemm_k(tmem, sX, kIn, sW1, kIn, kIn, kHid, false);
+        else if (layer == 1) gemm_k(tmem, sX, kHid, sW2, kHid, kHid, kHid, false);
+        else if (layer == 2) gemm_k(tmem, sX, kHid, sW3, kHid, kHid, kHid, false);
+        else gemm_k(tmem, sX, kHid, sW4, kHid, kHid, kOutPad, false);
+        mma_commit(bar);
+      }
+      ok = mbar_wait(bar, phase);
+      phase ^= 1;
+      if (__syncthreads_or(!ok)) { ok = false; break; }
+      tc_fence_after();
+      if (layer < 3) {
+        hidden_to_smem(lane, sX, t, nullptr);
+      } else {
+        float o[kOutPad];
+        tmem_ld16(lane, o);
+        tmem_ld16(lane + 16, o + 16);
+        tmem_ld16(lane + 32, o + 32);
+        if (r < n) {
+          Mixture m;
+          decode_mixture(o, m);
+          float4* out = mix + 10 * size_t(r);
+          out[0] = make_float4(m.pi[0], m.pi[1], m.pi[2], m.pi[3]);
+          out[1] = make_float4(m.pi[4], m.pi[5], m.pi[6], m.pi[7]);
+#pragma unroll
+          for (int k = 0; k < kLobes; ++k) out[2 + k] = make_float4(m.mx[k], m.my[k], m.mz[k], m.kappa[k]);
+        }
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (!ok) {
+    if (t == 0) atomicExch(err, 1);
+    mbar_wait(bar, phase ^ 1);  // the chain that timed out, once more (bounded)
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, kInferCols);
+  }
+}
+
+// ------------------------------------------------------------- training ----
+// dLoss/d(raw outputs) of one sample, loss = -w log q(wi).
+__device__ __forceinline__ float loss_grad(const float* o, float wx, float wy, float wz, float w, float* g) {
+  float amax = o[0];
+#pragma unroll
+  for (int k = 1; k < kLobes; ++k) amax = fmaxf(amax, o[k]);
+  float se = 0.f;
+#pragma unroll
+  for (int k = 0; k < kLobes; ++k) se += expf(o[k] - amax);
+  const float lse_a = amax + logf(se);
+  float lp[kLobes], mu[kLobes][3], kap[kLobes], cw[kLobes], il[kLobes];
+  float lmax = -INFINITY;
+#pragma unroll
+  for (int k = 0; k < kLobes; ++k) {
+    float x = o[8 + 3 * k], y = o[9 + 3 * k], z = o[10 + 3 * k];
+    float l = sqrtf(x * x + y * y + z * z);
+    if (l > 1e-12f) {
+      il[k] = 1.f / l;
+      mu[k][0] = x * il[k]; mu[k][1] = y * il[k]; mu[k][2] = z * il[k];
+    } else {
+      il[k] = 0.f;
+      mu[k][0] = 0.f; mu[k][1] = 0.f; mu[k][2] = 1.f;
+    }
+    kap[k] = expf(fminf(fmaxf(o[32 + k], kLogKappaMin), kLogKappaMax));
+    cw[k] = mu[k][0] * wx + mu[k][1] * wy + mu[k][2] * wz;
+    lp[k] = (o[k] - lse_a) + vmf_log_norm(kap[k]) + kap[k] * (cw[k] - 1.f);
+    lmax = fmaxf(lmax, lp[k]);
+  }
+  float sq = 0.f;
+#pragma unroll
+  for (int k = 0; k < kLobes; ++k) sq += expf(lp[k] - lmax);
+  const float lq = lmax + logf(sq);
+#pragma unroll
+  for (int k = 0; k < kLobes; ++k) {
+    float rk = expf(lp[k] - lq);
+    float pk = expf(o[k] - lse_a);
+    g[k] = -w * (rk - pk);
+    float s = -w * rk * kap[k] * il[k];
+    g[8 + 3 * k] = s * (wx - cw[k] * mu[k][0]);
+    g[9 + 3 * k] = s * (wy - cw[k] * mu[k][1]);
+    g[10 + 3 * k] = s * (wz - cw[k] * mu[k][2]);
+    bool inside = o[32 + k] > kLogKappaMin && o[32 + k] < kLogKappaMax;
+    float dk = 1.f - 2.f * kap[k] / expm1f(2.f * kap[k]) + kap[k] * (cw[k] - 1.f);
+    g[32 + k] = inside ? -w * rk * dk : 0.f;
+  }
+  return -w * lq;
+}
+
+// Writes v (64 values of row r) transposed: element (k, r) of a [rows][128]
+// batch-contiguous tile at s.
+__device__ __forceinline__ void write_transposed(uint32_t s, int r, const float* v, int nv) {
+  for (int k = 0; k < nv; ++k) st_shared_u16(s + ik_off(k, r, kRows), bf16_bits(v[k]));
+}
+
+// Reads row r of an interleaved [128][64] BF16 tile.
+__device__ __forceinline__ void read_row64(const uint8_t* base, int r, float* v) {
+#pragma unroll
+  for (int c = 0; c < kHid; c += 8) {
+    uint4 q = *reinterpret_cast<const uint4*>(base + ik_off(r, c, kHid));
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      float2 f = __bfloat1622float2(h[i]);
+      v[c + 2 * i] = f.x;
+      v[c + 2 * i + 1] = f.y;
+    }
+  }
+}
+
+// delta = ReLU'(X) * dX for row r: dX from TMEM scratch, X from the row tile.
+// Writes delta rows (when rows != 0) and delta^T.
+__device__ __forceinline__ void backprop_delta(uint32_t lane_taddr, const uint8_t* xrow, uint32_t s_rows,
+                                               uint32_t s_t, int r) {
+  float x[kHid], d[kHid];
+  read_row64(xrow, r, x);
+#pragma unroll
+  for (int c = 0; c < kHid; c += 16) tmem_ld16(lane_taddr + c, d + c);
+#pragma unroll
+  for (int k = 0; k < kHid; ++k) d[k] = x[k] > 0.f ? d[k] : 0.f;
+  if (s_rows) {
+#pragma unroll
+    for (int c = 0; c < kHid; c += 8)
+      st_shared_v4(s_rows + ik_off(r, c, kHid), pack_bf16(d[c], d[c + 1]), pack_bf16(d[c + 2], d[c + 3]),
+                   pack_bf16(d[c + 4], d[c + 5]), pack_bf16(d[c + 6], d[c + 7]));
+  }
+  write_transposed(s_t, r, d, kHid);
+}
+
+__global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const float4* __restrict__ samples, int n,
+                                                        float inv_n, float* __restrict__ grad,
+                                                        float* __restrict__ loss_sum, int* err) {
+  extern __shared__ __align__(1024) uint8_t sm[];
+  const int t = threadIdx.x, warp = t >> 5;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kTMisc);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + kTMisc + 8);
+  const uint32_t bar = smem_u32(mbar);
+  const uint32_t sW1 = smem_u32(sm + kSW1), sW2 = smem_u32(sm + kSW2), sW3 = smem_u32(sm + kSW3),
+                 sW4 = smem_u32(sm + kSW4), sW2T = smem_u32(sm + kTW2T), sW3T = smem_u32(sm + kTW3T),
+                 sW4T = smem_u32(sm + kTW4T), sX1 = smem_u32(sm + kTX1), sX2 = smem_u32(sm + kTX2),
+                 sX3 = smem_u32(sm + kTX3), sR = smem_u32(sm + kTR), sDR = smem_u32(sm + kTDR),
+                 sDT = smem_u32(sm + kTDT);
+  load_weights(sm + kSW1, net.w + kOffW1, kHid, kIn, kHid, false);
+  load_weights(sm + kSW2, net.w + kOffW2, kHid, kHid, kHid, false);
+  load_weights(sm + kSW3, net.w + kOffW3, kHid, kHid, kHid, false);
+  load_weights(sm + kSW4, net.w + kOffW4, kOut, kHid, kOutPad, false);
+  load_weights(sm + kTW2T, net.w + kOffW2, kHid, kHid, kHid, true);
+  load_weights(sm + kTW3T, net.w + kOffW3, kHid, kHid, kHid, true);
+  load_weights(sm + kTW4T, net.w + kOffW4, kOut, kHid, kOutPad, true);
+  if (t == 0) mbar_init(bar, 1);
+  if (warp == 0) tmem_alloc(smem_u32(tslot), kTrainCols);
+  handoff();
+  const uint32_t tmem = *tslot;
+  const uint32_t lane = tmem + (uint32_t(warp * 32) << 16);
+  const int ntiles = (n + kRows - 1) / kRows;
+  uint32_t phase = 0;
+  bool ok = true, first = true;
+  float loss = 0.f;
+
+  // One chain of products, then the wait; false when the wait timed out.
+  auto sync_chain = [&]() -> bool {
+    if (t == 0) mma_commit(bar);
+    bool fine = mbar_wait(bar, phase);
+    phase ^= 1;
+    if (__syncthreads_or(!fine)) return false;
+    tc_fence_after();
+    return true;
+  };
+
+  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int r = tile * kRows + t;
+    float4 s0 = make_float4(net.lo[0], net.lo[1], net.lo[2], 0.f), s1 = make_float4(0.f, 0.f, 1.f, 0.f),
+           s2 = make_float4(0.f, 0.f, 1.f, 0.f), s3 = make_float4(0.f, 0.f, 1.f, 0.f);
+    if (r < n) {
+      s0 = samples[4 * size_t(r)];
+      s1 = samples[4 * size_t(r) + 1];
+      s2 = samples[4 * size_t(r) + 2];
+      s3 = samples[4 * size_t(r) + 3];
+    }
+    const float w = r < n ? s0.w * inv_n : 0.f;
+    const EncIn e = make_enc(net, s0.x, s0.y, s0.z, s1.x, s1.y, s1.z, s2.x, s2.y, s2.z);
+    write_enc_row(sR, t, e);
+    // ---- forward
+    float h[kHid];
+    handoff();
+    if (t == 0) gemm_k(tmem + kColScratch, sR, kIn, sW1, kIn, kIn, kHid, false);
+    if (!(ok = sync_chain())) break;
+    hidden_to_smem(lane + kColScratch, sX1, t, h);
+    write_transposed(sR, t, h, kHid);  // X1^T at R + 0
+    handoff();
+    if (t == 0) gemm_k(tmem + kColScratch, sX1, kHid, sW2, kHid, kHid, kHid, false);
+    if (!(ok = sync_chain())) break;
+    hidden_to_smem(lane + kColScratch, sX2, t, h);
+    write_transposed(sR + 16384, t, h, kHid);  // X2^T
+    handoff();
+    if (t == 0) gemm_k(tmem + kColScratch, sX2, kHid, sW3, kHid, kHid, kHid, false);
+    if (!(ok = sync_chain())) break;
+    hidden_to_smem(lane + kColScratch, sX3, t, h);
+    write_transposed(sR + 32768, t, h, kHid);  // X3^T
+    handoff();
+    if (t == 0) gemm_k(tmem + kColScratch, sX3, kHid, sW4, kHid, kHid, kOutPad, false);
+    if (!(ok = sync_chain())) break;
+    {
+      float o[kOutPad], g[kOutPad];
+      tmem_ld16(lane + kColScratch, o);
+      tmem_ld16(lane + kColScratch + 16, o + 16);
+      tmem_ld16(lane + kColScratch + 32, o + 32);
+      float ls = loss_grad(o, s3.x, s3.y, s3.z, w, g);
+      if (r < n) loss += ls;
+#pragma unroll
+      for (int j = kOut; j < kOutPad; ++j) g[j] = 0.f;
+#pragma unroll
+      for (int c = 0; c < kOutPad; c += 8)
+        st_shared_v4(sDR + ik_off(t, c, kOutPad), pack_bf16(g[c], g[c + 1]), pack_bf16(g[c + 2], g[c + 3]),
+                     pack_bf16(g[c + 4], g[c + 5]), pack_bf16(g[c + 6], g[c + 7]));
+      write_transposed(sDT, t, g, kOutPad);
+    }
+    // ---- backward: output layer
+    handoff();
+    if (t == 0) {
+      gemm_k(tmem + kColW4, sR + 32768, kRows, sDT, kRows, kRows, kOutPad, !first);
+      gemm_k(tmem + kColScratch, sDR, kOutPad, sW4T, kOutPad, kOutPad, kHid, false);
+    }
+    if (!(ok = sync_chain())) break;
+    backprop_delta(lane + kColScratch, sm + kTX3, sDR, sDT, t);
+    // ---- layer 3
+    handoff();
+    if (t == 0) {
+      gemm_k(tmem + kColW3, sR + 16384, kRows, sDT, kRows, kRows, kHid, !first);
+      gemm_k(tmem + kColScratch, sDR, kHid, sW3T, kHid, kHid, kHid, false);
+    }
+    if (!(ok = sync_chain())) break;
+    backprop_delta(lane + kColScratch, sm + kTX2, sDR, sDT, t);
+    // ---- layer 2
+    handoff();
+    if (t == 0) {
+      gemm_k(tmem + kColW2, sR, kRows, sDT, kRows, kRows, kHid, !first);
+      gemm_k(tmem + kColScratch, sDR, kHid, sW2T, kHid, kHid, kHid, false);
+    }
+    if (!(ok = sync_chain())) break;
+    backprop_delta(lane + kColScratch, sm + kTX1, 0u, sDT, t);
+    // ---- layer 1: the encoding again, transposed, into R
+    for (int f = 0; f < kIn; ++f) st_shared_u16(sR + ik_off(f, t, kRows), bf16_bits(enc_feature(e, f)));
+    handoff();
+    if (t == 0) {
+      gemm_k(tmem + kColW1lo, sR, kRows, sDT, kRows, kRows, kHid, !first);
+      gemm_k(tmem + kColW1hi, sR + ik_off(kRows, 0, kRows), kRows, sDT, kRows, kRows, kHid, !first);
+    }
+    if (!(ok = sync_chain())) break;
+    first = false;
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (ok && !first) {
+    // Weight gradients out of TMEM: lane = input feature, column = output.
+    float v[16];
+    for (int c = 0; c < kHid; c += 16) {
+      tmem_ld16(lane + kColW1lo + c, v);
+      for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW1 + (c + i) * kIn + t], v[i]);
+      tmem_ld16(lane + kColW1hi + c, v);
+      if (kRows + t < kIn)
+        for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW1 + (c + i) * kIn + kRows + t], v[i]);
+      tmem_ld16(lane + kColW2 + c, v);
+      if (t < kHid)
+        for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW2 + (c + i) * kHid + t], v[i]);
+      tmem_ld16(lane + kColW3 + c, v);
+      if (t < kHid)
+        for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW3 + (c + i) * kHid + t], v[i]);
+    }
+    for (int c = 0; c < kOutPad; c += 16) {
+      tmem_ld16(lane + kColW4 + c, v);
+      if (t < kHid)
+        for (int i = 0; i < 16; ++i)
+          if (c + i < kOut) atomicAdd(&grad[kOffW4 + (c + i) * kHid + t], v[i]);
+    }
+    atomicAdd(loss_sum, loss);
+  }
+  if (!ok) {
+    if (t == 0) atomicExch(err, 1);
+    mbar_wait(bar, phase ^ 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, kTrainCols);
+  }
+}
+
+// ----------------------------------------------------------------- Adam ----
+__global__ void k_guide_adam(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v,
+                             const float* __restrict__ g, __nv_bfloat16* __restrict__ w, int n, float lr, float b1,
+                             float b2, float eps, float bc1, float bc2) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float gi = g[i];
+  if (!isfinite(gi)) gi = 0.f;
+  float mi = b1 * m[i] + (1.f - b1) * gi;
+  float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  float pi = p[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+  p[i] = pi;
+  w[i] = __float2bfloat16_rn(pi);
+}
+
+__global__ void k_to_bf16(const float* __restrict__ p, __nv_bfloat16* __restrict__ w, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) w[i] = __float2bfloat16_rn(p[i]);
+}
+
+// ------------------------------------------------------------- host side ----
+GuideNet view(const gbrt_guide* g) {
+  GuideNet v;
+  v.w = g->d_w;
+  for (int k = 0; k < 3; ++k) {
+    v.lo[k] = g->bounds[k];
+    float ext = g->bounds[3 + k] - g->bounds[k];
+    v.inv_ext[k] = ext > 0.f ? 1.f / ext : 0.f;
+  }
+  return v;
+}
+
+cudaError_t launch_infer(const gbrt_guide* g, const float4* in, const int* count, int n_rows, float4* mix,
+                         cudaStream_t stream) {
+  k_guide_infer<<<g->infer_grid, kRows, kInferSmem, stream>>>(view(g), in, count, n_rows, mix, g->d_err);
+  return cudaGetLastError();
+}
+
+cudaError_t train(gbrt_guide* g, const float4* samples, int n, float lr, bool step, cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(g->d_g, 0, kParams * sizeof(float), stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(g->d_loss, 0, sizeof(float), stream);
+  if (e != cudaSuccess) return e;
+  if (n > 0) {
+    int tiles = (n + kRows - 1) / kRows;
+    int grid = std::min(g->train_grid, tiles);
+    k_guide_train<<<grid, kRows, kTrainSmem, stream>>>(view(g), samples, n, 1.f / float(n), g->d_g, g->d_loss,
+                                                       g->d_err);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  if (step) {
+    g->step += 1;
+    g->ready = true;
+    const float b1 = 0.9f, b2 = 0.999f;
+    float bc1 = float(1.0 - std::pow(double(b1), g->step)), bc2 = float(1.0 - std::pow(double(b2), g->step));
+    k_guide_adam<<<(kParams + 255) / 256, 256, 0, stream>>>(g->d_p, g->d_m, g->d_v, g->d_g, g->d_w, kParams, lr, b1,
+                                                            b2, 1e-8f, bc1, bc2);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+}  // namespace guide
+}  // namespace gbrt
+
+using namespace gbrt;
+using namespace gbrt::guide;
+
+namespace {
+
+// Seeded initial parameters: uniform in +-sqrt(6 / fan_in) (He et al. for
+// the ReLU layers), the output layer scaled by 0.1 so that the initial
+// mixture is close to eight broad lobes of equal weight.
+void init_params(std::vector<float>& p, unsigned long long seed) {
+  p.assign(kParams, 0.f);
+  unsigned long long s = seed ^ 0x5DEECE66Dull;
+  auto next = [&]() {
+    s += 0x9E3779B97F4A7C15ull;
+    unsigned long long z = s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return double(z >> 11) * (1.0 / 9007199254740992.0);
+  };
+  struct M { int off, n, fan; double scale; } ms[4] = {
+      {kOffW1, kW1, kIn, 1.0}, {kOffW2, kW2, kHid, 1.0}, {kOffW3, kW3, kHid, 1.0}, {kOffW4, kW4, kHid, 0.1}};
+  for (auto& m : ms) {
+    double a = std::sqrt(6.0 / m.fan) * m.scale;
+    for (int i = 0; i < m.n; ++i) p[m.off + i] = float((2.0 * next() - 1.0) * a);
+  }
+}
+
+gbrt_status check_guide(gbrt_guide* g) {
+  if (!g) return fail(nullptr, GBRT_ERR_INVALID_ARG, "guide: NULL handle");
+  cudaError_t e = cudaSetDevice(g->device);
+  if (e != cudaSuccess) return cuda_fail(g->ctx, e, "cudaSetDevice");
+  return GBRT_OK;
+}
+
+gbrt_status read_err(gbrt_guide* g, cudaStream_t stream) {
+  int err = 0;
+  cudaError_t e = cudaMemcpyAsync(&err, g->d_err, sizeof err, cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_fail(g->ctx, e, "guide");
+  if (err) {
+    cudaMemsetAsync(g->d_err, 0, sizeof(int), stream);
+    return fail(g->ctx, GBRT_ERR_TIMEOUT, "guide: a tensor-core wait timed out");
+  }
+  return GBRT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gbrt_status gbrt_guide_create(gbrt_ctx* ctx, const float bounds[6], uint64_t seed, gbrt_guide** out) {
+  if (!ctx || !bounds || !out) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_create: NULL argument");
+  *out = nullptr;
+  for (int k = 0; k < 3; ++k)
+    if (!(bounds[3 + k] >= bounds[k]) || !std::isfinite(bounds[k]) || !std::isfinite(bounds[3 + k]))
+      return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_create: bounds must be finite with hi >= lo");
+  GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  auto* g = new gbrt_guide();
+  g->ctx = ctx;
+  g->device = ctx->device;
+  std::memcpy(g->bounds, bounds, sizeof g->bounds);
+  cudaError_t e = cudaSuccess;
+  auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
+  A(cudaMalloc(&g->d_p, kParams * sizeof(float)));
+  A(cudaMalloc(&g->d_m, kParams * sizeof(float)));
+  A(cudaMalloc(&g->d_v, kParams * sizeof(float)));
+  A(cudaMalloc(&g->d_g, kParams * sizeof(float)));
+  A(cudaMalloc(&g->d_w, kParams * sizeof(__nv_bfloat16)));
+  A(cudaMalloc(&g->d_loss, sizeof(float)));
+  A(cudaMalloc(&g->d_err, sizeof(int)));
+  A(cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem));
+  A(cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem));
+  int per = 0;
+  if (e == cudaSuccess) A(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_infer, kRows, kInferSmem));
+  g->infer_grid = std::max(1, std::min(per, 2)) * ctx->num_sms;
+  g->train_grid = ctx->num_sms;
+  std::vector<float> p;
+  init_params(p, seed);
+  if (e == cudaSuccess) {
+    A(cudaMemcpy(g->d_p, p.data(), kParams * sizeof(float), cudaMemcpyHostToDevice));
+    A(cudaMemset(g->d_m, 0, kParams * sizeof(float)));
+    A(cudaMemset(g->d_v, 0, kParams * sizeof(float)));
+    A(cudaMemset(g->d_err, 0, sizeof(int)));
+    k_to_bf16<<<(kParams + 255) / 256, 256>>>(g->d_p, g->d_w, kParams);
+    A(cudaGetLastError());
+    A(cudaDeviceSynchronize());
+  }
+  if (e != cudaSuccess) {
+    gbrt_guide_destroy(g);
+    return cuda_fail(ctx, e, "gbrt_guide_create");
+  }
+  *out = g;
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_guide_destroy(gbrt_guide* g) {
+  if (!g) return GBRT_OK;
+  cudaSetDevice(g->device);
+  cudaDeviceSynchronize();
+  for (void* p : {(void*)g->d_p, (void*)g->d_m, (void*)g->d_v, (void*)g->d_g, (void*)g->d_w, (void*)g->d_loss,
+                  (void*)g->d_err})
+    if (p) cudaFree(p);
+  delete g;
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_guide_get_weights(gbrt_guide* g, float* out, size_t n) {
+  gbrt_status st = check_guide(g);
+  if (st != GBRT_OK) return st;
+  if (!out || n < size_t(kParams)) return fail(g->ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_get_weights: buffer");
+  GBRT_CUDA_TRY(g->ctx, cudaMemcpy(out, g->d_p, kParams * sizeof(float), cudaMemcpyDeviceToHost));
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_guide_set_weights(gbrt_guide* g, const float* w, size_t n) {
+  gbrt_status st = check_guide(g);
+  if (st != GBRT_OK) return st;
+  if (!w || n != size_t(kParams)) return fail(g->ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_set_weights: size");
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(w[i])) return fail(g->ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_set_weights: non-finite");
+  GBRT_CUDA_TRY(g->ctx, cudaMemcpy(g->d_p, w, kParams * sizeof(float), cudaMemcpyHostToDevice));
+  GBRT_CUDA_TRY(g->ctx, cudaMemset(g->d_m, 0, kParams * sizeof(float)));
+  GBRT_CUDA_TRY(g->ctx, cudaMemset(g->d_v, 0, kParams * sizeof(float)));
+  k_to_bf16<<<(kParams + 255) / 256, 256>>>(g->d_p, g->d_w, kParams);
+  GBRT_CUDA_TRY(g->ctx, cudaGetLastError());
+  GBRT_CUDA_TRY(g->ctx, cudaDeviceSynchronize());
+  g->step = 0;
+  g->ready = true;
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_guide_eval(gbrt_guide* g, const float* inputs, size_t n, float* out) {
+  gbrt_status st = check_guide(g);
+  if (st != GBRT_OK) return st;
+  if (!inputs || !out) return fail(g->ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_eval: NULL argument");
+  if (n == 0) return GBRT_OK;
+  if (n > (1u << 26)) return fail(g->ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_eval: too many rows");
+  cudaStream_t s = g->ctx->stream;
+  std::vector<float4> h(3 * n);
+  for (size_t i = 0; i < n; ++i) {
+    const float* r = inputs + 9 * i;
+    h[3 * i] = make_float4(r[0], r[1], r[2], 0.f);
+    h[3 * i + 1] = make_float4(r[3], r[4], r[5], 0.f);
+    h[3 * i + 2] = make_float4(r[6], r[7], r[8], 0.f);
+  }
+  float4 *d_in = nullptr, *d_mix = nullptr;
+  cudaError_t e = cudaMallocAsync(&d_in, h.size() * sizeof(float4), s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_mix, 10 * n * sizeof(float4), s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = launch_infer(g, d_in, nullptr, int(n), d_mix, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_mix, 10 * n * sizeof(float4), cudaMemcpyDeviceToHost, s);
+  if (d_in) cudaFreeAsync(d_in, s);
+  if (d_mix) cudaFreeAsync(d_mix, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(g->ctx, e, "gbrt_guide_eval");
+  return read_err(g, s);
+}
+
+static gbrt_status upload_samples(gbrt_guide* g, const float* samples, size_t n, float4** d_out) {
+  std::vector<float4> h(4 * n);
+  for (size_t i = 0; i < n; ++i) {
+    const float* r = samples + 13 * i;
+    h[4 * i] = make_float4(r[0], r[1], r[2], r[12]);
+    h[4 * i + 1] = make_float4(r[3], r[4], r[5], 0.f);
+    h[4 * i + 2] = make_float4(r[6], r[7], r[8], 0.f);
+    h[4 * i + 3] = make_float4(r[9], r[10], r[11], 0.f);
+  }
+  cudaStream_t s = g->ctx->stream;
+  cudaError_t e = cudaMallocAsync(d_out, h.size() * sizeof(float4), s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(*d_out, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(g->ctx, e, "guide samples");
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_guide_gradient(gbrt_guide* g, const float* samples, size_t n, float* grad, float* loss) {
+  gbrt_status st = check_guide(g);
+  if (st != GBRT_OK) return st;
+  if (!samples || !grad || n == 0 || n > (1u << 26))
+    return fail(g->ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_gradient: bad argument");
+  float4* d = nullptr;
+  if ((st = upload_samples(g, samples, n, &d)) != GBRT_OK) return st;
+  cudaStream_t s = g->ctx->stream;
+  cudaError_t e = train(g, d, int(n), 0.f, false, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(grad, g->d_g, kParams * sizeof(float), cudaMemcpyDeviceToHost, s);
+  float l = 0.f;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&l, g->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(g->ctx, e, "gbrt_guide_gradient");
+  if (loss) *loss = l;
+  return read_err(g, s);
+}
+
+gbrt_status gbrt_guide_train_step(gbrt_guide* g, const float* samples, size_t n, float learning_rate, float* loss) {
+  gbrt_status st = check_guide(g);
+  if (st != GBRT_OK) return st;
+  if (!samples || n == 0 || n > (1u << 26) || !(learning_rate > 0.f))
+    return fail(g->ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_train_step: bad argument");
+  float4* d = nullptr;
+  if ((st = upload_samples(g, samples, n, &d)) != GBRT_OK) return st;
+  cudaStream_t s = g->ctx->stream;
+  cudaError_t e = train(g, d, int(n), learning_rate, true, s);
+  float l = 0.f;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&l, g->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(g->ctx, e, "gbrt_guide_train_step");
+  if (loss) *loss = l;
+  return read_err(g, s);
+}
+
+}  // extern "C"

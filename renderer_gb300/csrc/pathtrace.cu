@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "gbrt_internal.h"
+#include "guide_internal.h"
 #include "shading.cuh"
 #include "traverse.cuh"
 
@@ -61,6 +62,9 @@ struct PTParams {
   float term_p;            // termination probability
   float inv_log1mp;        // 1 / log(1 - term_p), for the geometric draw
   int physical;            // GBRT_SEM_PHYSICAL
+  int guided;              // sample non-specular vertices from the guide's mixtures too
+  float guide_frac;        // probability of sampling the guide (one-sample MIS)
+  int record;              // write training records for the guide
 };
 
 // Path state, structure of arrays indexed by slot (path index - g0).
@@ -82,7 +86,24 @@ struct PTState {
   unsigned long long* work;   // work counters of the persistent kernels
   unsigned long long* tally;  // [0] extension rays, [1] shadow rays, [2] non-finite samples
   int* err;
+  // Path guiding (null when unused).
+  float4* gin;     // per extension-queue entry: (point, guided), (normal facing wo, -), (wo, -)
+  float4* mix;     // per extension-queue entry: the vertex's mixture (ten float4)
+  float4* rec;     // training records, kRecords x 5 float4 per slot, record-major
+  float4* tsamp;   // training samples, four float4 each
+  int* tcount;     // training samples written
+  int tcap;        // capacity of tsamp
+  int nslots;      // slots allocated (stride of rec)
 };
+
+// Training records of the guide: the first kRecords guided vertices of a
+// path. Record component c of record r of a slot is rec[(5 r + c) nslots +
+// slot]: (point, pdf), (normal, wi.x), (wo, wi.y), (throughput after the
+// vertex, wi.z), (radiance of the path when the next vertex was reached).
+// ctl.z of a guided path: records written (low 4 bits), kRecOpen while the
+// last record waits for its radiance snapshot.
+constexpr int kRecords = 4;
+constexpr int kRecOpen = 0x100;
 
 // ------------------------------------------------------------- raygen ----
 __global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
@@ -457,9 +478,17 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
 // (weighted by the light count), emission on BSDF-sampled hits, both combined
 // by the power heuristic; Russian roulette with survival 1 - p from the
 // fourth vertex on. Path state: alpha.xyz throughput, alpha.w the pdf of the
-// last BSDF sample, ctl = (vertex index, -, -, last vertex specular).
+// last sampled direction, ctl = (vertex index, -, guide records, last vertex
+// specular).
+//
+// With guiding, a non-specular vertex samples its direction from the
+// vertex's vMF mixture with probability guide_frac and from the BSDF
+// otherwise (one-sample MIS: the pdf of either choice is the mixture
+// guide_frac q + (1 - guide_frac) p_bsdf, used in the throughput and in both
+// power heuristics).
 __device__ __forceinline__ void nee_phys(const DeviceScene& S, const PTState& st, int slot, unsigned long long key,
-                                         unsigned base, const PhysBsdf& b, V3f x, V3f n, V3f wo, V3f alpha) {
+                                         unsigned base, const PhysBsdf& b, V3f x, V3f n, V3f wo, V3f alpha,
+                                         const float4* M, float frac) {
   const int nL = S.n_lights;
   const float pChoose = 1.f / float(nL);
   const int li = min(stream_index(key, base + 3, nL), nL - 1);
@@ -500,6 +529,7 @@ __device__ __forceinline__ void nee_phys(const DeviceScene& S, const PTState& st
   float pb;
   V3f f = phys_eval(b, n, wo, wi, pb);
   if (is_zero(f)) return;
+  if (M) pb = frac * guide::mixture_pdf(M, wi.x, wi.y, wi.z) + (1.f - frac) * pb;
   float w = delta ? 1.f : power_heuristic(pl, pb);
   float sc = fabsf(dot(n, wi)) * w / pl;
   V3f c = v3(alpha.x * f.x * Le.x * sc, alpha.y * f.y * Le.y * sc, alpha.z * f.z * Le.z * sc);
@@ -511,6 +541,35 @@ __device__ __forceinline__ void nee_phys(const DeviceScene& S, const PTState& st
   st.sh_slot[e] = slot;
 }
 
+// Normal (unflipped) and material of a surface hit that is not an emitter.
+__device__ __forceinline__ void surface_normal(const DeviceScene& S, const RawHit& h, V3f x, V3f& nrm, int& mat) {
+  if (h.rec >= 0) {
+    const int4 m = __ldg(&S.meta[h.rec]);
+    const float4* rp = S.recs + 3 * int64_t(h.rec);
+    const float4 a = __ldg(rp);
+    const int kind = __float_as_int(a.w);
+    mat = m.y;
+    if (kind == kRecTriangle) {
+      if (m.z >= 0) {
+        const float* nn = S.tri_nrm + 12 * int64_t(m.z);
+        float w0 = 1.f - h.u - h.v;
+        nrm = normalize(w0 * ld3(nn) + h.u * ld3(nn + 3) + h.v * ld3(nn + 6));
+      } else {
+        const float4 b = __ldg(rp + 1), cc = __ldg(rp + 2);
+        V3f p1 = v3(a.x, a.y, a.z), p2 = v3(b.x, b.y, b.z), p3 = v3(cc.x, cc.y, cc.z);
+        nrm = normalize(cross(p1 - p2, p1 - p3));
+      }
+    } else {
+      nrm = normalize(x - v3(a.x, a.y, a.z));  // sphere
+    }
+  } else {
+    const float4 pl = __ldg(&S.planes[-2 - h.rec]);
+    nrm = normalize(v3(pl.x, pl.y, pl.z));
+    mat = S.plane_meta[-2 - h.rec].y;
+  }
+}
+
+template <bool GUIDED>
 __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P, PTState st, int cur) {
   const int n = st.counts[cur];
   const int nxt = cur ^ 1;
@@ -519,8 +578,14 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
     const int slot = st.ext_slot[cur][q];
     const RawHit h = st.hits[q];
     const float4 ro = st.ext[cur][2 * q], rd = st.ext[cur][2 * q + 1];
-    const int4 c = st.ctl[slot];
+    int4 c = st.ctl[slot];
     const int i = c.x;
+    if (GUIDED && P.record && (c.z & kRecOpen)) {
+      // The radiance the path had gathered before this vertex: the rest of
+      // the path is what the last recorded direction brought in.
+      st.rec[size_t(5 * ((c.z & 15) - 1) + 4) * st.nslots + slot] = st.L[slot];
+      c.z &= ~kRecOpen;
+    }
     const bool prevSpec = c.w != 0;
     const float4 a4 = st.alpha[slot];
     const V3f alpha = v3(a4.x, a4.y, a4.z);
@@ -538,16 +603,11 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
       continue;
     }
     const V3f x = v3(ro.x, ro.y, ro.z) + h.t * d;
-    V3f nrm;
-    int mat = -1;
     if (h.rec >= 0) {
-      const int4 m = __ldg(&S.meta[h.rec]);
-      const float4* rp = S.recs + 3 * int64_t(h.rec);
-      const float4 a = __ldg(rp);
-      const int kind = __float_as_int(a.w);
-      if (m.w >= 0) {
+      const int lt = __ldg(&S.meta[h.rec]).w;
+      if (lt >= 0) {
         // An area light: emission on its front side (AreaLight is one-sided).
-        const DevLight& Lt = S.lights[m.w];
+        const DevLight& Lt = S.lights[lt];
         float dl = len(d);
         float cl = dot(-(1.f / dl) * d, ld3(Lt.nhat));
         if (cl > 0.f) {
@@ -564,25 +624,10 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
         }
         continue;
       }
-      mat = m.y;
-      if (kind == kRecTriangle) {
-        if (m.z >= 0) {
-          const float* nn = S.tri_nrm + 12 * int64_t(m.z);
-          float w0 = 1.f - h.u - h.v;
-          nrm = normalize(w0 * ld3(nn) + h.u * ld3(nn + 3) + h.v * ld3(nn + 6));
-        } else {
-          const float4 b = __ldg(rp + 1), cc = __ldg(rp + 2);
-          V3f p1 = v3(a.x, a.y, a.z), p2 = v3(b.x, b.y, b.z), p3 = v3(cc.x, cc.y, cc.z);
-          nrm = normalize(cross(p1 - p2, p1 - p3));
-        }
-      } else {
-        nrm = normalize(x - v3(a.x, a.y, a.z));  // sphere
-      }
-    } else {
-      const float4 pl = __ldg(&S.planes[-2 - h.rec]);
-      nrm = normalize(v3(pl.x, pl.y, pl.z));
-      mat = S.plane_meta[-2 - h.rec].y;
     }
+    V3f nrm;
+    int mat = -1;
+    surface_normal(S, h, x, nrm, mat);
     const PhysBsdf b = phys_bsdf(S.materials, mat);
     if (b.kind <= 0) continue;
     const unsigned long long key = stream_key(P.seed, P.g0 + (unsigned long long)slot);
@@ -590,22 +635,113 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
     const V3f wo = -normalize(d);
     const bool flipped = dot(nrm, wo) < 0.f;
     if (flipped) nrm = -nrm;
-    if (b.kind <= 3 && S.n_lights > 0) nee_phys(S, st, slot, key, base, b, x, nrm, wo, alpha);
+    const bool guideHere = GUIDED && P.guided && b.kind >= 1 && b.kind <= 3;
+    const float4* M = guideHere ? st.mix + 10 * size_t(q) : nullptr;
+    if (b.kind <= 3 && S.n_lights > 0) nee_phys(S, st, slot, key, base, b, x, nrm, wo, alpha, M, P.guide_frac);
     V3f wi, wgt;
     float pdf;
     bool spec;
-    if (!phys_sample(b, nrm, wo, flipped, stream_u(key, base), stream_u(key, base + 1), stream_u(key, base + 2), wi,
-                     wgt, pdf, spec))
+    const float u0 = stream_u(key, base), u1 = stream_u(key, base + 1), u2 = stream_u(key, base + 2);
+    if (guideHere) {
+      if (stream_u(key, base + 7) < P.guide_frac) {
+        guide::mixture_sample(M, u0, u1, u2, wi.x, wi.y, wi.z);
+      } else if (!phys_sample(b, nrm, wo, flipped, u0, u1, u2, wi, wgt, pdf, spec)) {
+        continue;
+      }
+      float pb;
+      V3f f = phys_eval(b, nrm, wo, wi, pb);
+      pdf = P.guide_frac * guide::mixture_pdf(M, wi.x, wi.y, wi.z) + (1.f - P.guide_frac) * pb;
+      if (is_zero(f) || !(pdf > 0.f)) continue;
+      wgt = (dot(nrm, wi) / pdf) * f;
+      spec = false;
+    } else if (!phys_sample(b, nrm, wo, flipped, u0, u1, u2, wi, wgt, pdf, spec)) {
       continue;
+    }
     V3f na = mulc(alpha, wgt);
     if (i + 1 >= 3 && P.term_p > 0.f) {
       if (stream_u(key, base + 6) < P.term_p) continue;
       na = (1.f / (1.f - P.term_p)) * na;
     }
     if (i + 1 >= P.D) continue;
+    int z = 0;
+    if (GUIDED) {
+      z = c.z;
+      if (P.record && b.kind >= 1 && b.kind <= 3 && (z & 15) < kRecords) {
+        const size_t r = size_t(5 * (z & 15)) * st.nslots + slot;
+        const size_t ns = size_t(st.nslots);
+        st.rec[r] = make_float4(x.x, x.y, x.z, pdf);
+        st.rec[r + ns] = make_float4(nrm.x, nrm.y, nrm.z, wi.x);
+        st.rec[r + 2 * ns] = make_float4(wo.x, wo.y, wo.z, wi.y);
+        st.rec[r + 3 * ns] = make_float4(na.x, na.y, na.z, wi.z);
+        z = ((z & 15) + 1) | kRecOpen;
+      }
+    }
     st.alpha[slot] = make_float4(na.x, na.y, na.z, pdf);
-    st.ctl[slot] = make_int4(i + 1, c.y, 0, spec ? 1 : 0);
+    st.ctl[slot] = make_int4(i + 1, c.y, z, spec ? 1 : 0);
     push_ext(st, nxt, slot, x, wi);
+  }
+}
+
+// ------------------------------------------------------------ guiding ----
+// Network inputs of the current extension queue: a surface vertex with a
+// non-specular BSDF gets (point, 1), (normal facing wo), (wo); everything
+// else a neutral row that the guided shade ignores.
+__global__ void __launch_bounds__(256) k_guide_prep(DeviceScene S, PTState st, int cur) {
+  const int n = st.counts[cur];
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const RawHit h = st.hits[q];
+    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = make_float4(0.f, 0.f, 1.f, 0.f), r2 = r1;
+    if (h.rec != -1 && !(h.rec >= 0 && __ldg(&S.meta[h.rec]).w >= 0)) {
+      const float4 ro = st.ext[cur][2 * q], rd = st.ext[cur][2 * q + 1];
+      const V3f d = v3(rd.x, rd.y, rd.z);
+      const V3f x = v3(ro.x, ro.y, ro.z) + h.t * d;
+      V3f nrm;
+      int mat = -1;
+      surface_normal(S, h, x, nrm, mat);
+      const PhysBsdf b = phys_bsdf(S.materials, mat);
+      if (b.kind >= 1 && b.kind <= 3) {
+        const V3f wo = -normalize(d);
+        if (dot(nrm, wo) < 0.f) nrm = -nrm;
+        r0 = make_float4(x.x, x.y, x.z, 1.f);
+        r1 = make_float4(nrm.x, nrm.y, nrm.z, 0.f);
+        r2 = make_float4(wo.x, wo.y, wo.z, 0.f);
+      }
+    }
+    st.gin[3 * size_t(q)] = r0;
+    st.gin[3 * size_t(q) + 1] = r1;
+    st.gin[3 * size_t(q) + 2] = r2;
+  }
+}
+
+// Training samples from the records of a finished batch. The radiance that
+// arrived along a recorded direction is what the path gathered after the
+// record's snapshot, divided by the throughput up to that direction; the
+// target is its mean over the channels times |cos| at the vertex, and the
+// sample weight target / pdf (pdf: the density the direction was drawn from).
+__global__ void __launch_bounds__(256) k_guide_collect(PTParams P, PTState st) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= P.nb) return;
+  const int nrec = st.ctl[slot].z & 15;
+  if (nrec == 0) return;
+  const float4 L = st.L[slot];
+  const size_t ns = size_t(st.nslots);
+  for (int r = 0; r < nrec; ++r) {
+    const size_t b = size_t(5 * r) * ns + slot;
+    const float4 r0 = st.rec[b], r1 = st.rec[b + ns], r2 = st.rec[b + 2 * ns], r3 = st.rec[b + 3 * ns],
+                 sn = st.rec[b + 4 * ns];
+    float li = 0.f;
+    if (r3.x > 0.f) li += (L.x - sn.x) / r3.x;
+    if (r3.y > 0.f) li += (L.y - sn.y) / r3.y;
+    if (r3.z > 0.f) li += (L.z - sn.z) / r3.z;
+    const float cosi = fabsf(r1.x * r1.w + r1.y * r2.w + r1.z * r3.w);
+    const float w = (li * (1.f / 3.f)) * cosi / r0.w;
+    if (!(w > 0.f) || !isfinite(w)) continue;
+    const int e = agg_push(st.tcount);
+    if (e >= st.tcap) continue;
+    st.tsamp[4 * size_t(e)] = make_float4(r0.x, r0.y, r0.z, w);
+    st.tsamp[4 * size_t(e) + 1] = make_float4(r1.x, r1.y, r1.z, 0.f);
+    st.tsamp[4 * size_t(e) + 2] = make_float4(r2.x, r2.y, r2.z, 0.f);
+    st.tsamp[4 * size_t(e) + 3] = make_float4(r1.w, r2.w, r3.w, 0.f);
   }
 }
 
@@ -776,7 +912,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kSh, kTraceBlock, 0);
   const int shadowGrid = std::max(1, per) * ctx->num_sms;
   const int shadeGrid = ctx->num_sms * 8;
-  auto kShade = P.physical ? k_shade_phys : k_shade;
+  auto kShade = P.physical ? k_shade_phys<false> : k_shade;
   cudaEvent_t ev0, ev1;
   cudaEventCreate(&ev0);
   cudaEventCreate(&ev1);
@@ -991,7 +1127,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kSh, kTraceBlock, 0);
   const int shadowGrid = std::max(1, per) * ctx->num_sms;
   const int shadeGrid = ctx->num_sms * 8;
-  auto kShade = P.physical ? k_shade_phys : k_shade;
+  auto kShade = P.physical ? k_shade_phys<false> : k_shade;
   auto t0 = std::chrono::steady_clock::now();
   unsigned long long launches = 0;
   for (unsigned long long g0 = 0; g0 < total; g0 += (unsigned long long)B) {
@@ -1038,6 +1174,201 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
   }
   if (err) return fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render_device_noalloc: traversal stack overflow");
   return GBRT_OK;
+}
+
+// ------------------------------------------------------ guided render ----
+// gbrt_render_guided: passes of the physical estimator; with a guide, the
+// first train_passes passes record training samples and each is followed by
+// steps_per_pass Adam steps; vertices sample the guide once it has been
+// trained (or given weights). The film is the mean over all passes.
+static unsigned long long pass_seed(unsigned long long seed, int pass) {
+  unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(pass + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render_params* prm,
+                                      gbrt_guide* g, const gbrt_guide_params* gp, float* film,
+                                      gbrt_guide_stats* stats) {
+  gbrt_ctx* ctx = s->ctx;
+  if (!cam || !prm || !gp || !film) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: NULL argument");
+  if (cam->width <= 0 || cam->height <= 0 || prm->x_samples <= 0 || prm->y_samples <= 0 || prm->max_depth <= 0 ||
+      prm->max_depth > 64)
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: bad camera or render parameters");
+  if (prm->semantics != GBRT_SEM_PHYSICAL)
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: needs the physical estimator (GBRT_SEM_PHYSICAL)");
+  if (!(prm->termination_prob >= 0.f && prm->termination_prob < 1.f))
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: termination probability outside [0, 1)");
+  if (!(gp->guide_fraction >= 0.f && gp->guide_fraction <= 1.f) || gp->passes < 0 || gp->train_passes < 0 ||
+      gp->steps_per_pass < 0 || (gp->passes == 0 && !(gp->time_budget_ms > 0.f)))
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: bad guide parameters");
+  const bool useGuide = g && gp->guide_fraction > 0.f;
+  const bool training = useGuide && gp->train_passes > 0 && gp->steps_per_pass > 0;
+  if (training && (gp->batch_samples <= 0 || !(gp->learning_rate > 0.f)))
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: training needs batch_samples and learning_rate");
+  if (g && g->device != s->device)
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: guide and scene live on different devices");
+  cudaStream_t stream = ctx->stream;
+  GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  const unsigned long long npix = (unsigned long long)cam->width * cam->height;
+  const int spp = prm->x_samples * prm->y_samples;
+  const unsigned long long total = npix * (unsigned long long)spp;
+  long long B = prm->batch_paths > 0 ? prm->batch_paths : (1ll << 22);
+  B = std::max<long long>(1, std::min<long long>(B, (long long)total));
+
+  Buffers buf(stream);
+  PTState st;
+  std::memset(&st, 0, sizeof st);
+  cudaError_t e = cudaSuccess;
+  auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
+  A(buf.alloc(&st.alpha, B)); A(buf.alloc(&st.L, B)); A(buf.alloc(&st.ctl, B));
+  A(buf.alloc(&st.pv_p, 1)); A(buf.alloc(&st.pv_n, 1)); A(buf.alloc(&st.pv_d, 1)); A(buf.alloc(&st.pv_a, 1));
+  A(buf.alloc(&st.ext[0], 2 * B)); A(buf.alloc(&st.ext[1], 2 * B));
+  A(buf.alloc(&st.ext_slot[0], B)); A(buf.alloc(&st.ext_slot[1], B));
+  A(buf.alloc(&st.hits, B));
+  A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
+  A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
+  long long tcap = 0;
+  if (useGuide) {
+    A(buf.alloc(&st.gin, 3 * B));
+    A(buf.alloc(&st.mix, 10 * B));
+    if (training) {
+      A(buf.alloc(&st.rec, 5ll * kRecords * B));
+      tcap = std::min<long long>((long long)gp->steps_per_pass * gp->batch_samples, 1ll << 25);
+      A(buf.alloc(&st.tsamp, 4 * tcap));
+      A(buf.alloc(&st.tcount, 1));
+    }
+  }
+  st.tcap = int(tcap);
+  st.nslots = int(B);
+  double* d_sum = nullptr;
+  float* d_film = nullptr;
+  A(buf.alloc(&d_sum, npix * 3));
+  A(buf.alloc(&d_film, npix * 3));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "guided render buffers");
+  A(cudaMemsetAsync(d_sum, 0, npix * 3 * sizeof(double), stream));
+  A(cudaMemsetAsync(st.tally, 0, 8 * sizeof(unsigned long long), stream));
+  A(cudaMemsetAsync(st.err, 0, sizeof(int), stream));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "guided render set-up");
+
+  const TraceKernels tk = pick_kernels(s, false);
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tk.ext, kTraceBlock, 0);
+  const int traceGrid = std::max(1, per) * ctx->num_sms;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tk.sh, kTraceBlock, 0);
+  const int shadowGrid = std::max(1, per) * ctx->num_sms;
+  const int shadeGrid = ctx->num_sms * 8;
+  cudaEvent_t ev0, ev1, t0, t1;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(ev0, stream);
+  int passes = 0, steps = 0;
+  unsigned long long samples = 0;
+  double train_ms = 0.0, elapsed = 0.0;
+  gbrt_status status = GBRT_OK;
+  for (int pass = 0;; ++pass) {
+    if (gp->passes > 0 && pass >= gp->passes) break;
+    PTParams P;
+    init_params(P, *cam, *prm, total);
+    P.seed = pass_seed(prm->seed, pass);
+    const bool record = training && pass < gp->train_passes;
+    P.guided = (useGuide && g->ready) ? 1 : 0;
+    P.guide_frac = gp->guide_fraction;
+    P.record = record ? 1 : 0;
+    if (record) A(cudaMemsetAsync(st.tcount, 0, sizeof(int), stream));
+    auto kShade = (P.guided || P.record) ? k_shade_phys<true> : k_shade_phys<false>;
+    for (unsigned long long g0 = 0; g0 < total && e == cudaSuccess; g0 += (unsigned long long)B) {
+      P.g0 = g0;
+      P.nb = int(std::min<unsigned long long>((unsigned long long)B, total - g0));
+      k_raygen<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
+      for (int it = 0; it < P.D; ++it) {
+        int cur = it & 1;
+        tk.ext<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
+        if (P.guided) {
+          k_guide_prep<<<shadeGrid, 256, 0, stream>>>(s->view, st, cur);
+          A(guide::launch_infer(g, st.gin, st.counts + cur, 0, st.mix, stream));
+        }
+        kShade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
+        tk.sh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
+      }
+      unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
+      k_accumulate<<<unsigned((p1 - p0 + 256) / 256), 256, 0, stream>>>(P, st, d_sum, nullptr);
+      if (record) k_guide_collect<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
+      A(cudaGetLastError());
+    }
+    if (e != cudaSuccess) break;
+    ++passes;
+    if (record) {
+      int cnt = 0;
+      A(cudaMemcpyAsync(&cnt, st.tcount, sizeof cnt, cudaMemcpyDeviceToHost, stream));
+      A(cudaStreamSynchronize(stream));
+      const int avail = int(std::min<long long>(cnt, tcap));
+      cudaEventRecord(t0, stream);
+      for (int k = 0; k < gp->steps_per_pass && avail > 0 && e == cudaSuccess; ++k) {
+        int start = int((long long)k * gp->batch_samples % avail);
+        int n = std::min(gp->batch_samples, avail - start);
+        A(guide::train(g, st.tsamp + 4 * size_t(start), n, gp->learning_rate, true, stream));
+        g->ready = true;
+        ++steps;
+      }
+      cudaEventRecord(t1, stream);
+      A(cudaStreamSynchronize(stream));
+      float tms = 0.f;
+      cudaEventElapsedTime(&tms, t0, t1);
+      train_ms += tms;
+      samples += (unsigned long long)avail;
+    }
+    cudaEventRecord(ev1, stream);
+    A(cudaEventSynchronize(ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    elapsed = ms;
+    if (e != cudaSuccess) break;
+    if (gp->passes == 0 && elapsed >= gp->time_budget_ms) break;
+  }
+  if (e == cudaSuccess && passes > 0) {
+    size_t n3 = size_t(npix) * 3;
+    k_finalize<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_sum, d_film, n3, 1.0 / (double(spp) * passes));
+    A(cudaGetLastError());
+    A(cudaMemcpyAsync(film, d_film, n3 * sizeof(float), cudaMemcpyDeviceToHost, stream));
+  }
+  unsigned long long tally[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int err = 0, gerr = 0;
+  float loss = 0.f;
+  A(cudaMemcpyAsync(tally, st.tally, sizeof tally, cudaMemcpyDeviceToHost, stream));
+  A(cudaMemcpyAsync(&err, st.err, sizeof err, cudaMemcpyDeviceToHost, stream));
+  if (g) {
+    A(cudaMemcpyAsync(&gerr, g->d_err, sizeof gerr, cudaMemcpyDeviceToHost, stream));
+    A(cudaMemcpyAsync(&loss, g->d_loss, sizeof loss, cudaMemcpyDeviceToHost, stream));
+  }
+  A(cudaStreamSynchronize(stream));
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gbrt_render_guided");
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    stats->passes = passes;
+    stats->train_steps = steps;
+    stats->paths = (unsigned long long)passes * total;
+    stats->train_samples = samples;
+    stats->total_ms = elapsed;
+    stats->train_ms = train_ms;
+    stats->last_loss = steps > 0 ? loss : 0.f;
+    stats->extension_rays = tally[0];
+    stats->shadow_rays = tally[1];
+    stats->nonfinite = tally[2];
+  }
+  if (gerr) {
+    cudaMemsetAsync(g->d_err, 0, sizeof(int), stream);
+    return fail(ctx, GBRT_ERR_TIMEOUT, "gbrt_render_guided: a tensor-core wait timed out");
+  }
+  if (err) return fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render_guided: traversal stack overflow");
+  return status;
 }
 
 }  // namespace gbrt
@@ -1087,6 +1418,14 @@ gbrt_status gbrt_render_device_noalloc(gbrt_scene* s, const gbrt_camera* cam, co
   if (!s) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_render_device_noalloc: NULL scene");
   clear_error(s->ctx);
   return render_noalloc_impl(s, cam, prm, d_film, d_sum, d_sumsq, stats);
+}
+
+gbrt_status gbrt_render_guided(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render_params* prm,
+                               gbrt_guide* guide, const gbrt_guide_params* gp, float* film,
+                               gbrt_guide_stats* stats) {
+  if (!s) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: NULL scene");
+  clear_error(s->ctx);
+  return render_guided_impl(s, cam, prm, guide, gp, film, stats);
 }
 
 }  // extern "C"

@@ -304,6 +304,12 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     planeMeta[i] = make_int2(pid, matIndex(pl.material));
   }
 
+  float sb[6] = {0, 0, 0, 0, 0, 0};
+  for (size_t i = 0; i < boxes.size(); ++i)
+    for (int k = 0; k < 3; ++k) {
+      sb[k] = i ? std::min(sb[k], boxes[i].lo[k]) : boxes[i].lo[k];
+      sb[3 + k] = i ? std::max(sb[3 + k], boxes[i].hi[k]) : boxes[i].hi[k];
+    }
   BuildOptions bo;
   BuildResult br = build_bvh(boxes, bo);
   if (br.max_depth > kMaxTreeDepth)
@@ -373,6 +379,7 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   s->max_depth4 = c4.max_depth;
   s->sah_cost = br.sah_cost;
   s->n_prims = int32_t(nPrims);
+  std::memcpy(s->bounds, sb, sizeof sb);
   s->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   *out = s;
   return GBRT_OK;
@@ -384,6 +391,12 @@ gbrt_status gbrt_scene_destroy(gbrt_scene* s) {
   cudaSetDevice(s->device);
   free_scene(s);  // cudaFree waits for work using the memory
   delete s;
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_scene_bounds(const gbrt_scene* s, float bounds[6]) {
+  if (!s || !bounds) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_scene_bounds: NULL argument");
+  std::memcpy(bounds, s->bounds, sizeof s->bounds);
   return GBRT_OK;
 }
 

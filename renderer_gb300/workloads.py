@@ -11,6 +11,14 @@ icosphere_scene()  an icosahedron subdivided 8 times (1,310,720 triangles)
                    of albedo 0.6, a 1024x512 lat-long sky (seeded gradient and a
                    0.5 degree sun disc of radiance 5e4) and one area light;
                    1024x1024, 8x8 spp, max depth 12.
+two_rooms()        two diffuse rooms (each 4 x 3 x 3, albedo 0.7) sharing a
+                   wall with a 0.2-wide door gap, a 0.3 x 0.3 area light of
+                   radiance 200 on the far room's ceiling, the camera in the
+                   near room, a glossy Blinn floor (exponent 200) and a
+                   500,000-triangle displaced grid (500 x 500 quads) on the
+                   near room's side wall; 1024x768. Lit almost only through
+                   the door: the case path guiding is for (physical
+                   semantics).
 Spectra are BGR. Values given in RGB below are swapped on the way in.
 """
 import numpy as np
@@ -204,3 +212,59 @@ def icosphere_scene(levels=8, seed=0, width=1024, height=1024, env_size=(1024, 5
 
 def icosphere_params(seed=0):
     return render_params(8, 8, 0.5, 12, seed)
+
+
+# ------------------------------------------------------------------ two rooms
+def displaced_grid(n, x0, x1, y0, y1, z_wall, depth, seed=0):
+    """n x n quads (2 n^2 triangles) of the heightfield z = z_wall - depth *
+    (1 + fbm(x, y)) / 2 over [x0, x1] x [y0, y1], with smooth normals."""
+    xs = np.linspace(x0, x1, n + 1)
+    ys = np.linspace(y0, y1, n + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    P2 = np.stack([X.ravel(), Y.ravel(), np.zeros(X.size)], 1)
+    h = 0.5 * (1.0 + fbm(P2 * 1.5, seed))
+    P = np.stack([X.ravel(), Y.ravel(), z_wall - depth * h], 1)
+    idx = np.arange((n + 1) * (n + 1)).reshape(n + 1, n + 1)
+    a, b, c, d = idx[:-1, :-1].ravel(), idx[1:, :-1].ravel(), idx[1:, 1:].ravel(), idx[:-1, 1:].ravel()
+    F = np.concatenate([np.stack([a, b, c], 1), np.stack([a, c, d], 1)])
+    tri = P[F]
+    fn = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    N = np.zeros_like(P)
+    for col in range(3):
+        for k in range(3):
+            N[:, col] += np.bincount(F[:, k], weights=fn[:, col], minlength=len(P))
+    N /= np.linalg.norm(N, axis=1, keepdims=True)
+    return tri.reshape(-1, 9).astype(np.float32), N[F].reshape(-1, 9).astype(np.float32)
+
+
+def two_rooms(width=1024, height=768, mesh_quads=500, seed=0):
+    s = SceneData()
+    white = s.add_material(_abi.MAT_DIFFUSE, kd=bgr((0.7, 0.7, 0.7)))
+    floor = s.add_material(_abi.MAT_BLINN, kd=bgr((0.25, 0.25, 0.25)), ks=bgr((0.45, 0.45, 0.45)), exponent=200.0)
+    relief = s.add_material(_abi.MAT_DIFFUSE, kd=bgr((0.7, 0.6, 0.5)))
+    q = []
+    for x0 in (0.0, 4.0):   # per room: floor, ceiling
+        q.append(((x0, 0, 0), (x0 + 4, 0, 0), (x0 + 4, 0, 3), (x0, 0, 3), floor))
+        q.append(((x0, 3, 0), (x0, 3, 3), (x0 + 4, 3, 3), (x0 + 4, 3, 0), white))
+    q.append(((0, 0, 0), (0, 0, 3), (0, 3, 3), (0, 3, 0), white))          # end wall x = 0
+    q.append(((8, 0, 0), (8, 3, 0), (8, 3, 3), (8, 0, 3), white))          # end wall x = 8
+    q.append(((0, 0, 0), (0, 3, 0), (8, 3, 0), (8, 0, 0), white))          # side wall z = 0
+    q.append(((0, 0, 3), (8, 0, 3), (8, 3, 3), (0, 3, 3), white))          # side wall z = 3
+    # shared wall x = 4 with a door gap z in [1.4, 1.6], y in [0, 2.2]
+    q.append(((4, 0, 0), (4, 0, 1.4), (4, 3, 1.4), (4, 3, 0), white))
+    q.append(((4, 0, 1.6), (4, 0, 3), (4, 3, 3), (4, 3, 1.6), white))
+    q.append(((4, 2.2, 1.4), (4, 2.2, 1.6), (4, 3, 1.6), (4, 3, 1.4), white))
+    s.quads = q
+    pos, nrm = displaced_grid(mesh_quads, 0.6, 3.4, 0.2, 2.6, 2.97, 0.3, seed)
+    s.tri_pos = pos
+    s.tri_nrm = nrm
+    s.tri_mat = np.full(len(pos), relief, np.int32)
+    s.lights = [dict(type=_abi.LIGHT_AREA, origin=(5.85, 2.999, 1.35), u=(0.3, 0, 0), v=(0, 0, 0.3),
+                     intensity=(200.0, 200.0, 200.0))]
+    s.camera = dict(eye=(0.4, 1.5, 0.6), look_at=(4.0, 1.1, 1.8), up=(0, 1, 0), fov=1.0471976, width=width,
+                    height=height)
+    return s
+
+
+def two_rooms_params(x_samples=1, y_samples=1, seed=0, max_depth=12, termination_prob=0.5):
+    return render_params(x_samples, y_samples, termination_prob, max_depth, seed, semantics=_abi.SEM_PHYSICAL)

@@ -1,0 +1,222 @@
+"""Neural path guiding: the network kernels against the FP64 restatement
+(oracle/guide_ref.py), training, and the guided estimator against the plain
+physical one.
+
+CPU tests pin the restatement itself (its gradient against finite
+differences, its mixture's normalisation); GPU tests compare the tcgen05
+kernels with it and check what guiding does to a render."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import guide_ref as gr
+
+
+def _unit(v):
+    return v / np.linalg.norm(v, axis=-1, keepdims=True)
+
+
+def random_inputs(n, bounds, rng):
+    lo, hi = np.asarray(bounds[:3]), np.asarray(bounds[3:])
+    p = lo + rng.random((n, 3)) * (hi - lo)
+    return np.concatenate([p, _unit(rng.normal(size=(n, 3))), _unit(rng.normal(size=(n, 3)))], 1).astype(np.float32)
+
+
+def random_samples(n, bounds, rng):
+    x = random_inputs(n, bounds, rng)
+    wi = _unit(rng.normal(size=(n, 3)))
+    w = rng.exponential(1.0, size=(n, 1))
+    return np.concatenate([x, wi, w], 1).astype(np.float32)
+
+
+def init_weights(seed=0):
+    rng = np.random.default_rng(seed)
+    parts = []
+    for (a, b), s in zip(gr.SHAPES, (1, 1, 1, 0.1)):
+        lim = math.sqrt(6 / b) * s
+        parts.append(rng.uniform(-lim, lim, a * b))
+    return np.concatenate(parts).astype(np.float32)
+
+
+BOUNDS = np.array([-1.0, 0.0, -2.0, 3.0, 2.0, 1.0], np.float32)
+
+
+# ------------------------------------------------------------------ CPU ----
+def test_reference_gradient_matches_finite_differences():
+    rng = np.random.default_rng(1)
+    w = init_weights(1).astype(np.float64)
+    s = random_samples(40, BOUNDS, rng)
+    _, g = gr.loss_and_grad(w, s, BOUNDS, bf16=False)
+    for i in rng.choice(len(w), 24, replace=False):
+        h = 1e-6
+        wp, wm = w.copy(), w.copy()
+        wp[i] += h
+        wm[i] -= h
+        lp, _ = gr.loss_and_grad(wp, s, BOUNDS, bf16=False)
+        lm, _ = gr.loss_and_grad(wm, s, BOUNDS, bf16=False)
+        assert g[i] == pytest.approx((lp - lm) / (2 * h), rel=1e-4, abs=1e-9)
+
+
+def test_reference_mixture_integrates_to_one():
+    rng = np.random.default_rng(2)
+    mix = gr.mixture(init_weights(2) * 4, random_inputs(3, BOUNDS, rng), BOUNDS, bf16=False)
+    n = 200000
+    k = np.arange(n) + 0.5
+    z = 1 - 2 * k / n
+    phi = np.pi * (1 + 5 ** 0.5) * k
+    r = np.sqrt(1 - z * z)
+    d = np.stack([r * np.cos(phi), r * np.sin(phi), z], 1)
+    for m in mix:
+        integral = gr.mixture_pdf(np.repeat(m[None], n, 0), d).mean() * 4 * np.pi
+        assert integral == pytest.approx(1.0, rel=2e-3)
+
+
+def test_encoding_layout():
+    x = np.array([[0.5, 1.0, -0.5, 0, 0, 1, 0, 0, 1]], np.float32)
+    e = gr.encode(x, BOUNDS).numpy()[0]
+    assert e.shape == (208,)
+    # position x normalised to 0.375: band 0 of coordinate 0 is sin/cos(0.375 pi)
+    assert e[0] == pytest.approx(math.sin(0.375 * math.pi)) and e[1] == pytest.approx(math.cos(0.375 * math.pi))
+    # outgoing direction +z: theta = 0 -> the first theta bin is the largest
+    assert np.argmax(e[144:176]) == 0
+
+
+# ------------------------------------------------------------------ GPU ----
+@pytest.fixture
+def guide(ctx):
+    from renderer_gb300.guiding import Guide
+    g = Guide(ctx, BOUNDS, seed=3)
+    yield g
+    g.close()
+
+
+@pytest.mark.gpu
+def test_guide_eval_matches_reference(guide):
+    rng = np.random.default_rng(4)
+    w = init_weights(4) * 3  # larger weights: non-trivial mixtures
+    guide.set_weights(w)
+    assert np.array_equal(guide.weights(), w)
+    x = random_inputs(1000 + 77, BOUNDS, rng)  # a ragged last tile
+    got = guide.eval(x)
+    ref = gr.mixture(w, x, BOUNDS, bf16=True)
+    # Both sides round the same tensors to bfloat16; FP32 and FP64 sums can
+    # still round a hidden activation to neighbouring bfloat16 values (one
+    # ulp, 2^-8 relative), which these large weights amplify in a few rows.
+    dpi = np.abs(got[:, :8] - ref[:, :8])
+    assert np.quantile(dpi, 0.99) < 1e-4 and dpi.max() < 3e-2
+    gl, rl = got[:, 8:].reshape(-1, 8, 4), ref[:, 8:].reshape(-1, 8, 4)
+    cosang = (gl[..., :3] * rl[..., :3]).sum(-1)
+    assert np.quantile(cosang, 0.01) > 0.99999 and cosang.min() > 0.99
+    dk = np.abs(gl[..., 3] / rl[..., 3] - 1)
+    assert np.quantile(dk, 0.99) < 1e-3 and dk.max() < 0.1
+    d = _unit(rng.normal(size=(len(x), 3)))
+    dq = np.abs(gr.mixture_pdf(got, d) / gr.mixture_pdf(ref, d) - 1)
+    assert np.quantile(dq, 0.99) < 1e-3
+
+
+@pytest.mark.gpu
+def test_guide_gradient_matches_reference(guide):
+    rng = np.random.default_rng(5)
+    w = init_weights(5) * 2
+    guide.set_weights(w)
+    s = random_samples(4096 + 333, BOUNDS, rng)
+    g, loss = guide.gradient(s)
+    lr, gref = gr.loss_and_grad(w, s, BOUNDS, bf16=True)
+    assert loss == pytest.approx(lr, rel=2e-3)
+    o = 0
+    for a, b in gr.SHAPES:
+        x, y = g[o:o + a * b].astype(np.float64), gref[o:o + a * b]
+        o += a * b
+        cos = x @ y / (np.linalg.norm(x) * np.linalg.norm(y))
+        rel = np.linalg.norm(x - y) / np.linalg.norm(y)
+        assert cos > 0.999 and rel < 3e-2, ((a, b), cos, rel)
+
+
+@pytest.mark.gpu
+def test_guide_learns_a_lobe(guide):
+    """Samples drawn from one vMF lobe at every position: the trained mixture
+    puts its mass there."""
+    rng = np.random.default_rng(6)
+    mu = _unit(np.array([0.3, 0.5, -0.8]))
+    kappa = 40.0
+
+    def vmf(n):
+        u1, u2 = rng.random(n), rng.random(n)
+        w = 1 + np.log(u1 + (1 - u1) * np.exp(-2 * kappa)) / kappa
+        t = _unit(np.cross(mu, [1.0, 0, 0]))
+        b = np.cross(mu, t)
+        s = np.sqrt(np.clip(1 - w * w, 0, 1))
+        return (s * np.cos(2 * np.pi * u2))[:, None] * t + (s * np.sin(2 * np.pi * u2))[:, None] * b + w[:, None] * mu
+
+    losses = []
+    for it in range(300):
+        x = random_inputs(4096, BOUNDS, rng)
+        s = np.concatenate([x, vmf(4096), np.ones((4096, 1))], 1).astype(np.float32)
+        losses.append(guide.train_step(s, 1e-2))
+    assert losses[-1] < losses[0] - 2.0
+    x = random_inputs(256, BOUNDS, rng)
+    q = gr.mixture_pdf(guide.eval(x), np.repeat(mu[None], 256, 0))
+    true_peak = kappa / (2 * np.pi * (1 - np.exp(-2 * kappa)))
+    assert np.median(q) > 0.3 * true_peak
+
+
+def _small_rooms(ctx, w=64, h=48, quads=24):
+    from renderer_gb300.runtime import GpuScene
+    from renderer_gb300.workloads import two_rooms
+    data = two_rooms(w, h, mesh_quads=quads)
+    return GpuScene(ctx, data), data.camera_struct()
+
+
+@pytest.mark.gpu
+def test_guided_render_needs_physical_semantics(ctx):
+    from renderer_gb300 import GbrtError
+    from renderer_gb300.guiding import guide_params, render_guided
+    from renderer_gb300.scene import render_params
+    sc, cam = _small_rooms(ctx)
+    with pytest.raises(GbrtError):
+        render_guided(sc, cam, render_params(1, 1, 0.5, 8, 0), None, guide_params(passes=1))
+
+
+@pytest.mark.gpu
+def test_guide_off_matches_plain_physical_render(ctx):
+    """guide = NULL is the physical estimator: one pass equals gbrt_render
+    with the pass's seed... statistically; many passes converge to it."""
+    from renderer_gb300.guiding import guide_params, render_guided
+    from renderer_gb300.runtime import PerPixelRenderer
+    from renderer_gb300.workloads import two_rooms_params
+    sc, cam = _small_rooms(ctx)
+    prm = two_rooms_params(4, 4, seed=1)
+    film, st = render_guided(sc, cam, prm, None, guide_params(passes=16))
+    assert st.passes == 16 and st.train_steps == 0
+    r = PerPixelRenderer(sc, cam, {"pt-x-samples": 16, "pt-y-samples": 16, "pt-termination-prob": 0.5},
+                         seed=7, max_depth=12)
+    r.params.semantics = 1
+    plain = r.render()
+    assert film.mean() == pytest.approx(plain.mean(), rel=0.03)
+
+
+@pytest.mark.gpu
+def test_guided_render_is_unbiased_and_helps(ctx):
+    """The two rooms, lit through the door: a guide trained online by the
+    renderer (512 Adam steps on its own radiance samples) leaves the image's
+    expectation unchanged and, at equal samples per pixel, lowers the relMSE
+    against a 16,384-spp render."""
+    from renderer_gb300.guiding import Guide, guide_params, render_guided, scene_bounds
+    from renderer_gb300.workloads import two_rooms_params
+    sc, cam = _small_rooms(ctx, 128, 96, 24)
+    ref, _ = render_guided(sc, cam, two_rooms_params(8, 8, seed=11), None, guide_params(passes=256))
+    plain, _ = render_guided(sc, cam, two_rooms_params(8, 8, seed=12), None, guide_params(passes=4))
+    g = Guide(ctx, scene_bounds(sc), seed=1)
+    gp = guide_params(0.5, passes=16, train_passes=16, steps_per_pass=32, batch_samples=1 << 16, learning_rate=1e-2)
+    trained, st = render_guided(sc, cam, two_rooms_params(8, 8, seed=13), g, gp)
+    guided, st2 = render_guided(sc, cam, two_rooms_params(8, 8, seed=14), g, guide_params(0.5, passes=4))
+    g.close()
+    assert st.train_steps == 512 and st.train_samples > 0 and st2.train_steps == 0
+    assert trained.mean() == pytest.approx(ref.mean(), rel=0.02)
+    assert guided.mean() == pytest.approx(ref.mean(), rel=0.02)
+
+    def relmse(x):
+        return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    assert relmse(guided) < 0.75 * relmse(plain), (relmse(guided), relmse(plain))
