@@ -178,6 +178,120 @@ def run_reference(args, ws, rank, dist):
     print(json.dumps(line))
 
 
+GUIDED_WORKLOAD = ("two rooms 4x3x3 (albedo 0.7) joined by a 0.2-wide door, 0.3x0.3 area light of radiance 200 "
+                   "in the far room, 500,000-triangle displaced grid, Blinn floor (exponent 200), 1024x768, "
+                   "physical semantics, max depth 12, RR p=0.5")
+
+
+def interp_time(curve, target):
+    """Time at which relMSE reaches target, log-log interpolation along a
+    (ms, relmse) curve sorted by time; None when the curve never gets there."""
+    import math
+    pts = sorted(curve)
+    for (t0, e0), (t1, e1) in zip(pts, pts[1:]):
+        if e0 > target >= e1:
+            f = (math.log(target) - math.log(e0)) / (math.log(e1) - math.log(e0))
+            return math.exp(math.log(t0) + f * (math.log(t1) - math.log(t0)))
+    if pts and pts[0][1] <= target:
+        return pts[0][0]
+    return None
+
+
+def run_guided(args):
+    """Equal-time relMSE of guided against plain GPU path tracing on the
+    two-room scene, both against a high-sample render of the plain physical
+    estimator accumulated in FP64; plus the network kernels' tensor rates."""
+    import numpy as np
+
+    from renderer_gb300 import _abi, workloads
+    from renderer_gb300.guiding import Guide, guide_params, render_guided, scene_bounds
+    from renderer_gb300.runtime import Context, GpuScene
+
+    ctx = Context(0)
+    s = workloads.two_rooms(1024, 768, mesh_quads=500)
+    gs = GpuScene(ctx, s)
+    cam = s.camera_struct()
+    bounds = scene_bounds(gs)
+
+    def prm(xs, seed, flags=0):
+        p = workloads.two_rooms_params(xs, xs, seed=seed)
+        p.flags = flags
+        return p
+
+    def train_gp(budget_ms=0.0, passes=0):
+        return guide_params(args.guide_fraction, passes=passes, train_passes=args.train_passes,
+                            steps_per_pass=args.train_steps, batch_samples=1 << 18, learning_rate=1e-2,
+                            time_budget_ms=budget_ms, flags=_abi.GUIDE_PIXEL_RELATIVE)
+
+    if args.profile:
+        g = Guide(ctx, bounds, seed=1)
+        gp = guide_params(args.guide_fraction, passes=2, train_passes=2, steps_per_pass=2, batch_samples=1 << 18)
+        _, st = render_guided(gs, cam, prm(1, 1), g, gp)
+        _, st2 = render_guided(gs, cam, prm(1, 2), g, guide_params(args.guide_fraction, passes=1))
+        print(json.dumps({"profile": "guided", "train_steps": st.train_steps, "infer_rows": st2.infer_rows}))
+        return
+
+    ref_spp = max(1, args.ref_spp // 64) * 64
+    if args.ref_cache and os.path.exists(args.ref_cache):
+        z = np.load(args.ref_cache)
+        ref, ref_ms = z["film"], float(z["ms"])
+        assert int(z["spp"]) == ref_spp, "cached reference has another sample count"
+    else:
+        ref, st = render_guided(gs, cam, prm(8, 1), None, guide_params(passes=ref_spp // 64))
+        ref_ms = st.total_ms
+        if args.ref_cache:
+            np.savez(args.ref_cache, film=ref, ms=ref_ms, spp=ref_spp)
+
+    def relmse(x):
+        return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    plain = []
+    for spp in args.spp_list:
+        img, st = render_guided(gs, cam, prm(1, 1000 + spp), None, guide_params(passes=spp))
+        plain.append((st.total_ms, relmse(img), spp))
+    guided = []
+    for t, _, spp in plain:
+        g = Guide(ctx, bounds, seed=7)
+        img, st = render_guided(gs, cam, prm(1, 2000 + spp), g, train_gp(budget_ms=t))
+        guided.append((st.total_ms, relmse(img), st.passes, st.train_steps, st.train_ms))
+        g.close()
+    # The network kernels in a trained guide's render, timed per launch.
+    g = Guide(ctx, bounds, seed=7)
+    _, tst = render_guided(gs, cam, prm(1, 3, _abi.RENDER_TIME_KERNELS), g, train_gp(passes=64))
+    _, ist = render_guided(gs, cam, prm(1, 4, _abi.RENDER_TIME_KERNELS), g,
+                           guide_params(args.guide_fraction, passes=16))
+    g.close()
+    f_inf = 2 * (208 * 64 + 64 * 64 + 64 * 64 + 64 * 40)
+    f_train = 2 * f_inf + 2 * (64 * 64 + 64 * 64 + 40 * 64)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0))
+    inf_tflops = ist.infer_rows * f_inf / (ist.infer_ms * 1e-3) / 1e12 if ist.infer_ms else None
+    tr_tflops = tst.train_steps * (1 << 18) * f_train / (tst.train_ms * 1e-3) / 1e12 if tst.train_ms else None
+    t_plain = interp_time([(t, e) for t, e, _ in plain], 0.01)
+    t_guided = interp_time([(t, e) for t, e, *_ in guided], 0.01)
+    line = {"metric": "equal-time relMSE, guided vs plain GPU PT", "unit": "relMSE", "higher_is_better": False,
+            "config": {"workload": GUIDED_WORKLOAD, "reference_spp": ref_spp,
+                       "reference_ms": ref_ms, "guide_fraction": args.guide_fraction,
+                       "train": "online, Adam lr 1e-2, %d step(s) of 2^18 samples after %s one-spp pass, "
+                                "sample weights relative to their pixel"
+                                % (args.train_steps, "every" if args.train_passes >= 1 << 20
+                                   else "each of the first %d" % args.train_passes),
+                       "passes": "inverse-variance weighted (the first, unguided pass seeds the mean)"},
+            "plain": [{"ms": t, "relmse": e, "spp": n} for t, e, n in plain],
+            "guided": [{"ms": t, "relmse": e, "spp": n, "train_steps": k, "train_ms": tm}
+                       for t, e, n, k, tm in guided],
+            "time_to_relmse_0.01_ms": {"plain": t_plain, "guided": t_guided,
+                                       "ratio": (t_guided / t_plain) if t_plain and t_guided else None},
+            "mlp": {"bound": "tensor", "unit": "TFLOP/s", "peak": tc_peak,
+                    "peak_kind": "measured" if "bf16_tflops" in peaks else "fallback",
+                    "inference": {"achieved": inf_tflops, "frac": inf_tflops / tc_peak if inf_tflops else None,
+                                  "rows": ist.infer_rows, "ms": ist.infer_ms, "flop_per_row": f_inf},
+                    "training": {"achieved": tr_tflops, "frac": tr_tflops / tc_peak if tr_tflops else None,
+                                 "steps": tst.train_steps, "ms": tst.train_ms, "flop_per_sample": f_train}}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -190,8 +304,19 @@ def main():
     ap.add_argument("--batch-paths", type=int, default=0)
     ap.add_argument("--profile", action="store_true",
                     help="for ncu: one untimed frame, then one frame, nothing else")
+    ap.add_argument("--guided", action="store_true",
+                    help="equal-time relMSE of neural path guiding against plain path tracing (two rooms)")
+    ap.add_argument("--ref-spp", type=int, default=65536)
+    ap.add_argument("--ref-cache", default="", help="npz file holding (or receiving) the reference render")
+    ap.add_argument("--spp-list", type=lambda x: [int(v) for v in x.split(",")], default=[16, 32, 64, 128, 256, 512])
+    ap.add_argument("--guide-fraction", type=float, default=0.5)
+    ap.add_argument("--train-passes", type=int, default=1 << 30, help="passes that train (default: all)")
+    ap.add_argument("--train-steps", type=int, default=1, help="Adam steps of 2^18 samples after a training pass")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.guided:
+        run_guided(args)
+        return
     ws, rank, local, dist = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank, dist)

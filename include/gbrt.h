@@ -377,8 +377,23 @@ typedef struct gbrt_guide_params {
   int32_t batch_samples;  /* training samples per step, e.g. 2^18 */
   float learning_rate;    /* e.g. 1e-2 */
   float time_budget_ms;   /* > 0 with passes = 0: equal-time rendering */
-  int32_t flags;          /* 0 */
+  int32_t guide_depth;    /* guide (and train on) path vertices i < guide_depth
+                             only (vertex 0 is the camera ray's hit); 0 = all */
+  int32_t flags;          /* gbrt_guide_flags */
 } gbrt_guide_params;
+
+typedef enum gbrt_guide_flags {
+  /* While a guide trains, passes are combined with weights inversely proportional
+   * to their relative squared deviation from the mean of the earlier passes
+   * (the first, unguided pass only seeds that mean), so that the noisy
+   * passes of an untrained network weigh little. This flag averages all
+   * passes with equal weights instead. Renders that do not train a guide
+   * always average equally. */
+  GBRT_GUIDE_EQUAL_WEIGHTS = 1,
+  /* Training samples weighted by their share of their pixel's value relative
+   * to sqrt(pixel^2 + 0.01) instead of by their radiance alone. */
+  GBRT_GUIDE_PIXEL_RELATIVE = 2
+} gbrt_guide_flags;
 
 typedef struct gbrt_guide_stats {
   int32_t passes;
@@ -392,6 +407,12 @@ typedef struct gbrt_guide_stats {
   double train_ms;
   float last_loss;
   int32_t pad;
+  /* With GBRT_RENDER_TIME_KERNELS: device time of the network's inference
+   * (input preparation included) and its launches; always: the rows (path
+   * vertices) the network evaluated. */
+  double infer_ms;
+  uint64_t infer_launches;
+  uint64_t infer_rows;
 } gbrt_guide_stats;
 
 /* Renders with the physical estimator (params->semantics must be

@@ -72,14 +72,15 @@ class Stats(C.Structure):
 class GuideParams(C.Structure):
     _fields_ = [("guide_fraction", C.c_float), ("passes", C.c_int32), ("train_passes", C.c_int32),
                 ("steps_per_pass", C.c_int32), ("batch_samples", C.c_int32), ("learning_rate", C.c_float),
-                ("time_budget_ms", C.c_float), ("flags", C.c_int32)]
+                ("time_budget_ms", C.c_float), ("guide_depth", C.c_int32), ("flags", C.c_int32)]
 
 
 class GuideStats(C.Structure):
     _fields_ = [("passes", C.c_int32), ("train_steps", C.c_int32), ("paths", C.c_uint64),
                 ("train_samples", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("nonfinite", C.c_uint64), ("total_ms", C.c_double), ("train_ms", C.c_double),
-                ("last_loss", C.c_float), ("pad", C.c_int32)]
+                ("last_loss", C.c_float), ("pad", C.c_int32), ("infer_ms", C.c_double),
+                ("infer_launches", C.c_uint64), ("infer_rows", C.c_uint64)]
 
 
 class Ray(C.Structure):
@@ -109,6 +110,7 @@ SCENE_WATERTIGHT = 1
 RENDER_TIME_KERNELS, RENDER_COUNT_TRAVERSAL = 1, 2
 NOALLOC_MAX_BATCH = 65536
 GUIDE_PARAMS, GUIDE_INPUT, GUIDE_OUTPUT, GUIDE_SAMPLE = 24064, 9, 40, 13
+GUIDE_EQUAL_WEIGHTS, GUIDE_PIXEL_RELATIVE = 1, 2
 
 P = C.c_void_p
 

@@ -39,11 +39,19 @@ namespace gbrt {
 namespace guide {
 
 // ------------------------------------------------------------ layouts ----
-// Inference: weights (49,152 B) and one activation tile [128][208] (53,248
-// B) reused for every layer; two blocks fit on an SM.
+// Shared by both kernels: the four weight matrices (49,152 B).
 constexpr int kSW1 = 0, kSW2 = 26624, kSW3 = 34816, kSW4 = 43008, kSWEnd = 49152;
-constexpr int kInferX = kSWEnd, kInferMisc = kInferX + 53248, kInferSmem = kInferMisc + 64;
-constexpr uint32_t kInferCols = 64;
+
+// Inference: one block per SM of kInferWG warpgroups that share the weights;
+// each warpgroup runs its own 128-row tile through the network with its own
+// 28,672-byte activation buffer, TMEM columns, mbarrier and named barrier.
+// Layer 1 takes the 208 input features in two halves (112 + 96) so that the
+// buffer holds one half at a time.
+constexpr int kInferWG = 6;
+constexpr int kEncA = 14, kEncB = 12;  // groups of 8 features in the two halves
+constexpr int kInferBuf = kRows * kEncA * 8 * 2;
+constexpr int kInferMisc = kSWEnd + kInferWG * kInferBuf, kInferSmem = kInferMisc + 8 * kInferWG + 16;
+constexpr uint32_t kInferCols = 512;  // 64 per warpgroup, rounded up to a power of two
 
 // Training: weights, transposed weights for dX, three activation tiles, the
 // region R (X0 rows in the forward pass, then the transposed X1..X3 at
@@ -57,7 +65,9 @@ constexpr uint32_t kTrainCols = 512;
 constexpr uint32_t kColScratch = 0, kColW1lo = 64, kColW1hi = 128, kColW2 = 192, kColW3 = 256, kColW4 = 320;
 
 static_assert(kTrainSmem <= 232448, "training tile exceeds the shared memory of a block");
-static_assert(2 * kInferSmem <= 233472, "two inference blocks must fit on an SM");
+static_assert(kInferSmem <= 232448, "inference block exceeds the shared memory of a block");
+static_assert(64 * kInferWG <= int(kInferCols), "TMEM columns of the inference block");
+static_assert(kEncA + kEncB == kIn / 8, "encoding halves");
 
 // Layer input ReLU(TMEM columns [0, 64)) of row r into an interleaved
 // [128][64] tile at s; also returns the values (for the transposed copy).
@@ -88,16 +98,47 @@ __device__ __forceinline__ void handoff() {
   tc_fence_after();
 }
 
+// The same within one warpgroup (named barrier id, 128 threads).
+__device__ __forceinline__ void wg_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ bool wg_sync_or(int id, bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred q, p;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, %2, 128, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(r)
+      : "r"(uint32_t(pred)), "r"(id)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void wg_handoff(int id) {
+  fence_async_smem();
+  tc_fence_before();
+  wg_sync(id);
+  tc_fence_after();
+}
+
+// Encoding groups [g0, g1) of row r into an interleaved [128][8 (g1 - g0)] tile.
+__device__ __forceinline__ void write_enc_range(uint32_t s, int r, const EncIn& e, int g0, int g1) {
+  const int K = 8 * (g1 - g0);
+  for (int g = g0; g < g1; ++g) {
+    float f[8];
+    enc_group(e, g, f);
+    st_shared_v4(s + ik_off(r, 8 * (g - g0), K), pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]),
+                 pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+  }
+}
+
 // ------------------------------------------------------------ inference ----
-__global__ void __launch_bounds__(128) k_guide_infer(GuideNet net, const float4* __restrict__ in,
-                                                     const int* __restrict__ count, int n_rows,
-                                                     float4* __restrict__ mix, int* err) {
+__global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net, const float4* __restrict__ in,
+                                                                   const int* __restrict__ count, int n_rows,
+                                                                   float4* __restrict__ mix, int* err) {
   extern __shared__ __align__(1024) uint8_t sm[];
-  const int t = threadIdx.x, warp = t >> 5;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kInferMisc);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + kInferMisc + 8);
+  const int wg = threadIdx.x >> 7, t = threadIdx.x & 127, warp = threadIdx.x >> 5;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kInferMisc) + wg;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + kInferMisc + 8 * kInferWG);
   const uint32_t sW1 = smem_u32(sm + kSW1), sW2 = smem_u32(sm + kSW2), sW3 = smem_u32(sm + kSW3),
-                 sW4 = smem_u32(sm + kSW4), sX = smem_u32(sm + kInferX), bar = smem_u32(mbar);
+                 sW4 = smem_u32(sm + kSW4), sX = smem_u32(sm + kSWEnd + wg * kInferBuf), bar = smem_u32(mbar);
+  const int bid = 1 + wg;  // named barrier of this warpgroup
   load_weights(sm + kSW1, net.w + kOffW1, kHid, kIn, kHid, false);
   load_weights(sm + kSW2, net.w + kOffW2, kHid, kHid, kHid, false);
   load_weights(sm + kSW3, net.w + kOffW3, kHid, kHid, kHid, false);
@@ -105,13 +146,24 @@ __global__ void __launch_bounds__(128) k_guide_infer(GuideNet net, const float4*
   if (t == 0) mbar_init(bar, 1);
   if (warp == 0) tmem_alloc(smem_u32(tslot), kInferCols);
   handoff();
-  const uint32_t tmem = *tslot;
-  const uint32_t lane = tmem + (uint32_t(warp * 32) << 16);
+  const uint32_t tbase = *tslot;
+  const uint32_t tmem = tbase + 64 * wg;
+  const uint32_t lane = tmem + (uint32_t((warp & 3) * 32) << 16);
   const int n = count ? *count : n_rows;
   const int ntiles = (n + kRows - 1) / kRows;
   uint32_t phase = 0;
   bool ok = true;
-  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+  // One chain of products committed to this warpgroup's barrier, then the
+  // wait; false (for the whole warpgroup) when the wait timed out.
+  auto chain_wait = [&]() -> bool {
+    if (t == 0) mma_commit(bar);
+    bool fine = mbar_wait(bar, phase);
+    phase ^= 1;
+    if (wg_sync_or(bid, !fine)) return false;
+    tc_fence_after();
+    return true;
+  };
+  for (int tile = blockIdx.x * kInferWG + wg; tile < ntiles; tile += gridDim.x * kInferWG) {
     const int r = tile * kRows + t;
     EncIn e;
     if (r < n) {
@@ -120,21 +172,25 @@ __global__ void __launch_bounds__(128) k_guide_infer(GuideNet net, const float4*
     } else {
       e = make_enc(net, net.lo[0], net.lo[1], net.lo[2], 0.f, 0.f, 1.f, 0.f, 0.f, 1.f);
     }
-    write_enc_row(sX, t, e);
-    // Three hidden layers, then the output layer (N = 48, 40 used).
-    for (int layer = 0; layer < 4; ++layer) {
-      handoff();
+    // Layer 1 in two halves of the input.
+    write_enc_range(sX, t, e, 0, kEncA);
+    wg_handoff(bid);
+    if (t == 0) gemm_k(tmem, sX, 8 * kEncA, sW1, kIn, 8 * kEncA, kHid, false);
+    if (!(ok = chain_wait())) break;
+    write_enc_range(sX, t, e, kEncA, kEncA + kEncB);
+    wg_handoff(bid);
+    if (t == 0) gemm_k(tmem, sX, 8 * kEncB, sW1 + kEncA * 128, kIn, 8 * kEncB, kHid, true);
+    if (!(ok = chain_wait())) break;
+    hidden_to_smem(lane, sX, t, nullptr);
+    // Layers 2 and 3, then the output layer (N = 48, 40 used).
+    for (int layer = 1; layer < 4; ++layer) {
+      wg_handoff(bid);
       if (t == 0) {
-        if (layer == 0) gemm_k(tmem, sX, kIn, sW1, kIn, kIn, kHid, false);
-        else if (layer == 1) gemm_k(tmem, sX, kHid, sW2, kHid, kHid, kHid, false);
+        if (layer == 1) gemm_k(tmem, sX, kHid, sW2, kHid, kHid, kHid, false);
         else if (layer == 2) gemm_k(tmem, sX, kHid, sW3, kHid, kHid, kHid, false);
         else gemm_k(tmem, sX, kHid, sW4, kHid, kHid, kOutPad, false);
-        mma_commit(bar);
       }
-      ok = mbar_wait(bar, phase);
-      phase ^= 1;
-      if (__syncthreads_or(!ok)) { ok = false; break; }
-      tc_fence_after();
+      if (!(ok = chain_wait())) break;
       if (layer < 3) {
         hidden_to_smem(lane, sX, t, nullptr);
       } else {
@@ -145,16 +201,13 @@ __global__ void __launch_bounds__(128) k_guide_infer(GuideNet net, const float4*
         if (r < n) {
           Mixture m;
           decode_mixture(o, m);
-          float4* out = mix + 10 * size_t(r);
-          out[0] = make_float4(m.pi[0], m.pi[1], m.pi[2], m.pi[3]);
-          out[1] = make_float4(m.pi[4], m.pi[5], m.pi[6], m.pi[7]);
-#pragma unroll
-          for (int k = 0; k < kLobes; ++k) out[2 + k] = make_float4(m.mx[k], m.my[k], m.mz[k], m.kappa[k]);
+          store_mixture(mix + kMixStride * size_t(r), m);
         }
       }
     }
+    if (!ok) break;
     tc_fence_before();
-    __syncthreads();
+    wg_sync(bid);
   }
   if (!ok) {
     if (t == 0) atomicExch(err, 1);
@@ -164,7 +217,7 @@ __global__ void __launch_bounds__(128) k_guide_infer(GuideNet net, const float4*
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    tmem_dealloc(tmem, kInferCols);
+    tmem_dealloc(tbase, kInferCols);
   }
 }
 
@@ -256,9 +309,15 @@ __device__ __forceinline__ void backprop_delta(uint32_t lane_taddr, const uint8_
   write_transposed(s_t, r, d, kHid);
 }
 
-__global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const float4* __restrict__ samples, int n,
-                                                        float inv_n, float* __restrict__ grad,
-                                                        float* __restrict__ loss_sum, int* err) {
+// One optimizer step's gradient over a window of the sample buffer: with
+// n_avail = min(*avail, cap) samples written (n_avail = cap when avail is
+// null), step k uses samples [start, start + n) with start = k * batch mod
+// n_avail and n = min(batch, n_avail - start), read on the device so that
+// the host never waits for the sample count.
+__global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const float4* __restrict__ base,
+                                                        const int* __restrict__ avail, int cap, int k, int batch,
+                                                        float* __restrict__ grad, float* __restrict__ loss_sum,
+                                                        int* err) {
   extern __shared__ __align__(1024) uint8_t sm[];
   const int t = threadIdx.x, warp = t >> 5;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kTMisc);
@@ -281,6 +340,11 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
   handoff();
   const uint32_t tmem = *tslot;
   const uint32_t lane = tmem + (uint32_t(warp * 32) << 16);
+  const int n_avail = avail ? min(*avail, cap) : cap;
+  const int start = n_avail > 0 ? int((long long)k * batch % n_avail) : 0;
+  const int n = min(batch, n_avail - start);
+  const float inv_n = n > 0 ? 1.f / float(n) : 0.f;
+  const float4* samples = base + 4 * size_t(start);
   const int ntiles = (n + kRows - 1) / kRows;
   uint32_t phase = 0;
   bool ok = true, first = true;
@@ -452,18 +516,20 @@ GuideNet view(const gbrt_guide* g) {
 
 cudaError_t launch_infer(const gbrt_guide* g, const float4* in, const int* count, int n_rows, float4* mix,
                          cudaStream_t stream) {
-  k_guide_infer<<<g->infer_grid, kRows, kInferSmem, stream>>>(view(g), in, count, n_rows, mix, g->d_err);
+  k_guide_infer<<<g->infer_grid, kRows * kInferWG, kInferSmem, stream>>>(view(g), in, count, n_rows, mix,
+                                                                         g->d_err);
   return cudaGetLastError();
 }
 
-cudaError_t train(gbrt_guide* g, const float4* samples, int n, float lr, bool step, cudaStream_t stream) {
+cudaError_t train_window(gbrt_guide* g, const float4* samples, const int* avail, int cap, int k, int batch,
+                         float lr, bool step, cudaStream_t stream) {
   cudaError_t e = cudaMemsetAsync(g->d_g, 0, kParams * sizeof(float), stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(g->d_loss, 0, sizeof(float), stream);
   if (e != cudaSuccess) return e;
-  if (n > 0) {
-    int tiles = (n + kRows - 1) / kRows;
+  if (cap > 0 && batch > 0) {
+    int tiles = (std::min(batch, cap) + kRows - 1) / kRows;
     int grid = std::min(g->train_grid, tiles);
-    k_guide_train<<<grid, kRows, kTrainSmem, stream>>>(view(g), samples, n, 1.f / float(n), g->d_g, g->d_loss,
+    k_guide_train<<<grid, kRows, kTrainSmem, stream>>>(view(g), samples, avail, cap, k, batch, g->d_g, g->d_loss,
                                                        g->d_err);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
@@ -477,6 +543,10 @@ cudaError_t train(gbrt_guide* g, const float4* samples, int n, float lr, bool st
     e = cudaGetLastError();
   }
   return e;
+}
+
+cudaError_t train(gbrt_guide* g, const float4* samples, int n, float lr, bool step, cudaStream_t stream) {
+  return train_window(g, samples, nullptr, n, 0, n, lr, step, stream);
 }
 
 }  // namespace guide
@@ -554,9 +624,7 @@ gbrt_status gbrt_guide_create(gbrt_ctx* ctx, const float bounds[6], uint64_t see
   A(cudaMalloc(&g->d_err, sizeof(int)));
   A(cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem));
   A(cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem));
-  int per = 0;
-  if (e == cudaSuccess) A(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_infer, kRows, kInferSmem));
-  g->infer_grid = std::max(1, std::min(per, 2)) * ctx->num_sms;
+  g->infer_grid = ctx->num_sms;
   g->train_grid = ctx->num_sms;
   std::vector<float> p;
   init_params(p, seed);
@@ -629,10 +697,12 @@ gbrt_status gbrt_guide_eval(gbrt_guide* g, const float* inputs, size_t n, float*
   }
   float4 *d_in = nullptr, *d_mix = nullptr;
   cudaError_t e = cudaMallocAsync(&d_in, h.size() * sizeof(float4), s);
-  if (e == cudaSuccess) e = cudaMallocAsync(&d_mix, 10 * n * sizeof(float4), s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_mix, kMixStride * n * sizeof(float4), s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = launch_infer(g, d_in, nullptr, int(n), d_mix, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_mix, 10 * n * sizeof(float4), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(out, 10 * sizeof(float4), d_mix, kMixStride * sizeof(float4), 10 * sizeof(float4), n,
+                          cudaMemcpyDeviceToHost, s);
   if (d_in) cudaFreeAsync(d_in, s);
   if (d_mix) cudaFreeAsync(d_mix, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

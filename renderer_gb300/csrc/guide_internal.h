@@ -32,7 +32,7 @@ GuideNet view(const gbrt_guide* g);
 
 // Mixture of every row of a queue: rows are three float4 (point, -), (normal
 // facing the viewer, -), (outgoing direction, -); the row count is *count on
-// the device (or n_rows when count is null). Writes ten float4 per row.
+// the device (or n_rows when count is null). Writes kMixStride float4 per row.
 cudaError_t launch_infer(const gbrt_guide* g, const float4* in, const int* count, int n_rows, float4* mix,
                          cudaStream_t stream);
 
@@ -40,6 +40,11 @@ cudaError_t launch_infer(const gbrt_guide* g, const float4* in, const int* count
 // weight), (normal, -), (outgoing, -), (sampled direction, -)) into d_g and
 // d_loss (zeroed first); with step, also one Adam step.
 cudaError_t train(gbrt_guide* g, const float4* samples, int n, float lr, bool step, cudaStream_t stream);
+
+// The same over step k's window of a sample buffer whose fill count
+// (capped at cap) is read on the device: samples [k batch mod n, ... + batch).
+cudaError_t train_window(gbrt_guide* g, const float4* samples, const int* avail, int cap, int k, int batch,
+                         float lr, bool step, cudaStream_t stream);
 
 }  // namespace guide
 }  // namespace gbrt

@@ -33,6 +33,10 @@ constexpr int kW1 = kHid * kIn, kW2 = kHid * kHid, kW3 = kHid * kHid, kW4 = kOut
 constexpr int kOffW1 = 0, kOffW2 = kW1, kOffW3 = kW1 + kW2, kOffW4 = kW1 + kW2 + kW3;
 constexpr int kParams = kW1 + kW2 + kW3 + kW4;
 constexpr float kLogKappaMin = -4.f, kLogKappaMax = 9.f;
+// A stored mixture: (pi0..3), (pi4..7), (mean, kappa) per lobe, then the
+// normalised lobe weights c_k = pi_k kappa_k / (2 pi (1 - exp(-2 kappa_k)))
+// in two float4, so that q(w) = sum_k c_k exp(kappa_k (mean_k . w - 1)).
+constexpr int kMixStride = 12;
 constexpr float kPi = 3.14159265358979323846f;
 
 // Device view of a network.
@@ -293,17 +297,29 @@ __device__ __forceinline__ void decode_mixture(const float* o, Mixture& m) {
   }
 }
 
-// Mixture pdf (solid angle) of the unit direction (x, y, z). The ten float4
-// of a stored mixture: (pi0..3), (pi4..7), then (mean, kappa) per lobe.
+// Writes a decoded mixture in the stored layout (kMixStride float4).
+__device__ __forceinline__ void store_mixture(float4* out, const Mixture& m) {
+  float c[kLobes];
+#pragma unroll
+  for (int k = 0; k < kLobes; ++k) c[k] = m.pi[k] * expf(vmf_log_norm(m.kappa[k]));
+  out[0] = make_float4(m.pi[0], m.pi[1], m.pi[2], m.pi[3]);
+  out[1] = make_float4(m.pi[4], m.pi[5], m.pi[6], m.pi[7]);
+#pragma unroll
+  for (int k = 0; k < kLobes; ++k) out[2 + k] = make_float4(m.mx[k], m.my[k], m.mz[k], m.kappa[k]);
+  out[10] = make_float4(c[0], c[1], c[2], c[3]);
+  out[11] = make_float4(c[4], c[5], c[6], c[7]);
+}
+
+// Mixture pdf (solid angle) of the unit direction (x, y, z).
 __device__ __forceinline__ float mixture_pdf(const float4* M, float x, float y, float z) {
-  float4 p0 = M[0], p1 = M[1];
-  float pis[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+  float4 c0 = M[10], c1 = M[11];
+  float cs[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
   float q = 0.f;
 #pragma unroll
   for (int k = 0; k < kLobes; ++k) {
     float4 l = M[2 + k];
-    float c = l.x * x + l.y * y + l.z * z;
-    q += pis[k] * expf(vmf_log_norm(l.w) + l.w * (c - 1.f));
+    float d = l.x * x + l.y * y + l.z * z;
+    q += cs[k] * __expf(l.w * (d - 1.f));
   }
   return q;
 }

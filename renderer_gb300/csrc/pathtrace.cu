@@ -65,6 +65,11 @@ struct PTParams {
   int guided;              // sample non-specular vertices from the guide's mixtures too
   float guide_frac;        // probability of sampling the guide (one-sample MIS)
   int record;              // write training records for the guide
+  int guide_depth;         // guide vertices i < guide_depth only (0: all)
+  int train_relative;      // training weights relative to the sample's pixel
+  const double* film_sum;  // sums of the earlier passes (pixel estimates for the training weights)
+  const double* pass_sum;  // sums of the current pass
+  double inv_samples;      // 1 / samples per pixel in film_sum + pass_sum
 };
 
 // Path state, structure of arrays indexed by slot (path index - g0).
@@ -88,8 +93,8 @@ struct PTState {
   int* err;
   // Path guiding (null when unused).
   float4* gin;     // per extension-queue entry: (point, guided), (normal facing wo, -), (wo, -)
-  float4* mix;     // per extension-queue entry: the vertex's mixture (ten float4)
-  float4* rec;     // training records, kRecords x 5 float4 per slot, record-major
+  float4* mix;     // per extension-queue entry: the vertex's mixture (guide::kMixStride float4)
+  float4* rec;     // training records, kRecords x kRecComp float4 per slot, record-major
   float4* tsamp;   // training samples, four float4 each
   int* tcount;     // training samples written
   int tcap;        // capacity of tsamp
@@ -97,12 +102,14 @@ struct PTState {
 };
 
 // Training records of the guide: the first kRecords guided vertices of a
-// path. Record component c of record r of a slot is rec[(5 r + c) nslots +
+// path. Record component c of record r of a slot is rec[(6 r + c) nslots +
 // slot]: (point, pdf), (normal, wi.x), (wo, wi.y), (throughput after the
-// vertex, wi.z), (radiance of the path when the next vertex was reached).
+// vertex, wi.z), (radiance of the path when the next vertex was reached),
+// (mean throughput before the vertex, -, -, -).
 // ctl.z of a guided path: records written (low 4 bits), kRecOpen while the
 // last record waits for its radiance snapshot.
 constexpr int kRecords = 4;
+constexpr int kRecComp = 6;
 constexpr int kRecOpen = 0x100;
 
 // ------------------------------------------------------------- raygen ----
@@ -583,7 +590,7 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
     if (GUIDED && P.record && (c.z & kRecOpen)) {
       // The radiance the path had gathered before this vertex: the rest of
       // the path is what the last recorded direction brought in.
-      st.rec[size_t(5 * ((c.z & 15) - 1) + 4) * st.nslots + slot] = st.L[slot];
+      st.rec[size_t(kRecComp * ((c.z & 15) - 1) + 4) * st.nslots + slot] = st.L[slot];
       c.z &= ~kRecOpen;
     }
     const bool prevSpec = c.w != 0;
@@ -635,8 +642,9 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
     const V3f wo = -normalize(d);
     const bool flipped = dot(nrm, wo) < 0.f;
     if (flipped) nrm = -nrm;
-    const bool guideHere = GUIDED && P.guided && b.kind >= 1 && b.kind <= 3;
-    const float4* M = guideHere ? st.mix + 10 * size_t(q) : nullptr;
+    const bool depthOk = P.guide_depth == 0 || i < P.guide_depth;
+    const bool guideHere = GUIDED && P.guided && depthOk && b.kind >= 1 && b.kind <= 3;
+    const float4* M = guideHere ? st.mix + guide::kMixStride * size_t(q) : nullptr;
     if (b.kind <= 3 && S.n_lights > 0) nee_phys(S, st, slot, key, base, b, x, nrm, wo, alpha, M, P.guide_frac);
     V3f wi, wgt;
     float pdf;
@@ -666,13 +674,14 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
     int z = 0;
     if (GUIDED) {
       z = c.z;
-      if (P.record && b.kind >= 1 && b.kind <= 3 && (z & 15) < kRecords) {
-        const size_t r = size_t(5 * (z & 15)) * st.nslots + slot;
+      if (P.record && depthOk && b.kind >= 1 && b.kind <= 3 && (z & 15) < kRecords) {
+        const size_t r = size_t(kRecComp * (z & 15)) * st.nslots + slot;
         const size_t ns = size_t(st.nslots);
         st.rec[r] = make_float4(x.x, x.y, x.z, pdf);
         st.rec[r + ns] = make_float4(nrm.x, nrm.y, nrm.z, wi.x);
         st.rec[r + 2 * ns] = make_float4(wo.x, wo.y, wo.z, wi.y);
         st.rec[r + 3 * ns] = make_float4(na.x, na.y, na.z, wi.z);
+        st.rec[r + 5 * ns] = make_float4((alpha.x + alpha.y + alpha.z) * (1.f / 3.f), 0.f, 0.f, 0.f);
         z = ((z & 15) + 1) | kRecOpen;
       }
     }
@@ -688,6 +697,7 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
 // else a neutral row that the guided shade ignores.
 __global__ void __launch_bounds__(256) k_guide_prep(DeviceScene S, PTState st, int cur) {
   const int n = st.counts[cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&st.tally[7], (unsigned long long)n);
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const RawHit h = st.hits[q];
     float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = make_float4(0.f, 0.f, 1.f, 0.f), r2 = r1;
@@ -717,7 +727,11 @@ __global__ void __launch_bounds__(256) k_guide_prep(DeviceScene S, PTState st, i
 // arrived along a recorded direction is what the path gathered after the
 // record's snapshot, divided by the throughput up to that direction; the
 // target is its mean over the channels times |cos| at the vertex, and the
-// sample weight target / pdf (pdf: the density the direction was drawn from).
+// sample weight target / pdf (pdf: the density the direction was drawn
+// from). With GBRT_GUIDE_PIXEL_RELATIVE the weight is also scaled to the
+// sample's share of its pixel: times the throughput from the camera to the
+// vertex, over sqrt(p^2 + 0.01) with p the pixel's current estimate (the
+// denominator of relMSE), so that dim regions weigh as much as bright ones.
 __global__ void __launch_bounds__(256) k_guide_collect(PTParams P, PTState st) {
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= P.nb) return;
@@ -725,16 +739,22 @@ __global__ void __launch_bounds__(256) k_guide_collect(PTParams P, PTState st) {
   if (nrec == 0) return;
   const float4 L = st.L[slot];
   const size_t ns = size_t(st.nslots);
+  const unsigned long long pix = (P.g0 + (unsigned long long)slot) / unsigned(P.spp);
+  const double* ps = P.film_sum + 3 * pix;
+  const double* pc = P.pass_sum + 3 * pix;
+  const float pl = float((ps[0] + ps[1] + ps[2] + pc[0] + pc[1] + pc[2]) * (1.0 / 3.0) * P.inv_samples);
+  const float inv_pix = rsqrtf(pl * pl + 0.01f);
   for (int r = 0; r < nrec; ++r) {
-    const size_t b = size_t(5 * r) * ns + slot;
+    const size_t b = size_t(kRecComp * r) * ns + slot;
     const float4 r0 = st.rec[b], r1 = st.rec[b + ns], r2 = st.rec[b + 2 * ns], r3 = st.rec[b + 3 * ns],
-                 sn = st.rec[b + 4 * ns];
+                 sn = st.rec[b + 4 * ns], r5 = st.rec[b + 5 * ns];
     float li = 0.f;
     if (r3.x > 0.f) li += (L.x - sn.x) / r3.x;
     if (r3.y > 0.f) li += (L.y - sn.y) / r3.y;
     if (r3.z > 0.f) li += (L.z - sn.z) / r3.z;
     const float cosi = fabsf(r1.x * r1.w + r1.y * r2.w + r1.z * r3.w);
-    const float w = (li * (1.f / 3.f)) * cosi / r0.w;
+    float w = (li * (1.f / 3.f)) * cosi / r0.w;
+    if (P.train_relative) w *= r5.x * inv_pix;
     if (!(w > 0.f) || !isfinite(w)) continue;
     const int e = agg_push(st.tcount);
     if (e >= st.tcap) continue;
@@ -1181,6 +1201,54 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
 // first train_passes passes record training samples and each is followed by
 // steps_per_pass Adam steps; vertices sample the guide once it has been
 // trained (or given weights). The film is the mean over all passes.
+// Relative squared deviation of a pass from the mean of the earlier passes,
+// summed over pixels and channels: sum ((x - m)^2 / (m^2 + 0.01)), x the
+// pass's mean (its sums times inv_pass), m the earlier passes' mean (their
+// sums times inv_prev).
+__global__ void __launch_bounds__(256) k_pass_deviation(const double* __restrict__ pass_sum,
+                                                        const double* __restrict__ prev_sum, size_t n3,
+                                                        double inv_pass, double inv_prev, double* out) {
+  double acc = 0.0;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n3; i += size_t(gridDim.x) * blockDim.x) {
+    double x = pass_sum[i] * inv_pass, m = prev_sum[i] * inv_prev;
+    double d = x - m;
+    if (isfinite(d)) acc += d * d / (m * m + 0.01);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  __shared__ double part[8];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    for (int k = 0; k < int(blockDim.x >> 5); ++k) b += part[k];
+    atomicAdd(out, b);
+  }
+}
+
+// prev_sum += pass_sum; with a deviation (dev != null), weighted += w *
+// pass_sum and wtotal += w for w = n3 / *dev. Thread 0 also adds the pass's
+// training samples (min(*tcount, tcap)) to *tsamples.
+__global__ void k_pass_combine(const double* __restrict__ pass_sum, double* __restrict__ prev_sum,
+                               double* __restrict__ weighted, size_t n3, const double* dev, double* wtotal,
+                               const int* tcount, int tcap, unsigned long long* tsamples) {
+  size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const double w = (dev && *dev > 0.0) ? double(n3) / *dev : 0.0;
+  if (i == 0) {
+    if (dev) *wtotal += w;
+    if (tcount) *tsamples += (unsigned long long)min(*tcount, tcap);
+  }
+  if (i >= n3) return;
+  double x = pass_sum[i];
+  prev_sum[i] += x;
+  if (w > 0.0) weighted[i] += w * x;
+}
+
+__global__ void k_finalize_weighted(const double* __restrict__ weighted, float* __restrict__ film, size_t n3,
+                                    double inv_spp, const double* wtotal) {
+  size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n3) film[i] = float(weighted[i] * inv_spp / *wtotal);
+}
+
 static unsigned long long pass_seed(unsigned long long seed, int pass) {
   unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(pass + 1);
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -1201,7 +1269,7 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   if (!(prm->termination_prob >= 0.f && prm->termination_prob < 1.f))
     return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: termination probability outside [0, 1)");
   if (!(gp->guide_fraction >= 0.f && gp->guide_fraction <= 1.f) || gp->passes < 0 || gp->train_passes < 0 ||
-      gp->steps_per_pass < 0 || (gp->passes == 0 && !(gp->time_budget_ms > 0.f)))
+      gp->steps_per_pass < 0 || gp->guide_depth < 0 || (gp->passes == 0 && !(gp->time_budget_ms > 0.f)))
     return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: bad guide parameters");
   const bool useGuide = g && gp->guide_fraction > 0.f;
   const bool training = useGuide && gp->train_passes > 0 && gp->steps_per_pass > 0;
@@ -1232,9 +1300,9 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   long long tcap = 0;
   if (useGuide) {
     A(buf.alloc(&st.gin, 3 * B));
-    A(buf.alloc(&st.mix, 10 * B));
+    A(buf.alloc(&st.mix, guide::kMixStride * B));
     if (training) {
-      A(buf.alloc(&st.rec, 5ll * kRecords * B));
+      A(buf.alloc(&st.rec, (long long)kRecComp * kRecords * B));
       tcap = std::min<long long>((long long)gp->steps_per_pass * gp->batch_samples, 1ll << 25);
       A(buf.alloc(&st.tsamp, 4 * tcap));
       A(buf.alloc(&st.tcount, 1));
@@ -1242,12 +1310,25 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   }
   st.tcap = int(tcap);
   st.nslots = int(B);
-  double* d_sum = nullptr;
+  // Films: the current pass, the sum of all passes, the inverse-variance
+  // weighted sum, and the deviation accumulator.
+  const size_t n3 = size_t(npix) * 3;
+  double *d_pass = nullptr, *d_sum = nullptr, *d_wsum = nullptr, *d_dev = nullptr, *d_wtot = nullptr;
   float* d_film = nullptr;
-  A(buf.alloc(&d_sum, npix * 3));
-  A(buf.alloc(&d_film, npix * 3));
+  A(buf.alloc(&d_pass, n3));
+  A(buf.alloc(&d_sum, n3));
+  A(buf.alloc(&d_wsum, n3));
+  A(buf.alloc(&d_dev, 1));
+  A(buf.alloc(&d_wtot, 1));
+  A(buf.alloc(&d_film, n3));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "guided render buffers");
-  A(cudaMemsetAsync(d_sum, 0, npix * 3 * sizeof(double), stream));
+  A(cudaMemsetAsync(d_sum, 0, n3 * sizeof(double), stream));
+  A(cudaMemsetAsync(d_wsum, 0, n3 * sizeof(double), stream));
+  A(cudaMemsetAsync(d_wtot, 0, sizeof(double), stream));
+  // Inverse-variance weighting of the passes when a guide is used: a pass
+  // sampled by a network still in training is noisier than later ones.
+  const bool weighted = training && !(gp->flags & GBRT_GUIDE_EQUAL_WEIGHTS);
+
   A(cudaMemsetAsync(st.tally, 0, 8 * sizeof(unsigned long long), stream));
   A(cudaMemsetAsync(st.err, 0, sizeof(int), stream));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "guided render set-up");
@@ -1266,8 +1347,10 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   cudaEventCreate(&t1);
   cudaEventRecord(ev0, stream);
   int passes = 0, steps = 0;
-  unsigned long long samples = 0;
-  double train_ms = 0.0, elapsed = 0.0;
+  unsigned long long infer_launches = 0;
+  double train_ms = 0.0, elapsed = 0.0, infer_ms = 0.0;
+  const bool timeK = (prm->flags & GBRT_RENDER_TIME_KERNELS) != 0;
+  std::vector<cudaEvent_t> iev;
   gbrt_status status = GBRT_OK;
   for (int pass = 0;; ++pass) {
     if (gp->passes > 0 && pass >= gp->passes) break;
@@ -1278,6 +1361,12 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     P.guided = (useGuide && g->ready) ? 1 : 0;
     P.guide_frac = gp->guide_fraction;
     P.record = record ? 1 : 0;
+    P.guide_depth = gp->guide_depth;
+    P.train_relative = (gp->flags & GBRT_GUIDE_PIXEL_RELATIVE) ? 1 : 0;
+    P.film_sum = d_sum;
+    P.pass_sum = d_pass;
+    P.inv_samples = 1.0 / (double(spp) * (pass + 1));
+    A(cudaMemsetAsync(d_pass, 0, n3 * sizeof(double), stream));
     if (record) A(cudaMemsetAsync(st.tcount, 0, sizeof(int), stream));
     auto kShade = (P.guided || P.record) ? k_shade_phys<true> : k_shade_phys<false>;
     for (unsigned long long g0 = 0; g0 < total && e == cudaSuccess; g0 += (unsigned long long)B) {
@@ -1287,51 +1376,79 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
       for (int it = 0; it < P.D; ++it) {
         int cur = it & 1;
         tk.ext<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
-        if (P.guided) {
+        if (P.guided && (P.guide_depth == 0 || it < P.guide_depth)) {
+          cudaEvent_t ea = nullptr, eb = nullptr;
+          if (timeK) {
+            cudaEventCreate(&ea);
+            cudaEventCreate(&eb);
+            cudaEventRecord(ea, stream);
+          }
           k_guide_prep<<<shadeGrid, 256, 0, stream>>>(s->view, st, cur);
           A(guide::launch_infer(g, st.gin, st.counts + cur, 0, st.mix, stream));
+          if (timeK) {
+            cudaEventRecord(eb, stream);
+            iev.push_back(ea);
+            iev.push_back(eb);
+          }
+          ++infer_launches;
         }
         kShade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
         tk.sh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
       }
       unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
-      k_accumulate<<<unsigned((p1 - p0 + 256) / 256), 256, 0, stream>>>(P, st, d_sum, nullptr);
+      k_accumulate<<<unsigned((p1 - p0 + 256) / 256), 256, 0, stream>>>(P, st, d_pass, nullptr);
       if (record) k_guide_collect<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
       A(cudaGetLastError());
     }
     if (e != cudaSuccess) break;
+    // Fold the pass into the films. The first pass of a weighted render only
+    // serves as the first mean (it was sampled without the guide).
+    const bool wpass = weighted && pass > 0;
+    if (wpass) {
+      A(cudaMemsetAsync(d_dev, 0, sizeof(double), stream));
+      k_pass_deviation<<<ctx->num_sms * 4, 256, 0, stream>>>(d_pass, d_sum, n3, 1.0 / spp, 1.0 / (double(spp) * pass),
+                                                             d_dev);
+    }
+    k_pass_combine<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_pass, d_sum, d_wsum, n3, wpass ? d_dev : nullptr,
+                                                                   d_wtot, record ? st.tcount : nullptr, int(tcap),
+                                                                   st.tally + 3);
+    A(cudaGetLastError());
     ++passes;
     if (record) {
-      int cnt = 0;
-      A(cudaMemcpyAsync(&cnt, st.tcount, sizeof cnt, cudaMemcpyDeviceToHost, stream));
-      A(cudaStreamSynchronize(stream));
-      const int avail = int(std::min<long long>(cnt, tcap));
-      cudaEventRecord(t0, stream);
-      for (int k = 0; k < gp->steps_per_pass && avail > 0 && e == cudaSuccess; ++k) {
-        int start = int((long long)k * gp->batch_samples % avail);
-        int n = std::min(gp->batch_samples, avail - start);
-        A(guide::train(g, st.tsamp + 4 * size_t(start), n, gp->learning_rate, true, stream));
+      // Steps over the pass's samples; their count stays on the device.
+      if (timeK) cudaEventRecord(t0, stream);
+      for (int k = 0; k < gp->steps_per_pass && e == cudaSuccess; ++k) {
+        A(guide::train_window(g, st.tsamp, st.tcount, int(tcap), k, gp->batch_samples, gp->learning_rate, true,
+                              stream));
         g->ready = true;
         ++steps;
       }
-      cudaEventRecord(t1, stream);
-      A(cudaStreamSynchronize(stream));
-      float tms = 0.f;
-      cudaEventElapsedTime(&tms, t0, t1);
-      train_ms += tms;
-      samples += (unsigned long long)avail;
+      if (timeK) {
+        cudaEventRecord(t1, stream);
+        A(cudaEventSynchronize(t1));
+        float tms = 0.f;
+        cudaEventElapsedTime(&tms, t0, t1);
+        train_ms += tms;
+      }
     }
-    cudaEventRecord(ev1, stream);
-    A(cudaEventSynchronize(ev1));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, ev0, ev1);
-    elapsed = ms;
     if (e != cudaSuccess) break;
-    if (gp->passes == 0 && elapsed >= gp->time_budget_ms) break;
+    if (gp->passes == 0) {
+      // Equal-time rendering: the device clock decides after every pass.
+      cudaEventRecord(ev1, stream);
+      A(cudaEventSynchronize(ev1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev0, ev1);
+      elapsed = ms;
+      if (elapsed >= gp->time_budget_ms) break;
+    }
   }
+  const bool timedAtEnd = gp->passes > 0;
+  if (timedAtEnd) cudaEventRecord(ev1, stream);
   if (e == cudaSuccess && passes > 0) {
-    size_t n3 = size_t(npix) * 3;
-    k_finalize<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_sum, d_film, n3, 1.0 / (double(spp) * passes));
+    if (weighted && passes > 1)
+      k_finalize_weighted<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_wsum, d_film, n3, 1.0 / spp, d_wtot);
+    else
+      k_finalize<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_sum, d_film, n3, 1.0 / (double(spp) * passes));
     A(cudaGetLastError());
     A(cudaMemcpyAsync(film, d_film, n3 * sizeof(float), cudaMemcpyDeviceToHost, stream));
   }
@@ -1345,23 +1462,37 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     A(cudaMemcpyAsync(&loss, g->d_loss, sizeof loss, cudaMemcpyDeviceToHost, stream));
   }
   A(cudaStreamSynchronize(stream));
+  if (timedAtEnd && e == cudaSuccess) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    elapsed = ms;
+  }
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
+  for (size_t k = 0; k + 1 < iev.size(); k += 2) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, iev[k], iev[k + 1]);
+    infer_ms += ms;
+  }
+  for (cudaEvent_t x : iev) cudaEventDestroy(x);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "gbrt_render_guided");
   if (stats) {
     std::memset(stats, 0, sizeof *stats);
     stats->passes = passes;
     stats->train_steps = steps;
     stats->paths = (unsigned long long)passes * total;
-    stats->train_samples = samples;
+    stats->train_samples = tally[3];
     stats->total_ms = elapsed;
     stats->train_ms = train_ms;
     stats->last_loss = steps > 0 ? loss : 0.f;
     stats->extension_rays = tally[0];
     stats->shadow_rays = tally[1];
     stats->nonfinite = tally[2];
+    stats->infer_ms = infer_ms;
+    stats->infer_launches = infer_launches;
+    stats->infer_rows = tally[7];
   }
   if (gerr) {
     cudaMemsetAsync(g->d_err, 0, sizeof(int), stream);
