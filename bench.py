@@ -304,6 +304,8 @@ def main():
     ap.add_argument("--batch-paths", type=int, default=0)
     ap.add_argument("--profile", action="store_true",
                     help="for ncu: one untimed frame, then one frame, nothing else")
+    ap.add_argument("--gpu-build", action="store_true",
+                    help="build the BVH on the GPU (GBRT_SCENE_GPU_BUILD) instead of the host's binned SAH")
     ap.add_argument("--guided", action="store_true",
                     help="equal-time relMSE of neural path guiding against plain path tracing (two rooms)")
     ap.add_argument("--ref-spp", type=int, default=65536)
@@ -331,6 +333,8 @@ def main():
 
     torch.cuda.set_device(local)
     s = workloads.icosphere_scene(levels=8, seed=0)
+    if args.gpu_build:
+        s.flags = _abi.SCENE_GPU_BUILD
     cam = s.camera_struct()
     H, W = cam.height, cam.width
     ctx = Context(local)
@@ -430,6 +434,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "paths_per_step": tot["paths"] // args.steps,
+                       "bvh_build": "gpu (linear BVH)" if args.gpu_build else "host (binned SAH)",
                        "l2": "inputs larger than L2 (scene ~240 MB, path state ~1.2 GB per wavefront)",
                        "scene_build_ms": info["build_ms"], "bvh_nodes": info["nodes"],
                        "bvh_max_depth": info["max_depth"], "wall_s_timed": wall,

@@ -145,7 +145,14 @@ typedef enum gbrt_scene_flags {
    * (src/triangle.cpp:30-56). The renderer's test leaves cracks and overlaps
    * along shared edges; with this flag no ray slips through a closed mesh, at
    * the price of decisions that differ from the renderer's near edges. */
-  GBRT_SCENE_WATERTIGHT = 1
+  GBRT_SCENE_WATERTIGHT = 1,
+  /* Build the BVH on the GPU (linear BVH over Morton codes, collapsed to the
+   * same 4-wide nodes) instead of the host's binned SAH: milliseconds
+   * instead of seconds for multi-million-triangle scenes, at some cost in
+   * traversal speed. Hits are the same; only exact-t ties may resolve
+   * differently. A tree too deep for the traversal stack falls back to the
+   * host build. gbrt_scene_info then reports max_depth 0 and SAH cost 0. */
+  GBRT_SCENE_GPU_BUILD = 2
 } gbrt_scene_flags;
 
 /* Camera(cop, lookAt, up, fov[radians, full vertical], resolution),

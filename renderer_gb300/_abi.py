@@ -106,7 +106,7 @@ ENV_ANGULAR, ENV_LATLONG = range(2)
 # gbrt_semantics
 SEM_REFERENCE, SEM_PHYSICAL = range(2)
 # gbrt_scene_flags / gbrt_render_flags
-SCENE_WATERTIGHT = 1
+SCENE_WATERTIGHT, SCENE_GPU_BUILD = 1, 2
 RENDER_TIME_KERNELS, RENDER_COUNT_TRAVERSAL = 1, 2
 NOALLOC_MAX_BATCH = 65536
 GUIDE_PARAMS, GUIDE_INPUT, GUIDE_OUTPUT, GUIDE_SAMPLE = 24064, 9, 40, 13

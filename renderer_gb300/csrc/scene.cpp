@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "bvh_build.h"
+#include "bvh_gpu.h"
 #include "gbrt_internal.h"
 
 namespace gbrt {
@@ -83,6 +84,39 @@ gbrt_status upload(gbrt_scene* s, const std::vector<T>& host, const T** dst) {
   GBRT_CUDA_TRY(s->ctx, cudaMemcpy(p, host.data(), bytes, cudaMemcpyHostToDevice));
   *dst = static_cast<const T*>(p);
   return GBRT_OK;
+}
+
+// Uploads records and meta in input order and gathers them into the leaf
+// order of a GPU-built tree (order: leaf position -> input index).
+gbrt_status gather_leaf_order(gbrt_scene* s, const std::vector<float4>& recv, const std::vector<int4>& meta,
+                              const unsigned* order) {
+  const float4* rin = nullptr;
+  const int4* min_ = nullptr;
+  std::vector<void*> keep;
+  keep.swap(s->allocations);
+  gbrt_status st = upload(s, recv, &rin);
+  if (st == GBRT_OK) st = upload(s, meta, &min_);
+  std::vector<void*> temps;
+  temps.swap(s->allocations);
+  s->allocations.swap(keep);
+  void *rout = nullptr, *mout = nullptr;
+  if (st == GBRT_OK) {
+    cudaError_t e = cudaMalloc(&rout, recv.size() * sizeof(float4));
+    if (e == cudaSuccess) s->allocations.push_back(rout);
+    if (e == cudaSuccess) e = cudaMalloc(&mout, meta.size() * sizeof(int4));
+    if (e == cudaSuccess) s->allocations.push_back(mout);
+    if (e == cudaSuccess)
+      e = gpu_gather_records(rin, min_, order, int64_t(meta.size()), static_cast<float4*>(rout),
+                             static_cast<int4*>(mout), s->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->stream);
+    if (e != cudaSuccess) st = cuda_fail(s->ctx, e, "gbrt_scene_create: record gather");
+  }
+  for (void* p : temps) cudaFree(p);
+  if (st == GBRT_OK) {
+    s->view.recs = static_cast<const float4*>(rout);
+    s->view.meta = static_cast<const int4*>(mout);
+  }
+  return st;
 }
 
 void free_scene(gbrt_scene* s) {
@@ -310,20 +344,41 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
       sb[k] = i ? std::min(sb[k], boxes[i].lo[k]) : boxes[i].lo[k];
       sb[3 + k] = i ? std::max(sb[3 + k], boxes[i].hi[k]) : boxes[i].hi[k];
     }
-  BuildOptions bo;
-  BuildResult br = build_bvh(boxes, bo);
-  if (br.max_depth > kMaxTreeDepth)
-    return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: BVH deeper than the traversal stack");
+  // The BVH: on the GPU when asked (falling back to the host when the tree
+  // would be too deep for the traversal stack), else binned SAH on the host.
+  GpuBuild gb{};
+  bool gpuBuilt = false;
+  if ((d->flags & GBRT_SCENE_GPU_BUILD) && !boxes.empty()) {
+    GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaError_t ce = gpu_build_bvh4(boxes, BuildOptions().max_leaf, ctx->stream, &gb);
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "gbrt_scene_create: GPU BVH build");
+    gpuBuilt = !gb.too_deep;
+  }
+  BuildResult br;
+  Collapsed c4;
   std::vector<float4> recv(recs.size() * 3);
   std::vector<int4> meta(recs.size());
-  for (size_t k = 0; k < br.order.size(); ++k) {
-    const Rec& r = recs[br.order[k]];
-    std::memcpy(&recv[3 * k], r.v, sizeof r.v);
-    meta[k] = make_int4(r.meta[0], r.meta[1], r.meta[2], r.meta[3]);
+  std::vector<float4> nodes;
+  if (gpuBuilt) {
+    // records in input order; the device gathers them into leaf order
+    for (size_t k = 0; k < recs.size(); ++k) {
+      std::memcpy(&recv[3 * k], recs[k].v, sizeof recs[k].v);
+      meta[k] = make_int4(recs[k].meta[0], recs[k].meta[1], recs[k].meta[2], recs[k].meta[3]);
+    }
+  } else {
+    BuildOptions bo;
+    br = build_bvh(boxes, bo);
+    if (br.max_depth > kMaxTreeDepth)
+      return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: BVH deeper than the traversal stack");
+    for (size_t k = 0; k < br.order.size(); ++k) {
+      const Rec& r = recs[br.order[k]];
+      std::memcpy(&recv[3 * k], r.v, sizeof r.v);
+      meta[k] = make_int4(r.meta[0], r.meta[1], r.meta[2], r.meta[3]);
+    }
+    c4 = collapse_bvh4(br);
+    nodes.resize(c4.nodes.size() * 8);
+    if (!c4.nodes.empty()) std::memcpy(nodes.data(), c4.nodes.data(), c4.nodes.size() * sizeof(Node4));
   }
-  Collapsed c4 = collapse_bvh4(br);
-  std::vector<float4> nodes(c4.nodes.size() * 8);
-  if (!c4.nodes.empty()) std::memcpy(nodes.data(), c4.nodes.data(), c4.nodes.size() * sizeof(Node4));
 
   std::vector<DevMaterial> mats(size_t(d->n_materials));
   for (int i = 0; i < d->n_materials; ++i) {
@@ -339,22 +394,43 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   }
 
   auto* s = new (std::nothrow) gbrt_scene();
-  if (!s) return fail(ctx, GBRT_ERR_OOM, "gbrt_scene_create: out of host memory");
+  if (!s) {
+    if (gpuBuilt) {
+      cudaFree(gb.nodes);
+      cudaFree(gb.order);
+    }
+    return fail(ctx, GBRT_ERR_OOM, "gbrt_scene_create: out of host memory");
+  }
+  if (gpuBuilt) {
+    // The scene owns the GPU-built nodes; order is freed after the gather.
+    s->allocations.push_back(gb.nodes);
+  }
   s->ctx = ctx;
   s->device = ctx->device;
   s->watertight = (d->flags & GBRT_SCENE_WATERTIGHT) != 0;
   DeviceScene& v = s->view;
   gbrt_status st;
   std::vector<float> envTex;
-  if ((st = upload(s, nodes, &v.nodes)) != GBRT_OK || (st = upload(s, recv, &v.recs)) != GBRT_OK ||
-      (st = upload(s, meta, &v.meta)) != GBRT_OK || (st = upload(s, nrm, &v.tri_nrm)) != GBRT_OK ||
+  if (gpuBuilt) {
+    st = gather_leaf_order(s, recv, meta, gb.order);
+    cudaFree(gb.order);
+    v.nodes = gb.nodes;
+    if (st != GBRT_OK) {
+      free_scene(s);
+      delete s;
+      return st;
+    }
+  }
+  if ((!gpuBuilt && ((st = upload(s, nodes, &v.nodes)) != GBRT_OK || (st = upload(s, recv, &v.recs)) != GBRT_OK ||
+                     (st = upload(s, meta, &v.meta)) != GBRT_OK)) ||
+      (st = upload(s, nrm, &v.tri_nrm)) != GBRT_OK ||
       (st = upload(s, planes, &v.planes)) != GBRT_OK || (st = upload(s, planeMeta, &v.plane_meta)) != GBRT_OK ||
       (st = upload(s, mats, &v.materials)) != GBRT_OK || (st = upload(s, lights, &v.lights)) != GBRT_OK) {
     free_scene(s);
     delete s;
     return st;
   }
-  v.n_nodes = int64_t(c4.nodes.size());
+  v.n_nodes = gpuBuilt ? gb.n_nodes : int64_t(c4.nodes.size());
   v.n_recs = int64_t(recs.size());
   v.n_planes = d->n_planes;
   v.n_materials = d->n_materials;
@@ -374,10 +450,10 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     v.env_mapping = e->mapping;
     for (int k = 0; k < 3; ++k) v.env_coef[k] = d->lights[envLight].intensity[k];
   }
-  s->n_leaves = br.leaves;
-  s->max_depth = br.max_depth;
-  s->max_depth4 = c4.max_depth;
-  s->sah_cost = br.sah_cost;
+  s->n_leaves = gpuBuilt ? gb.leaves : br.leaves;
+  s->max_depth = gpuBuilt ? 0 : br.max_depth;
+  s->max_depth4 = gpuBuilt ? gb.depth4 : c4.max_depth;
+  s->sah_cost = gpuBuilt ? 0.0 : br.sah_cost;
   s->n_prims = int32_t(nPrims);
   std::memcpy(s->bounds, sb, sizeof sb);
   s->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
