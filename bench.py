@@ -292,6 +292,54 @@ def run_guided(args):
     print(json.dumps(line))
 
 
+def run_quality(args):
+    """relMSE of the benchmark images against 65,536-spp renders accumulated
+    in FP64: the Cornell box (256x256, 16 spp, depth 8, reference semantics)
+    rendered by the GPU and by the oracle, and the icosphere frame (64 spp)."""
+    import numpy as np
+
+    from oracle.binding import OracleScene
+    from renderer_gb300 import workloads
+    from renderer_gb300.runtime import Context, GpuScene, PerPixelRenderer
+
+    def relmse(x, ref):
+        return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    ctx = Context(0)
+    out = {"metric": "relMSE vs 65,536-spp FP64-accumulated render", "unit": "relMSE", "higher_is_better": False,
+           "images": []}
+    # Cornell box
+    s = workloads.cornell_box(256, 256)
+    gs = GpuScene(ctx, s)
+    cam = s.camera_struct()
+
+    def gpu(xs, seed, depth, batch=0):
+        r = PerPixelRenderer(gs, cam, {"pt-x-samples": xs, "pt-y-samples": xs, "pt-termination-prob": 0.5},
+                             seed=seed, max_depth=depth, batch_paths=batch)
+        t = time.perf_counter()
+        img = r.render()
+        return img, time.perf_counter() - t
+    ref, tref = gpu(256, 7, 8)
+    img, t = gpu(4, 1, 8)
+    t0 = time.perf_counter()
+    orc = OracleScene(s).render(cam, workloads.cornell_params(8, 3), rng_mode=0)
+    tcpu = time.perf_counter() - t0
+    out["images"].append({"config": "Cornell box 256x256, 16 spp, depth 8, RR p=0.5 (reference semantics)",
+                          "reference": {"spp": 65536, "s": tref}, "gpu": {"relmse": relmse(img, ref), "s": t},
+                          "oracle_cpu": {"relmse": relmse(orc["film"], ref), "s": tcpu},
+                          "gpu_vs_oracle_mean": float(img.mean() / orc["film"].mean())})
+    del gs
+    # icosphere frame
+    s = workloads.icosphere_scene(levels=8, seed=0)
+    gs = GpuScene(ctx, s)
+    cam = s.camera_struct()
+    ref, tref = gpu(256, 7, 12)
+    img, t = gpu(8, 1, 12)
+    out["images"].append({"config": WORKLOAD, "reference": {"spp": 65536, "s": tref},
+                          "gpu": {"relmse": relmse(img, ref), "s": t}})
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -314,8 +362,13 @@ def main():
     ap.add_argument("--guide-fraction", type=float, default=0.5)
     ap.add_argument("--train-passes", type=int, default=1 << 30, help="passes that train (default: all)")
     ap.add_argument("--train-steps", type=int, default=1, help="Adam steps of 2^18 samples after a training pass")
+    ap.add_argument("--quality", action="store_true",
+                    help="relMSE of the Cornell box and icosphere images against 65,536-spp renders")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.quality:
+        run_quality(args)
+        return
     if args.guided:
         run_guided(args)
         return

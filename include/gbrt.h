@@ -62,7 +62,12 @@ typedef enum gbrt_material_type {
   GBRT_MAT_MIRROR = 2,      /* MirrorMaterial, src/mirrormaterial.cpp:31-41   */
   GBRT_MAT_PHONG = 3,       /* PhongMaterial, src/phongmaterial.cpp:31-81     */
   GBRT_MAT_BLINN = 4,       /* BlinnMaterial, src/blinnmaterial.cpp:34-84     */
-  GBRT_MAT_TRANSPARENT = 5  /* TransparentMaterial, src/transparentmaterial.cpp:34-80 */
+  GBRT_MAT_TRANSPARENT = 5, /* TransparentMaterial, src/transparentmaterial.cpp:34-80 */
+  /* TextureMaterial, src/texturematerial.cpp:33-74: a diffuse material whose
+   * albedo at texture coordinates (u, v) is pow(kd * T(u, v), exponent), T
+   * the bilinear sample of textures[texture] at (frac(u) (W - 1),
+   * frac(1 - v) (H - 1)) with the border replicated (cv::getRectSubPix). */
+  GBRT_MAT_TEXTURE = 6
 } gbrt_material_type;
 
 typedef struct gbrt_material {
@@ -72,7 +77,16 @@ typedef struct gbrt_material {
   float exponent;    /* phong/blinn exponent                               */
   float ior;         /* transparent: refraction coefficient                */
   float coefficient; /* mirror: coefficient (ignored, as in the renderer)  */
+  int32_t texture;   /* texture: index into gbrt_scene_desc.textures       */
 } gbrt_material;
+
+/* A texture image, height x width x 3 float BGR, row 0 at the top (the
+ * texels of cv::imread(...) converted with scale 1/255, as the renderer
+ * loads them, src/texturematerial.cpp:48-60). */
+typedef struct gbrt_texture {
+  int32_t width, height;
+  const float* texels;  /* host pointer, copied by gbrt_scene_create */
+} gbrt_texture;
 
 /* Quad(p1,p2,p3,p4): triangles (p1,p2,p4) and (p4,p2,p3), src/quad.h:32. */
 typedef struct gbrt_quad {
@@ -127,8 +141,9 @@ typedef struct gbrt_scene_desc {
   const gbrt_material* materials; int32_t n_materials;
   /* triangle soup: n_tri x 9 positions (p1,p2,p3); optional n_tri x 9 normals
    * (a triangle whose three normals are not all non-zero uses its geometric
-   * normal, src/sceneast.cpp:514-521); optional n_tri x 6 texcoords; material
-   * per triangle (NULL: all use material 0). */
+   * normal, src/sceneast.cpp:514-521); optional n_tri x 6 texcoords (NULL:
+   * (0,0), (0,1), (1,0), the Triangle constructor's default, src/triangle.h:
+   * 35-36); material per triangle (NULL: all use material 0). */
   const float* tri_pos; const float* tri_nrm; const float* tri_uv;
   const int32_t* tri_mat; int64_t n_tri;
   const gbrt_quad* quads; int32_t n_quads;
@@ -137,6 +152,7 @@ typedef struct gbrt_scene_desc {
   const gbrt_light* lights; int32_t n_lights;
   const gbrt_env_map* env;  /* NULL if no environment map */
   int32_t flags;            /* gbrt_scene_flags */
+  const gbrt_texture* textures; int32_t n_textures;
 } gbrt_scene_desc;
 
 typedef enum gbrt_scene_flags {

@@ -219,6 +219,7 @@ struct Hit {
   Ray ray;
   int prim = -1;
   float bu = 0, bv = 0;
+  float tu = 0, tv = 0;  /* texcoords, src/hitrecord.h:59 (default (0, 0)) */
   Hit() = default;
   Hit(float tt, const Ray& r, const Material* m, V3 n, int p, float u = 0, float v = 0)
       : mat(m), t(tt), point(r.evaluate(tt)), normal(n.normalized()), ray(r), prim(p), bu(u), bv(v) {}
@@ -241,6 +242,8 @@ struct Material {
   virtual V3 outDirection(const Hit& hit, Sample s, float& pdf, C3& brdf) const = 0;
 };
 
+struct DiffuseMaterial;
+
 /* DarkMatter, src/darkmatter.cpp:32-39. */
 struct DarkMatter : Material {
   V3 outDirection(const Hit&, Sample, float& pdf, C3& brdf) const override {
@@ -255,6 +258,51 @@ struct DiffuseMaterial : Material {
   C3 color;
   explicit DiffuseMaterial(C3 c) : color(c) {}
   C3 brdf(const Hit&, V3) const override { return color * float(1 / M_PI); }
+  V3 outDirection(const Hit& hit, Sample s, float& pdf, C3& b) const override {
+    V3 n = hit.normal;
+    if (dot(n.normalized(), hit.ray.d.normalized()) > 0) n = n * -1.f;
+    V3 out = s.cosineDirection(n, pdf);
+    b = brdf(hit, out);
+    return out;
+  }
+};
+
+/* TextureMaterial, src/texturematerial.cpp:33-74: AbstractDiffuseMaterial
+ * whose brdf is pow(get(texcoords), gamma) / pi, get = the bilinear sample
+ * of a 1 x 1 cv::getRectSubPix patch at (frac(u) (W - 1), frac(1 - v) (H - 1))
+ * (border replicated) times the coefficient. The texels are those of
+ * cv::imread scaled by 1/255 (load, :48-60), given here already scaled. */
+struct TextureMaterial : Material {
+  int W, H;
+  std::vector<float> tex;
+  C3 coef;
+  float gamma;
+  TextureMaterial(int w, int h, const float* texels, C3 c, float g)
+      : W(w), H(h), tex(texels, texels + size_t(w) * h * 3), coef(c), gamma(g) {}
+  static float wrap(float x) {
+    float f = std::fmod(x, 1.f);
+    if (f < 0) f += 1;
+    return f;
+  }
+  C3 get(float u, float v) const {
+    float x = wrap(u) * float(W - 1), y = wrap(1 - v) * float(H - 1);
+    float fx = std::floor(x), fy = std::floor(y);
+    float a = x - fx, b = y - fy;
+    int x0 = std::min(std::max(int(fx), 0), W - 1), y0 = std::min(std::max(int(fy), 0), H - 1);
+    int x1 = std::min(x0 + 1, W - 1), y1 = std::min(y0 + 1, H - 1);
+    float w00 = (1 - a) * (1 - b), w10 = a * (1 - b), w01 = (1 - a) * b, w11 = a * b;
+    float r[3];
+    for (int c = 0; c < 3; ++c)
+      r[c] = tex[(size_t(y0) * W + x0) * 3 + c] * w00 + tex[(size_t(y0) * W + x1) * 3 + c] * w10 +
+             tex[(size_t(y1) * W + x0) * 3 + c] * w01 + tex[(size_t(y1) * W + x1) * 3 + c] * w11;
+    return C3(r[0] * coef.b, r[1] * coef.g, r[2] * coef.r);
+  }
+  C3 albedo(const Hit& h) const {
+    C3 g = get(h.tu, h.tv);
+    if (gamma == 1.f) return g;
+    return C3(std::pow(g.b, gamma), std::pow(g.g, gamma), std::pow(g.r, gamma));
+  }
+  C3 brdf(const Hit& h, V3) const override { return albedo(h) * float(1 / M_PI); }
   V3 outDirection(const Hit& hit, Sample s, float& pdf, C3& b) const override {
     V3 n = hit.normal;
     if (dot(n.normalized(), hit.ray.d.normalized()) > 0) n = n * -1.f;
@@ -411,9 +459,12 @@ struct Intersectable {
   virtual void contained(std::vector<Intersectable*>& out) { out.push_back(this); }
 };
 
-/* Triangle, src/triangle.h:35-38, src/triangle.cpp:30-65. */
+/* Triangle, src/triangle.h:35-38, src/triangle.cpp:30-65. Texture
+ * coordinates default to (0,0), (0,1), (1,0) as in the constructors without
+ * them. */
 struct Triangle : Intersectable {
   V3 p1, p2, p3, n1, n2, n3;
+  float t1[2] = {0, 0}, t2[2] = {0, 1}, t3[2] = {1, 0};
   const Material* mat;
   Triangle(V3 a, V3 b, V3 c, const Material* m) : p1(a), p2(b), p3(c), mat(m) {
     n1 = cross(a - b, a - c).normalized(); n2 = n1; n3 = n1;
@@ -435,7 +486,12 @@ struct Triangle : Intersectable {
     if (v < 0 || u + v > 1) return Hit();
     V3 normal = (1 - u - v) * n1 + u * n2 + v * n3;
     if (normal == V3()) return Hit();
-    return Hit(t, ray, mat, normal, prim, u, v);
+    Hit h(t, ray, mat, normal, prim, u, v);
+    /* (1 - u - v) * t1 + u * t2 + v * t3 (cv::Point2f arithmetic) */
+    float w0 = 1 - u - v;
+    h.tu = w0 * t1[0] + u * t2[0] + v * t3[0];
+    h.tv = w0 * t1[1] + u * t2[1] + v * t3[1];
+    return h;
   }
   AABB bbox() const override { AABB b; b.includePoint(p1); b.includePoint(p2); b.includePoint(p3); return b; }
 };
@@ -461,7 +517,7 @@ struct Sphere : Intersectable {
   Sphere(V3 cc, float rr, const Material* m) : c(cc), r(rr), mat(m) {}
   Hit intersect(const Ray& ray) const override {
     if (prim == tIgnorePrim) return Hit();
-    struct P { float t; V3 n; };
+    struct P { float t; V3 n; float tu, tv; };
     std::list<P> params;
     V3 diff = ray.o - c;
     float r2 = r * r;
@@ -472,14 +528,22 @@ struct Sphere : Intersectable {
     if (disc >= 0) {
       float rd = std::sqrt(disc);
       P p;
-      p.t = (-b - rd) / (2 * a); p.n = ray.evaluate(p.t).affine() - c; params.push_back(p);
-      p.t = (-b + rd) / (2 * a); p.n = ray.evaluate(p.t).affine() - c; params.push_back(p);
+      /* texcoord (acos(n.z / r) / pi, atan2(n.x, n.y) / pi / 2 + 0.5), src/sphere.cpp:44-50 */
+      auto uvOf = [&](P& q) {
+        q.tu = float(std::acos(double(q.n.z / r)) / M_PI);
+        q.tv = float(std::atan2(double(q.n.x), double(q.n.y)) / M_PI / 2 + 0.5);
+      };
+      p.t = (-b - rd) / (2 * a); p.n = ray.evaluate(p.t).affine() - c; uvOf(p); params.push_back(p);
+      p.t = (-b + rd) / (2 * a); p.n = ray.evaluate(p.t).affine() - c; uvOf(p); params.push_back(p);
     }
     if (params.empty() || ray.from > params.back().t) return Hit();
     for (auto& p : params) {
       if (p.t >= ray.from) {
         if (p.t > ray.to) return Hit();
-        return Hit(p.t, ray, mat, p.n, prim);
+        Hit h(p.t, ray, mat, p.n, prim);
+        h.tu = p.tu;
+        h.tv = p.tv;
+        return h;
       }
     }
     return Hit();
@@ -753,6 +817,12 @@ static Scene* buildScene(const gbrt_scene_desc* d, bool useBVH) {
       case GBRT_MAT_PHONG: mm = new PhongMaterial(spec3(m.kd), spec3(m.ks), m.exponent); break;
       case GBRT_MAT_BLINN: mm = new BlinnMaterial(spec3(m.kd), spec3(m.ks), m.exponent); break;
       case GBRT_MAT_TRANSPARENT: mm = new TransparentMaterial(m.ior); break;
+      case GBRT_MAT_TEXTURE:
+        if (m.texture >= 0 && m.texture < d->n_textures) {
+          const gbrt_texture& tx = d->textures[m.texture];
+          mm = new TextureMaterial(tx.width, tx.height, tx.texels, spec3(m.kd), m.exponent);
+        }
+        break;
       default: mm = nullptr;
     }
     if (mm) { s->mats.emplace_back(mm); s->matTable.push_back(mm); }
@@ -793,6 +863,12 @@ static Scene* buildScene(const gbrt_scene_desc* d, bool useBVH) {
       if (useN) t = new Triangle(vec3(p), vec3(p + 3), vec3(p + 6), vec3(n), vec3(n + 3), vec3(n + 6), m);
     }
     if (!useN) t = new Triangle(vec3(p), vec3(p + 3), vec3(p + 6), m);
+    if (d->tri_uv) {
+      const float* uv = d->tri_uv + 6 * i;
+      t->t1[0] = uv[0]; t->t1[1] = uv[1];
+      t->t2[0] = uv[2]; t->t2[1] = uv[3];
+      t->t3[0] = uv[4]; t->t3[1] = uv[5];
+    }
     t->prim = pid;
     s->pool.emplace_back(t);
     top.push_back(t);
@@ -959,9 +1035,11 @@ struct PhysBsdf {
   float e = 0, ior = 1, pd = 1;
 };
 
-static PhysBsdf physOf(const Material* m) {
+static PhysBsdf physOf(const Hit& h) {
+  const Material* m = h.mat;
   PhysBsdf b;
   if (auto* d = dynamic_cast<const DiffuseMaterial*>(m)) { b.kind = 1; b.kd = d->color; }
+  else if (auto* tx = dynamic_cast<const TextureMaterial*>(m)) { b.kind = 1; b.kd = tx->albedo(h); }
   else if (auto* ph = dynamic_cast<const PhongMaterial*>(m)) { b.kind = 2; b.kd = ph->color; b.ks = ph->spec; b.e = ph->e; }
   else if (auto* bl = dynamic_cast<const BlinnMaterial*>(m)) { b.kind = 3; b.kd = bl->kd; b.ks = bl->ks; b.e = bl->e; }
   else if (dynamic_cast<const MirrorMaterial*>(m)) b.kind = 4;
@@ -1080,7 +1158,7 @@ static C3 physRadiance(const Scene& s, const Ray& primary, int D, float p, U&& u
       Lsum = Lsum + mul(alpha, em->get(dn)) * w;
       break;
     }
-    PhysBsdf b = physOf(h.mat);
+    PhysBsdf b = physOf(h);
     if (b.kind <= 0) break;
     V3 x = h.point.affine();
     V3 wo = -ray.d.normalized();

@@ -10,7 +10,11 @@ F3 = C.c_float * 3
 
 class Material(C.Structure):
     _fields_ = [("type", C.c_int32), ("kd", F3), ("ks", F3), ("exponent", C.c_float),
-                ("ior", C.c_float), ("coefficient", C.c_float)]
+                ("ior", C.c_float), ("coefficient", C.c_float), ("texture", C.c_int32)]
+
+
+class Texture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("texels", C.POINTER(C.c_float))]
 
 
 class Quad(C.Structure):
@@ -43,7 +47,8 @@ class SceneDesc(C.Structure):
                 ("spheres", C.POINTER(Sphere)), ("n_spheres", C.c_int32),
                 ("planes", C.POINTER(Plane)), ("n_planes", C.c_int32),
                 ("lights", C.POINTER(Light)), ("n_lights", C.c_int32),
-                ("env", C.POINTER(EnvMap)), ("flags", C.c_int32)]
+                ("env", C.POINTER(EnvMap)), ("flags", C.c_int32),
+                ("textures", C.POINTER(Texture)), ("n_textures", C.c_int32)]
 
 
 class Camera(C.Structure):
@@ -98,7 +103,7 @@ STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "CANCELLED", 
                 6: "NUMERIC", 7: "PARSE", 8: "IO", 9: "UNSUPPORTED"}
 
 # gbrt_material_type
-MAT_DARK, MAT_DIFFUSE, MAT_MIRROR, MAT_PHONG, MAT_BLINN, MAT_TRANSPARENT = range(6)
+MAT_DARK, MAT_DIFFUSE, MAT_MIRROR, MAT_PHONG, MAT_BLINN, MAT_TRANSPARENT, MAT_TEXTURE = range(7)
 # gbrt_light_type
 LIGHT_AREA, LIGHT_POINT, LIGHT_ENV, LIGHT_BLACK, LIGHT_CONE = range(5)
 # gbrt_env_mapping

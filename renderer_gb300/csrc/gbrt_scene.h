@@ -13,6 +13,7 @@
 //   tri_nrm: per smooth triangle 3 normals (9 floats, padded to 12)
 //   planes : n_planes x float4 plane vector; plane_meta (prim, material)
 //   materials, lights: small tables; env texels H x W x 3 float (BGR)
+//   textures: texels of every texture (BGR), their table, per-triangle uv
 // Planes have unbounded boxes and live outside the BVH; the environment map is
 // what a ray with tmax = +inf sees when it hits nothing else.
 #pragma once
@@ -34,6 +35,7 @@ enum DevMatKind : int32_t {
   kMatPhong = GBRT_MAT_PHONG,
   kMatBlinn = GBRT_MAT_BLINN,
   kMatTransparent = GBRT_MAT_TRANSPARENT,
+  kMatTexture = GBRT_MAT_TEXTURE,
 };
 
 struct alignas(16) DevMaterial {
@@ -43,7 +45,7 @@ struct alignas(16) DevMaterial {
   float exponent;
   float ior;
   float rho_d, rho_s;  // lum(kd), lum(ks) for Phong lobe selection
-  float pad;
+  int32_t tex;         // texture material: texture index (gamma in exponent)
 };
 
 struct alignas(16) DevLight {
@@ -73,6 +75,14 @@ struct DeviceScene {
   int32_t env_light;      // light index / prim id of the environment map, -1 if none
   int32_t env_w, env_h, env_mapping;
   float env_coef[3];
+  // Textures (null when no material uses one): texels of all textures one
+  // after the other (3 floats, BGR), per texture (first texel, W, H, -), and
+  // per triangle its three texture coordinates (6 floats, input order; the
+  // triangle of primitive id p is p - tri_pid0).
+  const float* tex_texels;
+  const int4* tex_info;
+  const float* tri_uv;
+  int32_t n_textures, tri_pid0;
 };
 
 // Internal hit encoding of the traversal kernels.

@@ -272,6 +272,8 @@ __device__ __forceinline__ void load_pending(const PTState& st, int slot, Vertex
   pv.n = v3(pn.x, pn.y, pn.z);
   pv.d = v3(pd.x, pd.y, pd.z);
   pv.mat = __float_as_int(pp.w);
+  pv.tu = pd.w;
+  pv.tv = a.w;
   pa = v3(a.x, a.y, a.z);
   k = __float_as_int(pn.w);
 }
@@ -318,7 +320,7 @@ __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, con
     return;  // BlackLight
   }
   if (is_zero(Le)) return;
-  V3f f = brdf_eval(S.materials, vx, dir);
+  V3f f = brdf_eval(S, vx, dir);
   float inCos = dot(-normalize(dir), vx.n);
   float outCos = dot(-normalize(vx.d), vx.n);
   if (signum(inCos) != signum(outCos)) return;
@@ -362,6 +364,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
     Vertex vx;
     vx.d = d;
     vx.mat = -1;
+    vx.tu = 0.f;
+    vx.tv = 0.f;
     int light = -1;
     if (envHit) {
       light = S.env_light;
@@ -376,6 +380,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
         const int kind = __float_as_int(a.w);
         vx.mat = m.y;
         light = m.w;
+        if (S.tri_uv) hit_texcoords(S, h.rec, h.u, h.v, vx.p, vx.tu, vx.tv);
         if (kind == kRecTriangle) {
           if (m.z >= 0) {
             const float* nn = S.tri_nrm + 12 * int64_t(m.z);
@@ -410,7 +415,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
         Vertex pv; V3f pa; int k;
         load_pending(st, slot, pv, pa, k);
         V3f dir = envHit ? -vx.p : pv.p - vx.p;
-        V3f f = brdf_eval(S.materials, pv, dir);
+        V3f f = brdf_eval(S, pv, dir);
         float inCos = dot(-normalize(dir), pv.n);
         float outCos = dot(-normalize(pv.d), pv.n);
         if (signum(inCos) == signum(outCos)) {
@@ -426,7 +431,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
     }
     float pdf;
     V3f f;
-    const V3f out = out_direction(S.materials, vx, stream_u(key, dim_path(i)), stream_u(key, dim_path(i) + 1), pdf, f);
+    const V3f out = out_direction(S, vx, stream_u(key, dim_path(i)), stream_u(key, dim_path(i) + 1), pdf, f);
     if (mat_specular(S.materials, vx.mat)) {
       // Specular vertices are not stored (lines 87-91).
       if (i == plen - 1 && plen < P.D) plen++;
@@ -471,8 +476,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
     } else {
       st.pv_p[slot] = make_float4(vx.p.x, vx.p.y, vx.p.z, __int_as_float(vx.mat));
       st.pv_n[slot] = make_float4(vx.n.x, vx.n.y, vx.n.z, __int_as_float(k));
-      st.pv_d[slot] = make_float4(d.x, d.y, d.z, 0.f);
-      st.pv_a[slot] = make_float4(alpha.x, alpha.y, alpha.z, 0.f);
+      st.pv_d[slot] = make_float4(d.x, d.y, d.z, vx.tu);
+      st.pv_a[slot] = make_float4(alpha.x, alpha.y, alpha.z, vx.tv);
       st.alpha[slot] = make_float4(na.x, na.y, na.z, 0.f);
       st.ctl[slot] = make_int4(i, plen, nst, 1);
       push_ext(st, nxt, slot, vx.p, out);
@@ -635,7 +640,9 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
     V3f nrm;
     int mat = -1;
     surface_normal(S, h, x, nrm, mat);
-    const PhysBsdf b = phys_bsdf(S.materials, mat);
+    float tu = 0.f, tv = 0.f;
+    if (S.tri_uv) hit_texcoords(S, h.rec, h.u, h.v, x, tu, tv);
+    const PhysBsdf b = phys_bsdf(S, mat, tu, tv);
     if (b.kind <= 0) continue;
     const unsigned long long key = stream_key(P.seed, P.g0 + (unsigned long long)slot);
     const unsigned base = dim_phys(i);
@@ -708,7 +715,7 @@ __global__ void __launch_bounds__(256) k_guide_prep(DeviceScene S, PTState st, i
       V3f nrm;
       int mat = -1;
       surface_normal(S, h, x, nrm, mat);
-      const PhysBsdf b = phys_bsdf(S.materials, mat);
+      const PhysBsdf b = phys_bsdf(S, mat, 0.f, 0.f);  // only its kind matters here
       if (b.kind >= 1 && b.kind <= 3) {
         const V3f wo = -normalize(d);
         if (dot(nrm, wo) < 0.f) nrm = -nrm;
@@ -787,6 +794,51 @@ __global__ void __launch_bounds__(256) k_accumulate(PTParams P, PTState st, doub
   size_t o = size_t(p) * 3;
   sum[o] += s0; sum[o + 1] += s1; sum[o + 2] += s2;
   if (sumsq) { sumsq[o] += q0; sumsq[o + 1] += q1; sumsq[o + 2] += q2; }
+}
+
+// The same with one warp per pixel, for many samples per pixel.
+__global__ void __launch_bounds__(256) k_accumulate_warp(PTParams P, PTState st, double* sum, double* sumsq) {
+  const unsigned long long p0 = P.g0 / unsigned(P.spp);
+  const unsigned long long p1 = (P.g0 + unsigned(P.nb) - 1) / unsigned(P.spp);
+  const unsigned long long p = p0 + (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (p > p1) return;  // whole warps leave together
+  const unsigned long long gb = max(P.g0, p * unsigned(P.spp));
+  const unsigned long long ge = min(P.g0 + unsigned(P.nb), (p + 1) * unsigned(P.spp));
+  double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0;
+  unsigned long long bad = 0;
+  for (unsigned long long g = gb + lane; g < ge; g += 32) {
+    float4 L = st.L[g - P.g0];
+    if (!isfinite(L.x) || !isfinite(L.y) || !isfinite(L.z)) { ++bad; continue; }
+    s0 += L.x; s1 += L.y; s2 += L.z;
+    q0 += double(L.x) * L.x; q1 += double(L.y) * L.y; q2 += double(L.z) * L.z;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    s2 += __shfl_down_sync(0xffffffffu, s2, o);
+    q0 += __shfl_down_sync(0xffffffffu, q0, o);
+    q1 += __shfl_down_sync(0xffffffffu, q1, o);
+    q2 += __shfl_down_sync(0xffffffffu, q2, o);
+    bad += __shfl_down_sync(0xffffffffu, bad, o);
+  }
+  if (lane == 0) {
+    if (bad) atomicAdd(&st.tally[2], bad);
+    size_t o = size_t(p) * 3;
+    sum[o] += s0; sum[o + 1] += s1; sum[o + 2] += s2;
+    if (sumsq) { sumsq[o] += q0; sumsq[o + 1] += q1; sumsq[o + 2] += q2; }
+  }
+}
+
+// Accumulation of a batch: a thread per pixel for few samples per pixel, a
+// warp per pixel for many.
+static void launch_accumulate(const PTParams& P, const PTState& st, double* sum, double* sumsq, cudaStream_t stream) {
+  const unsigned long long p0 = P.g0 / unsigned(P.spp), p1 = (P.g0 + unsigned(P.nb) - 1) / unsigned(P.spp);
+  const unsigned long long np = p1 - p0 + 1;
+  if (P.spp >= 64)
+    k_accumulate_warp<<<unsigned((np * 32 + 255) / 256), 256, 0, stream>>>(P, st, sum, sumsq);
+  else
+    k_accumulate<<<unsigned((np + 255) / 256), 256, 0, stream>>>(P, st, sum, sumsq);
 }
 
 __global__ void k_finalize(const double* sum, float* film, size_t n3, double inv_spp) {
@@ -966,7 +1018,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
     }
     unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
     unsigned long long np = p1 - p0 + 1;
-    k_accumulate<<<unsigned((np + 255) / 256), 256, 0, stream>>>(P, st, d_sum, d_sumsq);
+    launch_accumulate(P, st, d_sum, d_sumsq, stream);
     ++launches;
     A(cudaGetLastError());
     if (e != cudaSuccess) break;
@@ -1163,7 +1215,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
       launches += 3;
     }
     unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
-    k_accumulate<<<unsigned((p1 - p0 + 1 + 255) / 256), 256, 0, stream>>>(P, st, d_sum, d_sumsq);
+    launch_accumulate(P, st, d_sum, d_sumsq, stream);
     ++launches;
     A(cudaGetLastError());
     if (e != cudaSuccess) break;
@@ -1396,7 +1448,7 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
         tk.sh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
       }
       unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
-      k_accumulate<<<unsigned((p1 - p0 + 256) / 256), 256, 0, stream>>>(P, st, d_pass, nullptr);
+      launch_accumulate(P, st, d_pass, nullptr, stream);
       if (record) k_guide_collect<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
       A(cudaGetLastError());
     }

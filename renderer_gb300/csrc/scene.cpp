@@ -200,6 +200,18 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   if ((d->n_materials && !d->materials) || (d->n_tri && !d->tri_pos) || (d->n_quads && !d->quads) ||
       (d->n_spheres && !d->spheres) || (d->n_planes && !d->planes) || (d->n_lights && !d->lights))
     return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: NULL array with a non-zero count");
+  if (d->n_textures < 0 || (d->n_textures && !d->textures))
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: bad texture table");
+  for (int i = 0; i < d->n_textures; ++i)
+    if (d->textures[i].width <= 0 || d->textures[i].height <= 0 || !d->textures[i].texels)
+      return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: texture without an image");
+  bool anyTexture = false;
+  for (int i = 0; i < d->n_materials; ++i)
+    if (d->materials[i].type == GBRT_MAT_TEXTURE) {
+      if (d->materials[i].texture < 0 || d->materials[i].texture >= d->n_textures)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: texture material without a texture");
+      anyTexture = true;
+    }
   int envLights = 0;
   for (int i = 0; i < d->n_lights; ++i) {
     int ty = d->lights[i].type;
@@ -385,7 +397,8 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     const gbrt_material& m = d->materials[i];
     DevMaterial& dm = mats[i];
     std::memset(&dm, 0, sizeof dm);
-    dm.type = (m.type >= GBRT_MAT_DARK && m.type <= GBRT_MAT_TRANSPARENT) ? m.type : GBRT_MAT_DARK;
+    dm.type = (m.type >= GBRT_MAT_DARK && m.type <= GBRT_MAT_TEXTURE) ? m.type : GBRT_MAT_DARK;
+    dm.tex = m.type == GBRT_MAT_TEXTURE ? m.texture : -1;
     for (int k = 0; k < 3; ++k) { dm.kd[k] = m.kd[k]; dm.ks[k] = m.ks[k]; }
     dm.exponent = m.exponent;
     dm.ior = m.ior;
@@ -436,6 +449,30 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   v.n_materials = d->n_materials;
   v.n_lights = d->n_lights;
   v.env_light = -1;
+  if (anyTexture) {
+    // Texels of all textures back to back, their table, and the triangles'
+    // texture coordinates (the Triangle constructor's default without any).
+    std::vector<float> texels;
+    std::vector<int4> info(size_t(d->n_textures));
+    for (int i = 0; i < d->n_textures; ++i) {
+      const gbrt_texture& t = d->textures[i];
+      info[i] = make_int4(int(texels.size() / 3), t.width, t.height, 0);
+      texels.insert(texels.end(), t.texels, t.texels + size_t(t.width) * t.height * 3);
+    }
+    std::vector<float> uv(size_t(d->n_tri) * 6);
+    for (int64_t i = 0; i < d->n_tri; ++i) {
+      static const float kDefault[6] = {0, 0, 0, 1, 1, 0};
+      std::memcpy(&uv[6 * i], d->tri_uv ? d->tri_uv + 6 * i : kDefault, 6 * sizeof(float));
+    }
+    if ((st = upload(s, texels, &v.tex_texels)) != GBRT_OK || (st = upload(s, info, &v.tex_info)) != GBRT_OK ||
+        (st = upload(s, uv, &v.tri_uv)) != GBRT_OK) {
+      free_scene(s);
+      delete s;
+      return st;
+    }
+    v.n_textures = d->n_textures;
+  }
+  v.tri_pid0 = d->n_lights;
   if (envLight >= 0) {
     const gbrt_env_map* e = d->env;
     envTex.assign(e->texels, e->texels + size_t(e->width) * e->height * 3);

@@ -15,10 +15,12 @@
 // Differences, for the GPU layout: instances are flattened by transforming
 // their primitives (a sphere needs a similarity transform); a pre-built
 // b(left, right, box) node contributes its children (the BVH is rebuilt);
-// box(min, max, m) becomes six quads; CSG operations and texture images are
-// not part of the GPU path (texture materials fall back to a diffuse material
-// of their colour coefficient); an environment map that
-// fails to load becomes a BlackLight, as in the renderer
+// box(min, max, m) becomes six quads; CSG operations are not part of the GPU
+// path. Texture images are read from PPM (P6/P3), PFM and Radiance files
+// (formats the repository decodes itself; PNG/JPEG need an image codec
+// library that is not part of this build) and scaled by 1/255 like the
+// renderer's cv::imread + convertTo; an unreadable image gives DarkMatter.
+// An environment map that fails to load becomes a BlackLight, as in the renderer
 // (src/sceneast.cpp:598-610). As an extension, environmentmap("f", c,
 // "latlong") selects an equirectangular image.
 #include <algorithm>
@@ -543,10 +545,54 @@ bool readPFM(const std::string& path, std::vector<float>& bgr, int& W, int& H, s
   return true;
 }
 
+// Netpbm colour images (P6 binary, P3 ASCII) with at most 8 bits per sample:
+// samples 0..maxval, returned as they are (the caller scales them).
+bool readPPM(const std::string& path, std::vector<float>& bgr, int& W, int& H, std::string& why) {
+  std::string data;
+  if (!readFile(path, data)) { why = "cannot read " + path; return false; }
+  size_t pos = 0;
+  auto token = [&]() -> std::string {
+    while (pos < data.size()) {
+      if (data[pos] == '#') { while (pos < data.size() && data[pos] != '\n') ++pos; }
+      else if (std::isspace((unsigned char)data[pos])) ++pos;
+      else break;
+    }
+    size_t b = pos;
+    while (pos < data.size() && !std::isspace((unsigned char)data[pos]) && data[pos] != '#') ++pos;
+    return data.substr(b, pos - b);
+  };
+  std::string magic = token();
+  if (magic != "P6" && magic != "P3") { why = path + ": not a P6/P3 image"; return false; }
+  long w = std::atol(token().c_str()), h = std::atol(token().c_str()), mx = std::atol(token().c_str());
+  if (w <= 0 || h <= 0 || mx <= 0 || mx > 255 || w > 65536 || h > 65536) {
+    why = path + ": unsupported size or sample depth";
+    return false;
+  }
+  W = int(w);
+  H = int(h);
+  bgr.assign(size_t(W) * H * 3, 0.f);
+  if (magic == "P6") {
+    ++pos;  // the single whitespace after maxval
+    if (data.size() < pos + size_t(W) * H * 3) { why = path + ": truncated"; return false; }
+    for (size_t i = 0; i < size_t(W) * H; ++i)
+      for (int c = 0; c < 3; ++c) bgr[i * 3 + (2 - c)] = float((unsigned char)data[pos + i * 3 + c]);
+  } else {
+    for (size_t i = 0; i < size_t(W) * H; ++i)
+      for (int c = 0; c < 3; ++c) {
+        std::string t = token();
+        if (t.empty()) { why = path + ": truncated"; return false; }
+        bgr[i * 3 + (2 - c)] = float(std::atol(t.c_str()));
+      }
+  }
+  return true;
+}
+
 bool readImage(const std::string& path, std::vector<float>& bgr, int& W, int& H, std::string& why) {
   std::string lower = path;
   std::transform(lower.begin(), lower.end(), lower.begin(), ::tolower);
   if (lower.size() >= 4 && lower.substr(lower.size() - 4) == ".pfm") return readPFM(path, bgr, W, H, why);
+  if (lower.size() >= 4 && (lower.substr(lower.size() - 4) == ".ppm" || lower.substr(lower.size() - 4) == ".pnm"))
+    return readPPM(path, bgr, W, H, why);
   return readHDR(path, bgr, W, H, why);
 }
 
@@ -573,8 +619,11 @@ void readMTL(const std::string& path, std::map<std::string, MatNode>& out) {
     MatNode m;
     if (cur.illum <= 2) {
       if (!cur.tex.empty()) {
+        // relative to the MTL file, with Windows separators turned around
+        std::string tex = cur.tex;
+        std::replace(tex.begin(), tex.end(), '\\', '/');
         m.kind = -2;
-        m.ident = cur.tex;
+        m.ident = joinPath(dirOf(path), tex);
         m.kd = (cur.kd.x != 0 || cur.kd.y != 0 || cur.kd.z != 0) ? cur.kd : V3{1, 1, 1};
         m.exponent = 1;
       } else if ((cur.ks.x == 0 && cur.ks.y == 0 && cur.ks.z == 0) || cur.ns == 0) {
@@ -706,7 +755,10 @@ bool readOBJ(const std::string& path, std::vector<ObjTri>& tris, std::map<std::s
 // -------------------------------------------------------- parsed scene ----
 struct gbrt_parsed_scene {
   std::vector<gbrt_material> materials;
-  std::vector<float> tri_pos, tri_nrm;
+  std::vector<float> tri_pos, tri_nrm, tri_uv;
+  std::vector<std::vector<float>> texels;  // per texture
+  std::vector<gbrt_texture> textures;
+  std::map<std::string, int> texture_ids;  // path -> texture
   std::vector<int32_t> tri_mat;
   std::vector<gbrt_quad> quads;
   std::vector<gbrt_sphere> spheres;
@@ -734,11 +786,42 @@ struct Builder {
 
   Builder(gbrt_parsed_scene& p, std::string dir) : ps(p), baseDir(std::move(dir)) {}
 
+  // The texture of an image file, loaded once (TextureMaterial::load,
+  // src/texturematerial.cpp:48-60: cv::imread converted with scale 1/255);
+  // -1 when it cannot be read.
+  int loadTexture(const std::string& file) {
+    std::string path = joinPath(baseDir, file);
+    auto it = ps.texture_ids.find(path);
+    if (it != ps.texture_ids.end()) return it->second;
+    std::vector<float> bgr;
+    int W = 0, H = 0;
+    std::string why;
+    int id = -1;
+    if (readImage(path, bgr, W, H, why)) {
+      for (float& x : bgr) x *= 1.f / 255.f;
+      ps.texels.push_back(std::move(bgr));
+      ps.textures.push_back(gbrt_texture{W, H, nullptr});
+      id = int(ps.textures.size()) - 1;
+    }
+    ps.texture_ids[path] = id;
+    return id;
+  }
+
   int addMat(const MatNode& m) {
     gbrt_material g{};
-    if (m.kind == -2) {  // texture image: diffuse with its colour coefficient
-      g.type = GBRT_MAT_DIFFUSE;
-      g.kd[0] = m.kd.z; g.kd[1] = m.kd.y; g.kd[2] = m.kd.x;
+    g.texture = -1;
+    if (m.kind == -2) {
+      // TextureMaterial(coefficient, gamma); an image that cannot be read
+      // gives DarkMatter (src/sceneast.cpp:345-365).
+      int tex = loadTexture(m.ident);
+      if (tex >= 0) {
+        g.type = GBRT_MAT_TEXTURE;
+        g.texture = tex;
+        g.kd[0] = m.kd.z; g.kd[1] = m.kd.y; g.kd[2] = m.kd.x;
+        g.exponent = m.exponent;
+      } else {
+        g.type = GBRT_MAT_DARK;
+      }
     } else {
       g.type = m.kind;
       // asSpectrum: RGB -> BGR (src/sceneast.cpp:410-414)
@@ -768,7 +851,10 @@ struct Builder {
     return addMat(m);
   }
 
-  void addTri(V3 a, V3 b, V3 c, const V3* n, int mat, const Mat4* xf) {
+  void addTri(V3 a, V3 b, V3 c, const V3* n, const float* uv, int mat, const Mat4* xf) {
+    static const float kDefaultUV[6] = {0, 0, 0, 1, 1, 0};
+    const float* t = uv ? uv : kDefaultUV;
+    ps.tri_uv.insert(ps.tri_uv.end(), t, t + 6);
     V3 p[3] = {a, b, c};
     for (int k = 0; k < 3; ++k) {
       V3 q = xf ? xf->point(p[k]) : p[k];
@@ -835,7 +921,7 @@ struct Builder {
         break;
       case Node::TRI: {
         bool smooth = !(isNull(n->n[0]) || isNull(n->n[1]) || isNull(n->n[2]));
-        addTri(n->p[0], n->p[1], n->p[2], smooth ? n->n : nullptr, resolveMat(n->mat), xf);
+        addTri(n->p[0], n->p[1], n->p[2], smooth ? n->n : nullptr, n->uv, resolveMat(n->mat), xf);
         break;
       }
       case Node::PLANE: {
@@ -913,7 +999,7 @@ struct Builder {
             }
             m = lt->second;
           }
-          addTri(t.p[0], t.p[1], t.p[2], t.hasN ? t.n : nullptr, m, xf);
+          addTri(t.p[0], t.p[1], t.p[2], t.hasN ? t.n : nullptr, t.uv, m, xf);
         }
         break;
       }
@@ -1089,6 +1175,7 @@ gbrt_status gbrt_parsed_scene_desc(const gbrt_parsed_scene* ps, gbrt_scene_desc*
   d->tri_pos = d->n_tri ? ps->tri_pos.data() : nullptr;
   d->tri_nrm = (d->n_tri && ps->any_smooth) ? ps->tri_nrm.data() : nullptr;
   d->tri_mat = d->n_tri ? ps->tri_mat.data() : nullptr;
+  d->tri_uv = d->n_tri ? ps->tri_uv.data() : nullptr;
   d->quads = ps->quads.empty() ? nullptr : ps->quads.data();
   d->n_quads = int32_t(ps->quads.size());
   d->spheres = ps->spheres.empty() ? nullptr : ps->spheres.data();
@@ -1098,6 +1185,10 @@ gbrt_status gbrt_parsed_scene_desc(const gbrt_parsed_scene* ps, gbrt_scene_desc*
   d->lights = ps->lights.empty() ? nullptr : ps->lights.data();
   d->n_lights = int32_t(ps->lights.size());
   d->env = ps->has_env ? &ps->env : nullptr;
+  auto* mps = const_cast<gbrt_parsed_scene*>(ps);
+  for (size_t i = 0; i < mps->textures.size(); ++i) mps->textures[i].texels = mps->texels[i].data();
+  d->textures = ps->textures.empty() ? nullptr : ps->textures.data();
+  d->n_textures = int32_t(ps->textures.size());
   if (cam) *cam = ps->camera;
   if (has_camera) *has_camera = ps->has_camera ? 1 : 0;
   return GBRT_OK;

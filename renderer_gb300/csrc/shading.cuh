@@ -105,7 +105,70 @@ struct Vertex {
   V3f n;     // normalised surface normal (unflipped)
   V3f d;     // direction of the ray that hit it (unnormalised)
   int mat;   // material index, -1 = DarkMatter
+  float tu, tv;  // texture coordinates (HitRecord::getTexCoords)
 };
+
+// ----------------------------------------------------------- Textures -----
+// Texture coordinates of a hit, HitRecord::getTexCoords: a triangle's
+// (1 - u - v) t1 + u t2 + v t3 (src/triangle.cpp:54) in the renderer's
+// operation order; a quad's halves carry the Triangle constructor's default
+// (0,0), (0,1), (1,0) (src/triangle.h:35, src/quad.h:32); a sphere's
+// (acos(n.z / r) / pi, atan2(n.x, n.y) / 2pi + 1/2) with n = x - centre
+// (src/sphere.cpp:44-50); other primitives (0, 0).
+__device__ __forceinline__ void hit_texcoords(const DeviceScene& S, int rec, float u, float v, V3f x, float& tu,
+                                              float& tv) {
+  tu = 0.f;
+  tv = 0.f;
+  if (!S.tri_uv || rec < 0) return;
+  const float4* rp = S.recs + 3 * int64_t(rec);
+  const float4 a = __ldg(rp);
+  const int kind = __float_as_int(a.w);
+  if (kind == kRecSphere) {
+    const float r = __ldg(rp + 1).x;
+    const V3f n = x - v3(a.x, a.y, a.z);
+    tu = acosf(n.z / r) * kInvPi;
+    tv = atan2f(n.x, n.y) * (0.5f * kInvPi) + 0.5f;
+    return;
+  }
+  if (kind != kRecTriangle) return;
+  const float w0 = __fsub_rn(__fsub_rn(1.f, u), v);
+  if (__float_as_int(__ldg(rp + 1).w) != 0) {
+    tu = __fadd_rn(__fadd_rn(__fmul_rn(w0, 0.f), __fmul_rn(u, 0.f)), __fmul_rn(v, 1.f));
+    tv = __fadd_rn(__fadd_rn(__fmul_rn(w0, 0.f), __fmul_rn(u, 1.f)), __fmul_rn(v, 0.f));
+    return;
+  }
+  const float* t = S.tri_uv + 6 * int64_t(__ldg(&S.meta[rec]).x - S.tri_pid0);
+  tu = __fadd_rn(__fadd_rn(__fmul_rn(w0, t[0]), __fmul_rn(u, t[2])), __fmul_rn(v, t[4]));
+  tv = __fadd_rn(__fadd_rn(__fmul_rn(w0, t[1]), __fmul_rn(u, t[3])), __fmul_rn(v, t[5]));
+}
+
+// TextureMaterial::get + brdf's pow (src/texturematerial.cpp:62-74): the
+// bilinear sample of the texture at (frac(u) (W - 1), frac(1 - v) (H - 1))
+// (cv::getRectSubPix of a 1 x 1 patch, border replicated), times the
+// coefficient kd, to the power gamma (the material's exponent).
+__device__ __forceinline__ V3f texture_albedo(const DeviceScene& S, const DevMaterial& m, float u, float v) {
+  const int4 ti = __ldg(&S.tex_info[m.tex]);
+  const int W = ti.y, H = ti.z;
+  float fu = fmodf(u, 1.f), fv = fmodf(1.f - v, 1.f);
+  if (fu < 0.f) fu += 1.f;
+  if (fv < 0.f) fv += 1.f;
+  const float x = fu * float(W - 1), y = fv * float(H - 1);
+  const float fx = floorf(x), fy = floorf(y);
+  const float a = x - fx, b = y - fy;
+  const int x0 = min(max(int(fx), 0), W - 1), y0 = min(max(int(fy), 0), H - 1);
+  const int x1 = min(x0 + 1, W - 1), y1 = min(y0 + 1, H - 1);
+  const float* T = S.tex_texels + 3 * int64_t(ti.x);
+  const float w00 = (1.f - a) * (1.f - b), w10 = a * (1.f - b), w01 = (1.f - a) * b, w11 = a * b;
+  V3f r;
+  float* rr = &r.x;
+  for (int c = 0; c < 3; ++c) {
+    float s = __ldg(T + (int64_t(y0) * W + x0) * 3 + c) * w00 + __ldg(T + (int64_t(y0) * W + x1) * 3 + c) * w10 +
+              __ldg(T + (int64_t(y1) * W + x0) * 3 + c) * w01 + __ldg(T + (int64_t(y1) * W + x1) * 3 + c) * w11;
+    s *= m.kd[c];
+    rr[c] = m.exponent == 1.f ? s : powf(s, m.exponent);
+  }
+  return r;
+}
 
 __device__ __forceinline__ V3f phong_spec(const DevMaterial& m, const Vertex& h, V3f dir) {
   V3f refl = reflect(dir, h.n);
@@ -121,12 +184,14 @@ __device__ __forceinline__ float blinn_G(V3f wi, V3f wo, V3f n) {
 
 // Material::brdf(hit, direction): direction points from the light towards the
 // surface (the renderer's convention).
-__device__ __forceinline__ V3f brdf_eval(const DevMaterial* mats, const Vertex& h, V3f dir) {
+__device__ __forceinline__ V3f brdf_eval(const DeviceScene& S, const Vertex& h, V3f dir) {
   if (h.mat < 0) return v3(0.f, 0.f, 0.f);
-  const DevMaterial& m = mats[h.mat];
+  const DevMaterial& m = S.materials[h.mat];
   switch (m.type) {
     case kMatDiffuse:
       return v3(m.kd[0] * kInvPi, m.kd[1] * kInvPi, m.kd[2] * kInvPi);
+    case kMatTexture:
+      return kInvPi * texture_albedo(S, m, h.tu, h.tv);
     case kMatPhong: {
       V3f s = phong_spec(m, h, dir);
       return v3(m.kd[0] * kInvPi + s.x, m.kd[1] * kInvPi + s.y, m.kd[2] * kInvPi + s.z);
@@ -154,18 +219,20 @@ __device__ __forceinline__ bool mat_specular(const DevMaterial* mats, int mat) {
 }
 
 // Material::outDirection(hit, sample, pdf, brdf).
-__device__ __forceinline__ V3f out_direction(const DevMaterial* mats, const Vertex& h, float sx, float sy, float& pdf,
+__device__ __forceinline__ V3f out_direction(const DeviceScene& S, const Vertex& h, float sx, float sy, float& pdf,
                                              V3f& brdf) {
   brdf = v3(0.f, 0.f, 0.f);
   pdf = 0.f;
   if (h.mat < 0) return v3(0.f, 0.f, 0.f);
-  const DevMaterial& m = mats[h.mat];
+  const DevMaterial& m = S.materials[h.mat];
   switch (m.type) {
-    case kMatDiffuse: {
+    case kMatDiffuse:
+    case kMatTexture: {  // AbstractDiffuseMaterial::outDirection
       V3f n = h.n;
       if (dot(n, normalize(h.d)) > 0.f) n = -n;
       V3f out = cosine_power_dir(n, sx, sy, 1.f, pdf);
-      brdf = v3(m.kd[0] * kInvPi, m.kd[1] * kInvPi, m.kd[2] * kInvPi);
+      brdf = m.type == kMatDiffuse ? v3(m.kd[0] * kInvPi, m.kd[1] * kInvPi, m.kd[2] * kInvPi)
+                                   : kInvPi * texture_albedo(S, m, h.tu, h.tv);
       return out;
     }
     case kMatMirror:
@@ -195,7 +262,7 @@ __device__ __forceinline__ V3f out_direction(const DevMaterial* mats, const Vert
       if (dot(wo, wh) < 0.f) { pdf = 0.f; return v3(0.f, 0.f, 0.f); }
       V3f out = -reflect(wo, wh);
       pdf /= 4.f * fmaxf(dot(wo, wh), 0.0001f);
-      brdf = brdf_eval(mats, h, out);
+      brdf = brdf_eval(S, h, out);
       return out;
     }
     case kMatTransparent: {
@@ -261,15 +328,16 @@ struct PhysBsdf {
   float e, ior, pd;
 };
 
-__device__ __forceinline__ PhysBsdf phys_bsdf(const DevMaterial* mats, int mat) {
+__device__ __forceinline__ PhysBsdf phys_bsdf(const DeviceScene& S, int mat, float tu, float tv) {
   PhysBsdf b;
   b.kind = 0; b.e = 0.f; b.ior = 1.f; b.pd = 1.f;
   b.kd = v3(0.f, 0.f, 0.f); b.ks = v3(0.f, 0.f, 0.f);
   if (mat < 0) return b;
-  const DevMaterial& m = mats[mat];
+  const DevMaterial& m = S.materials[mat];
   b.kd = ld3(m.kd); b.ks = ld3(m.ks); b.e = m.exponent; b.ior = m.ior;
   switch (m.type) {
     case kMatDiffuse: b.kind = 1; break;
+    case kMatTexture: b.kind = 1; b.kd = texture_albedo(S, m, tu, tv); break;
     case kMatPhong: b.kind = 2; break;
     case kMatBlinn: b.kind = 3; break;
     case kMatMirror: b.kind = 4; break;

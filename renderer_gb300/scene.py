@@ -23,6 +23,7 @@ class SceneData:
     materials: List[dict] = field(default_factory=list)
     tri_pos: Optional[np.ndarray] = None   # (N, 9) float32
     tri_nrm: Optional[np.ndarray] = None   # (N, 9) float32 or None
+    tri_uv: Optional[np.ndarray] = None    # (N, 6) float32 or None
     tri_mat: Optional[np.ndarray] = None   # (N,) int32 or None (all material 0)
     quads: List[tuple] = field(default_factory=list)     # (p1, p2, p3, p4, material)
     spheres: List[tuple] = field(default_factory=list)   # (center, radius, material)
@@ -32,12 +33,18 @@ class SceneData:
     env_mapping: int = _abi.ENV_ANGULAR
     camera: Optional[dict] = None          # {"eye", "look_at", "up", "fov", "width", "height"}
     flags: int = 0                         # gbrt_scene_flags
+    textures: List[np.ndarray] = field(default_factory=list)  # (H, W, 3) float32 BGR each
 
     # ------------------------------------------------------------ building
-    def add_material(self, type, kd=(0, 0, 0), ks=(0, 0, 0), exponent=0.0, ior=1.0, coefficient=1.0):
+    def add_material(self, type, kd=(0, 0, 0), ks=(0, 0, 0), exponent=0.0, ior=1.0, coefficient=1.0, texture=-1):
         self.materials.append(dict(type=type, kd=tuple(kd), ks=tuple(ks), exponent=float(exponent),
-                                   ior=float(ior), coefficient=float(coefficient)))
+                                   ior=float(ior), coefficient=float(coefficient), texture=int(texture)))
         return len(self.materials) - 1
+
+    def add_texture(self, texels):
+        """A (H, W, 3) BGR texture; returns its index."""
+        self.textures.append(np.ascontiguousarray(texels, np.float32))
+        return len(self.textures) - 1
 
     def n_tri(self):
         return 0 if self.tri_pos is None else int(self.tri_pos.shape[0])
@@ -63,7 +70,7 @@ class SceneData:
             arr = (_abi.Material * len(self.materials))()
             for i, m in enumerate(self.materials):
                 arr[i] = _abi.Material(m["type"], _f3(m["kd"]), _f3(m["ks"]), m["exponent"], m["ior"],
-                                       m["coefficient"])
+                                       m["coefficient"], m.get("texture", -1))
             keep.append(arr)
             d.materials = arr
             d.n_materials = len(self.materials)
@@ -75,6 +82,10 @@ class SceneData:
                 nrm = np.ascontiguousarray(self.tri_nrm, dtype=np.float32)
                 keep.append(nrm)
                 d.tri_nrm = nrm.ctypes.data_as(C.POINTER(C.c_float))
+            if self.tri_uv is not None:
+                uv = np.ascontiguousarray(self.tri_uv, dtype=np.float32)
+                keep.append(uv)
+                d.tri_uv = uv.ctypes.data_as(C.POINTER(C.c_float))
             if self.tri_mat is not None:
                 mat = np.ascontiguousarray(self.tri_mat, dtype=np.int32)
                 keep.append(mat)
@@ -118,6 +129,15 @@ class SceneData:
             keep.append(e)
             d.env = C.pointer(e)
         d.flags = int(self.flags)
+        if self.textures:
+            arr = (_abi.Texture * len(self.textures))()
+            for i, t in enumerate(self.textures):
+                t = np.ascontiguousarray(t, np.float32)
+                keep.append(t)
+                arr[i] = _abi.Texture(t.shape[1], t.shape[0], t.ctypes.data_as(C.POINTER(C.c_float)))
+            keep.append(arr)
+            d.textures = arr
+            d.n_textures = len(self.textures)
         return d, keep
 
     def camera_struct(self, width=None, height=None):

@@ -23,11 +23,16 @@ def _from_parsed(ps):
     for i in range(d.n_materials):
         m = d.materials[i]
         s.materials.append(dict(type=m.type, kd=tuple(m.kd), ks=tuple(m.ks), exponent=m.exponent, ior=m.ior,
-                                coefficient=m.coefficient))
+                                coefficient=m.coefficient, texture=m.texture))
+    for i in range(d.n_textures):
+        t = d.textures[i]
+        s.textures.append(np.ctypeslib.as_array(t.texels, shape=(t.height, t.width, 3)).copy())
     if d.n_tri:
         s.tri_pos = np.ctypeslib.as_array(d.tri_pos, shape=(d.n_tri, 9)).copy()
         if d.tri_nrm:
             s.tri_nrm = np.ctypeslib.as_array(d.tri_nrm, shape=(d.n_tri, 9)).copy()
+        if d.tri_uv:
+            s.tri_uv = np.ctypeslib.as_array(d.tri_uv, shape=(d.n_tri, 6)).copy()
         s.tri_mat = np.ctypeslib.as_array(d.tri_mat, shape=(d.n_tri,)).copy()
     for i in range(d.n_quads):
         q = d.quads[i]
