@@ -26,6 +26,7 @@
  *                                       renderer's Quad object, src/quad.h:32)
  *   [+0, +n_spheres)                    spheres
  *   [+0, +n_planes)                     planes
+ *   [+0, +n_csg)                        CSG objects (one id per object)
  *
  * Threading: calls on one gbrt_ctx are serialised by the caller; distinct
  * contexts are independent. All device memory is owned by the library.
@@ -137,6 +138,31 @@ typedef struct gbrt_env_map {
   const float* texels;    /* host pointer, copied by gbrt_scene_create */
 } gbrt_env_map;
 
+/* Constructive solid geometry, src/csgobject.cpp:25-44,
+ * src/csgoperation.cpp:27-97, src/sphere.cpp:29-56, src/axisalignedbox.cpp:
+ * 30-73. A CSG object is a tree of nodes: leaves are spheres (centre a,
+ * radius b[0]) and axis-aligned boxes (min a, max b) with a material;
+ * operations combine their left and right subtrees' interval lists. A hit is
+ * the first interval boundary at or beyond the ray's start; a box's exit
+ * boundary carries its entry face's normal, as in the renderer. At most
+ * GBRT_CSG_MAX_LEAVES leaves per object. */
+typedef enum gbrt_csg_op {
+  GBRT_CSG_SPHERE = 0,
+  GBRT_CSG_BOX = 1,
+  GBRT_CSG_ISECT = 2,  /* left and right, src/csgoperation.cpp:78-81 */
+  GBRT_CSG_UNION = 3,  /* left or right */
+  GBRT_CSG_DIFF = 4,   /* left and not right */
+  GBRT_CSG_XOR = 5     /* left xor right */
+} gbrt_csg_op;
+#define GBRT_CSG_MAX_LEAVES 8
+
+typedef struct gbrt_csg_node {
+  int32_t op;           /* gbrt_csg_op */
+  int32_t left, right;  /* operations: child node indices */
+  float a[3], b[3];     /* leaves: sphere (centre, radius in b[0]) or box (min, max) */
+  int32_t material;     /* leaves */
+} gbrt_csg_node;
+
 typedef struct gbrt_scene_desc {
   const gbrt_material* materials; int32_t n_materials;
   /* triangle soup: n_tri x 9 positions (p1,p2,p3); optional n_tri x 9 normals
@@ -153,6 +179,9 @@ typedef struct gbrt_scene_desc {
   const gbrt_env_map* env;  /* NULL if no environment map */
   int32_t flags;            /* gbrt_scene_flags */
   const gbrt_texture* textures; int32_t n_textures;
+  /* CSG objects: csg_roots[i] is the root node (in csg_nodes) of object i */
+  const gbrt_csg_node* csg_nodes; int32_t n_csg_nodes;
+  const int32_t* csg_roots; int32_t n_csg;
 } gbrt_scene_desc;
 
 typedef enum gbrt_scene_flags {

@@ -53,6 +53,7 @@
 #include <algorithm>
 #include <cstring>
 #include <list>
+#include <functional>
 #include <memory>
 #include <vector>
 #ifdef _OPENMP
@@ -551,6 +552,129 @@ struct Sphere : Intersectable {
   AABB bbox() const override { V3 rv(r, r, r); return AABB(c - rv, c + rv); }
 };
 
+/* ------------------------------------------------------------------ CSG --
+ * IntersectionParameter (src/csgobject.h:32-43), the leaves' interval lists
+ * (Sphere::getCSGIntersection, src/sphere.cpp:29-56; AxisAlignedBox::
+ * getCSGIntersection, src/axisalignedbox.cpp:30-73), CSGOperation (src/
+ * csgoperation.cpp:27-97) and CSGObject::intersect (src/csgobject.cpp:25-44),
+ * with std::list as in the renderer. */
+struct CsgParam {
+  float t = 0;
+  V3 normal;
+  float tu = 0, tv = 0;
+  const Material* mat = nullptr;
+};
+
+struct CsgNode {
+  virtual ~CsgNode() {}
+  virtual std::list<CsgParam> params(const Ray& ray) const = 0;
+  virtual AABB box() const = 0;
+};
+
+struct CsgSphere : CsgNode {
+  V3 c; float r; const Material* mat;
+  CsgSphere(V3 cc, float rr, const Material* m) : c(cc), r(rr), mat(m) {}
+  std::list<CsgParam> params(const Ray& ray) const override {
+    std::list<CsgParam> out;
+    V3 diff = ray.o - c;
+    float a = ray.d.lengthSquared();
+    float b = 2 * dot(ray.d, diff);
+    float cc = diff.lengthSquared() - r * r;
+    float disc = b * b - 4 * a * cc;
+    if (disc >= 0) {
+      float rd = std::sqrt(disc);
+      CsgParam p;
+      p.mat = mat;
+      for (int k = 0; k < 2; ++k) {
+        p.t = (k == 0 ? (-b - rd) : (-b + rd)) / (2 * a);
+        p.normal = ray.evaluate(p.t).affine() - c;
+        p.tu = float(std::acos(double(p.normal.z / r)) / M_PI);
+        p.tv = float(std::atan2(double(p.normal.x), double(p.normal.y)) / M_PI / 2 + 0.5);
+        out.push_back(p);
+      }
+    }
+    return out;
+  }
+  AABB box() const override { V3 rv(r, r, r); return AABB(c - rv, c + rv); }
+};
+
+struct CsgBox : CsgNode {
+  V3 lo, hi; const Material* mat;
+  CsgBox(V3 a, V3 b, const Material* m) : lo(a), hi(b), mat(m) {}
+  std::list<CsgParam> params(const Ray& ray) const override {
+    std::list<CsgParam> out;
+    CsgParam p;
+    p.mat = mat;
+    float tmin = -kInf, tmax = kInf;
+    for (int i = 0; i < 3; ++i) {
+      float a = 1 / ray.d[i];
+      V3 n;
+      float tn, tx;
+      if (a >= 0) { tn = (lo - ray.o)[i]; tx = (hi - ray.o)[i]; n.set(i, -1); }
+      else { tn = (hi - ray.o)[i]; tx = (lo - ray.o)[i]; n.set(i, 1); }
+      tn *= a;
+      tx *= a;
+      if (tn > tmin) { tmin = tn; p.normal = n; }
+      if (tx < tmax) tmax = tx;
+      if (tmin > tmax) return out;
+    }
+    p.t = tmin;
+    out.push_back(p);
+    p.t = tmax;  /* the exit keeps the entry face's normal */
+    out.push_back(p);
+    return out;
+  }
+  AABB box() const override { return AABB(lo, hi); }
+};
+
+struct CsgOp : CsgNode {
+  int op;  /* gbrt_csg_op */
+  std::unique_ptr<CsgNode> left, right;
+  bool inside(bool l, bool r) const {
+    switch (op) {
+      case GBRT_CSG_ISECT: return l && r;
+      case GBRT_CSG_UNION: return l || r;
+      case GBRT_CSG_DIFF: return l && !r;
+      default: return l != r;
+    }
+  }
+  std::list<CsgParam> params(const Ray& ray) const override {
+    bool li = false, ri = false;
+    std::list<CsgParam> L = left->params(ray), R = right->params(ray), out;
+    auto i = L.begin();
+    auto j = R.begin();
+    while (i != L.end() || j != R.end()) {
+      bool takeL = i != L.end() && (j == R.end() || i->t <= j->t);
+      bool was = inside(li, ri);
+      bool& cur = takeL ? li : ri;
+      cur = !cur;
+      if (was != inside(li, ri)) out.push_back(takeL ? *i : *j);
+      if (takeL) ++i; else ++j;
+    }
+    return out;
+  }
+  AABB box() const override { AABB b = left->box(); AABB c = right->box(); b.includeOther(c); return b; }
+};
+
+struct CsgObject : Intersectable {
+  std::unique_ptr<CsgNode> root;
+  Hit intersect(const Ray& ray) const override {
+    std::list<CsgParam> ps = root->params(ray);
+    if (ps.empty() || ray.from > ps.back().t) return Hit();
+    for (auto& p : ps) {
+      if (p.t >= ray.from) {
+        if (p.t > ray.to) return Hit();
+        Hit h(p.t, ray, p.mat, p.normal, prim);
+        h.tu = p.tu;
+        h.tv = p.tv;
+        return h;
+      }
+    }
+    return Hit();
+  }
+  AABB bbox() const override { return root->box(); }
+};
+
 /* Plane, src/plane.cpp:27-46. */
 struct Plane : Intersectable {
   V4 P; const Material* mat;
@@ -893,6 +1017,23 @@ static Scene* buildScene(const gbrt_scene_desc* d, bool useBVH) {
     pl->prim = pid;
     s->pool.emplace_back(pl);
     top.push_back(pl);
+  }
+  std::function<CsgNode*(int)> csgBuild = [&](int i) -> CsgNode* {
+    const gbrt_csg_node& nd = d->csg_nodes[i];
+    if (nd.op == GBRT_CSG_SPHERE) return new CsgSphere(vec3(nd.a), nd.b[0], mat(nd.material));
+    if (nd.op == GBRT_CSG_BOX) return new CsgBox(vec3(nd.a), vec3(nd.b), mat(nd.material));
+    auto* op = new CsgOp();
+    op->op = nd.op;
+    op->left.reset(csgBuild(nd.left));
+    op->right.reset(csgBuild(nd.right));
+    return op;
+  };
+  for (int i = 0; i < d->n_csg; ++i, ++pid) {
+    auto* o = new CsgObject();
+    o->root.reset(csgBuild(d->csg_roots[i]));
+    o->prim = pid;
+    s->pool.emplace_back(o);
+    top.push_back(o);
   }
   s->nPrims = pid;
   if (useBVH && !top.empty()) {

@@ -33,6 +33,7 @@ struct V3 {
   V3() = default;
   V3(float a, float b, float c) : x(a), y(b), z(c) {}
   float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+  void set(int i, float v) { (i == 0 ? x : (i == 1 ? y : z)) = v; }
   float& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
   bool isNull() const { return x == 0.f && y == 0.f && z == 0.f; }
   float lengthSquared() const { return x * x + y * y + z * z; }

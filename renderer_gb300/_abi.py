@@ -38,6 +38,11 @@ class EnvMap(C.Structure):
                 ("texels", C.POINTER(C.c_float))]
 
 
+class CsgNode(C.Structure):
+    _fields_ = [("op", C.c_int32), ("left", C.c_int32), ("right", C.c_int32), ("a", F3), ("b", F3),
+                ("material", C.c_int32)]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("materials", C.POINTER(Material)), ("n_materials", C.c_int32),
                 ("tri_pos", C.POINTER(C.c_float)), ("tri_nrm", C.POINTER(C.c_float)),
@@ -48,7 +53,9 @@ class SceneDesc(C.Structure):
                 ("planes", C.POINTER(Plane)), ("n_planes", C.c_int32),
                 ("lights", C.POINTER(Light)), ("n_lights", C.c_int32),
                 ("env", C.POINTER(EnvMap)), ("flags", C.c_int32),
-                ("textures", C.POINTER(Texture)), ("n_textures", C.c_int32)]
+                ("textures", C.POINTER(Texture)), ("n_textures", C.c_int32),
+                ("csg_nodes", C.POINTER(CsgNode)), ("n_csg_nodes", C.c_int32),
+                ("csg_roots", C.POINTER(C.c_int32)), ("n_csg", C.c_int32)]
 
 
 class Camera(C.Structure):
@@ -115,6 +122,8 @@ SCENE_WATERTIGHT, SCENE_GPU_BUILD = 1, 2
 RENDER_TIME_KERNELS, RENDER_COUNT_TRAVERSAL = 1, 2
 NOALLOC_MAX_BATCH = 65536
 GUIDE_PARAMS, GUIDE_INPUT, GUIDE_OUTPUT, GUIDE_SAMPLE = 24064, 9, 40, 13
+CSG_SPHERE, CSG_BOX, CSG_ISECT, CSG_UNION, CSG_DIFF, CSG_XOR = range(6)
+CSG_MAX_LEAVES = 8
 GUIDE_EQUAL_WEIGHTS, GUIDE_PIXEL_RELATIVE = 1, 2
 
 P = C.c_void_p

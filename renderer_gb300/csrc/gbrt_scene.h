@@ -8,6 +8,7 @@
 //              triangle      (p1, kind) (p2, -) (p3, prim)
 //              sphere        (centre, kind) (radius, 0, 0, -) (0, 0, 0, prim)
 //              parallelogram (origin, kind) (u, -) (v, prim)
+//              CSG object    (box lo, kind) (box hi, program start) (program length, 0, 0, prim)
 //            kind and prim are int bit patterns in the w lanes.
 //   meta   : n_recs x 16 B    (prim id, material, normal index or -1, light)
 //   tri_nrm: per smooth triangle 3 normals (9 floats, padded to 12)
@@ -24,7 +25,7 @@
 
 namespace gbrt {
 
-enum RecKind : int32_t { kRecTriangle = 0, kRecSphere = 1, kRecParallelogram = 2 };
+enum RecKind : int32_t { kRecTriangle = 0, kRecSphere = 1, kRecParallelogram = 2, kRecCSG = 3 };
 
 // Material kinds on the device (gbrt_material_type plus the two emitters that
 // are their own material in the renderer: AreaLight and EnvironmentMap).
@@ -83,6 +84,10 @@ struct DeviceScene {
   const int4* tex_info;
   const float* tri_uv;
   int32_t n_textures, tri_pid0;
+  // CSG: nodes as three float4, (a, op), (b, material), (left, right, -, -)
+  // (gbrt_csg_node), and the objects' postfix programs of node indices.
+  const float4* csg_nodes;
+  const int32_t* csg_prog;
 };
 
 // Internal hit encoding of the traversal kernels.

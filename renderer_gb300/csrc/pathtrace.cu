@@ -191,7 +191,7 @@ __device__ __forceinline__ void warp_add_counters(TraceCounters c, unsigned long
 // counts[0] and zeroes work[0]; k_extend on queue cur zeroes, before shade and
 // shadow run, counts[cur^1] (next extension queue), counts[2] (shadow queue),
 // work[cur^1] (next extend) and work[2] (this iteration's shadow pass).
-template <bool COUNT, bool WT, int STACK>
+template <bool COUNT, bool WT, int STACK, bool CSG>
 __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState st, int cur) {
   const int n = st.counts[cur];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -214,13 +214,13 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState s
     if (i >= n) continue;
     TRay r = make_tray(rays[2 * i], rays[2 * i + 1]);
     RawHit h;
-    h.rec = trace_ray<false, COUNT, WT, STACK>(S, r, -1, h.t, h.u, h.v, st.err, &cnt);
+    h.rec = trace_ray<false, COUNT, WT, STACK, CSG>(S, r, -1, h.t, h.u, h.v, st.err, &cnt);
     st.hits[i] = h;
   }
   if (COUNT) warp_add_counters(cnt, &st.tally[3], &st.tally[4]);
 }
 
-template <bool COUNT, bool WT, int STACK>
+template <bool COUNT, bool WT, int STACK, bool CSG>
 __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState st) {
   const int n = st.counts[2];
   if (blockIdx.x == 0 && threadIdx.x == 0) st.tally[1] += (unsigned long long)n;
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState s
     float4 c = st.sh_c[i];
     TRay r = make_tray(st.sh_ray[2 * i], st.sh_ray[2 * i + 1]);
     float t, u, v;
-    int32_t rec = trace_ray<true, COUNT, WT, STACK>(S, r, __float_as_int(c.w), t, u, v, st.err, &cnt);
+    int32_t rec = trace_ray<true, COUNT, WT, STACK, CSG>(S, r, __float_as_int(c.w), t, u, v, st.err, &cnt);
     if (rec == -1) {
       float4* L = st.L + st.sh_slot[i];
       atomicAdd(&L->x, c.x);
@@ -281,6 +281,7 @@ __device__ __forceinline__ void load_pending(const PTState& st, int slot, Vertex
 // Next-event estimation at a stored vertex: UniDiPathTracingIntegrator lines
 // 83-99 with Light::getIntensity for light lightIndex[k]. A non-zero
 // contribution goes to the shadow queue with its shadow ray.
+template <bool EXT>
 __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, const PTState& st, int slot,
                                     unsigned long long key, const Vertex& vx, V3f alpha, int k) {
   if (S.n_lights <= 0 || vx.mat < 0) return;
@@ -320,7 +321,7 @@ __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, con
     return;  // BlackLight
   }
   if (is_zero(Le)) return;
-  V3f f = brdf_eval(S, vx, dir);
+  V3f f = brdf_eval<EXT>(S, vx, dir);
   float inCos = dot(-normalize(dir), vx.n);
   float outCos = dot(-normalize(vx.d), vx.n);
   if (signum(inCos) != signum(outCos)) return;
@@ -338,6 +339,7 @@ __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, con
 // Renderer::createPath (src/renderer.cpp:73-104) for one iteration, with the
 // stored-vertex bookkeeping of UniDiPathTracingIntegrator::integrate(path)
 // done in streaming form (see the file comment).
+template <bool EXT>
 __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTState st, int cur) {
   const int n = st.counts[cur];
   const int nxt = cur ^ 1;
@@ -356,7 +358,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
       if (pend) {
         Vertex pv; V3f pa; int k;
         load_pending(st, slot, pv, pa, k);
-        nee(S, P, st, slot, key, pv, pa, k);
+        nee<EXT>(S, P, st, slot, key, pv, pa, k);
         st.ctl[slot] = make_int4(i, plen, nst, 0);
       }
       continue;
@@ -380,7 +382,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
         const int kind = __float_as_int(a.w);
         vx.mat = m.y;
         light = m.w;
-        if (S.tri_uv) hit_texcoords(S, h.rec, h.u, h.v, vx.p, vx.tu, vx.tv);
+        if (EXT && S.tri_uv) hit_texcoords(S, h.rec, h.u, h.v, vx.p, vx.tu, vx.tv);
         if (kind == kRecTriangle) {
           if (m.z >= 0) {
             const float* nn = S.tri_nrm + 12 * int64_t(m.z);
@@ -393,6 +395,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
           }
         } else if (kind == kRecSphere) {
           vx.n = normalize(vx.p - v3(a.x, a.y, a.z));
+        } else if (EXT && kind == kRecCSG) {
+          csg_surface(S, __float_as_int(h.u), v3(ro.x, ro.y, ro.z), d, vx.p, vx.n, vx.mat, vx.tu, vx.tv);
         } else {
           vx.n = ld3(S.lights[light].nhat);
         }
@@ -415,7 +419,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
         Vertex pv; V3f pa; int k;
         load_pending(st, slot, pv, pa, k);
         V3f dir = envHit ? -vx.p : pv.p - vx.p;
-        V3f f = brdf_eval(S, pv, dir);
+        V3f f = brdf_eval<EXT>(S, pv, dir);
         float inCos = dot(-normalize(dir), pv.n);
         float outCos = dot(-normalize(pv.d), pv.n);
         if (signum(inCos) == signum(outCos)) {
@@ -431,7 +435,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
     }
     float pdf;
     V3f f;
-    const V3f out = out_direction(S, vx, stream_u(key, dim_path(i)), stream_u(key, dim_path(i) + 1), pdf, f);
+    const V3f out = out_direction<EXT>(S, vx, stream_u(key, dim_path(i)), stream_u(key, dim_path(i) + 1), pdf, f);
     if (mat_specular(S.materials, vx.mat)) {
       // Specular vertices are not stored (lines 87-91).
       if (i == plen - 1 && plen < P.D) plen++;
@@ -441,7 +445,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
       } else if (pend) {
         Vertex pv; V3f pa; int k;
         load_pending(st, slot, pv, pa, k);
-        nee(S, P, st, slot, key, pv, pa, k);
+        nee<EXT>(S, P, st, slot, key, pv, pa, k);
         pend = false;
       }
       st.ctl[slot] = make_int4(i, plen, nst, pend ? 1 : 0);
@@ -452,7 +456,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
     if (pend) {
       Vertex pv; V3f pa; int k;
       load_pending(st, slot, pv, pa, k);
-      nee(S, P, st, slot, key, pv, pa, k);
+      nee<EXT>(S, P, st, slot, key, pv, pa, k);
     }
     const float4 a4 = st.alpha[slot];
     const V3f alpha = v3(a4.x, a4.y, a4.z);
@@ -471,7 +475,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
     }
     if (ends) {
       // This vertex is the last stored one: next-event estimation now.
-      nee(S, P, st, slot, key, vx, alpha, k);
+      nee<EXT>(S, P, st, slot, key, vx, alpha, k);
       st.ctl[slot] = make_int4(i, plen, nst, 0);
     } else {
       st.pv_p[slot] = make_float4(vx.p.x, vx.p.y, vx.p.z, __int_as_float(vx.mat));
@@ -553,8 +557,13 @@ __device__ __forceinline__ void nee_phys(const DeviceScene& S, const PTState& st
   st.sh_slot[e] = slot;
 }
 
-// Normal (unflipped) and material of a surface hit that is not an emitter.
-__device__ __forceinline__ void surface_normal(const DeviceScene& S, const RawHit& h, V3f x, V3f& nrm, int& mat) {
+// Normal (unflipped), material and texture coordinates of a surface hit that
+// is not an emitter; o, d: the ray.
+template <bool EXT>
+__device__ __forceinline__ void surface_normal(const DeviceScene& S, const RawHit& h, V3f o, V3f d, V3f x, V3f& nrm,
+                                               int& mat, float& tu, float& tv) {
+  tu = 0.f;
+  tv = 0.f;
   if (h.rec >= 0) {
     const int4 m = __ldg(&S.meta[h.rec]);
     const float4* rp = S.recs + 3 * int64_t(h.rec);
@@ -571,9 +580,13 @@ __device__ __forceinline__ void surface_normal(const DeviceScene& S, const RawHi
         V3f p1 = v3(a.x, a.y, a.z), p2 = v3(b.x, b.y, b.z), p3 = v3(cc.x, cc.y, cc.z);
         nrm = normalize(cross(p1 - p2, p1 - p3));
       }
+    } else if (EXT && kind == kRecCSG) {
+      csg_surface(S, __float_as_int(h.u), o, d, x, nrm, mat, tu, tv);
+      return;
     } else {
       nrm = normalize(x - v3(a.x, a.y, a.z));  // sphere
     }
+    if (EXT && S.tri_uv) hit_texcoords(S, h.rec, h.u, h.v, x, tu, tv);
   } else {
     const float4 pl = __ldg(&S.planes[-2 - h.rec]);
     nrm = normalize(v3(pl.x, pl.y, pl.z));
@@ -581,7 +594,7 @@ __device__ __forceinline__ void surface_normal(const DeviceScene& S, const RawHi
   }
 }
 
-template <bool GUIDED>
+template <bool GUIDED, bool EXT>
 __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P, PTState st, int cur) {
   const int n = st.counts[cur];
   const int nxt = cur ^ 1;
@@ -639,10 +652,9 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
     }
     V3f nrm;
     int mat = -1;
-    surface_normal(S, h, x, nrm, mat);
-    float tu = 0.f, tv = 0.f;
-    if (S.tri_uv) hit_texcoords(S, h.rec, h.u, h.v, x, tu, tv);
-    const PhysBsdf b = phys_bsdf(S, mat, tu, tv);
+    float tu, tv;
+    surface_normal<EXT>(S, h, v3(ro.x, ro.y, ro.z), d, x, nrm, mat, tu, tv);
+    const PhysBsdf b = phys_bsdf<EXT>(S, mat, tu, tv);
     if (b.kind <= 0) continue;
     const unsigned long long key = stream_key(P.seed, P.g0 + (unsigned long long)slot);
     const unsigned base = dim_phys(i);
@@ -714,8 +726,9 @@ __global__ void __launch_bounds__(256) k_guide_prep(DeviceScene S, PTState st, i
       const V3f x = v3(ro.x, ro.y, ro.z) + h.t * d;
       V3f nrm;
       int mat = -1;
-      surface_normal(S, h, x, nrm, mat);
-      const PhysBsdf b = phys_bsdf(S, mat, 0.f, 0.f);  // only its kind matters here
+      float tu, tv;
+      surface_normal<true>(S, h, v3(ro.x, ro.y, ro.z), d, x, nrm, mat, tu, tv);
+      const PhysBsdf b = phys_bsdf<true>(S, mat, tu, tv);
       if (b.kind >= 1 && b.kind <= 3) {
         const V3f wo = -normalize(d);
         if (dot(nrm, wo) < 0.f) nrm = -nrm;
@@ -835,7 +848,7 @@ __global__ void __launch_bounds__(256) k_accumulate_warp(PTParams P, PTState st,
 static void launch_accumulate(const PTParams& P, const PTState& st, double* sum, double* sumsq, cudaStream_t stream) {
   const unsigned long long p0 = P.g0 / unsigned(P.spp), p1 = (P.g0 + unsigned(P.nb) - 1) / unsigned(P.spp);
   const unsigned long long np = p1 - p0 + 1;
-  if (P.spp >= 64)
+  if (P.spp >= 256)
     k_accumulate_warp<<<unsigned((np * 32 + 255) / 256), 256, 0, stream>>>(P, st, sum, sumsq);
   else
     k_accumulate<<<unsigned((np + 255) / 256), 256, 0, stream>>>(P, st, sum, sumsq);
@@ -885,15 +898,31 @@ struct TraceKernels {
   void (*ext)(DeviceScene, PTState, int);
   void (*sh)(DeviceScene, PTState);
 };
-template <bool C, bool W>
+template <bool C, bool W, bool G>
 static TraceKernels pick_stack(bool shortStack) {
-  if (shortStack) return {k_extend<C, W, kShortStack>, k_shadow<C, W, kShortStack>};
-  return {k_extend<C, W, kStackSize>, k_shadow<C, W, kStackSize>};
+  if (shortStack) return {k_extend<C, W, kShortStack, G>, k_shadow<C, W, kShortStack, G>};
+  return {k_extend<C, W, kStackSize, G>, k_shadow<C, W, kStackSize, G>};
 }
+template <bool G>
+static TraceKernels pick_flags(bool count, bool wt, bool shortStack) {
+  if (count) return wt ? pick_stack<true, true, G>(shortStack) : pick_stack<true, false, G>(shortStack);
+  return wt ? pick_stack<false, true, G>(shortStack) : pick_stack<false, false, G>(shortStack);
+}
+// Traversal counters, watertight triangles, short stack when the tree is
+// shallow enough, the CSG leaf test only for scenes with CSG objects.
 static TraceKernels pick_kernels(const gbrt_scene* s, bool count) {
   const bool shortStack = stack_need(s->max_depth4) <= kShortStack;
-  if (count) return s->watertight ? pick_stack<true, true>(shortStack) : pick_stack<true, false>(shortStack);
-  return s->watertight ? pick_stack<false, true>(shortStack) : pick_stack<false, false>(shortStack);
+  if (s->view.csg_prog) return pick_flags<true>(count, s->watertight, shortStack);
+  return pick_flags<false>(count, s->watertight, shortStack);
+}
+
+// The shade kernel: estimator, guiding, and the texture / CSG code only for
+// scenes that have textures or CSG objects.
+static void (*pick_shade(const gbrt_scene* s, bool physical, bool guided))(DeviceScene, PTParams, PTState, int) {
+  const bool ext = s->view.tri_uv != nullptr || s->view.csg_prog != nullptr;
+  if (!physical) return ext ? k_shade<true> : k_shade<false>;
+  if (guided) return ext ? k_shade_phys<true, true> : k_shade_phys<true, false>;
+  return ext ? k_shade_phys<false, true> : k_shade_phys<false, false>;
 }
 
 static void init_params(PTParams& P, const gbrt_camera& cam, const gbrt_render_params& prm, unsigned long long total) {
@@ -984,7 +1013,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kSh, kTraceBlock, 0);
   const int shadowGrid = std::max(1, per) * ctx->num_sms;
   const int shadeGrid = ctx->num_sms * 8;
-  auto kShade = P.physical ? k_shade_phys<false> : k_shade;
+  auto kShade = pick_shade(s, P.physical != 0, false);
   cudaEvent_t ev0, ev1;
   cudaEventCreate(&ev0);
   cudaEventCreate(&ev1);
@@ -1199,7 +1228,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kSh, kTraceBlock, 0);
   const int shadowGrid = std::max(1, per) * ctx->num_sms;
   const int shadeGrid = ctx->num_sms * 8;
-  auto kShade = P.physical ? k_shade_phys<false> : k_shade;
+  auto kShade = pick_shade(s, P.physical != 0, false);
   auto t0 = std::chrono::steady_clock::now();
   unsigned long long launches = 0;
   for (unsigned long long g0 = 0; g0 < total; g0 += (unsigned long long)B) {
@@ -1420,7 +1449,7 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     P.inv_samples = 1.0 / (double(spp) * (pass + 1));
     A(cudaMemsetAsync(d_pass, 0, n3 * sizeof(double), stream));
     if (record) A(cudaMemsetAsync(st.tcount, 0, sizeof(int), stream));
-    auto kShade = (P.guided || P.record) ? k_shade_phys<true> : k_shade_phys<false>;
+    auto kShade = pick_shade(s, true, P.guided || P.record);
     for (unsigned long long g0 = 0; g0 < total && e == cudaSuccess; g0 += (unsigned long long)B) {
       P.g0 = g0;
       P.nb = int(std::min<unsigned long long>((unsigned long long)B, total - g0));

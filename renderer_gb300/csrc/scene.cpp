@@ -205,6 +205,8 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   for (int i = 0; i < d->n_textures; ++i)
     if (d->textures[i].width <= 0 || d->textures[i].height <= 0 || !d->textures[i].texels)
       return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: texture without an image");
+  if (d->n_csg < 0 || d->n_csg_nodes < 0 || (d->n_csg && (!d->csg_roots || !d->csg_nodes)))
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: bad CSG tables");
   bool anyTexture = false;
   for (int i = 0; i < d->n_materials; ++i)
     if (d->materials[i].type == GBRT_MAT_TEXTURE) {
@@ -349,6 +351,53 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     planes[i] = make_float4(pl.plane[0], pl.plane[1], pl.plane[2], pl.plane[3]);
     planeMeta[i] = make_int2(pid, matIndex(pl.material));
   }
+  // CSG objects: each a postfix program over the node table and one record
+  // whose box is the union of its leaves' boxes (CSGOperation::
+  // createBoundingBox, src/csgoperation.cpp:66-76).
+  std::vector<int32_t> csgProg;
+  for (int i = 0; i < d->n_csg; ++i, ++pid) {
+    const int32_t start = int32_t(csgProg.size());
+    int leaves = 0, visited = 0;
+    Box box{{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}};
+    bool ok = true;
+    // post-order walk with an explicit stack; (node, children pushed)
+    std::vector<std::pair<int32_t, bool>> stk{{d->csg_roots[i], false}};
+    while (!stk.empty() && ok) {
+      auto [nidx, expanded] = stk.back();
+      stk.pop_back();
+      if (nidx < 0 || nidx >= d->n_csg_nodes || ++visited > 2 * GBRT_CSG_MAX_LEAVES) { ok = false; break; }
+      const gbrt_csg_node& nd = d->csg_nodes[nidx];
+      if (nd.op == GBRT_CSG_SPHERE || nd.op == GBRT_CSG_BOX) {
+        if (!finite3(nd.a) || !finite3(nd.b) || ++leaves > GBRT_CSG_MAX_LEAVES) { ok = false; break; }
+        for (int k = 0; k < 3; ++k) {
+          float lo = nd.op == GBRT_CSG_BOX ? nd.a[k] : nd.a[k] - std::fabs(nd.b[0]);
+          float hi = nd.op == GBRT_CSG_BOX ? nd.b[k] : nd.a[k] + std::fabs(nd.b[0]);
+          box.lo[k] = std::min(box.lo[k], lo);
+          box.hi[k] = std::max(box.hi[k], hi);
+        }
+        csgProg.push_back(nidx);
+      } else if (nd.op >= GBRT_CSG_ISECT && nd.op <= GBRT_CSG_XOR) {
+        if (expanded) {
+          csgProg.push_back(nidx);
+        } else {
+          stk.push_back({nidx, true});
+          stk.push_back({nd.right, false});
+          stk.push_back({nd.left, false});
+        }
+      } else {
+        ok = false;
+      }
+    }
+    if (!ok)
+      return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: CSG object with a bad node or more than 8 leaves");
+    Rec r{};
+    r.v[0] = box.lo[0]; r.v[1] = box.lo[1]; r.v[2] = box.lo[2]; setW(r.v[3], kRecCSG);
+    r.v[4] = box.hi[0]; r.v[5] = box.hi[1]; r.v[6] = box.hi[2]; setW(r.v[7], start);
+    setW(r.v[8], int32_t(csgProg.size()) - start); setW(r.v[11], pid);
+    r.meta[0] = pid; r.meta[1] = -1; r.meta[2] = -1; r.meta[3] = -1;
+    recs.push_back(r);
+    boxes.push_back(box);
+  }
 
   float sb[6] = {0, 0, 0, 0, 0, 0};
   for (size_t i = 0; i < boxes.size(); ++i)
@@ -473,6 +522,24 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     v.n_textures = d->n_textures;
   }
   v.tri_pid0 = d->n_lights;
+  if (d->n_csg > 0) {
+    std::vector<float4> nodes4(size_t(d->n_csg_nodes) * 3);
+    for (int i = 0; i < d->n_csg_nodes; ++i) {
+      const gbrt_csg_node& nd = d->csg_nodes[i];
+      int32_t op = nd.op, mat = nd.op <= GBRT_CSG_BOX ? matIndex(nd.material) : -1;
+      float fo, fm, fl, fr;
+      std::memcpy(&fo, &op, 4); std::memcpy(&fm, &mat, 4);
+      std::memcpy(&fl, &nd.left, 4); std::memcpy(&fr, &nd.right, 4);
+      nodes4[3 * i] = make_float4(nd.a[0], nd.a[1], nd.a[2], fo);
+      nodes4[3 * i + 1] = make_float4(nd.b[0], nd.b[1], nd.b[2], fm);
+      nodes4[3 * i + 2] = make_float4(fl, fr, 0.f, 0.f);
+    }
+    if ((st = upload(s, nodes4, &v.csg_nodes)) != GBRT_OK || (st = upload(s, csgProg, &v.csg_prog)) != GBRT_OK) {
+      free_scene(s);
+      delete s;
+      return st;
+    }
+  }
   if (envLight >= 0) {
     const gbrt_env_map* e = d->env;
     envTex.assign(e->texels, e->texels + size_t(e->width) * e->height * 3);

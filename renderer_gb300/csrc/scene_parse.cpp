@@ -15,8 +15,9 @@
 // Differences, for the GPU layout: instances are flattened by transforming
 // their primitives (a sphere needs a similarity transform); a pre-built
 // b(left, right, box) node contributes its children (the BVH is rebuilt);
-// box(min, max, m) becomes six quads; CSG operations are not part of the GPU
-// path. Texture images are read from PPM (P6/P3), PFM and Radiance files
+// box(min, max, m) and isect / union / diff / xor trees of spheres and boxes
+// become CSG objects (a box under an instance must stay axis-aligned).
+// Texture images are read from PPM (P6/P3), PFM and Radiance files
 // (formats the repository decodes itself; PNG/JPEG need an image codec
 // library that is not part of this build) and scaled by 1/255 like the
 // renderer's cv::imread + convertTo; an unreadable image gives DarkMatter.
@@ -759,6 +760,8 @@ struct gbrt_parsed_scene {
   std::vector<std::vector<float>> texels;  // per texture
   std::vector<gbrt_texture> textures;
   std::map<std::string, int> texture_ids;  // path -> texture
+  std::vector<gbrt_csg_node> csg_nodes;
+  std::vector<int32_t> csg_roots;
   std::vector<int32_t> tri_mat;
   std::vector<gbrt_quad> quads;
   std::vector<gbrt_sphere> spheres;
@@ -942,32 +945,19 @@ struct Builder {
         gbrt_sphere s{};
         V3 c = n->p[0];
         float r = n->radius;
-        if (xf) {
-          V3 cx = xf->point(c);
-          V3 ax = xf->dir({1, 0, 0}), ay = xf->dir({0, 1, 0}), az = xf->dir({0, 0, 1});
-          auto L = [](V3 v) { return std::sqrt(double(v.x) * v.x + double(v.y) * v.y + double(v.z) * v.z); };
-          double sx = L(ax), sy = L(ay), sz = L(az);
-          if (std::fabs(sx - sy) > 1e-5 * sx || std::fabs(sx - sz) > 1e-5 * sx)
-            throw ParseError(GBRT_ERR_UNSUPPORTED, "instance of a sphere with a non-uniform scale");
-          c = cx;
-          r = float(r * sx);
-        }
+        sphereXf(c, r, xf);
         s.center[0] = c.x; s.center[1] = c.y; s.center[2] = c.z;
         s.radius = r;
         s.material = resolveMat(n->mat);
         ps.spheres.push_back(s);
         break;
       }
-      case Node::BOX: {
-        V3 lo = n->p[0], hi = n->p[1];
-        int m = resolveMat(n->mat);
-        V3 c[8];
-        for (int k = 0; k < 8; ++k) c[k] = {(k & 1) ? hi.x : lo.x, (k & 2) ? hi.y : lo.y, (k & 4) ? hi.z : lo.z};
-        const int f[6][4] = {{0, 2, 3, 1}, {4, 5, 7, 6}, {0, 1, 5, 4}, {2, 6, 7, 3}, {0, 4, 6, 2}, {1, 3, 7, 5}};
-        for (auto& q : f) {
-          V3 p[4] = {c[q[0]], c[q[1]], c[q[2]], c[q[3]]};
-          addQuad(p, m, xf);
-        }
+      case Node::BOX:  // an AxisAlignedBox is a CSG object of its own
+      case Node::CSG: {
+        int leaves = 0;
+        ps.csg_roots.push_back(csgNode(n, xf, leaves));
+        if (leaves > GBRT_CSG_MAX_LEAVES)
+          throw ParseError(GBRT_ERR_UNSUPPORTED, "CSG object with more than 8 spheres and boxes");
         break;
       }
       case Node::INSTANCE: {
@@ -1003,9 +993,66 @@ struct Builder {
         }
         break;
       }
-      case Node::CSG:
-        throw ParseError(GBRT_ERR_UNSUPPORTED, "CSG operation '" + n->op + "' is not part of the GPU path");
     }
+  }
+
+  // Instances move a sphere by a similarity transform (centre, radius).
+  static void sphereXf(V3& c, float& r, const Mat4* xf) {
+    if (!xf) return;
+    V3 cx = xf->point(c);
+    V3 ax = xf->dir({1, 0, 0}), ay = xf->dir({0, 1, 0}), az = xf->dir({0, 0, 1});
+    auto L = [](V3 v) { return std::sqrt(double(v.x) * v.x + double(v.y) * v.y + double(v.z) * v.z); };
+    double sx = L(ax), sy = L(ay), sz = L(az);
+    if (std::fabs(sx - sy) > 1e-5 * sx || std::fabs(sx - sz) > 1e-5 * sx)
+      throw ParseError(GBRT_ERR_UNSUPPORTED, "instance of a sphere with a non-uniform scale");
+    c = cx;
+    r = float(r * sx);
+  }
+
+  // A CSG tree into gbrt_csg_node entries; returns the root's index.
+  int32_t csgNode(const NodeP& n, const Mat4* xf, int& leaves) {
+    gbrt_csg_node g{};
+    g.left = g.right = -1;
+    if (n->kind == Node::SPHERE) {
+      V3 c = n->p[0];
+      float r = n->radius;
+      sphereXf(c, r, xf);
+      g.op = GBRT_CSG_SPHERE;
+      g.a[0] = c.x; g.a[1] = c.y; g.a[2] = c.z;
+      g.b[0] = r;
+      g.material = resolveMat(n->mat);
+      ++leaves;
+    } else if (n->kind == Node::BOX) {
+      V3 lo = n->p[0], hi = n->p[1];
+      if (xf) {
+        // axis-aligned only: no rotation or shear
+        for (int r = 0; r < 3; ++r)
+          for (int c = 0; c < 3; ++c)
+            if (r != c && xf->m[r][c] != 0.f)
+              throw ParseError(GBRT_ERR_UNSUPPORTED, "instance of a box that is not axis-aligned");
+        V3 a = xf->point(lo), b = xf->point(hi);
+        lo = {std::min(a.x, b.x), std::min(a.y, b.y), std::min(a.z, b.z)};
+        hi = {std::max(a.x, b.x), std::max(a.y, b.y), std::max(a.z, b.z)};
+      }
+      g.op = GBRT_CSG_BOX;
+      g.a[0] = lo.x; g.a[1] = lo.y; g.a[2] = lo.z;
+      g.b[0] = hi.x; g.b[1] = hi.y; g.b[2] = hi.z;
+      g.material = resolveMat(n->mat);
+      ++leaves;
+    } else if (n->kind == Node::CSG) {
+      g.op = n->op == "isect" ? GBRT_CSG_ISECT : n->op == "union" ? GBRT_CSG_UNION
+           : n->op == "diff" ? GBRT_CSG_DIFF : GBRT_CSG_XOR;
+      g.left = csgNode(n->children[0], xf, leaves);
+      g.right = csgNode(n->children[1], xf, leaves);
+      g.material = -1;
+    } else if (n->kind == Node::INSTANCE) {
+      Mat4 M = xf ? (*xf) * n->xf : n->xf;
+      return csgNode(n->children[0], &M, leaves);
+    } else {
+      throw ParseError(GBRT_ERR_PARSE, "a CSG operand must be a sphere, a box or a CSG operation");
+    }
+    ps.csg_nodes.push_back(g);
+    return int32_t(ps.csg_nodes.size()) - 1;
   }
   static bool isNull(V3 v) { return v.x == 0 && v.y == 0 && v.z == 0; }
 
@@ -1189,6 +1236,10 @@ gbrt_status gbrt_parsed_scene_desc(const gbrt_parsed_scene* ps, gbrt_scene_desc*
   for (size_t i = 0; i < mps->textures.size(); ++i) mps->textures[i].texels = mps->texels[i].data();
   d->textures = ps->textures.empty() ? nullptr : ps->textures.data();
   d->n_textures = int32_t(ps->textures.size());
+  d->csg_nodes = ps->csg_nodes.empty() ? nullptr : ps->csg_nodes.data();
+  d->n_csg_nodes = int32_t(ps->csg_nodes.size());
+  d->csg_roots = ps->csg_roots.empty() ? nullptr : ps->csg_roots.data();
+  d->n_csg = int32_t(ps->csg_roots.size());
   if (cam) *cam = ps->camera;
   if (has_camera) *has_camera = ps->has_camera ? 1 : 0;
   return GBRT_OK;

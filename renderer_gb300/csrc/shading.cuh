@@ -99,6 +99,42 @@ __device__ __forceinline__ V3f cosine_power_dir(V3f w, float sx, float sy, float
   return normalize(nd.x * u + nd.y * v + nd.z * w);
 }
 
+// ---------------------------------------------------------------- CSG -----
+// Surface of a CSG hit (leaf node index in the hit's u): the leaf's material;
+// a sphere leaf's normal x - centre and texture coordinates as a sphere's
+// (src/sphere.cpp:44-50); a box leaf's normal that of its slab entry face,
+// also for the exit boundary, and texture coordinates (0, 0)
+// (src/axisalignedbox.cpp:41-68). The slab is recomputed with the traversal's
+// roundings so that the entry face is the one the hit came from.
+__device__ __forceinline__ void csg_surface(const DeviceScene& S, int leaf, V3f o, V3f d, V3f x, V3f& n, int& mat,
+                                            float& tu, float& tv) {
+  const float4 A = __ldg(S.csg_nodes + 3 * leaf), B = __ldg(S.csg_nodes + 3 * leaf + 1);
+  mat = __float_as_int(B.w);
+  tu = 0.f;
+  tv = 0.f;
+  if (__float_as_int(A.w) == GBRT_CSG_SPHERE) {
+    const V3f nn = x - v3(A.x, A.y, A.z);
+    n = normalize(nn);
+    tu = acosf(nn.z / B.x) * kInvPi;
+    tv = atan2f(nn.x, nn.y) * (0.5f * kInvPi) + 0.5f;
+    return;
+  }
+  const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+  const float lo[3] = {A.x, A.y, A.z}, hi[3] = {B.x, B.y, B.z};
+  float tmin = -CUDART_INF_F;
+  float nr[3] = {0.f, 0.f, 0.f};
+  for (int k = 0; k < 3; ++k) {
+    const float inv = __fdiv_rn(1.f, dd[k]);
+    const float tn = __fmul_rn(inv >= 0.f ? __fsub_rn(lo[k], oo[k]) : __fsub_rn(hi[k], oo[k]), inv);
+    if (tn > tmin) {
+      tmin = tn;
+      nr[0] = nr[1] = nr[2] = 0.f;
+      nr[k] = inv >= 0.f ? -1.f : 1.f;
+    }
+  }
+  n = v3(nr[0], nr[1], nr[2]);
+}
+
 // --------------------------------------------------------- Materials -----
 struct Vertex {
   V3f p;     // hit point
@@ -109,6 +145,8 @@ struct Vertex {
 };
 
 // ----------------------------------------------------------- Textures -----
+// (The shading kernels take texture and CSG code only in their EXT
+// instantiation, for scenes that have either: it costs registers.)
 // Texture coordinates of a hit, HitRecord::getTexCoords: a triangle's
 // (1 - u - v) t1 + u t2 + v t3 (src/triangle.cpp:54) in the renderer's
 // operation order; a quad's halves carry the Triangle constructor's default
@@ -184,6 +222,7 @@ __device__ __forceinline__ float blinn_G(V3f wi, V3f wo, V3f n) {
 
 // Material::brdf(hit, direction): direction points from the light towards the
 // surface (the renderer's convention).
+template <bool EXT>
 __device__ __forceinline__ V3f brdf_eval(const DeviceScene& S, const Vertex& h, V3f dir) {
   if (h.mat < 0) return v3(0.f, 0.f, 0.f);
   const DevMaterial& m = S.materials[h.mat];
@@ -191,7 +230,8 @@ __device__ __forceinline__ V3f brdf_eval(const DeviceScene& S, const Vertex& h, 
     case kMatDiffuse:
       return v3(m.kd[0] * kInvPi, m.kd[1] * kInvPi, m.kd[2] * kInvPi);
     case kMatTexture:
-      return kInvPi * texture_albedo(S, m, h.tu, h.tv);
+      if (EXT) return kInvPi * texture_albedo(S, m, h.tu, h.tv);
+      return v3(0.f, 0.f, 0.f);
     case kMatPhong: {
       V3f s = phong_spec(m, h, dir);
       return v3(m.kd[0] * kInvPi + s.x, m.kd[1] * kInvPi + s.y, m.kd[2] * kInvPi + s.z);
@@ -219,6 +259,7 @@ __device__ __forceinline__ bool mat_specular(const DevMaterial* mats, int mat) {
 }
 
 // Material::outDirection(hit, sample, pdf, brdf).
+template <bool EXT>
 __device__ __forceinline__ V3f out_direction(const DeviceScene& S, const Vertex& h, float sx, float sy, float& pdf,
                                              V3f& brdf) {
   brdf = v3(0.f, 0.f, 0.f);
@@ -231,8 +272,8 @@ __device__ __forceinline__ V3f out_direction(const DeviceScene& S, const Vertex&
       V3f n = h.n;
       if (dot(n, normalize(h.d)) > 0.f) n = -n;
       V3f out = cosine_power_dir(n, sx, sy, 1.f, pdf);
-      brdf = m.type == kMatDiffuse ? v3(m.kd[0] * kInvPi, m.kd[1] * kInvPi, m.kd[2] * kInvPi)
-                                   : kInvPi * texture_albedo(S, m, h.tu, h.tv);
+      if (!EXT || m.type == kMatDiffuse) brdf = v3(m.kd[0] * kInvPi, m.kd[1] * kInvPi, m.kd[2] * kInvPi);
+      else brdf = kInvPi * texture_albedo(S, m, h.tu, h.tv);
       return out;
     }
     case kMatMirror:
@@ -262,7 +303,7 @@ __device__ __forceinline__ V3f out_direction(const DeviceScene& S, const Vertex&
       if (dot(wo, wh) < 0.f) { pdf = 0.f; return v3(0.f, 0.f, 0.f); }
       V3f out = -reflect(wo, wh);
       pdf /= 4.f * fmaxf(dot(wo, wh), 0.0001f);
-      brdf = brdf_eval(S, h, out);
+      brdf = brdf_eval<EXT>(S, h, out);
       return out;
     }
     case kMatTransparent: {
@@ -328,6 +369,7 @@ struct PhysBsdf {
   float e, ior, pd;
 };
 
+template <bool EXT>
 __device__ __forceinline__ PhysBsdf phys_bsdf(const DeviceScene& S, int mat, float tu, float tv) {
   PhysBsdf b;
   b.kind = 0; b.e = 0.f; b.ior = 1.f; b.pd = 1.f;
@@ -337,7 +379,10 @@ __device__ __forceinline__ PhysBsdf phys_bsdf(const DeviceScene& S, int mat, flo
   b.kd = ld3(m.kd); b.ks = ld3(m.ks); b.e = m.exponent; b.ior = m.ior;
   switch (m.type) {
     case kMatDiffuse: b.kind = 1; break;
-    case kMatTexture: b.kind = 1; b.kd = texture_albedo(S, m, tu, tv); break;
+    case kMatTexture:
+      b.kind = 1;
+      if (EXT) b.kd = texture_albedo(S, m, tu, tv);
+      break;
     case kMatPhong: b.kind = 2; break;
     case kMatBlinn: b.kind = 3; break;
     case kMatMirror: b.kind = 4; break;

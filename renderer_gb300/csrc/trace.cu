@@ -16,7 +16,7 @@
 
 namespace gbrt {
 
-template <bool ANY, bool WT, int STACK>
+template <bool ANY, bool WT, int STACK, bool CSG>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_api(DeviceScene S, const float4* __restrict__ rays, int64_t n, const int32_t* __restrict__ ignore,
                 gbrt_hit* __restrict__ hits, uint8_t* __restrict__ occluded, unsigned long long* work, int* err) {
@@ -32,13 +32,16 @@ __global__ void __launch_bounds__(kTraceBlock)
     TRay r = make_tray(a, b);
     float t, u, v;
     int ign = (ANY && ignore) ? ignore[i] : -1;
-    int32_t rec = trace_ray<ANY, false, WT, STACK>(S, r, ign, t, u, v, err, nullptr);
+    int32_t rec = trace_ray<ANY, false, WT, STACK, CSG>(S, r, ign, t, u, v, err, nullptr);
     if (ANY) {
       occluded[i] = rec != -1 ? 1 : 0;
     } else {
       gbrt_hit h;
       h.t = t; h.u = u; h.v = v;
-      if (rec >= 0) h.prim = __ldg(&S.meta[rec]).x;
+      if (rec >= 0) {
+        h.prim = __ldg(&S.meta[rec]).x;
+        if (CSG && __float_as_int(__ldg(S.recs + 3 * int64_t(rec)).w) == kRecCSG) h.u = h.v = 0.f;
+      }
       else if (rec <= -2) h.prim = S.plane_meta[-2 - rec].x;
       else if (S.env_light >= 0 && isinf(r.tmax) && r.tmax > 0.f) {
         h.t = CUDART_INF_F; h.prim = S.env_light; h.u = 0.f; h.v = 0.f;
@@ -56,6 +59,18 @@ int trace_grid(gbrt_ctx* ctx, const void* kernel) {
   return std::max(1, per_sm) * std::max(1, ctx->num_sms);
 }
 
+// The ray-query kernel for a scene: any / closest hit, watertight triangles,
+// short stack, CSG objects.
+template <bool G>
+static decltype(&k_trace_api<false, false, kStackSize, false>) pick_api(bool any, bool wt, bool shortStack) {
+  if (any) {
+    if (shortStack) return wt ? k_trace_api<true, true, kShortStack, G> : k_trace_api<true, false, kShortStack, G>;
+    return wt ? k_trace_api<true, true, kStackSize, G> : k_trace_api<true, false, kStackSize, G>;
+  }
+  if (shortStack) return wt ? k_trace_api<false, true, kShortStack, G> : k_trace_api<false, false, kShortStack, G>;
+  return wt ? k_trace_api<false, true, kStackSize, G> : k_trace_api<false, false, kStackSize, G>;
+}
+
 static gbrt_status launch_api(gbrt_scene* s, bool any, const gbrt_ray* d_rays, const int32_t* d_ignore, int64_t n,
                               gbrt_hit* d_hits, uint8_t* d_occ, cudaStream_t st) {
   gbrt_ctx* ctx = s->ctx;
@@ -63,14 +78,10 @@ static gbrt_status launch_api(gbrt_scene* s, bool any, const gbrt_ray* d_rays, c
   const float4* rays = reinterpret_cast<const float4*>(d_rays);
   // The short stack when the tree is shallow enough for it.
   const bool shortStack = stack_need(s->max_depth4) <= kShortStack;
-  decltype(&k_trace_api<false, false, kStackSize>) k;
-  if (any) {
-    if (shortStack) k = s->watertight ? k_trace_api<true, true, kShortStack> : k_trace_api<true, false, kShortStack>;
-    else k = s->watertight ? k_trace_api<true, true, kStackSize> : k_trace_api<true, false, kStackSize>;
-  } else {
-    if (shortStack) k = s->watertight ? k_trace_api<false, true, kShortStack> : k_trace_api<false, false, kShortStack>;
-    else k = s->watertight ? k_trace_api<false, true, kStackSize> : k_trace_api<false, false, kStackSize>;
-  }
+  const bool csg = s->view.csg_prog != nullptr;
+  decltype(&k_trace_api<false, false, kStackSize, false>) k;
+  if (csg) k = pick_api<true>(any, s->watertight, shortStack);
+  else k = pick_api<false>(any, s->watertight, shortStack);
   const int grid = trace_grid(ctx, (const void*)k);
   k<<<grid, kTraceBlock, 0, st>>>(s->view, rays, n, any ? d_ignore : nullptr, any ? nullptr : d_hits,
                                   any ? d_occ : nullptr, ctx->d_work, ctx->d_err);

@@ -249,6 +249,107 @@ __device__ __forceinline__ bool sphere_test(const TRay& r, float4 c, float rad, 
   return true;
 }
 
+// ------------------------------------------------------------------ CSG --
+// CSGObject::intersect over the interval lists of CSGOperation::
+// getCSGIntersection (src/csgobject.cpp:25-44, src/csgoperation.cpp:27-64):
+// the object's postfix program evaluates leaf lists (a sphere's two roots,
+// src/sphere.cpp:29-56; a box's slab entry and exit, src/axisalignedbox.cpp:
+// 30-73) and merges them in t order, keeping a boundary where the
+// operation's inside state changes. At most GBRT_CSG_MAX_LEAVES leaves, so
+// lists hold at most twice as many boundaries. Not inlined: its lists live
+// in local memory only while a CSG record is tested.
+struct CsgParam {
+  float t;
+  int leaf;  // node index of the leaf that produced the boundary
+};
+constexpr int kCsgList = 2 * GBRT_CSG_MAX_LEAVES;
+
+__device__ __forceinline__ bool csg_inside(int op, bool l, bool r) {
+  return op == GBRT_CSG_ISECT ? (l && r) : op == GBRT_CSG_UNION ? (l || r) : op == GBRT_CSG_DIFF ? (l && !r) : (l != r);
+}
+
+static __device__ __noinline__ bool csg_test(const DeviceScene& S, const TRay& r, int start, int len, float tlim,
+                                      float& t_out, int& leaf_out) {
+  CsgParam lists[GBRT_CSG_MAX_LEAVES][kCsgList];
+  int cnt[GBRT_CSG_MAX_LEAVES];
+  int sp = 0;
+  for (int i = 0; i < len; ++i) {
+    const int nidx = __ldg(S.csg_prog + start + i);
+    const float4 A = __ldg(S.csg_nodes + 3 * nidx), B = __ldg(S.csg_nodes + 3 * nidx + 1);
+    const int op = __float_as_int(A.w);
+    if (op == GBRT_CSG_SPHERE || op == GBRT_CSG_BOX) {
+      if (sp >= GBRT_CSG_MAX_LEAVES) return false;
+      CsgParam* out = lists[sp];
+      int n = 0;
+      if (op == GBRT_CSG_SPHERE) {
+        float dfx = fs(r.ox, A.x), dfy = fs(r.oy, A.y), dfz = fs(r.oz, A.z);
+        float a = dot3x(r.dx, r.dy, r.dz, r.dx, r.dy, r.dz);
+        float b = fm(2.f, dot3x(r.dx, r.dy, r.dz, dfx, dfy, dfz));
+        float c = fs(dot3x(dfx, dfy, dfz, dfx, dfy, dfz), fm(B.x, B.x));
+        float disc = fs(fm(b, b), fm(fm(4.f, a), c));
+        if (disc >= 0.f) {
+          float rd = __fsqrt_rn(disc), a2 = fm(2.f, a);
+          out[0] = CsgParam{fdv(fs(-b, rd), a2), nidx};
+          out[1] = CsgParam{fdv(fa(-b, rd), a2), nidx};
+          n = 2;
+        }
+      } else {
+        const float o[3] = {r.ox, r.oy, r.oz}, d[3] = {r.dx, r.dy, r.dz};
+        const float lo[3] = {A.x, A.y, A.z}, hi[3] = {B.x, B.y, B.z};
+        float tmin = -CUDART_INF_F, tmax = CUDART_INF_F;
+        bool empty = false;
+        for (int k = 0; k < 3 && !empty; ++k) {
+          float inv = fdv(1.f, d[k]);
+          float tn = inv >= 0.f ? fs(lo[k], o[k]) : fs(hi[k], o[k]);
+          float tx = inv >= 0.f ? fs(hi[k], o[k]) : fs(lo[k], o[k]);
+          tn = fm(tn, inv);
+          tx = fm(tx, inv);
+          if (tn > tmin) tmin = tn;
+          if (tx < tmax) tmax = tx;
+          if (tmin > tmax) empty = true;
+        }
+        if (!empty) {
+          out[0] = CsgParam{tmin, nidx};
+          out[1] = CsgParam{tmax, nidx};
+          n = 2;
+        }
+      }
+      cnt[sp++] = n;
+    } else {
+      if (sp < 2) return false;
+      const CsgParam* L = lists[sp - 2];
+      const CsgParam* R = lists[sp - 1];
+      const int nl = cnt[sp - 2], nr = cnt[sp - 1];
+      CsgParam tmp[kCsgList];
+      int n = 0, i0 = 0, j0 = 0;
+      bool li = false, ri = false;
+      while (i0 < nl || j0 < nr) {
+        const bool was = csg_inside(op, li, ri);
+        const bool takeL = i0 < nl && (j0 >= nr || L[i0].t <= R[j0].t);
+        const CsgParam p = takeL ? L[i0++] : R[j0++];
+        if (takeL) li = !li; else ri = !ri;
+        if (was != csg_inside(op, li, ri) && n < kCsgList) tmp[n++] = p;
+      }
+      for (int k = 0; k < n; ++k) lists[sp - 2][k] = tmp[k];
+      cnt[sp - 2] = n;
+      --sp;
+    }
+  }
+  if (sp != 1) return false;
+  const CsgParam* P = lists[0];
+  const int n = cnt[0];
+  if (n == 0 || r.tmin > P[n - 1].t) return false;
+  for (int k = 0; k < n; ++k) {
+    if (P[k].t >= r.tmin) {
+      if (P[k].t > r.tmax || !(P[k].t <= tlim)) return false;
+      t_out = P[k].t;
+      leaf_out = P[k].leaf;
+      return true;
+    }
+  }
+  return false;
+}
+
 // Plane (src/plane.cpp:29-31): t = dot((o,1), P) / -dot(d, P.xyz).
 __device__ __forceinline__ float plane_t(const TRay& r, float4 P) {
   float d = -dot3x(r.dx, r.dy, r.dz, P.x, P.y, P.z);
@@ -307,7 +408,7 @@ __device__ __forceinline__ bool trace_init(const DeviceScene& S, const TRay& r, 
 // quad wins over the second whenever it is hit: the first half replaces a
 // current best that is the same quad's second half even at a larger t, and the
 // second half never replaces the first.
-template <bool ANY, bool COUNT, bool WT, int STACK>
+template <bool ANY, bool COUNT, bool WT, int STACK, bool CSG>
 __device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& r, int ignore_prim, TState& ts,
                                            int* stack, int* err, TraceCounters* cnt) {
   const int32_t node = ts.node;
@@ -364,8 +465,12 @@ __device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& r, 
         else hit = tri_test_ref(r, a, b, c, tlim, t, u, v);
       } else if (kind == kRecSphere) {
         hit = sphere_test(r, a, b.x, tlim, t);
-      } else {
+      } else if (!CSG || kind == kRecParallelogram) {
         hit = pgram_test(r, a, b, c, tlim, t, u, v);
+      } else {
+        int leaf = -1;
+        hit = csg_test(S, r, __float_as_int(b.w), __float_as_int(c.x), tlim, t, leaf);
+        u = __int_as_float(leaf);
       }
       if (hit && ts.found && !displace) {
         // strictly closer, and a second half never displaces its first half
@@ -386,14 +491,14 @@ __device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& r, 
 // A whole ray in one call (the ray-query entry points). Returns the internal
 // hit encoding (RawHit::rec) and fills t/u/v. STACK is the capacity of the
 // traversal stack (stack_need(depth of the 4-wide tree)).
-template <bool ANY, bool COUNT, bool WT, int STACK>
+template <bool ANY, bool COUNT, bool WT, int STACK, bool CSG>
 __device__ __forceinline__ int32_t trace_ray(const DeviceScene& S, const TRay& r, int ignore_prim,
                                              float& t_best, float& u_best, float& v_best, int* err,
                                              TraceCounters* cnt) {
   TState ts;
   int stack[STACK];
   if (!trace_init<ANY>(S, r, ignore_prim, ts)) {
-    while (!trace_step<ANY, COUNT, WT, STACK>(S, r, ignore_prim, ts, stack, err, cnt)) {
+    while (!trace_step<ANY, COUNT, WT, STACK, CSG>(S, r, ignore_prim, ts, stack, err, cnt)) {
     }
   }
   t_best = ts.found ? ts.tcur : CUDART_NAN_F;

@@ -34,6 +34,8 @@ class SceneData:
     camera: Optional[dict] = None          # {"eye", "look_at", "up", "fov", "width", "height"}
     flags: int = 0                         # gbrt_scene_flags
     textures: List[np.ndarray] = field(default_factory=list)  # (H, W, 3) float32 BGR each
+    csg_nodes: List[tuple] = field(default_factory=list)  # (op, left, right, a3, b3, material)
+    csg_roots: List[int] = field(default_factory=list)
 
     # ------------------------------------------------------------ building
     def add_material(self, type, kd=(0, 0, 0), ks=(0, 0, 0), exponent=0.0, ior=1.0, coefficient=1.0, texture=-1):
@@ -50,7 +52,21 @@ class SceneData:
         return 0 if self.tri_pos is None else int(self.tri_pos.shape[0])
 
     def n_prims(self):
-        return len(self.lights) + self.n_tri() + len(self.quads) + len(self.spheres) + len(self.planes)
+        return len(self.lights) + self.n_tri() + len(self.quads) + len(self.spheres) + len(self.planes) + \
+            len(self.csg_roots)
+
+    def csg_leaf(self, op, a, b, material):
+        """A sphere (a = centre, b = (r, 0, 0)) or box (a = min, b = max) node."""
+        self.csg_nodes.append((op, -1, -1, tuple(a), tuple(b), int(material)))
+        return len(self.csg_nodes) - 1
+
+    def csg_op(self, op, left, right):
+        self.csg_nodes.append((op, int(left), int(right), (0, 0, 0), (0, 0, 0), -1))
+        return len(self.csg_nodes) - 1
+
+    def add_csg(self, root):
+        self.csg_roots.append(int(root))
+        return len(self.csg_roots) - 1
 
     def prim_offsets(self):
         """First primitive id of each type, in the order of include/gbrt.h."""
@@ -59,6 +75,7 @@ class SceneData:
         o["quads"] = o["tri"] + self.n_tri()
         o["spheres"] = o["quads"] + len(self.quads)
         o["planes"] = o["spheres"] + len(self.spheres)
+        o["csg"] = o["planes"] + len(self.planes)
         return o
 
     # ------------------------------------------------------------ C view
@@ -138,6 +155,16 @@ class SceneData:
             keep.append(arr)
             d.textures = arr
             d.n_textures = len(self.textures)
+        if self.csg_roots:
+            arr = (_abi.CsgNode * len(self.csg_nodes))()
+            for i, (op, l, r, a, b, m) in enumerate(self.csg_nodes):
+                arr[i] = _abi.CsgNode(op, l, r, _f3(a), _f3(b), m)
+            roots = (C.c_int32 * len(self.csg_roots))(*self.csg_roots)
+            keep += [arr, roots]
+            d.csg_nodes = arr
+            d.n_csg_nodes = len(self.csg_nodes)
+            d.csg_roots = roots
+            d.n_csg = len(self.csg_roots)
         return d, keep
 
     def camera_struct(self, width=None, height=None):

@@ -27,6 +27,10 @@ def _from_parsed(ps):
     for i in range(d.n_textures):
         t = d.textures[i]
         s.textures.append(np.ctypeslib.as_array(t.texels, shape=(t.height, t.width, 3)).copy())
+    for i in range(d.n_csg_nodes):
+        g = d.csg_nodes[i]
+        s.csg_nodes.append((g.op, g.left, g.right, tuple(g.a), tuple(g.b), g.material))
+    s.csg_roots = [d.csg_roots[i] for i in range(d.n_csg)]
     if d.n_tri:
         s.tri_pos = np.ctypeslib.as_array(d.tri_pos, shape=(d.n_tri, 9)).copy()
         if d.tri_nrm:

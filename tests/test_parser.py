@@ -85,8 +85,13 @@ def test_parse_errors_are_reported():
     with pytest.raises(GbrtError) as e:
         load_scene_string("intersectable = intersectables { quad([0 0 0], [1 0 0]) };")
     assert e.value.status == _abi.ERR_PARSE and "line 1" in str(e.value)
+    # CSG objects hold at most 8 spheres and boxes
+    leaf = "sphere([0 0 0], 1, a)"
+    tree = leaf
+    for _ in range(8):
+        tree = "union(%s, %s)" % (tree, leaf)
     with pytest.raises(GbrtError) as e:
-        load_scene_string("x = union(sphere([0 0 0], 1, a), sphere([1 0 0], 1, a));\nintersectable = x;")
+        load_scene_string("x = %s;\nintersectable = x;" % tree)
     assert e.value.status == _abi.ERR_UNSUPPORTED
 
 
