@@ -340,6 +340,91 @@ def run_quality(args):
     print(json.dumps(out))
 
 
+BATCH_WORKLOAD = ("64 seeded scenes: diffuse 4x3x4 box, 1-3 noise-displaced meshes (log-uniform 10k-2M triangles), "
+                  "2-8 spheres, materials uniform over diffuse/mirror/glass 1.5/Blinn 10-500, 1-4 area lights of "
+                  "radiance 5-50, 128^2-1024^2 pixels, 4-256 spp, max depth 8, RR p=0.5, reference semantics, "
+                  "BVH built on the GPU")
+
+
+def _batch_scene(i):
+    from renderer_gb300 import workloads
+    return workloads.batch_scene(i, 0)
+
+
+def run_batch(args):
+    """Many independent images in one call (gbrt_render_batch): aggregate
+    paths/s and per-image time over the seeded 64-scene batch. A step is the
+    whole batch; value = paths / device span of the batch (films resident),
+    e2e = paths / host wall time of the call (films copied to host memory)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+
+    import numpy as np
+
+    from renderer_gb300 import _abi
+    from renderer_gb300.batch import BatchJob, autotune, render_batch
+    from renderer_gb300.runtime import Context, GpuScene
+
+    t = time.perf_counter()
+    # scene generation (numpy) in spawned workers, before any device work
+    with cf.ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as ex:
+        scenes = list(ex.map(_batch_scene, range(args.batch_scenes)))
+    gen_s = time.perf_counter() - t
+    ctx = Context(0)
+    t = time.perf_counter()
+    gss = [GpuScene(ctx, s) for s, _ in scenes]
+    create_s = time.perf_counter() - t
+    jobs = [BatchJob(g, s.camera_struct(), p) for g, (s, p) in zip(gss, scenes)]
+    t = time.perf_counter()
+    S, B = autotune(ctx, jobs) if not args.batch_streams else (args.batch_streams, args.batch_paths or (1 << 22))
+    tune_s = time.perf_counter() - t
+    for _ in range(args.warmup):
+        render_batch(ctx, jobs)
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    dev_ms, wall_ms, paths, ext, sh, launches = 0.0, 0.0, 0, 0, 0, 0
+    per_image = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        films, job_ms, st = render_batch(ctx, jobs)
+        wall_ms += 1000 * (time.perf_counter() - t)
+        dev_ms += st.device_ms
+        paths += st.paths
+        ext += st.extension_rays
+        sh += st.shadow_rays
+        launches += st.kernel_launches
+        per_image.append(job_ms)
+    clk = clocks.stop()
+    per_image = np.mean(per_image, 0)
+    tri = [s.n_tri() for s, _ in scenes]
+    spp = [p.x_samples * p.y_samples for _, p in scenes]
+    res = [s.camera["width"] for s, _ in scenes]
+    d2h = sum(r * r * 3 * 4 for r in res)
+    h2d = len(jobs) * C.sizeof(_abi.BatchJob)
+    depth = max(p.max_depth for _, p in scenes)
+    line = {"metric": "paths/s (batch)", "value": paths / (dev_ms / 1000.0), "unit": "paths/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": BATCH_WORKLOAD, "scenes": len(jobs), "paths_per_step": paths // args.steps,
+                       "triangles_total": int(sum(tri)), "triangles_min": int(min(tri)),
+                       "triangles_max": int(max(tri)), "resolutions": {str(r): res.count(r) for r in sorted(set(res))},
+                       "spp": {str(v): spp.count(v) for v in sorted(set(spp))},
+                       "streams": S, "batch_paths": B, "autotune_s": tune_s, "scene_generation_s": gen_s,
+                       "scene_create_s": create_s,
+                       "l2": "inputs larger than L2 (33M triangles over 64 scenes, path state per stream > 129 MB)",
+                       "per_image_ms": {"mean_wall": wall_ms / args.steps / len(jobs),
+                                        "device_median": float(np.median(per_image)),
+                                        "device_max": float(np.max(per_image)),
+                                        "device_min": float(np.min(per_image))},
+                       "extension_rays_per_path": ext / max(paths, 1), "shadow_rays_per_path": sh / max(paths, 1),
+                       "max_depth": depth},
+            "e2e": {"value": paths / (wall_ms / 1000.0), "unit": "paths/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "clocks": clk}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -364,8 +449,15 @@ def main():
     ap.add_argument("--train-steps", type=int, default=1, help="Adam steps of 2^18 samples after a training pass")
     ap.add_argument("--quality", action="store_true",
                     help="relMSE of the Cornell box and icosphere images against 65,536-spp renders")
+    ap.add_argument("--batch", action="store_true",
+                    help="aggregate paths/s of the seeded 64-scene batch through gbrt_render_batch")
+    ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--batch-streams", type=int, default=0, help="streams for --batch (0: autotune)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.batch:
+        run_batch(args)
+        return
     if args.quality:
         run_quality(args)
         return

@@ -379,6 +379,42 @@ gbrt_status gbrt_tonemap_device(gbrt_ctx* ctx, const float* d_film_bgr,
 gbrt_status gbrt_write_image(const char* path, const float* film_bgr,
                              int32_t width, int32_t height, float gamma);
 
+/* ---- batches of renders (no counterpart in the renderer, which renders one
+ *      image per process). The jobs run concurrently on several CUDA
+ *      streams, each as the same wavefront as gbrt_render, so that many
+ *      small images keep the GPU busy; the host waits once, at the end. ---- */
+typedef struct gbrt_batch_job {
+  gbrt_scene* scene;            /* created on the same context */
+  gbrt_camera camera;
+  gbrt_render_params params;    /* batch_paths 0: the call's batch_paths */
+  float* film;                  /* host, H x W x 3 BGR */
+} gbrt_batch_job;
+
+typedef struct gbrt_batch_stats {
+  uint64_t paths, extension_rays, shadow_rays, nonfinite;
+  double wall_ms;               /* host wall time of the call */
+  int32_t streams;
+  int32_t pad;
+  int64_t batch_paths;          /* wavefront size used for jobs without their own */
+  double device_ms;             /* device time from the first job's start to the
+                                   last job's end (films not yet copied out) */
+  uint64_t kernel_launches;
+} gbrt_batch_stats;
+
+/* streams / batch_paths 0: the values gbrt_batch_autotune chose on this
+ * context (4 and 2^22 before any tuning). job_ms (optional, n doubles): each
+ * job's device time from its first to its last kernel. */
+gbrt_status gbrt_render_batch(gbrt_ctx* ctx, const gbrt_batch_job* jobs,
+                              int32_t n, int32_t streams, int64_t batch_paths,
+                              double* job_ms, gbrt_batch_stats* stats);
+/* Renders up to 8 of the jobs at one sample per pixel with 1, 2, 4 and 8
+ * streams and wavefronts of 2^20 and 2^22 paths, keeps the fastest pair on
+ * the context (for later calls with 0s) and returns it. Films are not
+ * written. */
+gbrt_status gbrt_batch_autotune(gbrt_ctx* ctx, const gbrt_batch_job* jobs,
+                                int32_t n, int32_t* streams,
+                                int64_t* batch_paths);
+
 /* ---- neural path guiding. No counterpart in the renderer, whose
  *      integrators sample the BSDF only (src/unidipathtracingintegrator.cpp:
  *      34-46); used with the physical estimator. ---------------------------

@@ -81,6 +81,17 @@ class Stats(C.Structure):
                 ("nodes_any", C.c_uint64), ("prims_any", C.c_uint64)]
 
 
+class BatchJob(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("params", RenderParams), ("film", C.c_void_p)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("nonfinite", C.c_uint64), ("wall_ms", C.c_double), ("streams", C.c_int32), ("pad", C.c_int32),
+                ("batch_paths", C.c_int64), ("device_ms", C.c_double),
+                ("kernel_launches", C.c_uint64)]
+
+
 class GuideParams(C.Structure):
     _fields_ = [("guide_fraction", C.c_float), ("passes", C.c_int32), ("train_passes", C.c_int32),
                 ("steps_per_pass", C.c_int32), ("batch_samples", C.c_int32), ("learning_rate", C.c_float),
@@ -152,6 +163,10 @@ SIGNATURES = [
     ("gbrt_tonemap", C.c_int, [P, C.c_int32, C.c_int32, C.c_float, P]),
     ("gbrt_tonemap_device", C.c_int, [P, P, C.c_int32, C.c_int32, C.c_float, P, P]),
     ("gbrt_write_image", C.c_int, [C.c_char_p, P, C.c_int32, C.c_int32, C.c_float]),
+    ("gbrt_render_batch", C.c_int, [P, C.POINTER(BatchJob), C.c_int32, C.c_int32, C.c_int64,
+                                    C.POINTER(C.c_double), C.POINTER(BatchStats)]),
+    ("gbrt_batch_autotune", C.c_int, [P, C.POINTER(BatchJob), C.c_int32, C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_int64)]),
     ("gbrt_guide_create", C.c_int, [P, C.POINTER(C.c_float), C.c_uint64, C.POINTER(P)]),
     ("gbrt_guide_destroy", C.c_int, [P]),
     ("gbrt_guide_get_weights", C.c_int, [P, P, C.c_size_t]),

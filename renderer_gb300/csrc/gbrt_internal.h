@@ -18,6 +18,10 @@ struct gbrt_ctx {
   // word, reused by every call on this context.
   unsigned long long* d_work = nullptr;
   int* d_err = nullptr;
+  // Streams of gbrt_render_batch and the tuned batch settings.
+  std::vector<cudaStream_t> batch_streams;
+  int batch_streams_tuned = 4;
+  long long batch_paths_tuned = 1ll << 22;
 };
 
 struct gbrt_scene {

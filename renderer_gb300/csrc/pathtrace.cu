@@ -1583,6 +1583,185 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   return status;
 }
 
+// -------------------------------------------------------------- batches ----
+// gbrt_render_batch: every job is the wavefront of gbrt_render, enqueued on
+// one of several streams without any host wait (stream-ordered buffers, the
+// counters copied to pinned memory); jobs on different streams overlap.
+struct JobOut {
+  unsigned long long tally[8];
+  int err;
+  int pad;
+};
+
+static cudaError_t enqueue_job(gbrt_scene* s, const gbrt_camera& cam, const gbrt_render_params& prm, float* d_film,
+                               long long cap, cudaStream_t stream, JobOut* h_out, unsigned long long* launches) {
+  gbrt_ctx* ctx = s->ctx;
+  const unsigned long long npix = (unsigned long long)cam.width * cam.height;
+  const int spp = prm.x_samples * prm.y_samples;
+  const unsigned long long total = npix * (unsigned long long)spp;
+  long long B = prm.batch_paths > 0 ? prm.batch_paths : cap;
+  B = std::max<long long>(1, std::min<long long>(B, (long long)total));
+  PTParams P;
+  init_params(P, cam, prm, total);
+  Buffers buf(stream);
+  PTState st;
+  std::memset(&st, 0, sizeof st);
+  cudaError_t e = cudaSuccess;
+  auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
+  double* d_sum = nullptr;
+  A(buf.alloc(&st.alpha, B)); A(buf.alloc(&st.L, B)); A(buf.alloc(&st.ctl, B));
+  A(buf.alloc(&st.pv_p, B)); A(buf.alloc(&st.pv_n, B)); A(buf.alloc(&st.pv_d, B)); A(buf.alloc(&st.pv_a, B));
+  A(buf.alloc(&st.ext[0], 2 * B)); A(buf.alloc(&st.ext[1], 2 * B));
+  A(buf.alloc(&st.ext_slot[0], B)); A(buf.alloc(&st.ext_slot[1], B));
+  A(buf.alloc(&st.hits, B));
+  A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
+  A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
+  A(buf.alloc(&d_sum, npix * 3));
+  if (e != cudaSuccess) return e;
+  A(cudaMemsetAsync(d_sum, 0, npix * 3 * sizeof(double), stream));
+  A(cudaMemsetAsync(st.tally, 0, 8 * sizeof(unsigned long long), stream));
+  A(cudaMemsetAsync(st.err, 0, sizeof(int), stream));
+  const TraceKernels tk = pick_kernels(s, false);
+  auto kShade = pick_shade(s, P.physical != 0, false);
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tk.ext, kTraceBlock, 0);
+  const int traceGrid = std::max(1, per) * ctx->num_sms;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tk.sh, kTraceBlock, 0);
+  const int shadowGrid = std::max(1, per) * ctx->num_sms;
+  const int shadeGrid = ctx->num_sms * 8;
+  for (unsigned long long g0 = 0; g0 < total && e == cudaSuccess; g0 += (unsigned long long)B) {
+    P.g0 = g0;
+    P.nb = int(std::min<unsigned long long>((unsigned long long)B, total - g0));
+    k_raygen<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
+    for (int it = 0; it < P.D; ++it) {
+      int cur = it & 1;
+      tk.ext<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
+      kShade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
+      tk.sh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
+    }
+    launch_accumulate(P, st, d_sum, nullptr, stream);
+    *launches += 2 + 3ull * unsigned(P.D);
+    A(cudaGetLastError());
+  }
+  const size_t n3 = size_t(npix) * 3;
+  k_finalize<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_sum, d_film, n3, 1.0 / spp);
+  *launches += 1;
+  A(cudaGetLastError());
+  A(cudaMemcpyAsync(h_out->tally, st.tally, sizeof h_out->tally, cudaMemcpyDeviceToHost, stream));
+  A(cudaMemcpyAsync(&h_out->err, st.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  return e;  // buf frees its arrays in stream order
+}
+
+static gbrt_status check_job(gbrt_ctx* ctx, const gbrt_batch_job& j) {
+  if (!j.scene || j.scene->ctx != ctx) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch: job scene");
+  const gbrt_camera& c = j.camera;
+  const gbrt_render_params& p = j.params;
+  if (c.width <= 0 || c.height <= 0 || p.x_samples <= 0 || p.y_samples <= 0 || p.max_depth <= 0 || p.max_depth > 64 ||
+      (p.semantics != GBRT_SEM_REFERENCE && p.semantics != GBRT_SEM_PHYSICAL) ||
+      !(p.termination_prob >= 0.f && p.termination_prob <= 1.f))
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch: bad camera or render parameters");
+  return GBRT_OK;
+}
+
+// Runs the jobs; films to device buffers, copied to the jobs' host films
+// when copy_out is set. Returns per-job device milliseconds in job_ms.
+static gbrt_status batch_impl(gbrt_ctx* ctx, const gbrt_batch_job* jobs, int n, int S, long long cap, bool copy_out,
+                              double* job_ms, gbrt_batch_stats* stats) {
+  GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  while (int(ctx->batch_streams.size()) < S) {
+    cudaStream_t q;
+    GBRT_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+    ctx->batch_streams.push_back(q);
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  JobOut* h_out = nullptr;
+  GBRT_CUDA_TRY(ctx, cudaMallocHost(&h_out, sizeof(JobOut) * size_t(n)));
+  std::vector<float*> films(size_t(n), nullptr);
+  std::vector<cudaEvent_t> ev(2 * size_t(n), nullptr);
+  // Longest job first, each onto the stream with the least work so far
+  // (paths x depth as the cost), so that the streams finish together.
+  std::vector<int> order(static_cast<size_t>(n));
+  std::vector<double> cost(static_cast<size_t>(n));
+  for (int j = 0; j < n; ++j) {
+    order[j] = j;
+    const gbrt_render_params& p = jobs[j].params;
+    cost[j] = double(jobs[j].camera.width) * jobs[j].camera.height * p.x_samples * p.y_samples * p.max_depth;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  std::vector<double> load(static_cast<size_t>(S), 0.0);
+  // Every stream starts after `begin` and records its own end, so that the
+  // batch's device span is max over streams of (end - begin).
+  cudaEvent_t begin = nullptr;
+  std::vector<cudaEvent_t> ends(size_t(S), nullptr);
+  unsigned long long launches = 0;
+  cudaError_t e = cudaEventCreate(&begin);
+  if (e == cudaSuccess) e = cudaEventRecord(begin, ctx->batch_streams[0]);
+  for (int k = 1; k < S && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(ctx->batch_streams[k], begin, 0);
+  for (int k = 0; k < n && e == cudaSuccess; ++k) {
+    const int j = order[k];
+    const int qi = int(std::min_element(load.begin(), load.end()) - load.begin());
+    load[qi] += cost[j];
+    cudaStream_t q = ctx->batch_streams[qi];
+    const gbrt_camera& c = jobs[j].camera;
+    std::memset(&h_out[j], 0, sizeof(JobOut));
+    cudaEventCreate(&ev[2 * j]);
+    cudaEventCreate(&ev[2 * j + 1]);
+    e = cudaMallocAsync(&films[j], size_t(c.width) * c.height * 3 * sizeof(float), q);
+    if (e != cudaSuccess) break;
+    cudaEventRecord(ev[2 * j], q);
+    e = enqueue_job(jobs[j].scene, c, jobs[j].params, films[j], cap, q, &h_out[j], &launches);
+    cudaEventRecord(ev[2 * j + 1], q);
+  }
+  for (int k = 0; k < S; ++k) {
+    if (cudaEventCreate(&ends[k]) == cudaSuccess) cudaEventRecord(ends[k], ctx->batch_streams[k]);
+  }
+  for (int k = 0; k < S; ++k) {
+    cudaError_t r = cudaStreamSynchronize(ctx->batch_streams[k]);
+    if (e == cudaSuccess) e = r;
+  }
+  double device_ms = 0.0;
+  for (int k = 0; k < S; ++k) {
+    float ms = 0.f;
+    if (begin && ends[k] && cudaEventElapsedTime(&ms, begin, ends[k]) == cudaSuccess)
+      device_ms = std::max(device_ms, double(ms));
+    if (ends[k]) cudaEventDestroy(ends[k]);
+  }
+  if (begin) cudaEventDestroy(begin);
+  gbrt_status status = e == cudaSuccess ? GBRT_OK : cuda_fail(ctx, e, "gbrt_render_batch");
+  if (stats) std::memset(stats, 0, sizeof *stats);
+  for (int j = 0; j < n; ++j) {
+    if (status == GBRT_OK && copy_out && jobs[j].film) {
+      const gbrt_camera& c = jobs[j].camera;
+      cudaError_t r = cudaMemcpy(jobs[j].film, films[j], size_t(c.width) * c.height * 3 * sizeof(float),
+                                 cudaMemcpyDeviceToHost);
+      if (r != cudaSuccess) status = cuda_fail(ctx, r, "gbrt_render_batch copy-out");
+    }
+    if (films[j]) cudaFree(films[j]);
+    float ms = 0.f;
+    if (ev[2 * j] && ev[2 * j + 1]) cudaEventElapsedTime(&ms, ev[2 * j], ev[2 * j + 1]);
+    if (job_ms) job_ms[j] = ms;
+    if (ev[2 * j]) cudaEventDestroy(ev[2 * j]);
+    if (ev[2 * j + 1]) cudaEventDestroy(ev[2 * j + 1]);
+    if (status == GBRT_OK && h_out[j].err) status = fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render_batch: stack overflow");
+    if (stats) {
+      const gbrt_camera& c = jobs[j].camera;
+      stats->paths += (unsigned long long)c.width * c.height * jobs[j].params.x_samples * jobs[j].params.y_samples;
+      stats->extension_rays += h_out[j].tally[0];
+      stats->shadow_rays += h_out[j].tally[1];
+      stats->nonfinite += h_out[j].tally[2];
+    }
+  }
+  cudaFreeHost(h_out);
+  if (stats) {
+    stats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    stats->streams = S;
+    stats->batch_paths = cap;
+    stats->device_ms = device_ms;
+    stats->kernel_launches = launches;
+  }
+  return status;
+}
+
 }  // namespace gbrt
 
 using namespace gbrt;
@@ -1638,6 +1817,70 @@ gbrt_status gbrt_render_guided(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   if (!s) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: NULL scene");
   clear_error(s->ctx);
   return render_guided_impl(s, cam, prm, guide, gp, film, stats);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+gbrt_status gbrt_render_batch(gbrt_ctx* ctx, const gbrt_batch_job* jobs, int32_t n, int32_t streams,
+                              int64_t batch_paths, double* job_ms, gbrt_batch_stats* stats) {
+  if (!ctx || (n > 0 && !jobs) || n < 0 || streams < 0 || streams > 64 || batch_paths < 0)
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch: bad argument");
+  clear_error(ctx);
+  for (int j = 0; j < n; ++j) {
+    gbrt_status st = check_job(ctx, jobs[j]);
+    if (st != GBRT_OK) return st;
+    if (!jobs[j].film) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch: job without a film");
+  }
+  const int S = streams > 0 ? streams : ctx->batch_streams_tuned;
+  const long long cap = batch_paths > 0 ? batch_paths : ctx->batch_paths_tuned;
+  if (n == 0) {
+    if (stats) {
+      std::memset(stats, 0, sizeof *stats);
+      stats->streams = S;
+      stats->batch_paths = cap;
+    }
+    return GBRT_OK;
+  }
+  return batch_impl(ctx, jobs, n, S, cap, true, job_ms, stats);
+}
+
+gbrt_status gbrt_batch_autotune(gbrt_ctx* ctx, const gbrt_batch_job* jobs, int32_t n, int32_t* streams,
+                                int64_t* batch_paths) {
+  if (!ctx || !jobs || n <= 0) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_batch_autotune: bad argument");
+  clear_error(ctx);
+  // A sample of the jobs at one sample per pixel.
+  std::vector<gbrt_batch_job> sample(jobs, jobs + std::min<int32_t>(n, 8));
+  for (auto& j : sample) {
+    gbrt_status st = check_job(ctx, j);
+    if (st != GBRT_OK) return st;
+    j.params.x_samples = 1;
+    j.params.y_samples = 1;
+    j.params.batch_paths = 0;
+  }
+  double best = 0.0;
+  int bestS = ctx->batch_streams_tuned;
+  long long bestB = ctx->batch_paths_tuned;
+  for (long long B : {1ll << 20, 1ll << 22}) {
+    for (int S : {1, 2, 4, 8}) {
+      gbrt_batch_stats st;
+      gbrt_status r = batch_impl(ctx, sample.data(), int(sample.size()), S, B, false, nullptr, &st);  // warm-up
+      if (r == GBRT_OK) r = batch_impl(ctx, sample.data(), int(sample.size()), S, B, false, nullptr, &st);
+      if (r != GBRT_OK) return r;
+      double rate = double(st.paths) / std::max(st.wall_ms, 1e-6);
+      if (rate > best) {
+        best = rate;
+        bestS = S;
+        bestB = B;
+      }
+    }
+  }
+  ctx->batch_streams_tuned = bestS;
+  ctx->batch_paths_tuned = bestB;
+  if (streams) *streams = bestS;
+  if (batch_paths) *batch_paths = bestB;
+  return GBRT_OK;
 }
 
 }  // extern "C"

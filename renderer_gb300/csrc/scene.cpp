@@ -184,6 +184,10 @@ gbrt_status gbrt_ctx_destroy(gbrt_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->d_work);
   cudaFree(ctx->d_err);
+  for (cudaStream_t s : ctx->batch_streams) {
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return GBRT_OK;

@@ -115,13 +115,27 @@ def value_noise(p, seed):
     w = t * t * (3.0 - 2.0 * t)
     i = f.astype(np.int64)
     out = np.zeros(len(p))
+    # The lattice values over the box of cells the points touch, when that box
+    # is small, hashed once and gathered (same values as hashing per point).
+    lo = i.min(0) if len(p) else np.zeros(3, np.int64)
+    ext = (i.max(0) + 2 - lo) if len(p) else np.ones(3, np.int64)
+    table = None
+    if int(np.prod(ext)) <= max(4 * len(p), 1 << 16):
+        g = np.meshgrid(*[np.arange(lo[a], lo[a] + ext[a]) for a in range(3)], indexing="ij")
+        table = _lattice(seed, g[0].ravel(), g[1].ravel(), g[2].ravel())
+        rel = i - lo
+        base = (rel[:, 0] * ext[1] + rel[:, 1]) * ext[2] + rel[:, 2]
     for dx in (0, 1):
         wx = w[:, 0] if dx else 1.0 - w[:, 0]
         for dy in (0, 1):
             wy = w[:, 1] if dy else 1.0 - w[:, 1]
             for dz in (0, 1):
                 wz = w[:, 2] if dz else 1.0 - w[:, 2]
-                out += wx * wy * wz * _lattice(seed, i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz)
+                if table is not None:
+                    v = table[base + (dx * ext[1] + dy) * ext[2] + dz]
+                else:
+                    v = _lattice(seed, i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz)
+                out += wx * wy * wz * v
     return out
 
 
@@ -268,3 +282,90 @@ def two_rooms(width=1024, height=768, mesh_quads=500, seed=0):
 
 def two_rooms_params(x_samples=1, y_samples=1, seed=0, max_depth=12, termination_prob=0.5):
     return render_params(x_samples, y_samples, termination_prob, max_depth, seed, semantics=_abi.SEM_PHYSICAL)
+
+
+# ------------------------------------------------------------- batch of scenes
+BATCH_RESOLUTIONS = (128, 256, 512, 1024)
+# x_samples x y_samples pairs covering 4 to 256 samples per pixel
+BATCH_SPP = ((2, 2), (2, 4), (4, 4), (4, 8), (8, 8), (8, 16), (16, 16))
+
+
+def _rotation(rng):
+    """A uniformly random rotation (QR of a Gaussian matrix, signs fixed)."""
+    q, r = np.linalg.qr(rng.standard_normal((3, 3)))
+    q = q * np.sign(np.diag(r))
+    if np.linalg.det(q) < 0:
+        q[:, 0] = -q[:, 0]
+    return q
+
+
+def _batch_material(s, rng):
+    kind = int(rng.integers(4))
+    if kind == 0:
+        return s.add_material(_abi.MAT_DIFFUSE, kd=tuple(rng.uniform(0.2, 0.85, 3)))
+    if kind == 1:
+        return s.add_material(_abi.MAT_MIRROR, coefficient=1.0)
+    if kind == 2:
+        return s.add_material(_abi.MAT_TRANSPARENT, ior=1.5)
+    kd = rng.uniform(0.1, 0.5, 3)
+    return s.add_material(_abi.MAT_BLINN, kd=tuple(kd), ks=tuple(np.full(3, 0.9 - kd.max())),
+                          exponent=float(rng.uniform(10.0, 500.0)))
+
+
+def batch_scene(index, seed=0):
+    """Scene `index` of the seeded batch: inside a diffuse 4 x 3 x 4 box open
+    towards the camera, 1-3 noise-displaced meshes (heightfield patches,
+    randomly rotated) with a log-uniform 10,000 to 2,000,000 triangles in
+    total, 2-8 spheres, every object's material drawn uniformly from diffuse,
+    mirror, glass (IOR 1.5) and Blinn (exponent 10-500), 1-4 ceiling area
+    lights of radiance 5-50, a square resolution from 128 to 1024 and 4 to 256
+    jittered samples per pixel. Returns (SceneData, gbrt_render_params): max
+    depth 8, Russian roulette p = 0.5, reference semantics, BVH built on the
+    GPU."""
+    rng = np.random.default_rng([int(seed), int(index), 0xC3])
+    s = SceneData()
+    s.flags = _abi.SCENE_GPU_BUILD
+    wall = s.add_material(_abi.MAT_DIFFUSE, kd=tuple(rng.uniform(0.5, 0.8, 3)))
+    s.quads = [
+        ((-2, 0, -2), (2, 0, -2), (2, 0, 2), (-2, 0, 2), wall),      # floor
+        ((-2, 3, -2), (-2, 3, 2), (2, 3, 2), (2, 3, -2), wall),      # ceiling
+        ((-2, 0, -2), (-2, 3, -2), (2, 3, -2), (2, 0, -2), wall),    # back
+        ((-2, 0, -2), (-2, 0, 2), (-2, 3, 2), (-2, 3, -2), wall),    # left
+        ((2, 0, -2), (2, 3, -2), (2, 3, 2), (2, 0, 2), wall),        # right
+    ]
+    n_tri = int(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
+    k = int(rng.integers(1, 4))
+    pos, nrm, mats = [], [], []
+    for m in range(k):
+        n = max(2, int(round(np.sqrt(n_tri / k / 2))))
+        half = float(rng.uniform(0.4, 1.2))
+        p, nn = displaced_grid(n, -half, half, -half, half, 0.0, 0.15 * half, seed=int(rng.integers(1 << 30)))
+        R = _rotation(rng)
+        c = np.array([rng.uniform(-1.0, 1.0), rng.uniform(0.8, 2.0), rng.uniform(-1.0, 1.0)])
+        pos.append((p.reshape(-1, 3) @ R.T + c).reshape(-1, 9))
+        nrm.append((nn.reshape(-1, 3) @ R.T).reshape(-1, 9))
+        mats.append(np.full(len(p), _batch_material(s, rng), np.int32))
+    s.tri_pos = np.concatenate(pos).astype(np.float32)
+    s.tri_nrm = np.concatenate(nrm).astype(np.float32)
+    s.tri_mat = np.concatenate(mats)
+    for _ in range(int(rng.integers(2, 9))):
+        r = float(rng.uniform(0.1, 0.45))
+        c = (rng.uniform(-1.5, 1.5), rng.uniform(r, 2.5), rng.uniform(-1.5, 1.5))
+        s.spheres.append((c, r, _batch_material(s, rng)))
+    for _ in range(int(rng.integers(1, 5))):
+        a, b = rng.uniform(0.3, 0.8, 2)
+        x, z = rng.uniform(-1.9, 1.9 - a), rng.uniform(-1.9, 1.9 - b)
+        le = float(rng.uniform(5.0, 50.0))
+        # u x v points down (-y)
+        s.lights.append(dict(type=_abi.LIGHT_AREA, origin=(x, 2.99, z), u=(a, 0, 0), v=(0, 0, b),
+                             intensity=(le, le, le)))
+    res = int(BATCH_RESOLUTIONS[rng.integers(len(BATCH_RESOLUTIONS))])
+    xs, ys = BATCH_SPP[rng.integers(len(BATCH_SPP))]
+    eye = (rng.uniform(-0.5, 0.5), rng.uniform(1.2, 1.8), rng.uniform(6.0, 7.0))
+    s.camera = dict(eye=eye, look_at=(0, 1.5, 0), up=(0, 1, 0), fov=FOV_40, width=res, height=res)
+    return s, render_params(xs, ys, 0.5, 8, seed=int(index))
+
+
+def batch_scenes(n=64, seed=0):
+    """The first n scenes of batch_scene's seeded sequence."""
+    return [batch_scene(i, seed) for i in range(n)]

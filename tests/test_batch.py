@@ -1,0 +1,130 @@
+"""Batches of renders (gbrt_render_batch, gbrt_batch_autotune) and the seeded
+64-scene batch workload.
+
+CPU: the workload generator is deterministic and draws what it promises
+(triangle counts, materials, lights, resolutions, samples per pixel). GPU:
+every film of a batch equals the film of the same job rendered alone by
+gbrt_render (same wavefront size; up to the order of float additions of
+shadow rays), whatever the number of streams; batch
+jobs match the oracle path by path; the statistics add up; autotuning keeps
+its choice on the context; bad jobs are refused with a status."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle.binding import OracleScene
+from renderer_gb300 import GbrtError, GpuScene, PerPixelRenderer, _abi, workloads
+from renderer_gb300.scene import render_params
+
+SMALL = (6, 8, 9)       # scenes of the batch with about 15,000 triangles
+MIXED = (3, 6, 8, 9, 11)
+
+
+def shrunk(i, res, xs, ys, seed=None):
+    s, p = workloads.batch_scene(i)
+    s.camera["width"] = s.camera["height"] = res
+    return s, render_params(xs, ys, p.termination_prob, p.max_depth, p.seed if seed is None else seed)
+
+
+def test_batch_workload_is_seeded_and_in_range():
+    a, pa = workloads.batch_scene(8)
+    b, pb = workloads.batch_scene(8)
+    assert np.array_equal(a.tri_pos, b.tri_pos) and a.spheres == b.spheres and a.lights == b.lights
+    assert (pa.x_samples, pa.y_samples) == (pb.x_samples, pb.y_samples)
+    c, _ = workloads.batch_scene(8, seed=1)
+    assert not np.array_equal(a.tri_pos, c.tri_pos)
+    for i in SMALL + (3, 11):
+        s, p = workloads.batch_scene(i)
+        assert 10_000 * 0.9 <= s.n_tri() <= 2_000_000 * 1.05
+        assert 1 <= len(s.lights) <= 4 and all(5 <= l["intensity"][0] <= 50 for l in s.lights)
+        assert 2 <= len(s.spheres) <= 8
+        assert s.camera["width"] == s.camera["height"] in workloads.BATCH_RESOLUTIONS
+        assert 4 <= p.x_samples * p.y_samples <= 256
+        assert s.flags & _abi.SCENE_GPU_BUILD
+        kinds = {m["type"] for m in s.materials[1:]}
+        assert kinds <= {_abi.MAT_DIFFUSE, _abi.MAT_MIRROR, _abi.MAT_TRANSPARENT, _abi.MAT_BLINN}
+        for m in s.materials:
+            if m["type"] == _abi.MAT_BLINN:
+                assert 10 <= m["exponent"] <= 500
+        # every mesh vertex inside the box
+        P = s.tri_pos.reshape(-1, 3)
+        assert P.min(0)[1] > -0.5 and P.max(0)[1] < 3.5
+
+
+@pytest.mark.gpu
+def test_batch_equals_individual_renders(ctx):
+    from renderer_gb300.batch import BatchJob, render_batch
+    scenes = [shrunk(i, 48 + 16 * k, 2, 1 + k % 3) for k, i in enumerate(MIXED)]
+    gss = [GpuScene(ctx, s) for s, _ in scenes]
+    jobs = [BatchJob(g, s.camera_struct(), p) for g, (s, p) in zip(gss, scenes)]
+    B = 1 << 14   # several wavefronts per job
+    alone = []
+    for g, (s, p) in zip(gss, scenes):
+        r = PerPixelRenderer(g, s.camera_struct(), {"pt-x-samples": p.x_samples, "pt-y-samples": p.y_samples},
+                             seed=p.seed, max_depth=p.max_depth, batch_paths=B)
+        alone.append(r.render())
+    for S in (1, 3, 8):
+        films, ms, st = render_batch(ctx, jobs, streams=S, batch_paths=B)
+        for f, a in zip(films, alone):
+            # the same paths; only the order in which a vertex's shadow rays
+            # (one per light) add into its radiance may differ (float atomics)
+            assert np.allclose(f, a, rtol=1e-5, atol=1e-7), np.abs(f - a).max()
+        assert st.streams == S and st.batch_paths == B
+        assert st.paths == sum(s.camera["width"] ** 2 * p.x_samples * p.y_samples for s, p in scenes)
+        assert st.extension_rays > st.paths and st.nonfinite == 0
+        assert st.device_ms > 0 and st.wall_ms >= st.device_ms * 0.5
+        assert (ms > 0).all()
+        waves = sum(-(-(s.camera["width"] ** 2 * p.x_samples * p.y_samples) // B) for s, p in scenes)
+        assert st.kernel_launches == sum(
+            (2 + 3 * p.max_depth) * -(-(s.camera["width"] ** 2 * p.x_samples * p.y_samples) // B) + 1
+            for s, p in scenes)
+        assert waves > len(scenes)
+
+
+@pytest.mark.gpu
+def test_batch_jobs_match_oracle_path_by_path(ctx):
+    from renderer_gb300.batch import BatchJob, render_batch
+    scenes = [shrunk(i, 32, 2, 2, seed=11 + i) for i in SMALL]
+    gss = [GpuScene(ctx, s) for s, _ in scenes]
+    films, _, st = render_batch(ctx, [BatchJob(g, s.camera_struct(), p) for g, (s, p) in zip(gss, scenes)],
+                                streams=2)
+    for f, (s, p) in zip(films, scenes):
+        o = OracleScene(s).render(s.camera_struct(), p, rng_mode=1)["film"].astype(np.float64)
+        a = f.astype(np.float64)
+        close = np.abs(a - o) <= 2e-3 * np.maximum(np.abs(o), 1e-3)
+        assert close.all(-1).mean() >= 0.97
+        assert a.sum() == pytest.approx(o.sum(), rel=2e-2)
+
+
+@pytest.mark.gpu
+def test_autotune_keeps_its_choice(ctx):
+    from renderer_gb300.batch import BatchJob, autotune, render_batch
+    scenes = [shrunk(i, 64, 1, 1) for i in SMALL]
+    gss = [GpuScene(ctx, s) for s, _ in scenes]
+    jobs = [BatchJob(g, s.camera_struct(), p) for g, (s, p) in zip(gss, scenes)]
+    S, B = autotune(ctx, jobs)
+    assert S in (1, 2, 4, 8) and B in (1 << 20, 1 << 22)
+    _, _, st = render_batch(ctx, jobs)
+    assert st.streams == S and st.batch_paths == B
+
+
+@pytest.mark.gpu
+def test_bad_jobs_are_refused(ctx):
+    from renderer_gb300 import lib
+    from renderer_gb300.batch import BatchJob, _jobs_array
+    s, p = shrunk(9, 16, 1, 1)
+    g = GpuScene(ctx, s)
+    cam = s.camera_struct()
+    arr = _jobs_array([BatchJob(g, cam, p)], None)   # no film
+    st = _abi.BatchStats()
+    assert lib().gbrt_render_batch(ctx.handle, arr, 1, 0, 0, None, C.byref(st)) == _abi.ERR_INVALID_ARG
+    bad = render_params(1, 1, 1.5, 8, 0)             # termination probability outside [0, 1]
+    from renderer_gb300.batch import render_batch
+    with pytest.raises(GbrtError):
+        render_batch(ctx, [BatchJob(g, cam, bad)])
+    with pytest.raises(GbrtError):
+        render_batch(ctx, [BatchJob(g, cam, p)], streams=65)
+    # an empty batch is a no-op
+    films, ms, st = render_batch(ctx, [])
+    assert films == [] and st.paths == 0
