@@ -425,6 +425,71 @@ def run_batch(args):
     print(json.dumps(line))
 
 
+def run_chains(args):
+    """The Markov-chain renderers on the Cornell box (256 x 256, max depth 5,
+    the renderer's defaults: Metropolis with 16 mutations per pixel, 10,000
+    bootstrap samples, large steps 0.1, termination 0.5; energy
+    redistribution with 100 mutations per chain and 2 x 2 initial samples per
+    pixel): paths traced per second of device time for several chain counts,
+    beside the oracle's restatement on the host cores (one chain per thread,
+    as the renderer runs)."""
+    import numpy as np
+
+    from oracle.binding import OracleScene
+    from renderer_gb300 import workloads
+    from renderer_gb300.chains import EnergyRedistributionRenderer, MetropolisRenderer, erpt_params, mlt_params
+    from renderer_gb300.runtime import Context, GpuScene
+    from renderer_gb300.scene import render_params
+
+    s = workloads.cornell_box(256, 256)
+    ctx = Context(0)
+    gs = GpuScene(ctx, s)
+    out = {"metric": "paths/s (Markov-chain renderers)", "unit": "paths/s", "higher_is_better": True,
+           "config": {"workload": "Cornell box 256x256, max depth 5, reference semantics"}, "mlt": [], "erpt": []}
+    for chains in args.mlt_chains:
+        r = MetropolisRenderer(gs, seed=1, max_depth=5, chains=chains)
+        for _ in range(args.warmup):
+            r.render()
+        ms, paths = 0.0, 0
+        for _ in range(args.steps):
+            r.render()
+            ms += r.stats.render_ms
+            paths += r.stats.paths
+        st = r.stats
+        out["mlt"].append({"chains": st.chains, "mutations_per_chain": st.mutations // st.chains,
+                           "value": paths / (ms / 1000.0), "ms_per_image": ms / args.steps,
+                           "acceptance": st.accepted / st.mutations, "kernel_launches": st.kernel_launches})
+    r = EnergyRedistributionRenderer(gs, seed=1, max_depth=5)
+    for _ in range(args.warmup):
+        r.render()
+    ms, paths = 0.0, 0
+    for _ in range(args.steps):
+        r.render()
+        ms += r.stats.render_ms
+        paths += r.stats.paths
+    st = r.stats
+    out["erpt"].append({"chains": st.chains, "value": paths / (ms / 1000.0), "ms_per_image": ms / args.steps,
+                        "acceptance": st.accepted / st.mutations, "kernel_launches": st.kernel_launches})
+    del gs
+    ctx.close()
+    if not args.no_cpu_baseline:
+        o = OracleScene(s)
+        cam = s.camera_struct()
+        t = time.perf_counter()
+        rr = o.render_mlt(cam, render_params(1, 1, 0.0, 5, 1), mlt_params(1, 10000), chains=64)
+        dt = time.perf_counter() - t
+        out["cpu_baseline_mlt"] = {"value": rr["paths"] / dt, "unit": "paths/s", "cores": 1, "kind": "port",
+                                   "sample": "1 mutation per pixel over 64 chains (%d paths, %.1f s)"
+                                   % (rr["paths"], dt)}
+        t = time.perf_counter()
+        re_ = o.render_erpt(cam, render_params(1, 1, 0.0, 5, 1), erpt_params(4, 1, 1))
+        dt = time.perf_counter() - t
+        out["cpu_baseline_erpt"] = {"value": re_["paths"] / dt, "unit": "paths/s", "cores": 1, "kind": "port",
+                                    "sample": "4 mutations per chain, 1 initial sample per pixel (%d paths, %.1f s)"
+                                    % (re_["paths"], dt)}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -453,8 +518,15 @@ def main():
                     help="aggregate paths/s of the seeded 64-scene batch through gbrt_render_batch")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-streams", type=int, default=0, help="streams for --batch (0: autotune)")
+    ap.add_argument("--chains", action="store_true",
+                    help="paths/s of the Metropolis and energy-redistribution renderers (Cornell box)")
+    ap.add_argument("--mlt-chains", type=lambda x: [int(v) for v in x.split(",")], default=[0, 4096, 1 << 20],
+                    help="chain counts for --chains (0: the library's default)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.chains:
+        run_chains(args)
+        return
     if args.batch:
         run_batch(args)
         return

@@ -516,6 +516,69 @@ gbrt_status gbrt_render_guided(gbrt_scene* scene, const gbrt_camera* camera,
                                gbrt_guide* guide, const gbrt_guide_params* gp,
                                float* film_bgr, gbrt_guide_stats* stats);
 
+/* ---- Markov-chain renderers over the primary sample space: the renderer's
+ *      MetropolisRenderer (src/metropolisrenderer.cpp:56-201) and
+ *      EnergyRedistributionRenderer (src/energyredistributionrenderer.cpp:
+ *      38-135), with MetropolisSample's mutations
+ *      (src/metropolissample.cpp:33-121). Reference semantics only. A sample
+ *      is a vector of 3 + 5 max_depth numbers in [0, 1]: camera position
+ *      over the image (0, 1), path length (2), direction sample i (3 + 2i,
+ *      4 + 2i), light sample k (3 + 2D + 3k, +1) and light choice (+2).
+ *      The chains run in parallel, one per path of a wavefront, and each
+ *      iteration traces every chain's proposal with the same extend / shade
+ *      / shadow kernels as gbrt_render. ---- */
+typedef struct gbrt_mlt_params {
+  int32_t mutations;        /* --met-mutations: mutations per pixel (16)      */
+  int32_t bootstrap;        /* --met-bootstrap: bootstrap samples (10000)     */
+  float large_step_prob;    /* --met-large-step-prob (0.1)                    */
+  float termination_prob;   /* --met-termination-prob (0.5)                   */
+  int64_t chains;           /* chains run in parallel (the renderer: its
+                               OpenMP threads); 0 = mutations x pixels / 16
+                               within [4096, 2^20]; at most mutations x
+                               pixels                                         */
+} gbrt_mlt_params;
+
+typedef struct gbrt_erpt_params {
+  int32_t mutations;        /* --erpt-mutations: mutations per chain (100)    */
+  int32_t x_samples;        /* --erpt-x-samples (2)                           */
+  int32_t y_samples;        /* --erpt-y-samples (2)                           */
+  int32_t pad;
+  int64_t batch_chains;     /* chains per wavefront; 0 = 2^20                 */
+} gbrt_erpt_params;
+
+typedef struct gbrt_chain_stats {
+  uint64_t paths;           /* paths traced (bootstrap / initial + proposals) */
+  uint64_t extension_rays, shadow_rays, nonfinite;
+  uint64_t chains;          /* Markov chains run                              */
+  uint64_t mutations;       /* proposals made                                 */
+  uint64_t accepted;        /* proposals accepted                             */
+  double normaliser;        /* MLT: b, the mean bootstrap luminance;
+                               ERPT: ed, the energy of one deposit            */
+  double render_ms;         /* device time                                    */
+  uint64_t kernel_launches;
+} gbrt_chain_stats;
+
+/* MetropolisRenderer::render. params supplies seed, max_depth (MAX_DEPTH)
+ * and semantics (GBRT_SEM_REFERENCE); the film (host, H x W x 3 BGR) is
+ * overwritten. Each chain starts from a bootstrap sample drawn in proportion
+ * to its luminance (systematic resampling over the chains; with one chain,
+ * the renderer's own choice) and makes mutations x pixels / chains
+ * mutations, depositing the current and the proposed sample with weights
+ * 1 - a and a. */
+gbrt_status gbrt_render_mlt(gbrt_scene* scene, const gbrt_camera* camera,
+                            const gbrt_render_params* params,
+                            const gbrt_mlt_params* mp, float* film_bgr,
+                            gbrt_chain_stats* stats);
+/* EnergyRedistributionRenderer::render: ed from one path per pixel corner
+ * (termination probability 0.1), then per pixel x_samples x y_samples
+ * jittered initial samples, each starting (int)(u + |c| / (mutations ed))
+ * chains of `mutations` small steps that deposit |c| ed / (|c| chains)
+ * per step. The film is overwritten. */
+gbrt_status gbrt_render_erpt(gbrt_scene* scene, const gbrt_camera* camera,
+                             const gbrt_render_params* params,
+                             const gbrt_erpt_params* ep, float* film_bgr,
+                             gbrt_chain_stats* stats);
+
 /* ---- scene files (SceneGrammar::parse + resolveVars + buildScene,
  *      src/sceneparser.cpp:36-156, src/sceneast.cpp:673-747,
  *      src/objreader.cpp:142-366) --------------------------------------- */

@@ -41,6 +41,13 @@ def lib():
                                  C.POINTER(C.c_uint64)]
         L.orc_camera_ray.argtypes = [C.POINTER(_abi.Camera), C.c_double, C.c_double, P]
         L.orc_tonemap.argtypes = [P, C.c_int, C.c_int, C.c_float, P]
+        L.orc_render_mlt.restype = C.c_int
+        L.orc_render_mlt.argtypes = [P, C.POINTER(_abi.Camera), C.POINTER(_abi.RenderParams),
+                                     C.POINTER(_abi.MltParams), C.c_int64, P, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_uint64)]
+        L.orc_render_erpt.restype = C.c_int
+        L.orc_render_erpt.argtypes = [P, C.POINTER(_abi.Camera), C.POINTER(_abi.RenderParams),
+                                      C.POINTER(_abi.ErptParams), P, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
         L.orc_stream_u.restype = C.c_float
         L.orc_stream_u.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32]
         _lib = L
@@ -89,6 +96,28 @@ class OracleScene:
         if rc != 0:
             raise RuntimeError("orc_render failed")
         return dict(film=film, sum=s, sumsq=q, paths=paths.value, rays=rays.value, shadow_rays=sh.value)
+
+    def render_mlt(self, camera, params, mp, chains):
+        """MetropolisRenderer with `chains` chains. Returns dict(film, b,
+        paths, mutations, accepted, chains)."""
+        film = np.zeros((camera.height, camera.width, 3), np.float32)
+        b = C.c_double()
+        counts = (C.c_uint64 * 4)()
+        if lib().orc_render_mlt(self.handle, C.byref(camera), C.byref(params), C.byref(mp), int(chains), _ptr(film),
+                                C.byref(b), counts) != 0:
+            raise RuntimeError("orc_render_mlt failed")
+        return dict(film=film, b=b.value, paths=counts[0], mutations=counts[1], accepted=counts[2], chains=counts[3])
+
+    def render_erpt(self, camera, params, ep):
+        """EnergyRedistributionRenderer. Returns dict(film, ed, paths,
+        mutations, accepted, chains)."""
+        film = np.zeros((camera.height, camera.width, 3), np.float32)
+        ed = C.c_double()
+        counts = (C.c_uint64 * 4)()
+        if lib().orc_render_erpt(self.handle, C.byref(camera), C.byref(params), C.byref(ep), _ptr(film), C.byref(ed),
+                                 counts) != 0:
+            raise RuntimeError("orc_render_erpt failed")
+        return dict(film=film, ed=ed.value, paths=counts[0], mutations=counts[1], accepted=counts[2], chains=counts[3])
 
     def close(self):
         if self.handle:

@@ -1529,6 +1529,260 @@ float orc_stream_u(uint64_t seed, uint64_t sample_id, uint32_t dim) {
 
 }  // extern "C"
 
+/* ================================================= Markov-chain renderers ==
+ * MetropolisRenderer::render (src/metropolisrenderer.cpp:56-201) and
+ * EnergyRedistributionRenderer::render (src/energyredistributionrenderer.cpp:
+ * 38-135) with MetropolisSample (src/metropolissample.cpp:33-121), restated
+ * with the counter-based stream in place of GSL and float primary-sample
+ * coordinates in place of QPointF's doubles. A sample is the vector
+ *   0,1 camera point over the image | 2 path length | 3+2i,4+2i direction
+ *   sample i | 3+2D+3k,+1 light sample k | 3+2D+3k+2 light choice k
+ * (D = max depth). The renderer's lightPathSamples and lightSample2 feed no
+ * computation of the unidirectional integrator and are not kept. The chains
+ * of the CUDA path run in parallel; here they run one after the other with
+ * the same keys, so both produce the same chains. */
+namespace chains {
+
+enum : uint64_t { kBoot = 1, kMutate = 2, kPick = 3, kEd = 4, kInit = 5, kFlow = 6 };
+inline uint64_t key(uint64_t seed, uint64_t tag, uint64_t id) { return streamKey(seed, (tag << 56) | id); }
+inline int dims(int D) { return 3 + 5 * D; }
+/* dimensions a small step moves: camera point, direction and light samples */
+inline bool moves(int d, int D) {
+  if (d == 2) return false;
+  if (d >= 3 + 2 * D) return (d - 3 - 2 * D) % 3 != 2;
+  return true;
+}
+
+/* mutate(qreal&, rng), src/metropolissample.cpp:62-78: a step of
+ * b exp(-log(b / a) u) (a = 1/1024, b = 1/64), negative when the second
+ * number is below 1/2, wrapped into [0, 1]. -log(16) rounded to float. */
+inline float mutateCoord(float s, float ux, float uy) {
+  const float b = 1.f / 64.f, logRatio = -2.772588722239781f;
+  float delta = b * std::exp(logRatio * ux);
+  if (uy < 0.5f) delta = -delta;
+  s += delta;
+  if (s < 0.f) s += 1.f;
+  if (s > 1.f) s -= 1.f;
+  return s;
+}
+
+/* cv::norm of a Vec3f: square root of the squares summed in double. */
+inline double cvNorm(C3 c) {
+  double s = double(c.b) * c.b;
+  s += double(c.g) * c.g;
+  s += double(c.r) * c.r;
+  return std::sqrt(s);
+}
+
+inline bool finite3(C3 c) { return std::isfinite(c.b) && std::isfinite(c.g) && std::isfinite(c.r); }
+
+struct Tracer {
+  Scene* s;
+  Camera camera;
+  int W, H, D, nL;
+  uint64_t paths = 0, rays = 0, shadow = 0, nonfinite = 0;
+  /* MetropolisSample::cameraPathFromSample (src/metropolissample.cpp:
+   * 120-127) + UniDiPathTracingIntegrator::integrate(path, ...): the path
+   * length from dimension 2 when p > 0 (MetropolisSample::mutatePathLength,
+   * :32-44), else D with Russian-roulette pdf 1. */
+  C3 trace(const float* u, float p) {
+    Draws dr;
+    dr.pathSamples.resize(D);
+    dr.lightSamples.resize(D);
+    dr.lightIndex.resize(D);
+    if (p > 0) {
+      int k = 0;
+      if (p < 1) k = int(std::floor(std::log(1.0 - double(u[2])) / std::log(1.0 - double(p))));
+      dr.pathLength = std::min(3 + std::max(k, 0), D);
+    } else dr.pathLength = D;
+    for (int i = 0; i < D; ++i) dr.pathSamples[i] = Sample(u[3 + 2 * i], u[4 + 2 * i]);
+    for (int k = 0; k < D; ++k) {
+      const float* l = u + 3 + 2 * D + 3 * k;
+      dr.lightSamples[k] = Sample(l[0], l[1]);
+      int li = nL > 0 ? int(l[2] * float(nL)) : 0;
+      dr.lightIndex[k] = std::min(li, std::max(nL - 1, 0));
+    }
+    float sx = u[0] * float(W), sy = u[1] * float(H);
+    Ray ray = camera.getRay(double(sx), double(sy));
+    Path path = createPath(ray, *s->root, dr, D, p > 0 ? p : 1.f, 3, &rays);
+    C3 c = integratePath(path, *s->root, s->lights, dr, &shadow);
+    ++paths;
+    if (!finite3(c)) { ++nonfinite; return C3(); }
+    return c;
+  }
+};
+
+/* MetropolisSample::getPos (src/metropolissample.cpp:129-136): the pixel of
+ * the camera point, clamped. */
+inline int pixelOf(float u, int n) { return std::max(0, std::min(int(double(u) * n), n - 1)); }
+
+}  // namespace chains
+
+extern "C" {
+
+/* MetropolisRenderer::render with `chains` parallel chains (the renderer: one
+ * per OpenMP thread). counts: paths traced, mutations, accepted, chains. */
+int orc_render_mlt(void* sp, const gbrt_camera* cam, const gbrt_render_params* prm, const gbrt_mlt_params* mp,
+                   int64_t chains_n, float* film, double* out_b, uint64_t* counts) {
+  using namespace chains;
+  Scene* s = static_cast<Scene*>(sp);
+  if (!s || !cam || !prm || !mp || chains_n <= 0 || mp->bootstrap <= 0 || mp->mutations <= 0) return 1;
+  Tracer tr;
+  tr.s = s;
+  tr.camera.init(vec3(cam->eye), vec3(cam->look_at), vec3(cam->up), cam->fov, cam->width, cam->height);
+  tr.W = cam->width; tr.H = cam->height; tr.D = prm->max_depth; tr.nL = int(s->lights.size());
+  const int D = tr.D, nd = dims(D), W = tr.W, H = tr.H;
+  const uint64_t seed = prm->seed;
+  /* Bootstrap (lines 77-100): large steps traced at full length
+   * (MetropolisSample starts with pathLength MAX_DEPTH, terminationProb 1). */
+  const int nb = mp->bootstrap;
+  std::vector<float> bootI(nb), u(nd);
+  std::vector<C3> bootL(nb);
+  float sumI = 0;
+  for (int i = 0; i < nb; ++i) {
+    uint64_t k = key(seed, kBoot, uint64_t(i));
+    for (int d = 0; d < nd; ++d) u[d] = streamU(k, d);
+    bootL[i] = tr.trace(u.data(), 0.f);
+    bootI[i] = lum(bootL[i]);
+    sumI += bootI[i];
+  }
+  const float b = sumI / nb;
+  /* Initial samples (lines 102-113) by systematic resampling: chain c takes
+   * the first bootstrap sample whose running sum exceeds (u + c) / chains of
+   * the total; with one chain this is the renderer's choice. */
+  std::vector<float> cum(nb);
+  float run = 0;
+  for (int i = 0; i < nb; ++i) { run += bootI[i]; cum[i] = run; }
+  const double u0 = streamU(key(seed, kPick, 0), 0);
+  const int64_t N = chains_n;
+  const int64_t total = int64_t(mp->mutations) * W * H;
+  const int64_t M = std::max<int64_t>(1, total / N);
+  std::vector<double> acc(size_t(W) * H * 3, 0.0);
+  auto deposit = [&](const float* su, float weight, C3 v) {
+    int x = pixelOf(su[0], W), y = pixelOf(su[1], H);
+    C3 dv = weight * v;
+    size_t o = (size_t(y) * W + x) * 3;
+    acc[o] += dv.b; acc[o + 1] += dv.g; acc[o + 2] += dv.r;
+  };
+  uint64_t accepted = 0;
+  std::vector<float> cur(nd), prop(nd);
+  for (int64_t c = 0; c < N; ++c) {
+    float off = float((u0 + double(c)) / double(N) * double(sumI));
+    int bi = int(std::upper_bound(cum.begin(), cum.end(), off) - cum.begin());
+    if (bi >= nb) bi = nb - 1;
+    uint64_t kb = key(seed, kBoot, uint64_t(bi));
+    for (int d = 0; d < nd; ++d) cur[d] = streamU(kb, d);
+    C3 curV = bootL[bi];
+    /* the chain (lines 131-190) */
+    for (int64_t t = 0; t < M; ++t) {
+      uint64_t k = key(seed, kMutate, uint64_t(t) * uint64_t(N) + uint64_t(c));
+      const bool large = streamU(k, 0) < mp->large_step_prob;
+      for (int d = 0; d < nd; ++d) {
+        if (d == 2) prop[d] = streamU(k, 2);
+        else if (large) prop[d] = streamU(k, 3 + 2 * d);
+        else prop[d] = moves(d, D) ? mutateCoord(cur[d], streamU(k, 3 + 2 * d), streamU(k, 4 + 2 * d)) : cur[d];
+      }
+      C3 newV = tr.trace(prop.data(), mp->termination_prob);
+      const float lc = lum(curV), ln = lum(newV);
+      float ratio = ln / lc;
+      float a = ratio < 1.f ? ratio : 1.f;  /* std::min<float>(1, ratio): NaN gives 1 */
+      if (lc > 0) deposit(cur.data(), 1 - a, curV * (1.f / lc * b / float(mp->mutations)));
+      if (ln > 0) deposit(prop.data(), a, newV * (1.f / ln * b / float(mp->mutations)));
+      if (streamU(k, 1) < a) { cur.swap(prop); curV = newV; ++accepted; }
+    }
+  }
+  for (size_t i = 0; i < acc.size(); ++i) film[i] = float(acc[i]);
+  if (out_b) *out_b = b;
+  if (counts) { counts[0] = tr.paths; counts[1] = uint64_t(N * M); counts[2] = accepted; counts[3] = uint64_t(N); }
+  return 0;
+}
+
+/* EnergyRedistributionRenderer::render. counts: paths traced, mutations,
+ * accepted, chains. */
+int orc_render_erpt(void* sp, const gbrt_camera* cam, const gbrt_render_params* prm, const gbrt_erpt_params* ep,
+                    float* film, double* out_ed, uint64_t* counts) {
+  using namespace chains;
+  Scene* s = static_cast<Scene*>(sp);
+  if (!s || !cam || !prm || !ep || ep->mutations <= 0 || ep->x_samples <= 0 || ep->y_samples <= 0) return 1;
+  Tracer tr;
+  tr.s = s;
+  tr.camera.init(vec3(cam->eye), vec3(cam->look_at), vec3(cam->up), cam->fov, cam->width, cam->height);
+  tr.W = cam->width; tr.H = cam->height; tr.D = prm->max_depth; tr.nL = int(s->lights.size());
+  const int D = tr.D, nd = dims(D), W = tr.W, H = tr.H, M = ep->mutations;
+  const int xs = ep->x_samples, ys = ep->y_samples, spp = xs * ys;
+  const uint64_t seed = prm->seed;
+  /* computeEd (lines 120-135): one path through each pixel corner with the
+   * integrator's termination probability 0.1, summed (here in double). */
+  double Sb = 0, Sg = 0, Sr = 0;
+  Draws dr;
+  for (int i = 0; i < H; ++i)
+    for (int j = 0; j < W; ++j) {
+      uint64_t k = key(seed, kEd, uint64_t(i) * W + j);
+      Ray ray = tr.camera.getRay(double(j), double(i));
+      drawPath(dr, D, 0.1f, tr.nL, nullptr, k);
+      Path path = createPath(ray, *s->root, dr, D, 0.1f, 3, &tr.rays);
+      C3 c = integratePath(path, *s->root, s->lights, dr, &tr.shadow);
+      ++tr.paths;
+      if (!finite3(c)) { ++tr.nonfinite; continue; }
+      Sb += c.b; Sg += c.g; Sr += c.r;
+    }
+  const float ed = float(cvNorm(C3(float(Sb), float(Sg), float(Sr))) / double(H * W * M));
+  std::vector<double> acc(size_t(W) * H * 3, 0.0);
+  std::vector<float> u(nd), y(nd), z(nd);
+  uint64_t chainId = 0, accepted = 0, mutations = 0;
+  for (int i = 0; i < H; ++i)
+    for (int j = 0; j < W; ++j)
+      for (int a = 0; a < xs; ++a)
+        for (int bb = 0; bb < ys; ++bb) {
+          /* JitteredSampler(xs, ys) point and MetropolisSample::initAtPixel */
+          const uint64_t g = (uint64_t(i) * W + j) * spp + uint64_t(a * ys + bb);
+          const uint64_t k = key(seed, kInit, g);
+          const double jx = (double(streamU(k, 0)) + a) / xs, jy = (double(streamU(k, 1)) + bb) / ys;
+          u[0] = float((j + jx) / W);
+          u[1] = float((i + jy) / H);
+          for (int d = 2; d < nd; ++d) u[d] = streamU(k, d);
+          const C3 c = tr.trace(u.data(), 0.f);
+          /* equalDispositionFlow (lines 83-118) */
+          const double nc = cvNorm(c);
+          const float me = float(M) * ed;
+          const int numChains = int(double(streamU(k, nd)) + nc / double(me));
+          if (numChains <= 0) continue;
+          const double sc = double(ed) / nc / numChains;
+          const C3 depVal(float(c.b * sc), float(c.g * sc), float(c.r * sc));
+          const double depNorm = cvNorm(depVal);
+          for (int r = 0; r < numChains; ++r, ++chainId) {
+            y = u;
+            C3 yV = c;
+            for (int m = 0; m < M; ++m) {
+              const uint64_t kk = key(seed, kFlow, chainId * uint64_t(M) + uint64_t(m));
+              for (int d = 0; d < nd; ++d)
+                z[d] = moves(d, D) ? mutateCoord(y[d], streamU(kk, 3 + 2 * d), streamU(kk, 4 + 2 * d)) : y[d];
+              const C3 zV = tr.trace(z.data(), 0.f);
+              ++mutations;
+              const float yLum = float(cvNorm(yV)), zLum = float(cvNorm(zV));
+              const float ratio = zLum / yLum;
+              const float q = ratio < 1.f ? ratio : 1.f;
+              const C3 yOld = yV;
+              if (q > streamU(kk, 1)) { y.swap(z); yV = zV; ++accepted; }
+              const int px = pixelOf(y[0], W), py = pixelOf(y[1], H);
+              const double in = 1.0 / cvNorm(yOld);
+              const float isp = 1.f / float(spp);
+              C3 t(float(depNorm * yOld.b), float(depNorm * yOld.g), float(depNorm * yOld.r));
+              t = C3(float(t.b * in), float(t.g * in), float(t.r * in));
+              t = t * isp;
+              size_t o = (size_t(py) * W + px) * 3;
+              acc[o] += t.b; acc[o + 1] += t.g; acc[o + 2] += t.r;
+            }
+          }
+        }
+  for (size_t i = 0; i < acc.size(); ++i) film[i] = float(acc[i]);
+  if (out_ed) *out_ed = ed;
+  if (counts) { counts[0] = tr.paths; counts[1] = mutations; counts[2] = accepted; counts[3] = chainId; }
+  return 0;
+}
+
+}  // extern "C"
+
 /* Tonemapper::map, src/tonemapper.cpp:31-56: RGB bytes of a BGR film. */
 extern "C" void orc_tonemap(const float* film, int w, int h, float gamma, unsigned char* rgb) {
   double ig = 1. / gamma;

@@ -92,6 +92,23 @@ class BatchStats(C.Structure):
                 ("kernel_launches", C.c_uint64)]
 
 
+class MltParams(C.Structure):
+    _fields_ = [("mutations", C.c_int32), ("bootstrap", C.c_int32), ("large_step_prob", C.c_float),
+                ("termination_prob", C.c_float), ("chains", C.c_int64)]
+
+
+class ErptParams(C.Structure):
+    _fields_ = [("mutations", C.c_int32), ("x_samples", C.c_int32), ("y_samples", C.c_int32), ("pad", C.c_int32),
+                ("batch_chains", C.c_int64)]
+
+
+class ChainStats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("nonfinite", C.c_uint64), ("chains", C.c_uint64), ("mutations", C.c_uint64),
+                ("accepted", C.c_uint64), ("normaliser", C.c_double), ("render_ms", C.c_double),
+                ("kernel_launches", C.c_uint64)]
+
+
 class GuideParams(C.Structure):
     _fields_ = [("guide_fraction", C.c_float), ("passes", C.c_int32), ("train_passes", C.c_int32),
                 ("steps_per_pass", C.c_int32), ("batch_samples", C.c_int32), ("learning_rate", C.c_float),
@@ -167,6 +184,10 @@ SIGNATURES = [
                                     C.POINTER(C.c_double), C.POINTER(BatchStats)]),
     ("gbrt_batch_autotune", C.c_int, [P, C.POINTER(BatchJob), C.c_int32, C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int64)]),
+    ("gbrt_render_mlt", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), C.POINTER(MltParams), P,
+                                  C.POINTER(ChainStats)]),
+    ("gbrt_render_erpt", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), C.POINTER(ErptParams), P,
+                                   C.POINTER(ChainStats)]),
     ("gbrt_guide_create", C.c_int, [P, C.POINTER(C.c_float), C.c_uint64, C.POINTER(P)]),
     ("gbrt_guide_destroy", C.c_int, [P]),
     ("gbrt_guide_get_weights", C.c_int, [P, P, C.c_size_t]),

@@ -70,6 +70,29 @@ struct PTParams {
   const double* film_sum;  // sums of the earlier passes (pixel estimates for the training weights)
   const double* pass_sum;  // sums of the current pass
   double inv_samples;      // 1 / samples per pixel in film_sum + pass_sum
+  const float* pss;        // primary samples of the Markov-chain renderers: dim d of slot s at pss[d * pss_stride + s]
+  int pss_stride;
+};
+
+// Where a path's random numbers come from. StreamSrc: the counter-based
+// stream of the path's sample index (the per-pixel renderers). PssSrc: a
+// stored primary-sample vector per slot (the Markov-chain renderers, whose
+// mutations move these numbers). Both use the dimension layout of dim_path /
+// dim_light.
+struct StreamSrc {
+  unsigned long long key;
+  __device__ __forceinline__ StreamSrc(const PTParams& P, int slot)
+      : key(stream_key(P.seed, P.g0 + (unsigned long long)slot)) {}
+  __device__ __forceinline__ float u(unsigned d) const { return stream_u(key, d); }
+  __device__ __forceinline__ int index(unsigned d, int n) const { return stream_index(key, d, n); }
+};
+struct PssSrc {
+  const float* p;
+  unsigned stride;
+  __device__ __forceinline__ PssSrc(const PTParams& P, int slot) : p(P.pss + slot), stride(unsigned(P.pss_stride)) {}
+  __device__ __forceinline__ float u(unsigned d) const { return __ldg(p + size_t(d) * stride); }
+  // floor(u * n) with the product in float, as the oracle computes it
+  __device__ __forceinline__ int index(unsigned d, int n) const { return int(__fmul_rn(u(d), float(n))); }
 };
 
 // Path state, structure of arrays indexed by slot (path index - g0).
@@ -113,6 +136,49 @@ constexpr int kRecComp = 6;
 constexpr int kRecOpen = 0x100;
 
 // ------------------------------------------------------------- raygen ----
+// Path length: min(3 + Geometric(p), D) (src/renderer.cpp:52-61), from the
+// uniform ul; D when p is 0.
+__device__ __forceinline__ int ref_path_length(const PTParams& P, float ul) {
+  if (!(P.term_p > 0.f)) return P.D;
+  int k = 0;
+  if (P.term_p < 1.f) {
+    // Geometric draw by inversion, floor(log(1 - u) / log(1 - p)). 1 - u is
+    // exact in float (u has 24 bits), so the float quotient differs from the
+    // double one the CPU oracle uses by a few ulp; only when it falls that
+    // close to an integer is it recomputed in double.
+    float x = logf(1.f - ul) * P.inv_log1mp;
+    float fx = floorf(x);
+    if (x - fx < 1e-5f * fmaxf(1.f, x) || fx + 1.f - x < 1e-5f * fmaxf(1.f, x))
+      fx = float(floor(log(1.0 - double(ul)) / log(1.0 - double(P.term_p))));
+    k = max(int(fx), 0);
+  }
+  return min(3 + k, P.D);
+}
+
+// A new path in slot: unit throughput, no radiance, the camera ray in the
+// first extension queue.
+__device__ __forceinline__ void start_path(const PTParams& P, const PTState& st, int slot, int plen, float dx,
+                                           float dy, float dz) {
+  st.alpha[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
+  st.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+  // ctl.w: reference semantics, "a stored vertex is pending"; physical
+  // semantics, "the previous vertex was specular (or the camera)".
+  st.ctl[slot] = make_int4(0, plen, 0, P.physical ? 1 : 0);
+  st.ext[0][2 * slot] = make_float4(P.cam.eye[0], P.cam.eye[1], P.cam.eye[2], kEps);
+  st.ext[0][2 * slot + 1] = make_float4(dx, dy, dz, CUDART_INF_F);
+  st.ext_slot[0][slot] = slot;
+}
+
+// Camera::getRay (src/camera.cpp:50-58) for the image point (sxp, syp) in
+// pixel units: image plane at z = -1 in camera space.
+__device__ __forceinline__ void camera_dir(const PTParams& P, float sxp, float syp, float& dx, float& dy, float& dz) {
+  float x = P.cam.l + (P.cam.r - P.cam.l) * (sxp + 0.5f) / float(P.cam.W);
+  float y = P.cam.t + (P.cam.b - P.cam.t) * (syp + 0.5f) / float(P.cam.H);
+  dx = x * P.cam.u[0] + y * P.cam.v[0] - P.cam.w[0];
+  dy = x * P.cam.u[1] + y * P.cam.v[1] - P.cam.w[1];
+  dz = x * P.cam.u[2] + y * P.cam.v[2] - P.cam.w[2];
+}
+
 __global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
   int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot == 0) {
@@ -135,39 +201,11 @@ __global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
   unsigned long long key = stream_key(P.seed, g);
   float sxp = float(px) + (stream_u(key, 0) + float(a)) / float(P.xs);
   float syp = float(py) + (stream_u(key, 1) + float(b)) / float(P.ys);
-  // Camera::getRay (src/camera.cpp:50-58): image plane at z = -1 in camera space.
-  float x = P.cam.l + (P.cam.r - P.cam.l) * (sxp + 0.5f) / float(P.cam.W);
-  float y = P.cam.t + (P.cam.b - P.cam.t) * (syp + 0.5f) / float(P.cam.H);
-  float dx = x * P.cam.u[0] + y * P.cam.v[0] - P.cam.w[0];
-  float dy = x * P.cam.u[1] + y * P.cam.v[1] - P.cam.w[1];
-  float dz = x * P.cam.u[2] + y * P.cam.v[2] - P.cam.w[2];
-  // Path length: min(3 + Geometric(p), D) (src/renderer.cpp:52-61). The
-  // physical estimator plays Russian roulette per vertex instead.
-  int plen = P.D;
-  if (P.term_p > 0.f && !P.physical) {
-    int k = 0;
-    if (P.term_p < 1.f) {
-      // Geometric draw by inversion, floor(log(1 - u) / log(1 - p)). 1 - u is
-      // exact in float (u has 24 bits), so the float quotient differs from the
-      // double one the CPU oracle uses by a few ulp; only when it falls that
-      // close to an integer is it recomputed in double.
-      float ul = stream_u(key, 2);
-      float x = logf(1.f - ul) * P.inv_log1mp;
-      float fx = floorf(x);
-      if (x - fx < 1e-5f * fmaxf(1.f, x) || fx + 1.f - x < 1e-5f * fmaxf(1.f, x))
-        fx = float(floor(log(1.0 - double(ul)) / log(1.0 - double(P.term_p))));
-      k = max(int(fx), 0);
-    }
-    plen = min(3 + k, P.D);
-  }
-  st.alpha[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
-  st.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-  // ctl.w: reference semantics, "a stored vertex is pending"; physical
-  // semantics, "the previous vertex was specular (or the camera)".
-  st.ctl[slot] = make_int4(0, plen, 0, P.physical ? 1 : 0);
-  st.ext[0][2 * slot] = make_float4(P.cam.eye[0], P.cam.eye[1], P.cam.eye[2], kEps);
-  st.ext[0][2 * slot + 1] = make_float4(dx, dy, dz, CUDART_INF_F);
-  st.ext_slot[0][slot] = slot;
+  float dx, dy, dz;
+  camera_dir(P, sxp, syp, dx, dy, dz);
+  // The physical estimator plays Russian roulette per vertex instead.
+  const int plen = P.physical ? P.D : ref_path_length(P, stream_u(key, 2));
+  start_path(P, st, slot, plen, dx, dy, dz);
 }
 
 // Adds a warp's traversal counters to two global totals (all lanes call it).
@@ -281,13 +319,13 @@ __device__ __forceinline__ void load_pending(const PTState& st, int slot, Vertex
 // Next-event estimation at a stored vertex: UniDiPathTracingIntegrator lines
 // 83-99 with Light::getIntensity for light lightIndex[k]. A non-zero
 // contribution goes to the shadow queue with its shadow ray.
-template <bool EXT>
+template <bool EXT, class R>
 __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, const PTState& st, int slot,
-                                    unsigned long long key, const Vertex& vx, V3f alpha, int k) {
+                                    const R& rs, const Vertex& vx, V3f alpha, int k) {
   if (S.n_lights <= 0 || vx.mat < 0) return;
   unsigned dl = dim_light(P.D, k);
-  float lx = stream_u(key, dl), ly = stream_u(key, dl + 1);
-  int li = min(stream_index(key, dl + 2, S.n_lights), S.n_lights - 1);  // floor(u * n)
+  float lx = rs.u(dl), ly = rs.u(dl + 1);
+  int li = min(rs.index(dl + 2, S.n_lights), S.n_lights - 1);  // floor(u * n)
   const DevLight& Lt = S.lights[li];
   V3f dir, Le, sd;
   float stmax;
@@ -339,7 +377,7 @@ __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, con
 // Renderer::createPath (src/renderer.cpp:73-104) for one iteration, with the
 // stored-vertex bookkeeping of UniDiPathTracingIntegrator::integrate(path)
 // done in streaming form (see the file comment).
-template <bool EXT>
+template <bool EXT, class R>
 __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTState st, int cur) {
   const int n = st.counts[cur];
   const int nxt = cur ^ 1;
@@ -350,7 +388,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
     int4 c = st.ctl[slot];
     int i = c.x, plen = c.y, nst = c.z;
     bool pend = c.w != 0;
-    const unsigned long long key = stream_key(P.seed, P.g0 + (unsigned long long)slot);
+    const R rs(P, slot);
     const V3f d = v3(rd.x, rd.y, rd.z);
     const bool envHit = h.rec == -1 && S.env_light >= 0 && isinf(rd.w) && rd.w > 0.f;
     if (h.rec == -1 && !envHit) {
@@ -358,7 +396,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
       if (pend) {
         Vertex pv; V3f pa; int k;
         load_pending(st, slot, pv, pa, k);
-        nee<EXT>(S, P, st, slot, key, pv, pa, k);
+        nee<EXT>(S, P, st, slot, rs, pv, pa, k);
         st.ctl[slot] = make_int4(i, plen, nst, 0);
       }
       continue;
@@ -435,7 +473,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
     }
     float pdf;
     V3f f;
-    const V3f out = out_direction<EXT>(S, vx, stream_u(key, dim_path(i)), stream_u(key, dim_path(i) + 1), pdf, f);
+    const V3f out = out_direction<EXT>(S, vx, rs.u(dim_path(i)), rs.u(dim_path(i) + 1), pdf, f);
     if (mat_specular(S.materials, vx.mat)) {
       // Specular vertices are not stored (lines 87-91).
       if (i == plen - 1 && plen < P.D) plen++;
@@ -445,7 +483,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
       } else if (pend) {
         Vertex pv; V3f pa; int k;
         load_pending(st, slot, pv, pa, k);
-        nee<EXT>(S, P, st, slot, key, pv, pa, k);
+        nee<EXT>(S, P, st, slot, rs, pv, pa, k);
         pend = false;
       }
       st.ctl[slot] = make_int4(i, plen, nst, pend ? 1 : 0);
@@ -456,7 +494,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
     if (pend) {
       Vertex pv; V3f pa; int k;
       load_pending(st, slot, pv, pa, k);
-      nee<EXT>(S, P, st, slot, key, pv, pa, k);
+      nee<EXT>(S, P, st, slot, rs, pv, pa, k);
     }
     const float4 a4 = st.alpha[slot];
     const V3f alpha = v3(a4.x, a4.y, a4.z);
@@ -475,7 +513,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
     }
     if (ends) {
       // This vertex is the last stored one: next-event estimation now.
-      nee<EXT>(S, P, st, slot, key, vx, alpha, k);
+      nee<EXT>(S, P, st, slot, rs, vx, alpha, k);
       st.ctl[slot] = make_int4(i, plen, nst, 0);
     } else {
       st.pv_p[slot] = make_float4(vx.p.x, vx.p.y, vx.p.z, __int_as_float(vx.mat));
@@ -920,7 +958,7 @@ static TraceKernels pick_kernels(const gbrt_scene* s, bool count) {
 // scenes that have textures or CSG objects.
 static void (*pick_shade(const gbrt_scene* s, bool physical, bool guided))(DeviceScene, PTParams, PTState, int) {
   const bool ext = s->view.tri_uv != nullptr || s->view.csg_prog != nullptr;
-  if (!physical) return ext ? k_shade<true> : k_shade<false>;
+  if (!physical) return ext ? k_shade<true, StreamSrc> : k_shade<false, StreamSrc>;
   if (guided) return ext ? k_shade_phys<true, true> : k_shade_phys<true, false>;
   return ext ? k_shade_phys<false, true> : k_shade_phys<false, false>;
 }
@@ -978,7 +1016,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   B = std::min<long long>(B, (long long)total);
   B = std::max<long long>(B, 1);
 
-  PTParams P;
+  PTParams P{};
   init_params(P, *cam, *prm, total);
 
   Buffers buf(stream);
@@ -1207,7 +1245,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
   const unsigned long long total = npix * (unsigned long long)spp;
   long long B = prm->batch_paths > 0 ? prm->batch_paths : kNoAllocBatch;
   B = std::max<long long>(1, std::min<long long>(B, (long long)total));
-  PTParams P;
+  PTParams P{};
   init_params(P, *cam, *prm, total);
 
   // The array keeps the previous call's contents: clear what starts at zero.
@@ -1435,7 +1473,7 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   gbrt_status status = GBRT_OK;
   for (int pass = 0;; ++pass) {
     if (gp->passes > 0 && pass >= gp->passes) break;
-    PTParams P;
+    PTParams P{};
     init_params(P, *cam, *prm, total);
     P.seed = pass_seed(prm->seed, pass);
     const bool record = training && pass < gp->train_passes;
@@ -1601,7 +1639,7 @@ static cudaError_t enqueue_job(gbrt_scene* s, const gbrt_camera& cam, const gbrt
   const unsigned long long total = npix * (unsigned long long)spp;
   long long B = prm.batch_paths > 0 ? prm.batch_paths : cap;
   B = std::max<long long>(1, std::min<long long>(B, (long long)total));
-  PTParams P;
+  PTParams P{};
   init_params(P, cam, prm, total);
   Buffers buf(stream);
   PTState st;
@@ -1884,3 +1922,7 @@ gbrt_status gbrt_batch_autotune(gbrt_ctx* ctx, const gbrt_batch_job* jobs, int32
 }
 
 }  // extern "C"
+
+// The Markov-chain renderers (Metropolis, energy redistribution) share this
+// translation unit's wavefront kernels.
+#include "chains.cuh"

@@ -53,19 +53,19 @@ __device__ __forceinline__ V3f ld3(const float* p) { return {p[0], p[1], p[2]}; 
 // owns the stream key = mix64(seed ^ mix64(sample_id + c)); its d-th uniform
 // is the top 24 bits of mix64(key + d * phi). The CPU oracle defines the same
 // stream, so both can draw identical numbers.
-__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+__host__ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
   return z ^ (z >> 31);
 }
-__device__ __forceinline__ unsigned long long stream_key(unsigned long long seed, unsigned long long sample_id) {
+__host__ __device__ __forceinline__ unsigned long long stream_key(unsigned long long seed, unsigned long long sample_id) {
   return mix64(seed ^ mix64(sample_id + 0x632BE59BD9B4E019ull));
 }
 // The top 24 bits of the d-th draw; stream_u is this value / 2^24.
-__device__ __forceinline__ unsigned stream_bits(unsigned long long key, unsigned dim) {
+__host__ __device__ __forceinline__ unsigned stream_bits(unsigned long long key, unsigned dim) {
   return unsigned(mix64(key + (unsigned long long)dim * 0x9E3779B97F4A7C15ull) >> 40);
 }
-__device__ __forceinline__ float stream_u(unsigned long long key, unsigned dim) {
+__host__ __device__ __forceinline__ float stream_u(unsigned long long key, unsigned dim) {
   return float(stream_bits(key, dim)) * (1.0f / 16777216.0f);
 }
 // floor(u * n) for u = bits / 2^24, exactly, in integer arithmetic.
