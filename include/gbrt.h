@@ -27,6 +27,7 @@
  *   [+0, +n_spheres)                    spheres
  *   [+0, +n_planes)                     planes
  *   [+0, +n_csg)                        CSG objects (one id per object)
+ *   [+0, +n_instances)                  mesh instances (one id per instance)
  *
  * Threading: calls on one gbrt_ctx are serialised by the caller; distinct
  * contexts are independent. All device memory is owned by the library.
@@ -163,6 +164,27 @@ typedef struct gbrt_csg_node {
   int32_t material;     /* leaves */
 } gbrt_csg_node;
 
+/* Instanced triangle meshes (a two-level BVH). A mesh is a triangle soup in
+ * its own space, built into its own BVH once; an instance places a mesh with
+ * an affine object-to-world transform. As IntersectableInstance
+ * (src/intersectableinstance.cpp:24-46, src/hitrecord.h:79-84): a ray is
+ * moved into the mesh's space by the inverse transform (the direction is not
+ * renormalised, so the ray parameter t is the same in both spaces) and the
+ * normal back by the inverse transpose. Mesh triangles take the default
+ * texture coordinates. Each instance is one primitive in the id space. */
+typedef struct gbrt_mesh {
+  const float* tri_pos;     /* n_tri x 9 */
+  const float* tri_nrm;     /* optional n_tri x 9 (as gbrt_scene_desc.tri_nrm) */
+  const int32_t* tri_mat;   /* optional n_tri (NULL: material 0) */
+  int64_t n_tri;
+} gbrt_mesh;
+
+typedef struct gbrt_instance {
+  float transform[12];      /* row-major 3 x 4, object -> world */
+  int32_t mesh;             /* index into gbrt_scene_desc.meshes */
+  int32_t pad;
+} gbrt_instance;
+
 typedef struct gbrt_scene_desc {
   const gbrt_material* materials; int32_t n_materials;
   /* triangle soup: n_tri x 9 positions (p1,p2,p3); optional n_tri x 9 normals
@@ -182,6 +204,9 @@ typedef struct gbrt_scene_desc {
   /* CSG objects: csg_roots[i] is the root node (in csg_nodes) of object i */
   const gbrt_csg_node* csg_nodes; int32_t n_csg_nodes;
   const int32_t* csg_roots; int32_t n_csg;
+  /* instanced meshes */
+  const gbrt_mesh* meshes; int32_t n_meshes;
+  const gbrt_instance* instances; int32_t n_instances;
 } gbrt_scene_desc;
 
 typedef enum gbrt_scene_flags {

@@ -759,6 +759,66 @@ static Intersectable* buildBVH(std::vector<Intersectable*> items, std::vector<st
   return node;
 }
 
+/* IntersectableInstance, src/intersectableinstance.cpp:24-46 with
+ * HitRecord::transform, src/hitrecord.h:79-84: the ray moved into the
+ * child's space by the inverse transform (origin as a point, direction as a
+ * vector, not renormalised, each row summed left to right), the hit point
+ * mapped back, the normal by the inverse transpose. Here the inverse is the
+ * affine one computed in double from the cofactors (as the CUDA path does)
+ * and the mapped normal is normalised; the hit reports the instance's id. */
+struct IntersectableInstance : Intersectable {
+  float fwd[12], inv[12];  /* row-major 3 x 4: object -> world, world -> object */
+  Intersectable* child = nullptr;
+  static V3 mapP(const float* m, V3 p) {
+    return V3(((m[0] * p.x + m[1] * p.y) + m[2] * p.z) + m[3], ((m[4] * p.x + m[5] * p.y) + m[6] * p.z) + m[7],
+              ((m[8] * p.x + m[9] * p.y) + m[10] * p.z) + m[11]);
+  }
+  static V3 mapV(const float* m, V3 v) {
+    return V3((m[0] * v.x + m[1] * v.y) + m[2] * v.z, (m[4] * v.x + m[5] * v.y) + m[6] * v.z,
+              (m[8] * v.x + m[9] * v.y) + m[10] * v.z);
+  }
+  Hit intersect(const Ray& ray) const override {
+    Ray tr(mapP(inv, ray.o), mapV(inv, ray.d), ray.from, ray.to);
+    Hit h = child->intersect(tr);
+    if (!h.intersects()) return h;
+    h.point = V4(mapP(fwd, h.point.affine()), 1);
+    h.ray = ray;
+    V3 n = h.normal;
+    h.normal = V3(inv[0] * n.x + inv[4] * n.y + inv[8] * n.z, inv[1] * n.x + inv[5] * n.y + inv[9] * n.z,
+                  inv[2] * n.x + inv[6] * n.y + inv[10] * n.z).normalized();
+    h.prim = prim;
+    return h;
+  }
+  /* IntersectableInstance::createBoundingBox: the child's box corners mapped */
+  AABB bbox() const override {
+    AABB c = child->bbox(), b;
+    for (int k = 0; k < 8; ++k)
+      b.includePoint(mapP(fwd, V3((k & 1) ? c.mx.x : c.mn.x, (k & 2) ? c.mx.y : c.mn.y, (k & 4) ? c.mx.z : c.mn.z)));
+    return b;
+  }
+};
+
+/* The prim id of an instanced mesh's triangles: never an ignored prim. */
+static const int kMeshTrianglePrim = -0x7ffffff0;
+
+/* Inverse of an affine row-major 3 x 4 matrix in double, rounded to float. */
+static bool affineInverse(const float in[12], float out[12]) {
+  const double a00 = in[0], a01 = in[1], a02 = in[2], a10 = in[4], a11 = in[5], a12 = in[6];
+  const double a20 = in[8], a21 = in[9], a22 = in[10];
+  const double c00 = a11 * a22 - a12 * a21, c01 = a12 * a20 - a10 * a22, c02 = a10 * a21 - a11 * a20;
+  const double det = a00 * c00 + a01 * c01 + a02 * c02;
+  if (!(det != 0.0) || !std::isfinite(det)) return false;
+  const double inv[3][3] = {{c00 / det, (a02 * a21 - a01 * a22) / det, (a01 * a12 - a02 * a11) / det},
+                            {c01 / det, (a00 * a22 - a02 * a20) / det, (a02 * a10 - a00 * a12) / det},
+                            {c02 / det, (a01 * a20 - a00 * a21) / det, (a00 * a11 - a01 * a10) / det}};
+  const double t[3] = {in[3], in[7], in[11]};
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) out[4 * r + c] = float(inv[r][c]);
+    out[4 * r + 3] = float(-(inv[r][0] * t[0] + inv[r][1] * t[1] + inv[r][2] * t[2]));
+  }
+  return true;
+}
+
 /* ---------------------------------------------------------------- Light -- */
 
 struct Light : Intersectable {
@@ -1034,6 +1094,35 @@ static Scene* buildScene(const gbrt_scene_desc* d, bool useBVH) {
     o->prim = pid;
     s->pool.emplace_back(o);
     top.push_back(o);
+  }
+  /* Instanced meshes: each instance gets a BVH of its mesh's triangles (the
+   * renderer's BVHCreator builds one per instance node, sceneast.cpp:
+   * 184-205). */
+  for (int i = 0; i < d->n_instances; ++i, ++pid) {
+    const gbrt_instance& in = d->instances[i];
+    const gbrt_mesh& gm = d->meshes[in.mesh];
+    std::vector<Intersectable*> tris;
+    for (int64_t k = 0; k < gm.n_tri; ++k) {
+      const float* p = gm.tri_pos + 9 * k;
+      const Material* m = mat(gm.tri_mat ? gm.tri_mat[k] : 0);
+      Triangle* t = nullptr;
+      if (gm.tri_nrm) {
+        const float* n = gm.tri_nrm + 9 * k;
+        if (!(vec3(n).isNull() || vec3(n + 3).isNull() || vec3(n + 6).isNull()))
+          t = new Triangle(vec3(p), vec3(p + 3), vec3(p + 6), vec3(n), vec3(n + 3), vec3(n + 6), m);
+      }
+      if (!t) t = new Triangle(vec3(p), vec3(p + 3), vec3(p + 6), m);
+      t->prim = kMeshTrianglePrim;
+      s->pool.emplace_back(t);
+      tris.push_back(t);
+    }
+    auto* inst = new IntersectableInstance();
+    std::memcpy(inst->fwd, in.transform, sizeof inst->fwd);
+    if (!affineInverse(in.transform, inst->inv)) { delete inst; continue; }
+    inst->child = buildBVH(tris, s->pool);
+    inst->prim = pid;
+    s->pool.emplace_back(inst);
+    top.push_back(inst);
   }
   s->nPrims = pid;
   if (useBVH && !top.empty()) {

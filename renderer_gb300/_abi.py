@@ -43,6 +43,15 @@ class CsgNode(C.Structure):
                 ("material", C.c_int32)]
 
 
+class Mesh(C.Structure):
+    _fields_ = [("tri_pos", C.POINTER(C.c_float)), ("tri_nrm", C.POINTER(C.c_float)),
+                ("tri_mat", C.POINTER(C.c_int32)), ("n_tri", C.c_int64)]
+
+
+class Instance(C.Structure):
+    _fields_ = [("transform", C.c_float * 12), ("mesh", C.c_int32), ("pad", C.c_int32)]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("materials", C.POINTER(Material)), ("n_materials", C.c_int32),
                 ("tri_pos", C.POINTER(C.c_float)), ("tri_nrm", C.POINTER(C.c_float)),
@@ -55,7 +64,9 @@ class SceneDesc(C.Structure):
                 ("env", C.POINTER(EnvMap)), ("flags", C.c_int32),
                 ("textures", C.POINTER(Texture)), ("n_textures", C.c_int32),
                 ("csg_nodes", C.POINTER(CsgNode)), ("n_csg_nodes", C.c_int32),
-                ("csg_roots", C.POINTER(C.c_int32)), ("n_csg", C.c_int32)]
+                ("csg_roots", C.POINTER(C.c_int32)), ("n_csg", C.c_int32),
+                ("meshes", C.POINTER(Mesh)), ("n_meshes", C.c_int32),
+                ("instances", C.POINTER(Instance)), ("n_instances", C.c_int32)]
 
 
 class Camera(C.Structure):

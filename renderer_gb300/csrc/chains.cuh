@@ -433,7 +433,7 @@ struct Wave {
 static Wave make_wave(gbrt_scene* s, bool pss) {
   Wave w;
   w.tk = pick_kernels(s, false);
-  const bool ext = s->view.tri_uv != nullptr || s->view.csg_prog != nullptr;
+  const bool ext = ext_scene(s);
   if (pss) w.shade = ext ? k_shade<true, PssSrc> : k_shade<false, PssSrc>;
   else w.shade = ext ? k_shade<true, StreamSrc> : k_shade<false, StreamSrc>;
   int per = 0;
@@ -456,7 +456,7 @@ static unsigned long long run_wave(gbrt_scene* s, const Wave& w, const PTParams&
   return 3ull * unsigned(P.D);
 }
 
-static cudaError_t alloc_state(Buffers& buf, PTState& st, long long B) {
+static cudaError_t alloc_state(gbrt_scene* s, Buffers& buf, PTState& st, long long B) {
   std::memset(&st, 0, sizeof st);
   cudaError_t e = cudaSuccess;
   auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
@@ -465,6 +465,7 @@ static cudaError_t alloc_state(Buffers& buf, PTState& st, long long B) {
   A(buf.alloc(&st.ext[0], 2 * B)); A(buf.alloc(&st.ext[1], 2 * B));
   A(buf.alloc(&st.ext_slot[0], B)); A(buf.alloc(&st.ext_slot[1], B));
   A(buf.alloc(&st.hits, B));
+  if (s->view.inst) A(buf.alloc(&st.hit_inst, B));
   A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
   A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
   if (e != cudaSuccess) return e;
@@ -541,7 +542,7 @@ static gbrt_status mlt_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_re
 
   Buffers buf(stream);
   PTState st;
-  cudaError_t e = alloc_state(buf, st, B);
+  cudaError_t e = alloc_state(s, buf, st, B);
   float *cur = nullptr, *prop = nullptr, *d_film = nullptr;
   float4 *curV = nullptr, *bootL = nullptr;
   double* d_sum = nullptr;
@@ -661,7 +662,7 @@ static gbrt_status erpt_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_r
 
   Buffers buf(stream);
   PTState st;
-  cudaError_t e = alloc_state(buf, st, B);
+  cudaError_t e = alloc_state(s, buf, st, B);
   chain::ErptArgs EA;
   std::memset(&EA, 0, sizeof EA);
   float* d_film = nullptr;

@@ -9,7 +9,13 @@
 //              sphere        (centre, kind) (radius, 0, 0, -) (0, 0, 0, prim)
 //              parallelogram (origin, kind) (u, -) (v, prim)
 //              CSG object    (box lo, kind) (box hi, program start) (program length, 0, 0, prim)
+//              instance      (box lo, kind) (instance, 0, 0, 0) (0, 0, 0, prim)
 //            kind and prim are int bit patterns in the w lanes.
+//   Two-level scenes: the nodes and records of every instanced mesh follow
+//   the top-level ones in the same arrays (absolute indices); a mesh's
+//   triangle records carry the prim id kMeshTriangle.
+//   inst   : n_inst x 64 B    world-to-object 3 x 4 rows (3 float4), then
+//                             (mesh root node, prim id, mesh, -) as ints
 //   meta   : n_recs x 16 B    (prim id, material, normal index or -1, light)
 //   tri_nrm: per smooth triangle 3 normals (9 floats, padded to 12)
 //   planes : n_planes x float4 plane vector; plane_meta (prim, material)
@@ -25,7 +31,14 @@
 
 namespace gbrt {
 
-enum RecKind : int32_t { kRecTriangle = 0, kRecSphere = 1, kRecParallelogram = 2, kRecCSG = 3 };
+enum RecKind : int32_t { kRecTriangle = 0, kRecSphere = 1, kRecParallelogram = 2, kRecCSG = 3, kRecInstance = 4 };
+
+// Prim id of an instanced mesh's triangle records (a hit reports its
+// instance's id instead); never equal to a shadow ray's ignored prim.
+constexpr int32_t kMeshTriangle = -0x7ffffff0;
+// Traversal stack entry that returns from an instance's mesh to world space
+// (no leaf encoding reaches it: records are fewer than 2^27).
+constexpr int32_t kInstPop = -0x7fffffff - 1;
 
 // Material kinds on the device (gbrt_material_type plus the two emitters that
 // are their own material in the renderer: AreaLight and EnvironmentMap).
@@ -88,6 +101,9 @@ struct DeviceScene {
   // (gbrt_csg_node), and the objects' postfix programs of node indices.
   const float4* csg_nodes;
   const int32_t* csg_prog;
+  // Instances (null when none): four float4 each, see above.
+  const float4* inst;
+  int32_t n_inst;
 };
 
 // Internal hit encoding of the traversal kernels.

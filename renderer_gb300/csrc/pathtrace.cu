@@ -107,6 +107,7 @@ struct PTState {
   float4* ext[2];  // extension queues: (o, tmin), (d, tmax) per entry
   int* ext_slot[2];
   RawHit* hits;
+  int* hit_inst;   // instance of each hit, two-level scenes only (else null)
   float4* sh_ray;  // shadow queue: (o, tmin), (d, tmax)
   float4* sh_c;    // contribution, ignore prim in w (int bits)
   int* sh_slot;
@@ -229,7 +230,7 @@ __device__ __forceinline__ void warp_add_counters(TraceCounters c, unsigned long
 // counts[0] and zeroes work[0]; k_extend on queue cur zeroes, before shade and
 // shadow run, counts[cur^1] (next extension queue), counts[2] (shadow queue),
 // work[cur^1] (next extend) and work[2] (this iteration's shadow pass).
-template <bool COUNT, bool WT, int STACK, bool CSG>
+template <bool COUNT, bool WT, int STACK, bool GEN>
 __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState st, int cur) {
   const int n = st.counts[cur];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -252,13 +253,15 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState s
     if (i >= n) continue;
     TRay r = make_tray(rays[2 * i], rays[2 * i + 1]);
     RawHit h;
-    h.rec = trace_ray<false, COUNT, WT, STACK, CSG>(S, r, -1, h.t, h.u, h.v, st.err, &cnt);
+    int32_t inst = -1;
+    h.rec = trace_ray<false, COUNT, WT, STACK, GEN>(S, r, -1, h.t, h.u, h.v, st.err, &cnt, &inst);
     st.hits[i] = h;
+    if (GEN && S.inst) st.hit_inst[i] = inst;
   }
   if (COUNT) warp_add_counters(cnt, &st.tally[3], &st.tally[4]);
 }
 
-template <bool COUNT, bool WT, int STACK, bool CSG>
+template <bool COUNT, bool WT, int STACK, bool GEN>
 __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState st) {
   const int n = st.counts[2];
   if (blockIdx.x == 0 && threadIdx.x == 0) st.tally[1] += (unsigned long long)n;
@@ -275,7 +278,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState s
     float4 c = st.sh_c[i];
     TRay r = make_tray(st.sh_ray[2 * i], st.sh_ray[2 * i + 1]);
     float t, u, v;
-    int32_t rec = trace_ray<true, COUNT, WT, STACK, CSG>(S, r, __float_as_int(c.w), t, u, v, st.err, &cnt);
+    int32_t rec = trace_ray<true, COUNT, WT, STACK, GEN>(S, r, __float_as_int(c.w), t, u, v, st.err, &cnt);
     if (rec == -1) {
       float4* L = st.L + st.sh_slot[i];
       atomicAdd(&L->x, c.x);
@@ -438,6 +441,10 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
         } else {
           vx.n = ld3(S.lights[light].nhat);
         }
+        if (EXT && S.inst) {
+          const int in = st.hit_inst[q];
+          if (in >= 0) vx.n = instance_normal(S, in, vx.n);
+        }
       } else {
         const float4 pl = __ldg(&S.planes[-2 - h.rec]);
         vx.n = normalize(v3(pl.x, pl.y, pl.z));
@@ -598,8 +605,8 @@ __device__ __forceinline__ void nee_phys(const DeviceScene& S, const PTState& st
 // Normal (unflipped), material and texture coordinates of a surface hit that
 // is not an emitter; o, d: the ray.
 template <bool EXT>
-__device__ __forceinline__ void surface_normal(const DeviceScene& S, const RawHit& h, V3f o, V3f d, V3f x, V3f& nrm,
-                                               int& mat, float& tu, float& tv) {
+__device__ __forceinline__ void surface_normal(const DeviceScene& S, const RawHit& h, int inst, V3f o, V3f d, V3f x,
+                                               V3f& nrm, int& mat, float& tu, float& tv) {
   tu = 0.f;
   tv = 0.f;
   if (h.rec >= 0) {
@@ -624,6 +631,7 @@ __device__ __forceinline__ void surface_normal(const DeviceScene& S, const RawHi
     } else {
       nrm = normalize(x - v3(a.x, a.y, a.z));  // sphere
     }
+    if (EXT && inst >= 0) nrm = instance_normal(S, inst, nrm);
     if (EXT && S.tri_uv) hit_texcoords(S, h.rec, h.u, h.v, x, tu, tv);
   } else {
     const float4 pl = __ldg(&S.planes[-2 - h.rec]);
@@ -691,7 +699,7 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
     V3f nrm;
     int mat = -1;
     float tu, tv;
-    surface_normal<EXT>(S, h, v3(ro.x, ro.y, ro.z), d, x, nrm, mat, tu, tv);
+    surface_normal<EXT>(S, h, (EXT && S.inst) ? st.hit_inst[q] : -1, v3(ro.x, ro.y, ro.z), d, x, nrm, mat, tu, tv);
     const PhysBsdf b = phys_bsdf<EXT>(S, mat, tu, tv);
     if (b.kind <= 0) continue;
     const unsigned long long key = stream_key(P.seed, P.g0 + (unsigned long long)slot);
@@ -765,7 +773,7 @@ __global__ void __launch_bounds__(256) k_guide_prep(DeviceScene S, PTState st, i
       V3f nrm;
       int mat = -1;
       float tu, tv;
-      surface_normal<true>(S, h, v3(ro.x, ro.y, ro.z), d, x, nrm, mat, tu, tv);
+      surface_normal<true>(S, h, S.inst ? st.hit_inst[q] : -1, v3(ro.x, ro.y, ro.z), d, x, nrm, mat, tu, tv);
       const PhysBsdf b = phys_bsdf<true>(S, mat, tu, tv);
       if (b.kind >= 1 && b.kind <= 3) {
         const V3f wo = -normalize(d);
@@ -947,17 +955,21 @@ static TraceKernels pick_flags(bool count, bool wt, bool shortStack) {
   return wt ? pick_stack<false, true, G>(shortStack) : pick_stack<false, false, G>(shortStack);
 }
 // Traversal counters, watertight triangles, short stack when the tree is
-// shallow enough, the CSG leaf test only for scenes with CSG objects.
+// shallow enough, the general leaves (CSG objects, instances) only for scenes
+// that have them.
 static TraceKernels pick_kernels(const gbrt_scene* s, bool count) {
   const bool shortStack = stack_need(s->max_depth4) <= kShortStack;
-  if (s->view.csg_prog) return pick_flags<true>(count, s->watertight, shortStack);
+  if (s->view.csg_prog || s->view.inst) return pick_flags<true>(count, s->watertight, shortStack);
   return pick_flags<false>(count, s->watertight, shortStack);
 }
 
-// The shade kernel: estimator, guiding, and the texture / CSG code only for
-// scenes that have textures or CSG objects.
+// The shade kernel: estimator, guiding, and the texture / CSG / instance code
+// only for scenes that have textures, CSG objects or instances.
+static bool ext_scene(const gbrt_scene* s) {
+  return s->view.tri_uv != nullptr || s->view.csg_prog != nullptr || s->view.inst != nullptr;
+}
 static void (*pick_shade(const gbrt_scene* s, bool physical, bool guided))(DeviceScene, PTParams, PTState, int) {
-  const bool ext = s->view.tri_uv != nullptr || s->view.csg_prog != nullptr;
+  const bool ext = ext_scene(s);
   if (!physical) return ext ? k_shade<true, StreamSrc> : k_shade<false, StreamSrc>;
   if (guided) return ext ? k_shade_phys<true, true> : k_shade_phys<true, false>;
   return ext ? k_shade_phys<false, true> : k_shade_phys<false, false>;
@@ -1020,7 +1032,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   init_params(P, *cam, *prm, total);
 
   Buffers buf(stream);
-  PTState st;
+  PTState st{};
   cudaError_t e = cudaSuccess;
   double* d_sum = d_sum_in;
   auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
@@ -1029,6 +1041,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   A(buf.alloc(&st.ext[0], 2 * B)); A(buf.alloc(&st.ext[1], 2 * B));
   A(buf.alloc(&st.ext_slot[0], B)); A(buf.alloc(&st.ext_slot[1], B));
   A(buf.alloc(&st.hits, B));
+  if (s->view.inst) A(buf.alloc(&st.hit_inst, B));
   A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
   A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
   if (!d_sum) A(buf.alloc(&d_sum, npix * 3));
@@ -1144,7 +1157,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
 constexpr long long kNoAllocBatch = GBRT_NOALLOC_MAX_BATCH;
 
 struct NoAllocLayout {
-  size_t off[19];
+  size_t off[20];
   size_t bytes;
 };
 
@@ -1152,7 +1165,7 @@ constexpr size_t noalloc_align(size_t x) { return (x + 255) & ~size_t(255); }
 
 static NoAllocLayout noalloc_layout() {
   const size_t B = size_t(kNoAllocBatch);
-  const size_t sizes[19] = {
+  const size_t sizes[20] = {
       B * sizeof(float4), B * sizeof(float4), B * sizeof(int4),                          // alpha, L, ctl
       B * sizeof(float4), B * sizeof(float4), B * sizeof(float4), B * sizeof(float4),    // pending vertex
       2 * B * sizeof(float4), 2 * B * sizeof(float4),                                    // ext[0], ext[1]
@@ -1160,10 +1173,11 @@ static NoAllocLayout noalloc_layout() {
       B * sizeof(RawHit),                                                                // hits
       4 * B * sizeof(float4), 2 * B * sizeof(float4), 2 * B * sizeof(int),               // shadow queue
       4 * sizeof(int), 4 * sizeof(unsigned long long), 8 * sizeof(unsigned long long),   // counts, work, tally
-      sizeof(int)};                                                                      // err
+      sizeof(int),                                                                       // err
+      B * sizeof(int)};                                                                  // hit_inst
   NoAllocLayout L{};
   size_t o = 0;
-  for (int i = 0; i < 19; ++i) {
+  for (int i = 0; i < 20; ++i) {
     L.off[i] = o;
     o += noalloc_align(sizes[i]);
   }
@@ -1171,7 +1185,7 @@ static NoAllocLayout noalloc_layout() {
   return L;
 }
 
-// 65,536 paths x 304 bytes + counters, rounded up: 20 MiB.
+// 65,536 paths x 308 bytes + counters, rounded up: 20 MiB.
 constexpr size_t kNoAllocScratchBytes = size_t(20) << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -1219,7 +1233,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
   if (gs != GBRT_OK) return gs;
   cudaStream_t stream = ctx->stream;
   auto at = [&](int i) { return static_cast<void*>(base + Lay.off[i]); };
-  PTState st;
+  PTState st{};
   st.alpha = static_cast<float4*>(at(0));
   st.L = static_cast<float4*>(at(1));
   st.ctl = static_cast<int4*>(at(2));
@@ -1239,6 +1253,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
   st.work = static_cast<unsigned long long*>(at(16));
   st.tally = static_cast<unsigned long long*>(at(17));
   st.err = static_cast<int*>(at(18));
+  st.hit_inst = s->view.inst ? static_cast<int*>(at(19)) : nullptr;
 
   const unsigned long long npix = (unsigned long long)cam->width * cam->height;
   const int spp = prm->x_samples * prm->y_samples;
@@ -1414,6 +1429,7 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   A(buf.alloc(&st.ext[0], 2 * B)); A(buf.alloc(&st.ext[1], 2 * B));
   A(buf.alloc(&st.ext_slot[0], B)); A(buf.alloc(&st.ext_slot[1], B));
   A(buf.alloc(&st.hits, B));
+  if (s->view.inst) A(buf.alloc(&st.hit_inst, B));
   A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
   A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
   long long tcap = 0;
@@ -1652,6 +1668,7 @@ static cudaError_t enqueue_job(gbrt_scene* s, const gbrt_camera& cam, const gbrt
   A(buf.alloc(&st.ext[0], 2 * B)); A(buf.alloc(&st.ext[1], 2 * B));
   A(buf.alloc(&st.ext_slot[0], B)); A(buf.alloc(&st.ext_slot[1], B));
   A(buf.alloc(&st.hits, B));
+  if (s->view.inst) A(buf.alloc(&st.hit_inst, B));
   A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
   A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
   A(buf.alloc(&d_sum, npix * 3));

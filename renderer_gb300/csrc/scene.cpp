@@ -119,6 +119,49 @@ gbrt_status gather_leaf_order(gbrt_scene* s, const std::vector<float4>& recv, co
   return st;
 }
 
+// Inverse of the affine map x -> A x + t given as a row-major 3 x 4 matrix
+// [A | t], computed in double from the cofactors and rounded to float (the
+// oracle computes it the same way). False when A is singular.
+bool affine_inverse(const float in[12], float out[12]) {
+  const double a00 = in[0], a01 = in[1], a02 = in[2], a10 = in[4], a11 = in[5], a12 = in[6];
+  const double a20 = in[8], a21 = in[9], a22 = in[10];
+  const double c00 = a11 * a22 - a12 * a21, c01 = a12 * a20 - a10 * a22, c02 = a10 * a21 - a11 * a20;
+  const double det = a00 * c00 + a01 * c01 + a02 * c02;
+  if (!(det != 0.0) || !std::isfinite(det)) return false;
+  const double inv[3][3] = {{c00 / det, (a02 * a21 - a01 * a22) / det, (a01 * a12 - a02 * a11) / det},
+                            {c01 / det, (a00 * a22 - a02 * a20) / det, (a02 * a10 - a00 * a12) / det},
+                            {c02 / det, (a01 * a20 - a00 * a21) / det, (a00 * a11 - a01 * a10) / det}};
+  const double t[3] = {in[3], in[7], in[11]};
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) out[4 * r + c] = float(inv[r][c]);
+    out[4 * r + 3] = float(-(inv[r][0] * t[0] + inv[r][1] * t[1] + inv[r][2] * t[2]));
+  }
+  return true;
+}
+
+// A point through a row-major 3 x 4 affine matrix, each row summed left to
+// right in float (QMatrix4x4::map of an affine matrix).
+F3 map_point(const float m[12], F3 p) {
+  return {((m[0] * p.x + m[1] * p.y) + m[2] * p.z) + m[3], ((m[4] * p.x + m[5] * p.y) + m[6] * p.z) + m[7],
+          ((m[8] * p.x + m[9] * p.y) + m[10] * p.z) + m[11]};
+}
+
+// Relocates the child references of a mesh's nodes to the scene-wide node and
+// record arrays.
+void relocate_node4(Node4& n, int64_t node0, int64_t rec0) {
+  for (int k = 0; k < 4; ++k) {
+    const int32_t r = n.ref[k];
+    if (r == kEmptyRef) continue;
+    if (r >= 0) {
+      n.ref[k] = int32_t(r + node0);
+    } else {
+      const uint32_t lv = ~uint32_t(r);
+      const uint32_t first = (lv >> 4) + uint32_t(rec0);
+      n.ref[k] = int32_t(~(first << 4 | (lv & 15u)));
+    }
+  }
+}
+
 void free_scene(gbrt_scene* s) {
   for (void* p : s->allocations) cudaFree(p);
   s->allocations.clear();
@@ -403,6 +446,115 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     boxes.push_back(box);
   }
 
+  // Instanced meshes: every mesh an instance uses gets its own tree over its
+  // triangles (in its own space); each instance is one record of the top-level
+  // tree, boxed by its mesh's box through its transform, and one entry of the
+  // instance table (world-to-object rows, mesh root, prim id).
+  if (d->n_meshes < 0 || d->n_instances < 0 || (d->n_instances && (!d->instances || !d->meshes)))
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: bad mesh or instance tables");
+  struct MeshTree {
+    Collapsed c4;
+    std::vector<Rec> recs;  // leaf order
+    Box box;
+    int64_t node0 = 0, rec0 = 0;
+    bool used = false;
+  };
+  std::vector<MeshTree> meshTrees(size_t(d->n_meshes));
+  std::vector<float4> instTab(size_t(d->n_instances) * 4);
+  for (int i = 0; i < d->n_instances; ++i) {
+    const gbrt_instance& in = d->instances[i];
+    if (in.mesh < 0 || in.mesh >= d->n_meshes)
+      return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: instance of a mesh that does not exist");
+    for (int k = 0; k < 12; ++k)
+      if (!std::isfinite(in.transform[k]))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: non-finite instance transform");
+    meshTrees[in.mesh].used = true;
+  }
+  int meshDepth = 0;
+  int64_t meshRecs = 0;
+  for (int m = 0; m < d->n_meshes; ++m) {
+    MeshTree& mt = meshTrees[m];
+    if (!mt.used) continue;
+    const gbrt_mesh& gm = d->meshes[m];
+    if (gm.n_tri <= 0 || !gm.tri_pos)
+      return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: instance of an empty mesh");
+    meshRecs += gm.n_tri;
+    if (nRecs + d->n_lights + d->n_csg + d->n_instances + meshRecs >= (int64_t(1) << 27))
+      return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: more than 2^27 bounded primitives");
+    std::vector<Rec> mrecs;
+    std::vector<Box> mboxes;
+    mrecs.reserve(size_t(gm.n_tri));
+    mboxes.reserve(size_t(gm.n_tri));
+    for (int64_t i = 0; i < gm.n_tri; ++i) {
+      const float* p = gm.tri_pos + 9 * i;
+      if (!finite3(p) || !finite3(p + 3) || !finite3(p + 6))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: non-finite mesh vertex");
+      int32_t nidx = -1;
+      if (gm.tri_nrm) {
+        const float* n = gm.tri_nrm + 9 * i;
+        F3 n1 = f3(n), n2 = f3(n + 3), n3 = f3(n + 6);
+        if (!isNull(n1) && !isNull(n2) && !isNull(n3)) {
+          nidx = int32_t(nrm.size() / 12);
+          if (nidx < 0) return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: too many smooth triangles");
+          F3 q[3] = {normalized(n1), normalized(n2), normalized(n3)};
+          for (int k = 0; k < 3; ++k) { nrm.push_back(q[k].x); nrm.push_back(q[k].y); nrm.push_back(q[k].z); }
+          for (int k = 0; k < 3; ++k) nrm.push_back(0.f);
+        }
+      }
+      F3 p1 = f3(p), p2 = f3(p + 3), p3 = f3(p + 6);
+      Rec r{};
+      r.v[0] = p1.x; r.v[1] = p1.y; r.v[2] = p1.z; setW(r.v[3], kRecTriangle);
+      r.v[4] = p2.x; r.v[5] = p2.y; r.v[6] = p2.z; setW(r.v[7], 0);
+      r.v[8] = p3.x; r.v[9] = p3.y; r.v[10] = p3.z; setW(r.v[11], kMeshTriangle);
+      r.meta[0] = kMeshTriangle; r.meta[1] = matIndex(gm.tri_mat ? gm.tri_mat[i] : 0); r.meta[2] = nidx;
+      r.meta[3] = -1;
+      mrecs.push_back(r);
+      mboxes.push_back(boxOf({p1, p2, p3}));
+    }
+    BuildResult mbr = build_bvh(mboxes, BuildOptions());
+    if (mbr.max_depth > kMaxTreeDepth)
+      return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: mesh BVH deeper than the traversal stack");
+    mt.recs.resize(mrecs.size());
+    for (size_t k = 0; k < mbr.order.size(); ++k) mt.recs[k] = mrecs[mbr.order[k]];
+    mt.c4 = collapse_bvh4(mbr);
+    meshDepth = std::max(meshDepth, mt.c4.max_depth);
+    mt.box = mboxes[0];
+    for (const Box& b : mboxes)
+      for (int k = 0; k < 3; ++k) { mt.box.lo[k] = std::min(mt.box.lo[k], b.lo[k]); mt.box.hi[k] = std::max(mt.box.hi[k], b.hi[k]); }
+  }
+  for (int i = 0; i < d->n_instances; ++i, ++pid) {
+    const gbrt_instance& in = d->instances[i];
+    float inv[12];
+    if (!affine_inverse(in.transform, inv))
+      return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: singular instance transform");
+    for (int r = 0; r < 3; ++r) instTab[4 * i + r] = make_float4(inv[4 * r], inv[4 * r + 1], inv[4 * r + 2], inv[4 * r + 3]);
+    float fpid, fmesh;
+    std::memcpy(&fpid, &pid, 4);
+    std::memcpy(&fmesh, &in.mesh, 4);
+    instTab[4 * i + 3] = make_float4(0.f, fpid, fmesh, 0.f);  // x: mesh root, set below
+    const Box& mb = meshTrees[in.mesh].box;
+    Box wb{{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}};
+    for (int c = 0; c < 8; ++c) {
+      F3 corner = {(c & 1) ? mb.hi[0] : mb.lo[0], (c & 2) ? mb.hi[1] : mb.lo[1], (c & 4) ? mb.hi[2] : mb.lo[2]};
+      F3 w = map_point(in.transform, corner);
+      const float wc[3] = {w.x, w.y, w.z};
+      for (int k = 0; k < 3; ++k) { wb.lo[k] = std::min(wb.lo[k], wc[k]); wb.hi[k] = std::max(wb.hi[k], wc[k]); }
+    }
+    // the box of the mapped corners, widened by a few ulp against the
+    // rounding of the ray's own transform
+    for (int k = 0; k < 3; ++k) {
+      const float e = 4e-6f * std::max(std::fabs(wb.lo[k]), std::fabs(wb.hi[k])) + 1e-30f;
+      wb.lo[k] -= e;
+      wb.hi[k] += e;
+    }
+    Rec r{};
+    r.v[0] = wb.lo[0]; r.v[1] = wb.lo[1]; r.v[2] = wb.lo[2]; setW(r.v[3], kRecInstance);
+    setW(r.v[4], i); setW(r.v[11], pid);
+    r.meta[0] = pid; r.meta[1] = -1; r.meta[2] = -1; r.meta[3] = -1;
+    recs.push_back(r);
+    boxes.push_back(wb);
+  }
+
   float sb[6] = {0, 0, 0, 0, 0, 0};
   for (size_t i = 0; i < boxes.size(); ++i)
     for (int k = 0; k < 3; ++k) {
@@ -413,7 +565,7 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   // would be too deep for the traversal stack), else binned SAH on the host.
   GpuBuild gb{};
   bool gpuBuilt = false;
-  if ((d->flags & GBRT_SCENE_GPU_BUILD) && !boxes.empty()) {
+  if ((d->flags & GBRT_SCENE_GPU_BUILD) && !boxes.empty() && d->n_instances == 0) {
     GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaError_t ce = gpu_build_bvh4(boxes, BuildOptions().max_leaf, ctx->stream, &gb);
     if (ce != cudaSuccess) return cuda_fail(ctx, ce, "gbrt_scene_create: GPU BVH build");
@@ -443,6 +595,30 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     c4 = collapse_bvh4(br);
     nodes.resize(c4.nodes.size() * 8);
     if (!c4.nodes.empty()) std::memcpy(nodes.data(), c4.nodes.data(), c4.nodes.size() * sizeof(Node4));
+    // the meshes' nodes and records after the top-level ones
+    int64_t node0 = int64_t(c4.nodes.size()), rec0 = int64_t(recs.size());
+    for (MeshTree& mt : meshTrees) {
+      if (!mt.used) continue;
+      mt.node0 = node0;
+      mt.rec0 = rec0;
+      for (Node4 n4 : mt.c4.nodes) {
+        relocate_node4(n4, node0, rec0);
+        const float4* f = reinterpret_cast<const float4*>(&n4);
+        nodes.insert(nodes.end(), f, f + 8);
+      }
+      for (const Rec& r : mt.recs) {
+        float4 f[3];
+        std::memcpy(f, r.v, sizeof r.v);
+        recv.insert(recv.end(), f, f + 3);
+        meta.push_back(make_int4(r.meta[0], r.meta[1], r.meta[2], r.meta[3]));
+      }
+      node0 += int64_t(mt.c4.nodes.size());
+      rec0 += int64_t(mt.recs.size());
+    }
+    for (int i = 0; i < d->n_instances; ++i) {
+      const int32_t root = int32_t(meshTrees[d->instances[i].mesh].node0);
+      std::memcpy(&instTab[4 * i + 3].x, &root, 4);
+    }
   }
 
   std::vector<DevMaterial> mats(size_t(d->n_materials));
@@ -496,8 +672,16 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     delete s;
     return st;
   }
-  v.n_nodes = gpuBuilt ? gb.n_nodes : int64_t(c4.nodes.size());
-  v.n_recs = int64_t(recs.size());
+  v.n_nodes = gpuBuilt ? gb.n_nodes : int64_t(nodes.size() / 8);
+  v.n_recs = int64_t(meta.size());
+  if (d->n_instances > 0) {
+    if ((st = upload(s, instTab, &v.inst)) != GBRT_OK) {
+      free_scene(s);
+      delete s;
+      return st;
+    }
+    v.n_inst = d->n_instances;
+  }
   v.n_planes = d->n_planes;
   v.n_materials = d->n_materials;
   v.n_lights = d->n_lights;
@@ -560,9 +744,15 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   }
   s->n_leaves = gpuBuilt ? gb.leaves : br.leaves;
   s->max_depth = gpuBuilt ? 0 : br.max_depth;
-  s->max_depth4 = gpuBuilt ? gb.depth4 : c4.max_depth;
+  // two levels: the top-level tree, the way into a mesh, the mesh's tree
+  s->max_depth4 = gpuBuilt ? gb.depth4 : (d->n_instances > 0 ? c4.max_depth + 1 + meshDepth : c4.max_depth);
+  if (3 * s->max_depth4 + 1 > 190) {  // the traversal kernels' longest stack
+    free_scene(s);
+    delete s;
+    return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: two-level tree deeper than the traversal stack");
+  }
   s->sah_cost = gpuBuilt ? 0.0 : br.sah_cost;
-  s->n_prims = int32_t(nPrims);
+  s->n_prims = int32_t(nPrims + d->n_csg + d->n_instances);
   std::memcpy(s->bounds, sb, sizeof sb);
   s->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   *out = s;

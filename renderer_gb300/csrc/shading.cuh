@@ -175,9 +175,25 @@ __device__ __forceinline__ void hit_texcoords(const DeviceScene& S, int rec, flo
     tv = __fadd_rn(__fadd_rn(__fmul_rn(w0, 0.f), __fmul_rn(u, 1.f)), __fmul_rn(v, 0.f));
     return;
   }
-  const float* t = S.tri_uv + 6 * int64_t(__ldg(&S.meta[rec]).x - S.tri_pid0);
+  const int64_t tri = int64_t(__ldg(&S.meta[rec]).x) - S.tri_pid0;
+  if (tri < 0) {  // an instanced mesh's triangle: the default coordinates
+    tu = v;
+    tv = u;
+    return;
+  }
+  const float* t = S.tri_uv + 6 * tri;
   tu = __fadd_rn(__fadd_rn(__fmul_rn(w0, t[0]), __fmul_rn(u, t[2])), __fmul_rn(v, t[4]));
   tv = __fadd_rn(__fadd_rn(__fmul_rn(w0, t[1]), __fmul_rn(u, t[3])), __fmul_rn(v, t[5]));
+}
+
+// HitRecord::transform's normal (src/hitrecord.h:79-84) for a hit on an
+// instance's mesh: the inverse transpose of the instance's linear part, i.e.
+// the transpose of its world-to-object rows, then normalised.
+__device__ __forceinline__ V3f instance_normal(const DeviceScene& S, int in, V3f n) {
+  const float4* M = S.inst + 4 * int64_t(in);
+  const float4 m0 = __ldg(M), m1 = __ldg(M + 1), m2 = __ldg(M + 2);
+  return normalize(v3(m0.x * n.x + m1.x * n.y + m2.x * n.z, m0.y * n.x + m1.y * n.y + m2.y * n.z,
+                      m0.z * n.x + m1.z * n.y + m2.z * n.z));
 }
 
 // TextureMaterial::get + brdf's pow (src/texturematerial.cpp:62-74): the

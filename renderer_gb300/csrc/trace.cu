@@ -16,7 +16,7 @@
 
 namespace gbrt {
 
-template <bool ANY, bool WT, int STACK, bool CSG>
+template <bool ANY, bool WT, int STACK, bool GEN>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_api(DeviceScene S, const float4* __restrict__ rays, int64_t n, const int32_t* __restrict__ ignore,
                 gbrt_hit* __restrict__ hits, uint8_t* __restrict__ occluded, unsigned long long* work, int* err) {
@@ -32,7 +32,8 @@ __global__ void __launch_bounds__(kTraceBlock)
     TRay r = make_tray(a, b);
     float t, u, v;
     int ign = (ANY && ignore) ? ignore[i] : -1;
-    int32_t rec = trace_ray<ANY, false, WT, STACK, CSG>(S, r, ign, t, u, v, err, nullptr);
+    int32_t inst = -1;
+    int32_t rec = trace_ray<ANY, false, WT, STACK, GEN>(S, r, ign, t, u, v, err, nullptr, &inst);
     if (ANY) {
       occluded[i] = rec != -1 ? 1 : 0;
     } else {
@@ -40,7 +41,8 @@ __global__ void __launch_bounds__(kTraceBlock)
       h.t = t; h.u = u; h.v = v;
       if (rec >= 0) {
         h.prim = __ldg(&S.meta[rec]).x;
-        if (CSG && __float_as_int(__ldg(S.recs + 3 * int64_t(rec)).w) == kRecCSG) h.u = h.v = 0.f;
+        if (GEN && __float_as_int(__ldg(S.recs + 3 * int64_t(rec)).w) == kRecCSG) h.u = h.v = 0.f;
+        if (GEN && inst >= 0) h.prim = __float_as_int(__ldg(S.inst + 4 * int64_t(inst) + 3).y);
       }
       else if (rec <= -2) h.prim = S.plane_meta[-2 - rec].x;
       else if (S.env_light >= 0 && isinf(r.tmax) && r.tmax > 0.f) {
@@ -60,7 +62,7 @@ int trace_grid(gbrt_ctx* ctx, const void* kernel) {
 }
 
 // The ray-query kernel for a scene: any / closest hit, watertight triangles,
-// short stack, CSG objects.
+// short stack, general leaves (CSG objects, instances).
 template <bool G>
 static decltype(&k_trace_api<false, false, kStackSize, false>) pick_api(bool any, bool wt, bool shortStack) {
   if (any) {
@@ -78,9 +80,9 @@ static gbrt_status launch_api(gbrt_scene* s, bool any, const gbrt_ray* d_rays, c
   const float4* rays = reinterpret_cast<const float4*>(d_rays);
   // The short stack when the tree is shallow enough for it.
   const bool shortStack = stack_need(s->max_depth4) <= kShortStack;
-  const bool csg = s->view.csg_prog != nullptr;
+  const bool gen = s->view.csg_prog != nullptr || s->view.inst != nullptr;
   decltype(&k_trace_api<false, false, kStackSize, false>) k;
-  if (csg) k = pick_api<true>(any, s->watertight, shortStack);
+  if (gen) k = pick_api<true>(any, s->watertight, shortStack);
   else k = pick_api<false>(any, s->watertight, shortStack);
   const int grid = trace_grid(ctx, (const void*)k);
   k<<<grid, kTraceBlock, 0, st>>>(s->view, rays, n, any ? d_ignore : nullptr, any ? nullptr : d_hits,

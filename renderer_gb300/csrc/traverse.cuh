@@ -371,7 +371,21 @@ struct TState {
   int32_t bestQuad;  // 0: not a quad half, 1: first half, 2: second half
   float bu, bv;
   bool found;
+  // Two-level scenes (GEN traversal only): the instance whose mesh is being
+  // traversed (-1: world space), the instance of the best hit, and the ray in
+  // that instance's space.
+  int32_t inst, bestInst;
+  TRay oray;
 };
+
+// IntersectableInstance::intersect's Ray::transform(inverseTransform)
+// (src/intersectableinstance.cpp:24-30): the origin mapped as a point, the
+// direction as a vector (not renormalised), each row summed left to right.
+__device__ __forceinline__ TRay instance_ray(const TRay& r, float4 m0, float4 m1, float4 m2) {
+  auto pt = [&](float4 m) { return fa(fa(fa(fm(m.x, r.ox), fm(m.y, r.oy)), fm(m.z, r.oz)), m.w); };
+  auto vec = [&](float4 m) { return fa(fa(fm(m.x, r.dx), fm(m.y, r.dy)), fm(m.z, r.dz)); };
+  return make_tray(make_float4(pt(m0), pt(m1), pt(m2), r.tmin), make_float4(vec(m0), vec(m1), vec(m2), r.tmax));
+}
 
 // Starts a ray: tests the planes (unbounded, kept out of the BVH; testing them
 // first gives the tree a tighter tmax). Returns true when the ray is already
@@ -387,6 +401,8 @@ __device__ __forceinline__ bool trace_init(const DeviceScene& S, const TRay& r, 
   ts.bv = 0.f;
   ts.sp = 0;
   ts.node = 0;
+  ts.inst = -1;
+  ts.bestInst = -1;
   for (int k = 0; k < S.n_planes; ++k) {
     if (ANY && S.plane_meta[k].x == ignore_prim) continue;
     float t = plane_t(r, __ldg(&S.planes[k]));
@@ -400,7 +416,10 @@ __device__ __forceinline__ bool trace_init(const DeviceScene& S, const TRay& r, 
 
 // One traversal step: one 4-wide node or one leaf. ANY: stop at the first
 // accepted hit and skip records whose prim id equals ignore_prim. WT:
-// watertight triangle test. Returns true when the ray is finished.
+// watertight triangle test. GEN: the general leaves, CSG objects and
+// instances (entering an instance pushes the rest of its leaf and a return
+// marker, then walks the mesh's tree with the ray in the mesh's space).
+// Returns true when the ray is finished.
 //
 // Acceptance: the first hit may lie anywhere in [tmin, tmax] (Ray::inRange is
 // inclusive); later hits must be strictly closer. One exception keeps
@@ -408,10 +427,11 @@ __device__ __forceinline__ bool trace_init(const DeviceScene& S, const TRay& r, 
 // quad wins over the second whenever it is hit: the first half replaces a
 // current best that is the same quad's second half even at a larger t, and the
 // second half never replaces the first.
-template <bool ANY, bool COUNT, bool WT, int STACK, bool CSG>
-__device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& r, int ignore_prim, TState& ts,
+template <bool ANY, bool COUNT, bool WT, int STACK, bool GEN>
+__device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& wr, int ignore_prim, TState& ts,
                                            int* stack, int* err, TraceCounters* cnt) {
   const int32_t node = ts.node;
+  const TRay& r = (GEN && ts.inst >= 0) ? ts.oray : wr;
   if (node >= 0) {
     // Offsets (in float4) of the near and far planes of each axis.
     const int nxo = r.ix >= 0.f ? 0 : 1, nyo = r.iy >= 0.f ? 2 : 3, nzo = r.iz >= 0.f ? 4 : 5;
@@ -465,8 +485,20 @@ __device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& r, 
         else hit = tri_test_ref(r, a, b, c, tlim, t, u, v);
       } else if (kind == kRecSphere) {
         hit = sphere_test(r, a, b.x, tlim, t);
-      } else if (!CSG || kind == kRecParallelogram) {
+      } else if (!GEN || kind == kRecParallelogram) {
         hit = pgram_test(r, a, b, c, tlim, t, u, v);
+      } else if (kind == kRecInstance) {
+        // The rest of this leaf after the instance, then the way back.
+        if (ts.sp + 2 > STACK) { *err = 1; return true; }
+        const int64_t rest = first + count - (k + 1);
+        if (rest > 0) stack[ts.sp++] = ~int32_t(uint32_t(k + 1) << 4 | uint32_t(rest - 1));
+        stack[ts.sp++] = kInstPop;
+        const int in = __float_as_int(b.x);
+        const float4* M = S.inst + 4 * int64_t(in);
+        ts.oray = instance_ray(wr, __ldg(M), __ldg(M + 1), __ldg(M + 2));
+        ts.inst = in;
+        ts.node = __float_as_int(__ldg(M + 3).x);
+        return false;
       } else {
         int leaf = -1;
         hit = csg_test(S, r, __float_as_int(b.w), __float_as_int(c.x), tlim, t, leaf);
@@ -479,31 +511,39 @@ __device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& r, 
       if (hit) {
         ts.tcur = t; ts.found = true; ts.best = int32_t(k); ts.bu = u; ts.bv = v;
         ts.bestPrim = prim; ts.bestQuad = quad;
+        if (GEN) ts.bestInst = ts.inst;
         if (ANY) return true;
       }
     }
   }
   if (ts.sp == 0) return true;
   ts.node = stack[--ts.sp];
+  if (GEN && ts.node == kInstPop) {  // back from a mesh to world space
+    ts.inst = -1;
+    if (ts.sp == 0) return true;
+    ts.node = stack[--ts.sp];
+  }
   return false;
 }
 
 // A whole ray in one call (the ray-query entry points). Returns the internal
-// hit encoding (RawHit::rec) and fills t/u/v. STACK is the capacity of the
-// traversal stack (stack_need(depth of the 4-wide tree)).
-template <bool ANY, bool COUNT, bool WT, int STACK, bool CSG>
+// hit encoding (RawHit::rec) and fills t/u/v, and with GEN the instance of the
+// hit (-1: none). STACK is the capacity of the traversal stack
+// (stack_need(depth of the 4-wide tree), both levels for two-level scenes).
+template <bool ANY, bool COUNT, bool WT, int STACK, bool GEN>
 __device__ __forceinline__ int32_t trace_ray(const DeviceScene& S, const TRay& r, int ignore_prim,
                                              float& t_best, float& u_best, float& v_best, int* err,
-                                             TraceCounters* cnt) {
+                                             TraceCounters* cnt, int32_t* inst_out = nullptr) {
   TState ts;
   int stack[STACK];
   if (!trace_init<ANY>(S, r, ignore_prim, ts)) {
-    while (!trace_step<ANY, COUNT, WT, STACK, CSG>(S, r, ignore_prim, ts, stack, err, cnt)) {
+    while (!trace_step<ANY, COUNT, WT, STACK, GEN>(S, r, ignore_prim, ts, stack, err, cnt)) {
     }
   }
   t_best = ts.found ? ts.tcur : CUDART_NAN_F;
   u_best = ts.bu;
   v_best = ts.bv;
+  if (GEN && inst_out) *inst_out = ts.bestInst;
   return ts.best;
 }
 

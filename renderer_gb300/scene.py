@@ -36,6 +36,8 @@ class SceneData:
     textures: List[np.ndarray] = field(default_factory=list)  # (H, W, 3) float32 BGR each
     csg_nodes: List[tuple] = field(default_factory=list)  # (op, left, right, a3, b3, material)
     csg_roots: List[int] = field(default_factory=list)
+    meshes: List[dict] = field(default_factory=list)     # {"pos" (N, 9), "nrm" (N, 9) or None, "mat" (N,) or None}
+    instances: List[tuple] = field(default_factory=list)  # (3x4 object->world transform, mesh index)
 
     # ------------------------------------------------------------ building
     def add_material(self, type, kd=(0, 0, 0), ks=(0, 0, 0), exponent=0.0, ior=1.0, coefficient=1.0, texture=-1):
@@ -53,7 +55,7 @@ class SceneData:
 
     def n_prims(self):
         return len(self.lights) + self.n_tri() + len(self.quads) + len(self.spheres) + len(self.planes) + \
-            len(self.csg_roots)
+            len(self.csg_roots) + len(self.instances)
 
     def csg_leaf(self, op, a, b, material):
         """A sphere (a = centre, b = (r, 0, 0)) or box (a = min, b = max) node."""
@@ -63,6 +65,19 @@ class SceneData:
     def csg_op(self, op, left, right):
         self.csg_nodes.append((op, int(left), int(right), (0, 0, 0), (0, 0, 0), -1))
         return len(self.csg_nodes) - 1
+
+    def add_mesh(self, pos, nrm=None, mat=None):
+        """A triangle mesh for instancing; returns its index."""
+        self.meshes.append(dict(pos=np.ascontiguousarray(pos, np.float32).reshape(-1, 9),
+                                nrm=None if nrm is None else np.ascontiguousarray(nrm, np.float32).reshape(-1, 9),
+                                mat=None if mat is None else np.ascontiguousarray(mat, np.int32).reshape(-1)))
+        return len(self.meshes) - 1
+
+    def add_instance(self, transform, mesh):
+        """Places mesh with a 3x4 (or 4x4) object-to-world transform."""
+        t = np.asarray(transform, np.float64)[:3, :4]
+        self.instances.append((t.astype(np.float32), int(mesh)))
+        return len(self.instances) - 1
 
     def add_csg(self, root):
         self.csg_roots.append(int(root))
@@ -76,6 +91,7 @@ class SceneData:
         o["spheres"] = o["quads"] + len(self.quads)
         o["planes"] = o["spheres"] + len(self.spheres)
         o["csg"] = o["planes"] + len(self.planes)
+        o["instances"] = o["csg"] + len(self.csg_roots)
         return o
 
     # ------------------------------------------------------------ C view
@@ -165,6 +181,27 @@ class SceneData:
             d.n_csg_nodes = len(self.csg_nodes)
             d.csg_roots = roots
             d.n_csg = len(self.csg_roots)
+        if self.instances:
+            marr = (_abi.Mesh * len(self.meshes))()
+            for i, m in enumerate(self.meshes):
+                keep.append(m["pos"])
+                marr[i].tri_pos = m["pos"].ctypes.data_as(C.POINTER(C.c_float))
+                if m["nrm"] is not None:
+                    keep.append(m["nrm"])
+                    marr[i].tri_nrm = m["nrm"].ctypes.data_as(C.POINTER(C.c_float))
+                if m["mat"] is not None:
+                    keep.append(m["mat"])
+                    marr[i].tri_mat = m["mat"].ctypes.data_as(C.POINTER(C.c_int32))
+                marr[i].n_tri = len(m["pos"])
+            iarr = (_abi.Instance * len(self.instances))()
+            for i, (t, mi) in enumerate(self.instances):
+                iarr[i].transform = (C.c_float * 12)(*[float(x) for x in np.asarray(t).reshape(-1)])
+                iarr[i].mesh = mi
+            keep += [marr, iarr]
+            d.meshes = marr
+            d.n_meshes = len(self.meshes)
+            d.instances = iarr
+            d.n_instances = len(self.instances)
         return d, keep
 
     def camera_struct(self, width=None, height=None):
