@@ -425,6 +425,99 @@ def run_batch(args):
     print(json.dumps(line))
 
 
+INSTANCED_WORKLOAD = ("8 instances of one 4,000,000-triangle noise-displaced terrain (two-level BVH), 200 spheres "
+                      "(diffuse/mirror/glass/Blinn), 2048x1024 lat-long sky with a sun; 16 seeded views at "
+                      "3840x2160, 1 spp each, max depth 16, RR p=0.5, physical semantics")
+
+
+def run_instanced(args):
+    """The instanced-terrain scene: 16 views of 3840 x 2160 at one sample per
+    pixel in one gbrt_render_batch call (a step = all 16 images). value =
+    paths / device span; e2e = paths / host wall time of the call, the 16
+    films (1.6 GB) copied to host memory. --compare-flat also renders the
+    same views of the scene with every instance flattened into one tree."""
+    import numpy as np
+
+    from renderer_gb300 import _abi, workloads
+    from renderer_gb300.batch import BatchJob, render_batch
+    from renderer_gb300.runtime import Context, GpuScene
+    from renderer_gb300.scene import SceneData, render_params
+
+    t = time.perf_counter()
+    s, cams = workloads.terrain_instances(seed=0, nx=args.terrain_nx, nz=args.terrain_nx // 2)
+    gen_s = time.perf_counter() - t
+    ctx = Context(0)
+    t = time.perf_counter()
+    gs = GpuScene(ctx, s)
+    create_s = time.perf_counter() - t
+    info = gs.info()
+
+    def measure(scene, tag):
+        jobs = []
+        for i, c in enumerate(cams):
+            sc = SceneData()
+            sc.camera = c
+            jobs.append(BatchJob(scene, sc.camera_struct(),
+                                 render_params(1, 1, 0.5, 16, 100 + i, semantics=_abi.SEM_PHYSICAL)))
+        for _ in range(args.warmup):
+            render_batch(ctx, jobs, streams=4)
+        clocks = ClockSampler(0)
+        clocks.start()
+        time.sleep(0.3)
+        dev, wall, paths, ext, sh = 0.0, 0.0, 0, 0, 0
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            films, _, st = render_batch(ctx, jobs, streams=4)
+            wall += time.perf_counter() - t0
+            dev += st.device_ms / 1000.0
+            paths += st.paths
+            ext += st.extension_rays
+            sh += st.shadow_rays
+        clk = clocks.stop()
+        return {"value": paths / dev, "e2e": paths / wall, "ms_per_step": 1000 * dev / args.steps,
+                "rays_per_s": (ext + sh) / dev, "extension_rays_per_path": ext / paths,
+                "shadow_rays_per_path": sh / paths, "clocks": clk, "film_mean": float(films[0].mean()),
+                "launches": st.kernel_launches}
+
+    r = measure(gs, "two-level")
+    tri = len(s.meshes[0]["pos"]) * len(s.instances)
+    line = {"metric": "paths/s (instanced terrain, 16 views)", "value": r["value"], "unit": "paths/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": INSTANCED_WORKLOAD, "paths_per_step": 16 * cams[0]["width"] * cams[0]["height"],
+                       "mesh_triangles": len(s.meshes[0]["pos"]), "instanced_triangles": tri,
+                       "scene_generation_s": gen_s, "scene_create_s": create_s, "bvh_nodes": info["nodes"],
+                       "rays_per_s": r["rays_per_s"], "extension_rays_per_path": r["extension_rays_per_path"],
+                       "shadow_rays_per_path": r["shadow_rays_per_path"],
+                       "l2": "inputs larger than L2 (mesh 4M triangles, path state per stream > 129 MB)"},
+            "e2e": {"value": r["e2e"], "unit": "paths/s", "h2d_bytes_per_step": 16 * C.sizeof(_abi.BatchJob),
+                    "d2h_bytes_per_step": 16 * cams[0]["width"] * cams[0]["height"] * 12},
+            "gpu_launches": r["launches"] * args.steps, "clocks": r["clocks"]}
+    if args.compare_flat:
+        del gs
+        f = SceneData(materials=s.materials, spheres=s.spheres, lights=s.lights, env=s.env, env_mapping=s.env_mapping,
+                      camera=s.camera)
+        P, N = [], []
+        m = s.meshes[0]
+        for M, _ in s.instances:
+            A = np.asarray(M)[:, :3].astype(np.float32)
+            tt = np.asarray(M)[:, 3].astype(np.float32)
+            P.append((m["pos"].reshape(-1, 3) @ A.T + tt).reshape(-1, 9))
+            nn = m["nrm"].reshape(-1, 3) @ np.linalg.inv(A.astype(np.float64))
+            N.append((nn / np.linalg.norm(nn, axis=1, keepdims=True)).astype(np.float32).reshape(-1, 9))
+        f.tri_pos = np.concatenate(P)
+        f.tri_nrm = np.concatenate(N)
+        f.tri_mat = np.concatenate([m["mat"]] * len(s.instances))
+        del P, N
+        t = time.perf_counter()
+        gf = GpuScene(ctx, f)
+        fc = time.perf_counter() - t
+        rf = measure(gf, "flat")
+        line["config"]["flattened"] = {"value": rf["value"], "scene_create_s": fc, "bvh_nodes": gf.info()["nodes"],
+                                       "film_mean": rf["film_mean"], "two_level_film_mean": r["film_mean"]}
+    print(json.dumps(line))
+
+
 def run_chains(args):
     """The Markov-chain renderers on the Cornell box (256 x 256, max depth 5,
     the renderer's defaults: Metropolis with 16 mutations per pixel, 10,000
@@ -518,6 +611,10 @@ def main():
                     help="aggregate paths/s of the seeded 64-scene batch through gbrt_render_batch")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-streams", type=int, default=0, help="streams for --batch (0: autotune)")
+    ap.add_argument("--instanced", action="store_true",
+                    help="16 views of the instanced-terrain scene (two-level BVH) through gbrt_render_batch")
+    ap.add_argument("--terrain-nx", type=int, default=2000, help="terrain quads along x (2000: 4M triangles)")
+    ap.add_argument("--compare-flat", action="store_true", help="with --instanced: also the flattened scene")
     ap.add_argument("--chains", action="store_true",
                     help="paths/s of the Metropolis and energy-redistribution renderers (Cornell box)")
     ap.add_argument("--mlt-chains", type=lambda x: [int(v) for v in x.split(",")], default=[0, 4096, 1 << 20],
@@ -526,6 +623,9 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.chains:
         run_chains(args)
+        return
+    if args.instanced:
+        run_instanced(args)
         return
     if args.batch:
         run_batch(args)

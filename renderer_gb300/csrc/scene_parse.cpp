@@ -12,8 +12,11 @@
 //               are taken from the scene file's directory (src/sceneast.cpp:811-815).
 //   build       buildScene / scene_builder (src/sceneast.cpp:321-728): the
 //               variables camera, lights and intersectable form the scene.
-// Differences, for the GPU layout: instances are flattened by transforming
-// their primitives (a sphere needs a similarity transform); a pre-built
+// Differences, for the GPU layout: an instance of a subtree of at least 1,024
+// triangles (obj / t / lists of them) under an affine transform becomes an
+// instance of a shared mesh (two-level BVH; the mesh keeps no texture
+// coordinates); other instances are flattened by transforming their
+// primitives (a sphere needs a similarity transform); a pre-built
 // b(left, right, box) node contributes its children (the BVH is rebuilt);
 // box(min, max, m) and isect / union / diff / xor trees of spheres and boxes
 // become CSG objects (a box under an instance must stay axis-aligned).
@@ -773,6 +776,15 @@ struct gbrt_parsed_scene {
   gbrt_camera camera{};
   bool has_camera = false;
   bool any_smooth = false;
+  // instanced meshes (triangles in the mesh's own space) and their instances
+  struct MeshData {
+    std::vector<float> pos, nrm;
+    std::vector<int32_t> mat;
+    bool smooth = false;
+  };
+  std::vector<MeshData> meshes;
+  std::vector<gbrt_mesh> mesh_descs;
+  std::vector<gbrt_instance> instances;
 };
 
 namespace {
@@ -962,22 +974,25 @@ struct Builder {
       }
       case Node::INSTANCE: {
         Mat4 M = xf ? (*xf) * n->xf : n->xf;
-        emit(n->children[0], &M);
+        const bool affine = M.m[3][0] == 0.f && M.m[3][1] == 0.f && M.m[3][2] == 0.f && M.m[3][3] == 1.f;
+        int64_t tris = 0;
+        if (affine && meshOnly(n->children[0], tris) && tris >= kInstanceMinTriangles) {
+          gbrt_instance in{};
+          for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 4; ++c) in.transform[4 * r + c] = M.m[r][c];
+          in.mesh = meshFor(n->children[0]);
+          ps.instances.push_back(in);
+        } else {
+          emit(n->children[0], &M);
+        }
         break;
       }
       case Node::OBJ: {
-        std::string path = joinPath(baseDir, n->file);
-        auto it = objCache.find(path);
-        if (it == objCache.end()) {
-          std::vector<ObjTri> tris;
-          std::map<std::string, MatNode> mats;
-          if (!readOBJ(path, tris, mats)) throw ParseError(GBRT_ERR_IO, "cannot open OBJ file " + path);
-          it = objCache.emplace(path, std::make_pair(std::move(tris), std::move(mats))).first;
-        }
-        for (auto& kv : it->second.second) objMats.emplace(kv.first, kv.second);
+        const auto& obj = loadObj(n);
+        for (auto& kv : obj.second) objMats.emplace(kv.first, kv.second);
         int deflt = resolveMat(n->mat);
         std::map<std::string, int> local;
-        for (const ObjTri& t : it->second.first) {
+        for (const ObjTri& t : obj.first) {
           int m = deflt;
           if (!t.mtl.empty()) {
             auto lt = local.find(t.mtl);
@@ -994,6 +1009,69 @@ struct Builder {
         break;
       }
     }
+  }
+
+  // An OBJ file's triangles and MTL materials, read once per path.
+  const std::pair<std::vector<ObjTri>, std::map<std::string, MatNode>>& loadObj(const NodeP& n) {
+    std::string path = joinPath(baseDir, n->file);
+    auto it = objCache.find(path);
+    if (it == objCache.end()) {
+      std::vector<ObjTri> tris;
+      std::map<std::string, MatNode> mats;
+      if (!readOBJ(path, tris, mats)) throw ParseError(GBRT_ERR_IO, "cannot open OBJ file " + path);
+      it = objCache.emplace(path, std::make_pair(std::move(tris), std::move(mats))).first;
+    }
+    return it->second;
+  }
+
+  // Smallest subtree an instance keeps as a shared mesh (smaller ones are
+  // cheaper flattened into the scene's own tree).
+  static constexpr int64_t kInstanceMinTriangles = 1024;
+
+  // Whether a subtree holds only triangles (obj files, t(...), lists of
+  // them), and how many.
+  bool meshOnly(const NodeP& n, int64_t& count) {
+    switch (n->kind) {
+      case Node::TRI: ++count; return true;
+      case Node::OBJ: count += int64_t(loadObj(n).first.size()); return true;
+      case Node::LIST:
+      case Node::BVH:
+        for (auto& c : n->children)
+          if (!meshOnly(c, count)) return false;
+        return true;
+      default: return false;
+    }
+  }
+
+  // The shared mesh of a subtree (its triangles in its own space), built once
+  // per subtree; obj(...) subtrees with the same file and material share one
+  // (the grammar has no references to intersectables, so every instance of
+  // a file writes its own obj(...)).
+  std::map<std::string, int> meshIds;
+  int meshFor(const NodeP& n) {
+    char ptr[32];
+    std::snprintf(ptr, sizeof ptr, "node:%p", static_cast<const void*>(n.get()));
+    const std::string key =
+        n->kind == Node::OBJ ? "obj:" + joinPath(baseDir, n->file) + ":" + std::to_string(resolveMat(n->mat)) : ptr;
+    auto it = meshIds.find(key);
+    if (it != meshIds.end()) return it->second;
+    std::vector<float> pos, nrm, uv;
+    std::vector<int32_t> mat;
+    bool smooth = false;
+    ps.tri_pos.swap(pos); ps.tri_nrm.swap(nrm); ps.tri_uv.swap(uv); ps.tri_mat.swap(mat);
+    std::swap(ps.any_smooth, smooth);
+    emit(n, nullptr);
+    ps.tri_pos.swap(pos); ps.tri_nrm.swap(nrm); ps.tri_uv.swap(uv); ps.tri_mat.swap(mat);
+    std::swap(ps.any_smooth, smooth);
+    gbrt_parsed_scene::MeshData md;
+    md.pos = std::move(pos);
+    md.nrm = std::move(nrm);
+    md.mat = std::move(mat);
+    md.smooth = smooth;
+    ps.meshes.push_back(std::move(md));
+    const int id = int(ps.meshes.size()) - 1;
+    meshIds[key] = id;
+    return id;
   }
 
   // Instances move a sphere by a similarity transform (centre, radius).
@@ -1240,6 +1318,19 @@ gbrt_status gbrt_parsed_scene_desc(const gbrt_parsed_scene* ps, gbrt_scene_desc*
   d->n_csg_nodes = int32_t(ps->csg_nodes.size());
   d->csg_roots = ps->csg_roots.empty() ? nullptr : ps->csg_roots.data();
   d->n_csg = int32_t(ps->csg_roots.size());
+  mps->mesh_descs.resize(ps->meshes.size());
+  for (size_t i = 0; i < ps->meshes.size(); ++i) {
+    const auto& m = ps->meshes[i];
+    gbrt_mesh& g = mps->mesh_descs[i];
+    g.tri_pos = m.pos.data();
+    g.tri_nrm = m.smooth ? m.nrm.data() : nullptr;
+    g.tri_mat = m.mat.data();
+    g.n_tri = int64_t(m.mat.size());
+  }
+  d->meshes = ps->mesh_descs.empty() ? nullptr : ps->mesh_descs.data();
+  d->n_meshes = int32_t(ps->mesh_descs.size());
+  d->instances = ps->instances.empty() ? nullptr : ps->instances.data();
+  d->n_instances = int32_t(ps->instances.size());
   if (cam) *cam = ps->camera;
   if (has_camera) *has_camera = ps->has_camera ? 1 : 0;
   return GBRT_OK;

@@ -38,6 +38,14 @@ def _from_parsed(ps):
         if d.tri_uv:
             s.tri_uv = np.ctypeslib.as_array(d.tri_uv, shape=(d.n_tri, 6)).copy()
         s.tri_mat = np.ctypeslib.as_array(d.tri_mat, shape=(d.n_tri,)).copy()
+    for i in range(d.n_meshes):
+        m = d.meshes[i]
+        s.add_mesh(np.ctypeslib.as_array(m.tri_pos, shape=(m.n_tri, 9)).copy(),
+                   np.ctypeslib.as_array(m.tri_nrm, shape=(m.n_tri, 9)).copy() if m.tri_nrm else None,
+                   np.ctypeslib.as_array(m.tri_mat, shape=(m.n_tri,)).copy())
+    for i in range(d.n_instances):
+        g = d.instances[i]
+        s.add_instance(np.array(list(g.transform), np.float32).reshape(3, 4), g.mesh)
     for i in range(d.n_quads):
         q = d.quads[i]
         s.quads.append(tuple(tuple(q.p[k]) for k in range(4)) + (q.material,))

@@ -369,3 +369,80 @@ def batch_scene(index, seed=0):
 def batch_scenes(n=64, seed=0):
     """The first n scenes of batch_scene's seeded sequence."""
     return [batch_scene(i, seed) for i in range(n)]
+
+
+# ------------------------------------------------------ instanced terrain
+def terrain(nx, nz, size_x, size_z, height, seed=0):
+    """A heightfield of nx x nz quads (2 nx nz triangles) over [-size_x/2,
+    size_x/2] x [-size_z/2, size_z/2], y = height (1 + fbm) / 2 from 4-octave
+    value noise, with smooth (area-weighted) normals."""
+    xs = np.linspace(-size_x / 2, size_x / 2, nx + 1)
+    zs = np.linspace(-size_z / 2, size_z / 2, nz + 1)
+    X, Z = np.meshgrid(xs, zs, indexing="ij")
+    P2 = np.stack([X.ravel() * 0.6, Z.ravel() * 0.6, np.zeros(X.size)], 1)
+    Y = 0.5 * height * (1.0 + fbm(P2, seed))
+    P = np.stack([X.ravel(), Y, Z.ravel()], 1)
+    idx = np.arange((nx + 1) * (nz + 1)).reshape(nx + 1, nz + 1)
+    a, b, c, d = idx[:-1, :-1].ravel(), idx[1:, :-1].ravel(), idx[1:, 1:].ravel(), idx[:-1, 1:].ravel()
+    F = np.concatenate([np.stack([a, c, b], 1), np.stack([a, d, c], 1)])
+    tri = P[F]
+    fn = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    N = np.zeros_like(P)
+    for col in range(3):
+        for k in range(3):
+            N[:, col] += np.bincount(F[:, k], weights=fn[:, col], minlength=len(P))
+    N /= np.linalg.norm(N, axis=1, keepdims=True)
+    return tri.reshape(-1, 9).astype(np.float32), N[F].reshape(-1, 9).astype(np.float32)
+
+
+def terrain_instances(seed=0, nx=2000, nz=1000, n_instances=8, n_spheres=200, width=3840, height=2160,
+                      env_size=(2048, 1024), views=16):
+    """Eight seeded copies (rotation about the vertical, scale 0.8-1.2,
+    translation) of one 4,000,000-triangle noise-displaced terrain (2000 x
+    1000 quads over 8 x 4 units) as instances of one mesh, 200 spheres of
+    mixed materials (diffuse, mirror, glass 1.5, Blinn 10-500) above it, and
+    a 2048 x 1024 lat-long sky with a sun as the only light. Returns
+    (SceneData, cameras): `views` seeded camera poses at width x height."""
+    rng = np.random.default_rng([int(seed), 0xC5])
+    s = SceneData()
+    s.env_mapping = _abi.ENV_LATLONG
+    sky, _ = synthetic_sky(env_size[0], env_size[1], seed=int(seed), sun_radiance=2e4)
+    s.env = sky
+    s.lights = [dict(type=_abi.LIGHT_ENV, intensity=(1.0, 1.0, 1.0))]
+    ground = s.add_material(_abi.MAT_DIFFUSE, kd=bgr((0.45, 0.4, 0.33)))
+    pos, nrm = terrain(nx, nz, 8.0, 4.0, 0.8, int(seed))
+    mi = s.add_mesh(pos, nrm, np.full(len(pos), ground, np.int32))
+    for k in range(n_instances):
+        ang = rng.uniform(0, 2 * np.pi)
+        sc = rng.uniform(0.8, 1.2)
+        c, sn = np.cos(ang), np.sin(ang)
+        R = np.array([[c, 0, sn], [0, 1, 0], [-sn, 0, c]]) * sc
+        t = ((k % 4) * 8.5 - 12.75 + rng.uniform(-0.5, 0.5), rng.uniform(-0.2, 0.2),
+             (k // 4) * 8.5 - 4.25 + rng.uniform(-0.5, 0.5))
+        M = np.zeros((3, 4))
+        M[:, :3] = R
+        M[:, 3] = t
+        s.add_instance(M, mi)
+    for _ in range(n_spheres):
+        kind = int(rng.integers(4))
+        if kind == 0:
+            m = s.add_material(_abi.MAT_DIFFUSE, kd=tuple(rng.uniform(0.2, 0.85, 3)))
+        elif kind == 1:
+            m = s.add_material(_abi.MAT_MIRROR)
+        elif kind == 2:
+            m = s.add_material(_abi.MAT_TRANSPARENT, ior=1.5)
+        else:
+            kd = rng.uniform(0.1, 0.5, 3)
+            m = s.add_material(_abi.MAT_BLINN, kd=tuple(kd), ks=tuple(np.full(3, 0.9 - kd.max())),
+                               exponent=float(rng.uniform(10, 500)))
+        r = float(rng.uniform(0.1, 0.6))
+        s.spheres.append(((rng.uniform(-17, 17), rng.uniform(1.0, 3.5), rng.uniform(-8, 8)), r, m))
+    cams = []
+    for _ in range(views):
+        a = rng.uniform(0, 2 * np.pi)
+        d = rng.uniform(14, 24)
+        eye = (d * np.cos(a), rng.uniform(3, 9), d * np.sin(a) * 0.7)
+        look = (rng.uniform(-4, 4), rng.uniform(0, 1.5), rng.uniform(-2, 2))
+        cams.append(dict(eye=eye, look_at=look, up=(0, 1, 0), fov=0.8, width=width, height=height))
+    s.camera = cams[0]
+    return s, cams

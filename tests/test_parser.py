@@ -81,6 +81,32 @@ def test_instances_are_flattened():
     np.testing.assert_allclose(p / np.abs(p).max(), [0, 1, 0, -1], atol=1e-6)
 
 
+def test_large_instanced_meshes_become_shared_meshes(tmp_path):
+    """An obj under instance(...) with at least 1,024 triangles is a shared
+    mesh (one per file and material) placed by each instance's transform (a
+    two-level BVH); nested transforms multiply; a small one stays
+    flattened."""
+    pos, _ = workloads.displaced_grid(24, -1, 1, -1, 1, 0, 0.2, 5)   # 1,152 triangles
+    write_obj(str(tmp_path / "relief.obj"), pos)
+    write_obj(str(tmp_path / "small.obj"), pos[:10])
+    text = """
+    grey = diffuse([0.5 0.5 0.5]);
+    intersectable = intersectables {
+      instance(translate([1 0 0]), obj("relief.obj", grey))
+      instance(translate([0 2 0]), instance(scale(2), obj("relief.obj", grey)))
+      instance(rotate(90, [0 1 0]), obj("small.obj", diffuse([1 1 1])))
+    };
+    """
+    (tmp_path / "s.scene").write_text(text)
+    s = load_scene(str(tmp_path / "s.scene"))
+    assert len(s.meshes) == 1 and len(s.instances) == 2 and s.n_tri() == 10
+    np.testing.assert_allclose(s.meshes[0]["pos"], pos, atol=1e-6)
+    t0, t1 = (np.asarray(t) for t, _ in s.instances)
+    np.testing.assert_allclose(t0, [[1, 0, 0, 1], [0, 1, 0, 0], [0, 0, 1, 0]], atol=1e-6)
+    np.testing.assert_allclose(t1, [[2, 0, 0, 0], [0, 2, 0, 2], [0, 0, 2, 0]], atol=1e-6)
+    assert s.prim_offsets()["instances"] == 10
+
+
 def test_parse_errors_are_reported():
     with pytest.raises(GbrtError) as e:
         load_scene_string("intersectable = intersectables { quad([0 0 0], [1 0 0]) };")
