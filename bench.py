@@ -207,13 +207,26 @@ def run_guided(args):
     from renderer_gb300.guiding import Guide, guide_params, render_guided, scene_bounds
     from renderer_gb300.runtime import Context, GpuScene
 
+    from renderer_gb300.scene import render_params
+
     ctx = Context(0)
-    s = workloads.two_rooms(1024, 768, mesh_quads=500)
+    terrain = args.guided_scene == "terrain"
+    if terrain:
+        s, cams = workloads.terrain_instances(seed=0, nx=args.terrain_nx, nz=args.terrain_nx // 2)
+        full_cam = dict(cams[0])
+        s.camera = dict(cams[0], width=args.guided_width, height=args.guided_height)
+        workload = ("instanced terrain (8 x 4M-triangle instances, 200 spheres, sky), view 0 at %dx%d, physical "
+                    "semantics, max depth 16, RR p=0.5" % (args.guided_width, args.guided_height))
+    else:
+        s = workloads.two_rooms(1024, 768, mesh_quads=500)
+        workload = GUIDED_WORKLOAD
     gs = GpuScene(ctx, s)
     cam = s.camera_struct()
     bounds = scene_bounds(gs)
 
     def prm(xs, seed, flags=0):
+        if terrain:
+            return render_params(xs, xs, 0.5, 16, seed, semantics=_abi.SEM_PHYSICAL, flags=flags)
         p = workloads.two_rooms_params(xs, xs, seed=seed)
         p.flags = flags
         return p
@@ -236,6 +249,16 @@ def run_guided(args):
         z = np.load(args.ref_cache)
         ref, ref_ms = z["film"], float(z["ms"])
         assert int(z["spp"]) == ref_spp, "cached reference has another sample count"
+    elif args.ref_guided:
+        # Both estimators are unbiased; a guided reference converges where the
+        # plain one keeps rare, very bright samples (a sun seen through BSDF
+        # sampling) at this sample count.
+        g = Guide(ctx, bounds, seed=3)
+        ref, st = render_guided(gs, cam, prm(8, 1), g, train_gp(passes=ref_spp // 64))
+        ref_ms = st.total_ms
+        g.close()
+        if args.ref_cache:
+            np.savez(args.ref_cache, film=ref, ms=ref_ms, spp=ref_spp)
     else:
         ref, st = render_guided(gs, cam, prm(8, 1), None, guide_params(passes=ref_spp // 64))
         ref_ms = st.total_ms
@@ -271,7 +294,8 @@ def run_guided(args):
     t_plain = interp_time([(t, e) for t, e, _ in plain], 0.01)
     t_guided = interp_time([(t, e) for t, e, *_ in guided], 0.01)
     line = {"metric": "equal-time relMSE, guided vs plain GPU PT", "unit": "relMSE", "higher_is_better": False,
-            "config": {"workload": GUIDED_WORKLOAD, "reference_spp": ref_spp,
+            "config": {"workload": workload, "reference_spp": ref_spp,
+                       "reference_estimator": "guided" if args.ref_guided else "plain",
                        "reference_ms": ref_ms, "guide_fraction": args.guide_fraction,
                        "train": "online, Adam lr 1e-2, %d step(s) of 2^18 samples after %s one-spp pass, "
                                 "sample weights relative to their pixel"
@@ -289,6 +313,22 @@ def run_guided(args):
                                   "rows": ist.infer_rows, "ms": ist.infer_ms, "flop_per_row": f_inf},
                     "training": {"achieved": tr_tflops, "frac": tr_tflops / tc_peak if tr_tflops else None,
                                  "steps": tst.train_steps, "ms": tst.train_ms, "flop_per_sample": f_train}}}
+    if terrain:
+        # Throughput at the full 3840 x 2160 view: one-sample passes, plain
+        # and with a trained guide.
+        del gs
+        s.camera = full_cam
+        gs = GpuScene(ctx, s)
+        fcam = s.camera_struct()
+        g = Guide(ctx, scene_bounds(gs), seed=7)
+        render_guided(gs, fcam, prm(1, 5), g, train_gp(passes=8))
+        _, pst = render_guided(gs, fcam, prm(1, 6), None, guide_params(passes=4))
+        _, gst = render_guided(gs, fcam, prm(1, 7), g, guide_params(args.guide_fraction, passes=4))
+        g.close()
+        line["full_view"] = {"resolution": "%dx%d" % (fcam.width, fcam.height),
+                             "plain_paths_per_s": pst.paths / (pst.total_ms * 1e-3),
+                             "guided_paths_per_s": gst.paths / (gst.total_ms * 1e-3),
+                             "guided_infer_ms_per_pass": gst.infer_ms / max(gst.passes, 1)}
     print(json.dumps(line))
 
 
@@ -600,6 +640,12 @@ def main():
     ap.add_argument("--guided", action="store_true",
                     help="equal-time relMSE of neural path guiding against plain path tracing (two rooms)")
     ap.add_argument("--ref-spp", type=int, default=65536)
+    ap.add_argument("--guided-scene", default="rooms", choices=["rooms", "terrain"],
+                    help="--guided on the two rooms or on view 0 of the instanced terrain")
+    ap.add_argument("--ref-guided", action="store_true",
+                    help="--guided: render the reference with a guide trained online (unbiased as well)")
+    ap.add_argument("--guided-width", type=int, default=960)
+    ap.add_argument("--guided-height", type=int, default=540)
     ap.add_argument("--ref-cache", default="", help="npz file holding (or receiving) the reference render")
     ap.add_argument("--spp-list", type=lambda x: [int(v) for v in x.split(",")], default=[16, 32, 64, 128, 256, 512])
     ap.add_argument("--guide-fraction", type=float, default=0.5)
