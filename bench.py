@@ -234,7 +234,8 @@ def run_guided(args):
     def train_gp(budget_ms=0.0, passes=0):
         return guide_params(args.guide_fraction, passes=passes, train_passes=args.train_passes,
                             steps_per_pass=args.train_steps, batch_samples=1 << 18, learning_rate=1e-2,
-                            time_budget_ms=budget_ms, flags=_abi.GUIDE_PIXEL_RELATIVE)
+                            time_budget_ms=budget_ms, guide_depth=args.guide_depth, flags=_abi.GUIDE_PIXEL_RELATIVE,
+                            warmup_steps=args.warmup_steps)
 
     if args.profile:
         g = Guide(ctx, bounds, seed=1)
@@ -297,6 +298,7 @@ def run_guided(args):
             "config": {"workload": workload, "reference_spp": ref_spp,
                        "reference_estimator": "guided" if args.ref_guided else "plain",
                        "reference_ms": ref_ms, "guide_fraction": args.guide_fraction,
+                       "guide_depth": args.guide_depth, "warmup_steps": args.warmup_steps,
                        "train": "online, Adam lr 1e-2, %d step(s) of 2^18 samples after %s one-spp pass, "
                                 "sample weights relative to their pixel"
                                 % (args.train_steps, "every" if args.train_passes >= 1 << 20
@@ -649,7 +651,12 @@ def main():
     ap.add_argument("--ref-cache", default="", help="npz file holding (or receiving) the reference render")
     ap.add_argument("--spp-list", type=lambda x: [int(v) for v in x.split(",")], default=[16, 32, 64, 128, 256, 512])
     ap.add_argument("--guide-fraction", type=float, default=0.5)
+    ap.add_argument("--guide-depth", type=int, default=0, help="guide vertices i < this only (0: all)")
+    ap.add_argument("--warmup-steps", type=int, default=0, help="BSDF-only passes until this many training steps")
     ap.add_argument("--train-passes", type=int, default=1 << 30, help="passes that train (default: all)")
+    ap.add_argument("--tuned", action="store_true",
+                    help="--guided with the best settings found on the two rooms: first bounce only, 32 warm-up "
+                         "steps, training during the first 64 passes")
     ap.add_argument("--train-steps", type=int, default=1, help="Adam steps of 2^18 samples after a training pass")
     ap.add_argument("--quality", action="store_true",
                     help="relMSE of the Cornell box and icosphere images against 65,536-spp renders")
@@ -667,6 +674,8 @@ def main():
                     help="chain counts for --chains (0: the library's default)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.tuned:
+        args.guide_depth, args.warmup_steps, args.train_passes = 1, 32, 64
     if args.chains:
         run_chains(args)
         return

@@ -493,6 +493,9 @@ typedef struct gbrt_guide_params {
   int32_t guide_depth;    /* guide (and train on) path vertices i < guide_depth
                              only (vertex 0 is the camera ray's hit); 0 = all */
   int32_t flags;          /* gbrt_guide_flags */
+  int32_t warmup_steps;   /* while training, passes sample the BSDF only until
+                             this many Adam steps are done (0: guide from the
+                             pass after the first step) */
 } gbrt_guide_params;
 
 typedef enum gbrt_guide_flags {

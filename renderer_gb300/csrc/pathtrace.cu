@@ -1493,7 +1493,8 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     init_params(P, *cam, *prm, total);
     P.seed = pass_seed(prm->seed, pass);
     const bool record = training && pass < gp->train_passes;
-    P.guided = (useGuide && g->ready) ? 1 : 0;
+    // While training, sample the guide once it has had warmup_steps steps.
+    P.guided = (useGuide && g->ready && (!training || steps >= gp->warmup_steps)) ? 1 : 0;
     P.guide_frac = gp->guide_fraction;
     P.record = record ? 1 : 0;
     P.guide_depth = gp->guide_depth;
