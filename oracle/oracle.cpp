@@ -1834,7 +1834,8 @@ int orc_render_erpt(void* sp, const gbrt_camera* cam, const gbrt_render_params* 
           /* equalDispositionFlow (lines 83-118) */
           const double nc = cvNorm(c);
           const float me = float(M) * ed;
-          const int numChains = int(double(streamU(k, nd)) + nc / double(me));
+          const double xc = double(streamU(k, nd)) + nc / double(me);
+          const int numChains = xc > 0.0 ? int(xc) : 0;  /* a black scene gives 0 / 0 */
           if (numChains <= 0) continue;
           const double sc = double(ed) / nc / numChains;
           const C3 depVal(float(c.b * sc), float(c.g * sc), float(c.r * sc));

@@ -139,6 +139,32 @@ def test_mlt_full_size_identities_and_image(ctx):
     assert np.median(np.abs(bm[bright] - bp[bright]) / bp[bright]) < 0.1
 
 
+def _dark_room(n):
+    """The Cornell room without its light: every path carries nothing."""
+    s = workloads.cornell_box(n, n)
+    s.lights = []
+    return s
+
+
+def test_oracle_chains_on_a_black_scene():
+    s = _dark_room(8)
+    o = OracleScene(s)
+    r = o.render_mlt(s.camera_struct(), render_params(1, 1, 0.0, 5, 1), mlt_params(4, 100), chains=4)
+    assert r["b"] == 0 and not r["film"].any()
+    e = o.render_erpt(s.camera_struct(), render_params(1, 1, 0.0, 5, 1), erpt_params(3, 1, 1))
+    assert e["chains"] == 0 and not e["film"].any()
+
+
+@pytest.mark.gpu
+def test_chain_renderers_on_a_black_scene(ctx):
+    s = _dark_room(16)
+    gs = GpuScene(ctx, s)
+    r = MetropolisRenderer(gs, options={"met-mutations": 4, "met-bootstrap": 200}, chains=64)
+    assert not r.render().any() and r.stats.normaliser == 0 and r.stats.nonfinite == 0
+    e = EnergyRedistributionRenderer(gs, options={"erpt-mutations": 3})
+    assert not e.render().any() and e.stats.chains == 0
+
+
 @pytest.mark.gpu
 def test_chain_renderers_refuse_other_estimators(ctx):
     from renderer_gb300 import check, lib
