@@ -125,7 +125,7 @@ struct MltArgs {
   float4* curV;          // current radiance
   double* sum;           // film sums, H x W x 3
   unsigned long long* accepted;
-  unsigned long long t;  // mutation index of the iteration
+  const unsigned long long* t;  // mutation index of the iteration (device counter, advanced by k_tick)
   int N, nd;
   float large_p;
   float b;               // mean bootstrap luminance
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(256) k_mlt_propose(PTParams P, PTState st, Mlt
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   reset_queues(P, st, c);
   if (c >= A.N) return;
-  const unsigned long long key = stream_key(P.seed, tag(kMutate, A.t * unsigned(A.N) + unsigned(c)));
+  const unsigned long long key = stream_key(P.seed, tag(kMutate, *A.t * unsigned(A.N) + unsigned(c)));
   const bool large = stream_u(key, 0) < A.large_p;
   for (int d = 0; d < A.nd; ++d) {
     const size_t o = size_t(d) * A.N + c;
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(256) k_mlt_propose(PTParams P, PTState st, Mlt
 __global__ void __launch_bounds__(256) k_mlt_accept(PTParams P, PTState st, MltArgs A) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= A.N) return;
-  const unsigned long long key = stream_key(P.seed, tag(kMutate, A.t * unsigned(A.N) + unsigned(c)));
+  const unsigned long long key = stream_key(P.seed, tag(kMutate, *A.t * unsigned(A.N) + unsigned(c)));
   const float4 nv = finite_or_zero(st.L[c], &st.tally[2]);
   const float4 cv = A.curV[c];
   const float lc = lum_bgr(cv), ln = lum_bgr(nv);
@@ -207,7 +207,8 @@ struct ErptArgs {
   unsigned long long* accepted;
   long long q0;          // first chain of the batch
   long long n_init;
-  int B, nd, xs, ys, M, m;
+  const unsigned long long* m;  // mutation of the chains (device counter, advanced by k_tick)
+  int B, nd, xs, ys, M;
   float ed;
 };
 
@@ -323,7 +324,7 @@ __global__ void __launch_bounds__(256) k_erpt_propose(PTParams P, PTState st, Er
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   reset_queues(P, st, slot);
   if (slot >= P.nb) return;
-  const unsigned long long id = (unsigned long long)(A.q0 + slot) * unsigned(A.M) + unsigned(A.m);
+  const unsigned long long id = (unsigned long long)(A.q0 + slot) * unsigned(A.M) + *A.m;
   const unsigned long long key = stream_key(P.seed, tag(kFlow, id));
   for (int d = 0; d < A.nd; ++d) {
     const size_t o = size_t(d) * A.B + slot;
@@ -339,7 +340,7 @@ __global__ void __launch_bounds__(256) k_erpt_propose(PTParams P, PTState st, Er
 __global__ void __launch_bounds__(256) k_erpt_accept(PTParams P, PTState st, ErptArgs A) {
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= P.nb) return;
-  const unsigned long long id = (unsigned long long)(A.q0 + slot) * unsigned(A.M) + unsigned(A.m);
+  const unsigned long long id = (unsigned long long)(A.q0 + slot) * unsigned(A.M) + *A.m;
   const unsigned long long key = stream_key(P.seed, tag(kFlow, id));
   const float4 zv = finite_or_zero(st.L[slot], &st.tally[2]);
   const float4 yv = A.yV[slot];
@@ -362,6 +363,9 @@ __global__ void __launch_bounds__(256) k_erpt_accept(PTParams P, PTState st, Erp
                   __double2float_rn(__dmul_rn(double(t.z), in)), 0.f);
   deposit(A.sum, P.cam.W, P.cam.H, A.y[slot], A.y[size_t(A.B) + slot], isp, t);
 }
+
+// Advances an iteration counter (the last node of an iteration's graph).
+__global__ void k_tick(unsigned long long* counter) { ++*counter; }
 
 // Inclusive prefix sums of n ints into long longs: per-block scans, a scan of
 // the block totals by one block, then the block offsets added.
@@ -449,11 +453,32 @@ static unsigned long long run_wave(gbrt_scene* s, const Wave& w, const PTParams&
                                    cudaStream_t stream) {
   for (int it = 0; it < P.D; ++it) {
     const int cur = it & 1;
-    w.tk.ext<<<w.traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
-    w.shade<<<w.shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
-    w.tk.sh<<<w.shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
+    w.tk.ext<<<cap_grid(w.traceGrid, P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st, cur);
+    w.shade<<<cap_grid(w.shadeGrid, P.nb, 256), 256, 0, stream>>>(s->view, P, st, cur);
+    w.tk.sh<<<cap_grid(w.shadowGrid, 2ll * P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st);
   }
   return 3ull * unsigned(P.D);
+}
+
+// Runs `iterations` times the launches that `enqueue` issues on stream: they
+// are captured once into a CUDA graph and the graph is replayed, so an
+// iteration of many small launches (few chains) costs one graph launch of
+// host time. The launches read their iteration number from a device counter
+// that the captured sequence advances.
+template <class F>
+static cudaError_t replay(cudaStream_t stream, long long iterations, F enqueue) {
+  if (iterations <= 0) return cudaSuccess;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  enqueue();
+  e = cudaStreamEndCapture(stream, &graph);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  for (long long k = 0; k < iterations && e == cudaSuccess; ++k) e = cudaGraphLaunch(exec, stream);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  return e;
 }
 
 static cudaError_t alloc_state(gbrt_scene* s, Buffers& buf, PTState& st, long long B) {
@@ -606,10 +631,13 @@ static gbrt_status mlt_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_re
     pick[c] = int(std::min<long long>(bi, nb - 1));
   }
   A(cudaMemcpyAsync(d_pick, pick.data(), sizeof(int) * N, cudaMemcpyHostToDevice, stream));
+  unsigned long long* d_iter = nullptr;
+  A(buf.alloc(&d_iter, 1));
+  A(cudaMemsetAsync(d_iter, 0, sizeof(unsigned long long), stream));
   chain::MltArgs MA;
   MA.cur = cur; MA.prop = prop; MA.curV = curV; MA.sum = d_sum; MA.accepted = d_acc;
   MA.N = int(N); MA.nd = nd; MA.large_p = mp->large_step_prob; MA.b = b; MA.mutations = float(mp->mutations);
-  MA.t = 0;
+  MA.t = d_iter;
   P.g0 = 0;
   P.nb = int(N);
   const int grid = int((N + 255) / 256);
@@ -623,12 +651,15 @@ static gbrt_status mlt_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_re
                      : 0.f;
   P.pss = prop;
   P.pss_stride = int(N);
-  for (long long t = 0; t < M && e == cudaSuccess; ++t) {
-    MA.t = (unsigned long long)t;
-    chain::k_mlt_propose<<<grid, 256, 0, stream>>>(P, st, MA);
-    launches += 2 + run_wave(s, wP, P, st, stream);
-    chain::k_mlt_accept<<<grid, 256, 0, stream>>>(P, st, MA);
-    A(cudaGetLastError());
+  if (e == cudaSuccess) {
+    unsigned long long per = 0;
+    A(replay(stream, M, [&] {
+      chain::k_mlt_propose<<<grid, 256, 0, stream>>>(P, st, MA);
+      per = 3 + run_wave(s, wP, P, st, stream);
+      chain::k_mlt_accept<<<grid, 256, 0, stream>>>(P, st, MA);
+      chain::k_tick<<<1, 1, 0, stream>>>(d_iter);
+    }));
+    launches += per * (unsigned long long)M;
   }
   unsigned long long acc = 0;
   if (e == cudaSuccess) A(cudaMemcpyAsync(&acc, d_acc, sizeof acc, cudaMemcpyDeviceToHost, stream));
@@ -678,6 +709,9 @@ static gbrt_status erpt_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_r
   A(buf.alloc(&d_sum, n3)); A(buf.alloc(&d_film, n3)); A(buf.alloc(&d_ed, 3));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "gbrt_render_erpt buffers");
   if (nblk > (long long)chain::kScanBlock * 4096) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_erpt: too many samples");
+  unsigned long long* d_iter = nullptr;
+  A(buf.alloc(&d_iter, 1));
+  EA.m = d_iter;
   EA.incl = incl;
   EA.sum = d_sum;
   EA.nd = nd; EA.xs = xs; EA.ys = ys; EA.M = M; EA.B = int(B); EA.n_init = n_init;
@@ -759,14 +793,16 @@ static gbrt_status erpt_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_r
     P.nb = nq;
     const int grid = (nq + 255) / 256;
     chain::k_erpt_chain_init<<<grid, 256, 0, stream>>>(P, EA, nq);
+    A(cudaMemsetAsync(d_iter, 0, sizeof(unsigned long long), stream));
     ++launches;
-    for (int m = 0; m < M && e == cudaSuccess; ++m) {
-      EA.m = m;
+    unsigned long long per = 0;
+    A(replay(stream, M, [&] {
       chain::k_erpt_propose<<<grid, 256, 0, stream>>>(P, st, EA);
-      launches += 2 + run_wave(s, wP, P, st, stream);
+      per = 3 + run_wave(s, wP, P, st, stream);
       chain::k_erpt_accept<<<grid, 256, 0, stream>>>(P, st, EA);
-      A(cudaGetLastError());
-    }
+      chain::k_tick<<<1, 1, 0, stream>>>(d_iter);
+    }));
+    launches += per * (unsigned long long)M;
   }
   paths += (unsigned long long)T * unsigned(M);
   unsigned long long acc = 0;

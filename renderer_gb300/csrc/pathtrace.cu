@@ -289,6 +289,14 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState s
   if (COUNT) warp_add_counters(cnt, &st.tally[5], &st.tally[6]);
 }
 
+// A persistent grid no larger than a wavefront of `items` needs (each warp
+// fetches 32 items at a time; a shade thread takes one): small wavefronts
+// then launch a few blocks instead of a full grid that exits at once.
+static inline int cap_grid(int full, long long items, int per_block) {
+  const long long need = (items + per_block - 1) / per_block;
+  return int(std::max<long long>(1, std::min<long long>(full, need)));
+}
+
 // -------------------------------------------------------------- shade ----
 // Queue push aggregated over the threads of a warp that reach it together
 // (one atomic per converged group), so a push can sit inside divergent code
@@ -1088,11 +1096,11 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
     for (int it = 0; it < P.D; ++it) {
       int cur = it & 1;
       if (timeK) mark();
-      kExt<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
+      kExt<<<cap_grid(traceGrid, P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st, cur);
       if (timeK) mark();
-      kShade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
+      kShade<<<cap_grid(shadeGrid, P.nb, 256), 256, 0, stream>>>(s->view, P, st, cur);
       if (timeK) mark();
-      kSh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
+      kSh<<<cap_grid(shadowGrid, 2ll * P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st);
       if (timeK) mark();
       launches += 3;
     }
@@ -1291,9 +1299,9 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
     ++launches;
     for (int it = 0; it < P.D; ++it) {
       int cur = it & 1;
-      kExt<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
-      kShade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
-      kSh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
+      kExt<<<cap_grid(traceGrid, P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st, cur);
+      kShade<<<cap_grid(shadeGrid, P.nb, 256), 256, 0, stream>>>(s->view, P, st, cur);
+      kSh<<<cap_grid(shadowGrid, 2ll * P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st);
       launches += 3;
     }
     unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
@@ -1511,7 +1519,7 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
       k_raygen<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
       for (int it = 0; it < P.D; ++it) {
         int cur = it & 1;
-        tk.ext<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
+        tk.ext<<<cap_grid(traceGrid, P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st, cur);
         if (P.guided && (P.guide_depth == 0 || it < P.guide_depth)) {
           cudaEvent_t ea = nullptr, eb = nullptr;
           if (timeK) {
@@ -1528,8 +1536,8 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
           }
           ++infer_launches;
         }
-        kShade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
-        tk.sh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
+        kShade<<<cap_grid(shadeGrid, P.nb, 256), 256, 0, stream>>>(s->view, P, st, cur);
+        tk.sh<<<cap_grid(shadowGrid, 2ll * P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st);
       }
       unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
       launch_accumulate(P, st, d_pass, nullptr, stream);
@@ -1691,9 +1699,9 @@ static cudaError_t enqueue_job(gbrt_scene* s, const gbrt_camera& cam, const gbrt
     k_raygen<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
     for (int it = 0; it < P.D; ++it) {
       int cur = it & 1;
-      tk.ext<<<traceGrid, kTraceBlock, 0, stream>>>(s->view, st, cur);
-      kShade<<<shadeGrid, 256, 0, stream>>>(s->view, P, st, cur);
-      tk.sh<<<shadowGrid, kTraceBlock, 0, stream>>>(s->view, st);
+      tk.ext<<<cap_grid(traceGrid, P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st, cur);
+      kShade<<<cap_grid(shadeGrid, P.nb, 256), 256, 0, stream>>>(s->view, P, st, cur);
+      tk.sh<<<cap_grid(shadowGrid, 2ll * P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st);
     }
     launch_accumulate(P, st, d_sum, nullptr, stream);
     *launches += 2 + 3ull * unsigned(P.D);
