@@ -234,7 +234,8 @@ def run_guided(args):
     def train_gp(budget_ms=0.0, passes=0):
         return guide_params(args.guide_fraction, passes=passes, train_passes=args.train_passes,
                             steps_per_pass=args.train_steps, batch_samples=1 << 18, learning_rate=1e-2,
-                            time_budget_ms=budget_ms, guide_depth=args.guide_depth, flags=_abi.GUIDE_PIXEL_RELATIVE,
+                            time_budget_ms=budget_ms, guide_depth=args.guide_depth,
+                            flags=0 if args.absolute_weights else _abi.GUIDE_PIXEL_RELATIVE,
                             warmup_steps=args.warmup_steps)
 
     if args.profile:
@@ -653,6 +654,8 @@ def main():
     ap.add_argument("--guide-fraction", type=float, default=0.5)
     ap.add_argument("--guide-depth", type=int, default=0, help="guide vertices i < this only (0: all)")
     ap.add_argument("--warmup-steps", type=int, default=0, help="BSDF-only passes until this many training steps")
+    ap.add_argument("--absolute-weights", action="store_true",
+                    help="--guided: training weights not relative to the sample's pixel")
     ap.add_argument("--train-passes", type=int, default=1 << 30, help="passes that train (default: all)")
     ap.add_argument("--tuned", action="store_true",
                     help="--guided with the best settings found on the two rooms: first bounce only, 32 warm-up "
