@@ -348,6 +348,13 @@ def run_quality(args):
     def relmse(x, ref):
         return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
 
+    def spread(x, ref):
+        """Per-pixel relative squared errors: median, and the mean without
+        the 0.1 % largest (rare, very bright samples dominate the mean)."""
+        e = ((x - ref) ** 2 / (ref ** 2 + 1e-2)).mean(-1).ravel()
+        e.sort()
+        return {"median": float(np.median(e)), "mean_without_top_0.1pct": float(e[: int(len(e) * 0.999)].mean())}
+
     ctx = Context(0)
     out = {"metric": "relMSE vs 65,536-spp FP64-accumulated render", "unit": "relMSE", "higher_is_better": False,
            "images": []}
@@ -368,8 +375,9 @@ def run_quality(args):
     orc = OracleScene(s).render(cam, workloads.cornell_params(8, 3), rng_mode=0)
     tcpu = time.perf_counter() - t0
     out["images"].append({"config": "Cornell box 256x256, 16 spp, depth 8, RR p=0.5 (reference semantics)",
-                          "reference": {"spp": 65536, "s": tref}, "gpu": {"relmse": relmse(img, ref), "s": t},
-                          "oracle_cpu": {"relmse": relmse(orc["film"], ref), "s": tcpu},
+                          "reference": {"spp": 65536, "s": tref},
+                          "gpu": {"relmse": relmse(img, ref), "s": t, **spread(img, ref)},
+                          "oracle_cpu": {"relmse": relmse(orc["film"], ref), "s": tcpu, **spread(orc["film"], ref)},
                           "gpu_vs_oracle_mean": float(img.mean() / orc["film"].mean())})
     del gs
     # icosphere frame
@@ -379,7 +387,7 @@ def run_quality(args):
     ref, tref = gpu(256, 7, 12)
     img, t = gpu(8, 1, 12)
     out["images"].append({"config": WORKLOAD, "reference": {"spp": 65536, "s": tref},
-                          "gpu": {"relmse": relmse(img, ref), "s": t}})
+                          "gpu": {"relmse": relmse(img, ref), "s": t, **spread(img, ref)}})
     print(json.dumps(out))
 
 
