@@ -117,13 +117,18 @@ __device__ __forceinline__ void wg_handoff(int id) {
   tc_fence_after();
 }
 
-// Encoding groups [g0, g1) of row r into an interleaved [128][8 (g1 - g0)] tile.
-__device__ __forceinline__ void write_enc_range(uint32_t s, int r, const EncIn& e, int g0, int g1) {
-  const int K = 8 * (g1 - g0);
-  for (int g = g0; g < g1; ++g) {
+// Encoding groups [G0, G1) of row r into an interleaved [128][8 (G1 - G0)]
+// tile. Unrolled, so that every group's coordinate, band and bin are
+// compile-time constants (no division, no indexing of the input by a
+// run-time value).
+template <int G0, int G1>
+__device__ __forceinline__ void write_enc_range(uint32_t s, int r, const EncIn& e) {
+  constexpr int K = 8 * (G1 - G0);
+#pragma unroll
+  for (int g = G0; g < G1; ++g) {
     float f[8];
     enc_group(e, g, f);
-    st_shared_v4(s + ik_off(r, 8 * (g - g0), K), pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]),
+    st_shared_v4(s + ik_off(r, 8 * (g - G0), K), pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]),
                  pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
   }
 }
@@ -154,10 +159,16 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
   uint32_t phase = 0;
   bool ok = true;
   // One chain of products committed to this warpgroup's barrier, then the
-  // wait; false (for the whole warpgroup) when the wait timed out.
+  // wait; false (for the whole warpgroup) when the wait timed out. One thread
+  // polls the mbarrier; the other 127 block at the named barrier, which
+  // issues nothing while the tensor cores work, so the warpgroups still
+  // encoding keep the issue slots.
   auto chain_wait = [&]() -> bool {
-    if (t == 0) mma_commit(bar);
-    bool fine = mbar_wait(bar, phase);
+    bool fine = true;
+    if (t == 0) {
+      mma_commit(bar);
+      fine = mbar_wait(bar, phase);
+    }
     phase ^= 1;
     if (wg_sync_or(bid, !fine)) return false;
     tc_fence_after();
@@ -173,11 +184,11 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
       e = make_enc(net, net.lo[0], net.lo[1], net.lo[2], 0.f, 0.f, 1.f, 0.f, 0.f, 1.f);
     }
     // Layer 1 in two halves of the input.
-    write_enc_range(sX, t, e, 0, kEncA);
+    write_enc_range<0, kEncA>(sX, t, e);
     wg_handoff(bid);
     if (t == 0) gemm_k(tmem, sX, 8 * kEncA, sW1, kIn, 8 * kEncA, kHid, false);
     if (!(ok = chain_wait())) break;
-    write_enc_range(sX, t, e, kEncA, kEncA + kEncB);
+    write_enc_range<kEncA, kEncA + kEncB>(sX, t, e);
     wg_handoff(bid);
     if (t == 0) gemm_k(tmem, sX, 8 * kEncB, sW1 + kEncA * 128, kIn, 8 * kEncB, kHid, true);
     if (!(ok = chain_wait())) break;
@@ -352,8 +363,11 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
 
   // One chain of products, then the wait; false when the wait timed out.
   auto sync_chain = [&]() -> bool {
-    if (t == 0) mma_commit(bar);
-    bool fine = mbar_wait(bar, phase);
+    bool fine = true;
+    if (t == 0) {  // one thread polls; the block waits at the barrier
+      mma_commit(bar);
+      fine = mbar_wait(bar, phase);
+    }
     phase ^= 1;
     if (__syncthreads_or(!fine)) return false;
     tc_fence_after();
@@ -432,8 +446,15 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
     }
     if (!(ok = sync_chain())) break;
     backprop_delta(lane + kColScratch, sm + kTX1, 0u, sDT, t);
-    // ---- layer 1: the encoding again, transposed, into R
-    for (int f = 0; f < kIn; ++f) st_shared_u16(sR + ik_off(f, t, kRows), bf16_bits(enc_feature(e, f)));
+    // ---- layer 1: the encoding again, transposed, into R (groups of eight
+    // features, unrolled like the row-wise writer)
+#pragma unroll
+    for (int g = 0; g < kIn / 8; ++g) {
+      float fv[8];
+      enc_group(e, g, fv);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) st_shared_u16(sR + ik_off(8 * g + q, t, kRows), bf16_bits(fv[q]));
+    }
     handoff();
     if (t == 0) {
       gemm_k(tmem + kColW1lo, sR, kRows, sDT, kRows, kRows, kHid, !first);

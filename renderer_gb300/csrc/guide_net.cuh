@@ -248,9 +248,10 @@ __device__ __forceinline__ void enc_group(const EncIn& e, int g, float* out) {
   }
 }
 
-// Writes row r's encoding into an interleaved [128][208] tile.
+// Writes row r's encoding into an interleaved [128][208] tile (unrolled:
+// every group's coordinate, band and bin are compile-time constants).
 __device__ __forceinline__ void write_enc_row(uint32_t s, int r, const EncIn& e) {
-#pragma unroll 2
+#pragma unroll
   for (int g = 0; g < kIn / 8; ++g) {
     float f[8];
     enc_group(e, g, f);
