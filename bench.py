@@ -666,8 +666,9 @@ def main():
                     help="--guided: training weights not relative to the sample's pixel")
     ap.add_argument("--train-passes", type=int, default=1 << 30, help="passes that train (default: all)")
     ap.add_argument("--tuned", action="store_true",
-                    help="--guided with the best settings found on the two rooms: first bounce only, 32 warm-up "
-                         "steps, training during the first 64 passes")
+                    help="--guided with the best settings found on the two rooms: sample weights not relative to "
+                         "their pixel, 8 Adam steps after each of the first 32 passes, BSDF-only passes for the "
+                         "first 128 steps")
     ap.add_argument("--train-steps", type=int, default=1, help="Adam steps of 2^18 samples after a training pass")
     ap.add_argument("--quality", action="store_true",
                     help="relMSE of the Cornell box and icosphere images against 65,536-spp renders")
@@ -686,7 +687,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.tuned:
-        args.guide_depth, args.warmup_steps, args.train_passes = 1, 32, 64
+        args.absolute_weights, args.train_steps, args.train_passes, args.warmup_steps = True, 8, 32, 128
     if args.chains:
         run_chains(args)
         return
