@@ -73,18 +73,19 @@ static_assert(kEncA + kEncB == kIn / 8, "encoding halves");
 // [128][64] tile at s; also returns the values (for the transposed copy).
 __device__ __forceinline__ void hidden_to_smem(uint32_t lane_taddr, uint32_t s, int r, float* h) {
 #pragma unroll
-  for (int c = 0; c < kHid; c += 16) {
-    float v[16];
-    tmem_ld16(lane_taddr + c, v);
+  for (int c = 0; c < kHid; c += 32) {
+    float v[32];
+    tmem_ld32(lane_taddr + c, v);
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.f);
-    st_shared_v4(s + ik_off(r, c, kHid), pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
-                 pack_bf16(v[6], v[7]));
-    st_shared_v4(s + ik_off(r, c + 8, kHid), pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]),
-                 pack_bf16(v[12], v[13]), pack_bf16(v[14], v[15]));
+    for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i], 0.f);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      st_shared_v4(s + ik_off(r, c + 8 * q, kHid), pack_bf16(v[8 * q], v[8 * q + 1]),
+                   pack_bf16(v[8 * q + 2], v[8 * q + 3]), pack_bf16(v[8 * q + 4], v[8 * q + 5]),
+                   pack_bf16(v[8 * q + 6], v[8 * q + 7]));
     if (h) {
 #pragma unroll
-      for (int i = 0; i < 16; ++i) h[c + i] = v[i];
+      for (int i = 0; i < 32; ++i) h[c + i] = v[i];
     }
   }
 }
@@ -206,8 +207,7 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
         hidden_to_smem(lane, sX, t, nullptr);
       } else {
         float o[kOutPad];
-        tmem_ld16(lane, o);
-        tmem_ld16(lane + 16, o + 16);
+        tmem_ld32(lane, o);
         tmem_ld16(lane + 32, o + 32);
         if (r < n) {
           Mixture m;
