@@ -433,7 +433,7 @@ gbrt_status gbrt_render_batch(gbrt_ctx* ctx, const gbrt_batch_job* jobs,
                               int32_t n, int32_t streams, int64_t batch_paths,
                               double* job_ms, gbrt_batch_stats* stats);
 /* Renders up to 8 of the jobs at one sample per pixel with 1, 2, 4 and 8
- * streams and wavefronts of 2^20 and 2^22 paths, keeps the fastest pair on
+ * streams and wavefronts of 2^20, 2^22 and 2^24 paths, keeps the fastest pair on
  * the context (for later calls with 0s) and returns it. Films are not
  * written. */
 gbrt_status gbrt_batch_autotune(gbrt_ctx* ctx, const gbrt_batch_job* jobs,
@@ -571,7 +571,7 @@ typedef struct gbrt_erpt_params {
   int32_t x_samples;        /* --erpt-x-samples (2)                           */
   int32_t y_samples;        /* --erpt-y-samples (2)                           */
   int32_t pad;
-  int64_t batch_chains;     /* chains per wavefront; 0 = 2^20                 */
+  int64_t batch_chains;     /* chains per wavefront; 0 = 2^22                 */
 } gbrt_erpt_params;
 
 typedef struct gbrt_chain_stats {

@@ -565,7 +565,7 @@ static gbrt_status mlt_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_re
   const long long B = std::max(N, Bb);
   const size_t n3 = size_t(W) * H * 3;
 
-  Buffers buf(stream);
+  Buffers buf(ctx, stream);
   PTState st;
   cudaError_t e = alloc_state(s, buf, st, B);
   float *cur = nullptr, *prop = nullptr, *d_film = nullptr;
@@ -688,10 +688,10 @@ static gbrt_status erpt_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_r
   const int xs = ep->x_samples, ys = ep->y_samples, spp = xs * ys, M = ep->mutations;
   const long long npix = (long long)W * H, n_init = npix * spp;
   const long long B = std::max<long long>(1, ep->batch_chains > 0 ? std::min<long long>(ep->batch_chains, 1ll << 26)
-                                                                  : (1ll << 20));
+                                                                  : (1ll << 22));
   const size_t n3 = size_t(npix) * 3;
 
-  Buffers buf(stream);
+  Buffers buf(ctx, stream);
   PTState st;
   cudaError_t e = alloc_state(s, buf, st, B);
   chain::ErptArgs EA;

@@ -18,6 +18,11 @@ struct gbrt_ctx {
   // word, reused by every call on this context.
   unsigned long long* d_work = nullptr;
   int* d_err = nullptr;
+  // The context's own stream-ordered memory pool: every per-call buffer
+  // (wavefront state, films, queries) comes from it, and it keeps freed
+  // memory reserved (release threshold unlimited), so that repeated renders
+  // with gigabyte-sized wavefronts do not go back to the driver each time.
+  cudaMemPool_t pool = nullptr;
   // Streams of gbrt_render_batch and the tuned batch settings.
   std::vector<cudaStream_t> batch_streams;
   int batch_streams_tuned = 4;
@@ -45,6 +50,15 @@ namespace gbrt {
 gbrt_status fail(gbrt_ctx* ctx, gbrt_status st, const std::string& msg);
 gbrt_status cuda_fail(gbrt_ctx* ctx, cudaError_t e, const char* what);
 void clear_error(gbrt_ctx* ctx);
+
+// Stream-ordered allocation from the context's pool (cudaFreeAsync frees).
+inline cudaError_t ctx_alloc(const gbrt_ctx* ctx, void** p, size_t bytes, cudaStream_t stream) {
+  return cudaMallocFromPoolAsync(p, bytes, ctx->pool, stream);
+}
+template <typename T>
+inline cudaError_t ctx_alloc(const gbrt_ctx* ctx, T** p, size_t bytes, cudaStream_t stream) {
+  return ctx_alloc(ctx, reinterpret_cast<void**>(p), bytes, stream);
+}
 
 #define GBRT_CUDA_TRY(ctx, expr)                              \
   do {                                                        \

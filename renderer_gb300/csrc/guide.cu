@@ -717,8 +717,8 @@ gbrt_status gbrt_guide_eval(gbrt_guide* g, const float* inputs, size_t n, float*
     h[3 * i + 2] = make_float4(r[6], r[7], r[8], 0.f);
   }
   float4 *d_in = nullptr, *d_mix = nullptr;
-  cudaError_t e = cudaMallocAsync(&d_in, h.size() * sizeof(float4), s);
-  if (e == cudaSuccess) e = cudaMallocAsync(&d_mix, kMixStride * n * sizeof(float4), s);
+  cudaError_t e = ctx_alloc(g->ctx, &d_in, h.size() * sizeof(float4), s);
+  if (e == cudaSuccess) e = ctx_alloc(g->ctx, &d_mix, kMixStride * n * sizeof(float4), s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = launch_infer(g, d_in, nullptr, int(n), d_mix, s);
   if (e == cudaSuccess)
@@ -741,7 +741,7 @@ static gbrt_status upload_samples(gbrt_guide* g, const float* samples, size_t n,
     h[4 * i + 3] = make_float4(r[9], r[10], r[11], 0.f);
   }
   cudaStream_t s = g->ctx->stream;
-  cudaError_t e = cudaMallocAsync(d_out, h.size() * sizeof(float4), s);
+  cudaError_t e = ctx_alloc(g->ctx, d_out, h.size() * sizeof(float4), s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(*d_out, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(g->ctx, e, "guide samples");

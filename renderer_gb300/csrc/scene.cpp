@@ -217,6 +217,19 @@ gbrt_status gbrt_ctx_create(int32_t device, gbrt_ctx** out) {
     delete c;
     return cuda_fail(nullptr, e, "cudaMalloc(ctx scratch)");
   }
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  if ((e = cudaMemPoolCreate(&c->pool, &props)) != cudaSuccess) {
+    cudaFree(c->d_work);
+    cudaFree(c->d_err);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return cuda_fail(nullptr, e, "cudaMemPoolCreate");
+  }
+  uint64_t keep = ~0ull;  // freed memory stays in the pool for the next call
+  cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   *out = c;
   return GBRT_OK;
 }
@@ -232,6 +245,7 @@ gbrt_status gbrt_ctx_destroy(gbrt_ctx* ctx) {
     cudaStreamDestroy(s);
   }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   delete ctx;
   return GBRT_OK;
 }

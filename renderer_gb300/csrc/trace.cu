@@ -131,8 +131,8 @@ gbrt_status gbrt_trace_closest(gbrt_scene* s, const gbrt_ray* rays, int64_t n, g
   GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
   gbrt_ray* d_r = nullptr;
   gbrt_hit* d_h = nullptr;
-  GBRT_CUDA_TRY(ctx, cudaMallocAsync(&d_r, size_t(n) * sizeof(gbrt_ray), ctx->stream));
-  cudaError_t e = cudaMallocAsync(&d_h, size_t(n) * sizeof(gbrt_hit), ctx->stream);
+  GBRT_CUDA_TRY(ctx, ctx_alloc(ctx, &d_r, size_t(n) * sizeof(gbrt_ray), ctx->stream));
+  cudaError_t e = ctx_alloc(ctx, &d_h, size_t(n) * sizeof(gbrt_hit), ctx->stream);
   if (e != cudaSuccess) { cudaFreeAsync(d_r, ctx->stream); return cuda_fail(ctx, e, "cudaMallocAsync(hits)"); }
   gbrt_status st = GBRT_OK;
   if ((e = cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream)) != cudaSuccess ||
@@ -163,9 +163,9 @@ gbrt_status gbrt_trace_any(gbrt_scene* s, const gbrt_ray* rays, const int32_t* i
   uint8_t* d_o = nullptr;
   cudaError_t e;
   gbrt_status st = GBRT_OK;
-  if ((e = cudaMallocAsync(&d_r, size_t(n) * sizeof(gbrt_ray), ctx->stream)) != cudaSuccess ||
-      (e = cudaMallocAsync(&d_o, size_t(n), ctx->stream)) != cudaSuccess ||
-      (ignore && (e = cudaMallocAsync(&d_i, size_t(n) * sizeof(int32_t), ctx->stream)) != cudaSuccess))
+  if ((e = ctx_alloc(ctx, &d_r, size_t(n) * sizeof(gbrt_ray), ctx->stream)) != cudaSuccess ||
+      (e = ctx_alloc(ctx, &d_o, size_t(n), ctx->stream)) != cudaSuccess ||
+      (ignore && (e = ctx_alloc(ctx, &d_i, size_t(n) * sizeof(int32_t), ctx->stream)) != cudaSuccess))
     st = cuda_fail(ctx, e, "cudaMallocAsync(trace_any)");
   if (st == GBRT_OK &&
       ((e = cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream)) != cudaSuccess ||
