@@ -819,7 +819,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "paths_per_step": tot["paths"] // args.steps,
                        "bvh_build": "gpu (linear BVH)" if args.gpu_build else "host (binned SAH)",
-                       "l2": "inputs larger than L2 (scene ~240 MB, path state ~1.2 GB per wavefront)",
+                       "l2": "inputs larger than L2 (scene ~240 MB, path state ~10 GB per wavefront)",
                        "scene_build_ms": info["build_ms"], "bvh_nodes": info["nodes"],
                        "bvh_max_depth": info["max_depth"], "wall_s_timed": wall,
                        "rays_per_s": (tot["ext_rays"] + tot["sh_rays"]) * ws / (ms / 1000.0),
