@@ -308,6 +308,12 @@ const char* gbrt_last_error(const gbrt_ctx* ctx);
  *      src/renderingmanager.cpp:8-59, src/renderer.cpp:131-145) ---------- */
 gbrt_status gbrt_ctx_create(int32_t device, gbrt_ctx** out);
 gbrt_status gbrt_ctx_destroy(gbrt_ctx* ctx);
+/* Per-call device buffers (wavefront state, films) come from a memory pool
+ * of the context that keeps freed memory reserved for the next call (about
+ * 10 GB after a render with the default wavefront). This returns the
+ * reserved, unused part to the driver (and reports how many bytes the pool
+ * still holds; may be NULL). */
+gbrt_status gbrt_ctx_trim(gbrt_ctx* ctx, uint64_t* reserved_bytes);
 
 /* ---- scene (replaces scene_builder::getScene + Intersectable::createBVH,
  *      src/sceneast.cpp:673-695, src/intersectable.cpp:11-14,

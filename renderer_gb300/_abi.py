@@ -196,6 +196,7 @@ SIGNATURES = [
                                     C.POINTER(C.c_double), C.POINTER(BatchStats)]),
     ("gbrt_batch_autotune", C.c_int, [P, C.POINTER(BatchJob), C.c_int32, C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int64)]),
+    ("gbrt_ctx_trim", C.c_int, [P, C.POINTER(C.c_uint64)]),
     ("gbrt_render_mlt", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), C.POINTER(MltParams), P,
                                   C.POINTER(ChainStats)]),
     ("gbrt_render_erpt", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), C.POINTER(ErptParams), P,

@@ -250,6 +250,21 @@ gbrt_status gbrt_ctx_destroy(gbrt_ctx* ctx) {
   return GBRT_OK;
 }
 
+gbrt_status gbrt_ctx_trim(gbrt_ctx* ctx, uint64_t* reserved_bytes) {
+  if (!ctx) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_ctx_trim: NULL context");
+  clear_error(ctx);
+  GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  GBRT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  for (cudaStream_t s : ctx->batch_streams) GBRT_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  GBRT_CUDA_TRY(ctx, cudaMemPoolTrimTo(ctx->pool, 0));
+  if (reserved_bytes) {
+    uint64_t v = 0;
+    GBRT_CUDA_TRY(ctx, cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrReservedMemCurrent, &v));
+    *reserved_bytes = v;
+  }
+  return GBRT_OK;
+}
+
 gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scene** out) {
   if (!ctx || !d || !out) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_scene_create: NULL argument");
   *out = nullptr;

@@ -46,6 +46,13 @@ class Context:
         check(lib().gbrt_ctx_create(int(device), C.byref(h)))
         self.handle = h
 
+    def trim(self):
+        """Returns the memory the context's pool keeps between calls to the
+        driver (gbrt_ctx_trim); the bytes it still holds."""
+        v = C.c_uint64()
+        check(lib().gbrt_ctx_trim(self.handle, C.byref(v)), self.handle)
+        return v.value
+
     def close(self):
         for sc in list(self._scenes):
             sc.close()

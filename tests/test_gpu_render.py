@@ -263,3 +263,14 @@ def test_physical_statistical_parity(ctx):
     assert (np.abs(z) > 4).sum() <= bound
     assert abs(z.mean()) < 0.05
     assert abs(ma.mean() - mb.mean()) / mb.mean() < 0.01
+
+
+@pytest.mark.gpu
+def test_context_pool_keeps_then_trims(ctx):
+    """Renders reuse the context pool's memory; trimming hands it back."""
+    s = workloads.cornell_box(64, 64)
+    r = PerPixelRenderer(GpuScene(ctx, s), options={"pt-x-samples": 2, "pt-y-samples": 2})
+    a = r.render()
+    b = r.render()
+    assert np.allclose(a, b, rtol=1e-6, atol=1e-7)  # same paths; shadow-ray adds are atomics
+    assert ctx.trim() == 0
