@@ -77,15 +77,13 @@ __device__ __forceinline__ void hidden_to_smem(uint32_t lane_taddr, uint32_t s, 
     float v[32];
     tmem_ld32(lane_taddr + c, v);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i], 0.f);
-#pragma unroll
     for (int q = 0; q < 4; ++q)
-      st_shared_v4(s + ik_off(r, c + 8 * q, kHid), pack_bf16(v[8 * q], v[8 * q + 1]),
-                   pack_bf16(v[8 * q + 2], v[8 * q + 3]), pack_bf16(v[8 * q + 4], v[8 * q + 5]),
-                   pack_bf16(v[8 * q + 6], v[8 * q + 7]));
+      st_shared_v4(s + ik_off(r, c + 8 * q, kHid), pack_relu_bf16(v[8 * q], v[8 * q + 1]),
+                   pack_relu_bf16(v[8 * q + 2], v[8 * q + 3]), pack_relu_bf16(v[8 * q + 4], v[8 * q + 5]),
+                   pack_relu_bf16(v[8 * q + 6], v[8 * q + 7]));
     if (h) {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) h[c + i] = v[i];
+      for (int i = 0; i < 32; ++i) h[c + i] = fmaxf(v[i], 0.f);
     }
   }
 }

@@ -177,6 +177,13 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&h);
 }
+// ReLU and the bfloat16 rounding of two values in one conversion (a in the
+// low half, as pack_bf16).
+__device__ __forceinline__ uint32_t pack_relu_bf16(float a, float b) {
+  uint32_t d;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+  return d;
+}
 __device__ __forceinline__ void st_shared_v4(uint32_t saddr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(saddr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
 }
@@ -235,31 +242,24 @@ __device__ __forceinline__ EncIn make_enc(const GuideNet& net, float px, float p
   return e;
 }
 
-// Feature f of the encoding (used by the transposed writer).
-__device__ __forceinline__ float enc_feature(const EncIn& e, int f) {
-  if (f < 144) {
-    int c = f / 24, j = (f % 24) >> 1;
-    float s, co;
-    sincospif(e.v[c] * float(1 << j), &s, &co);
-    return (f & 1) ? co : s;
-  }
-  f -= 144;
-  float v = f < 32 ? e.theta : e.phi;
-  float d = v - (float(f & 31) + 0.5f) * (1.f / kBlob);
-  if (f >= 32) d -= rintf(d);
-  d *= float(kBlob);
-  return __expf(-0.5f * d * d);
-}
-
-// Eight features of group g.
+// Eight features of group g. A frequency group holds bands j0 .. j0 + 3 of one
+// coordinate (j0 = 0, 4, 8): band j0 is evaluated directly, the next three by
+// the double-angle identities sin 2a = 2 sin a cos a, cos 2a = 1 - 2 sin^2 a.
+// Each doubling about doubles the absolute error of the one before, so the
+// features stay within ~1e-6 of the exact values (sincospif is within 1 ulp),
+// far below the bfloat16 rounding the layer input gets.
 __device__ __forceinline__ void enc_group(const EncIn& e, int g, float* out) {
   if (g < 18) {
+    const int c = g / 3, j0 = 4 * (g % 3);
+    float s, co;
+    sincospif(e.v[c] * float(1 << j0), &s, &co);
+    out[0] = s;
+    out[1] = co;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      int f = 8 * g + 2 * q;
-      int c = f / 24, j = (f % 24) >> 1;
-      float s, co;
-      sincospif(e.v[c] * float(1 << j), &s, &co);
+    for (int q = 1; q < 4; ++q) {
+      const float sc = s * co;
+      co = fmaf(-2.f * s, s, 1.f);
+      s = sc + sc;
       out[2 * q] = s;
       out[2 * q + 1] = co;
     }
@@ -301,6 +301,9 @@ __device__ __forceinline__ float vmf_log_norm(float k) {
   return logf(k) - logf(2.f * kPi) - logf(-expm1f(-2.f * k));
 }
 
+// Decodes the 40 raw outputs with the fast intrinsics (__expf, rsqrtf,
+// __frcp_rn): relative errors of a few 1e-7, below the bfloat16 rounding of
+// the layers that produced the outputs.
 __device__ __forceinline__ void decode_mixture(const float* o, Mixture& m) {
   float mx = o[0];
 #pragma unroll
@@ -308,29 +311,39 @@ __device__ __forceinline__ void decode_mixture(const float* o, Mixture& m) {
   float s = 0.f;
 #pragma unroll
   for (int k = 0; k < kLobes; ++k) {
-    m.pi[k] = expf(o[k] - mx);
+    m.pi[k] = __expf(o[k] - mx);
     s += m.pi[k];
   }
-  float is = 1.f / s;
+  const float is = __frcp_rn(s);
 #pragma unroll
   for (int k = 0; k < kLobes; ++k) {
     m.pi[k] *= is;
     float x = o[8 + 3 * k], y = o[9 + 3 * k], z = o[10 + 3 * k];
-    float l = sqrtf(x * x + y * y + z * z);
-    if (l > 1e-12f) {
-      m.mx[k] = x / l; m.my[k] = y / l; m.mz[k] = z / l;
+    float l2 = x * x + y * y + z * z;
+    if (l2 > 1e-24f) {
+      float il = rsqrtf(l2);
+      m.mx[k] = x * il; m.my[k] = y * il; m.mz[k] = z * il;
     } else {
       m.mx[k] = 0.f; m.my[k] = 0.f; m.mz[k] = 1.f;
     }
-    m.kappa[k] = expf(fminf(fmaxf(o[32 + k], kLogKappaMin), kLogKappaMax));
+    m.kappa[k] = __expf(fminf(fmaxf(o[32 + k], kLogKappaMin), kLogKappaMax));
   }
+}
+
+// 1 - exp(-x) for x >= 0: its Taylor series to x^4 below 1/8 (relative error
+// under x^4 / 120 = 2e-6), else with __expf (absolute error ~1e-7 on a
+// result above 0.11).
+__device__ __forceinline__ float one_minus_exp_neg(float x) {
+  if (x < 0.125f) return x * (1.f - x * (0.5f - x * (1.f / 6.f - x * (1.f / 24.f))));
+  return 1.f - __expf(-x);
 }
 
 // Writes a decoded mixture in the stored layout (kMixStride float4).
 __device__ __forceinline__ void store_mixture(float4* out, const Mixture& m) {
   float c[kLobes];
 #pragma unroll
-  for (int k = 0; k < kLobes; ++k) c[k] = m.pi[k] * expf(vmf_log_norm(m.kappa[k]));
+  for (int k = 0; k < kLobes; ++k)
+    c[k] = m.pi[k] * m.kappa[k] * __frcp_rn((2.f * kPi) * one_minus_exp_neg(2.f * m.kappa[k]));
   out[0] = make_float4(m.pi[0], m.pi[1], m.pi[2], m.pi[3]);
   out[1] = make_float4(m.pi[4], m.pi[5], m.pi[6], m.pi[7]);
 #pragma unroll
