@@ -270,6 +270,34 @@ def run_guided(args):
     def relmse(x):
         return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
 
+    if args.headroom:
+        # What a guide trained far beyond the equal-time budget gains at equal
+        # samples per pixel: train untimed (8 Adam steps of 2^18 samples after
+        # each training pass), then render with the weights frozen.
+        n = args.headroom_spp
+        img, st = render_guided(gs, cam, prm(1, 11), None, guide_params(passes=n))
+        p_err = relmse(img)
+        rows = []
+        for steps in args.headroom_steps:
+            g = Guide(ctx, bounds, seed=7)
+            passes = max(1, steps // 8)
+            render_guided(gs, cam, prm(1, 5), g,
+                          guide_params(args.guide_fraction, passes=passes, train_passes=passes, steps_per_pass=8,
+                                       batch_samples=1 << 18, learning_rate=1e-2, guide_depth=args.guide_depth,
+                                       flags=0 if args.absolute_weights else _abi.GUIDE_PIXEL_RELATIVE))
+            gimg, gst = render_guided(gs, cam, prm(1, 12), g,
+                                      guide_params(args.guide_fraction, passes=n, guide_depth=args.guide_depth))
+            g.close()
+            e = relmse(gimg)
+            rows.append({"train_steps": passes * 8, "relmse": e, "ms": gst.total_ms, "gain": p_err / e})
+        print(json.dumps({"metric": "relMSE at equal spp, pre-trained guide vs plain", "unit": "relMSE",
+                          "higher_is_better": False,
+                          "config": {"workload": workload, "spp": n, "guide_fraction": args.guide_fraction,
+                                     "guide_depth": args.guide_depth,
+                                     "weights": "absolute" if args.absolute_weights else "pixel-relative"},
+                          "plain": {"relmse": p_err, "ms": st.total_ms}, "guided": rows}))
+        return
+
     plain = []
     for spp in args.spp_list:
         img, st = render_guided(gs, cam, prm(1, 1000 + spp), None, guide_params(passes=spp))
@@ -670,6 +698,10 @@ def main():
                          "their pixel, 8 Adam steps after each of the first 32 passes, BSDF-only passes for the "
                          "first 128 steps")
     ap.add_argument("--train-steps", type=int, default=1, help="Adam steps of 2^18 samples after a training pass")
+    ap.add_argument("--headroom", action="store_true",
+                    help="--guided: relMSE at equal spp of guides pre-trained untimed for --headroom-steps steps")
+    ap.add_argument("--headroom-steps", type=lambda x: [int(v) for v in x.split(",")], default=[256, 2048, 8192])
+    ap.add_argument("--headroom-spp", type=int, default=128)
     ap.add_argument("--quality", action="store_true",
                     help="relMSE of the Cornell box and icosphere images against 65,536-spp renders")
     ap.add_argument("--batch", action="store_true",
