@@ -231,11 +231,13 @@ def run_guided(args):
         p.flags = flags
         return p
 
+    gflags = (0 if args.absolute_weights else _abi.GUIDE_PIXEL_RELATIVE) | (
+        _abi.GUIDE_PRODUCT if args.product_target else 0)
+
     def train_gp(budget_ms=0.0, passes=0):
         return guide_params(args.guide_fraction, passes=passes, train_passes=args.train_passes,
                             steps_per_pass=args.train_steps, batch_samples=1 << 18, learning_rate=1e-2,
-                            time_budget_ms=budget_ms, guide_depth=args.guide_depth,
-                            flags=0 if args.absolute_weights else _abi.GUIDE_PIXEL_RELATIVE,
+                            time_budget_ms=budget_ms, guide_depth=args.guide_depth, flags=gflags,
                             warmup_steps=args.warmup_steps)
 
     if args.profile:
@@ -284,7 +286,7 @@ def run_guided(args):
             render_guided(gs, cam, prm(1, 5), g,
                           guide_params(args.guide_fraction, passes=passes, train_passes=passes, steps_per_pass=8,
                                        batch_samples=1 << 18, learning_rate=1e-2, guide_depth=args.guide_depth,
-                                       flags=0 if args.absolute_weights else _abi.GUIDE_PIXEL_RELATIVE))
+                                       flags=gflags))
             gimg, gst = render_guided(gs, cam, prm(1, 12), g,
                                       guide_params(args.guide_fraction, passes=n, guide_depth=args.guide_depth))
             g.close()
@@ -294,7 +296,8 @@ def run_guided(args):
                           "higher_is_better": False,
                           "config": {"workload": workload, "spp": n, "guide_fraction": args.guide_fraction,
                                      "guide_depth": args.guide_depth,
-                                     "weights": "absolute" if args.absolute_weights else "pixel-relative"},
+                                     "weights": "absolute" if args.absolute_weights else "pixel-relative",
+                                     "target": "BSDF x radiance x cos" if args.product_target else "radiance x cos"},
                           "plain": {"relmse": p_err, "ms": st.total_ms}, "guided": rows}))
         return
 
@@ -329,9 +332,11 @@ def run_guided(args):
                        "reference_ms": ref_ms, "guide_fraction": args.guide_fraction,
                        "guide_depth": args.guide_depth, "warmup_steps": args.warmup_steps,
                        "train": "online, Adam lr 1e-2, %d step(s) of 2^18 samples after %s one-spp pass, "
-                                "sample weights relative to their pixel"
+                                "sample weights %s, target %s"
                                 % (args.train_steps, "every" if args.train_passes >= 1 << 20
-                                   else "each of the first %d" % args.train_passes),
+                                   else "each of the first %d" % args.train_passes,
+                                   "absolute" if args.absolute_weights else "relative to their pixel",
+                                   "BSDF x radiance x cos" if args.product_target else "radiance x cos"),
                        "passes": "inverse-variance weighted (the first, unguided pass seeds the mean)"},
             "plain": [{"ms": t, "relmse": e, "spp": n} for t, e, n in plain],
             "guided": [{"ms": t, "relmse": e, "spp": n, "train_steps": k, "train_ms": tm}
@@ -693,10 +698,12 @@ def main():
     ap.add_argument("--absolute-weights", action="store_true",
                     help="--guided: training weights not relative to the sample's pixel")
     ap.add_argument("--train-passes", type=int, default=1 << 30, help="passes that train (default: all)")
+    ap.add_argument("--product-target", action="store_true",
+                    help="--guided: the guide learns BSDF x incident radiance x cos (GBRT_GUIDE_PRODUCT)")
     ap.add_argument("--tuned", action="store_true",
-                    help="--guided with the best settings found on the two rooms: sample weights not relative to "
-                         "their pixel, 8 Adam steps after each of the first 32 passes, BSDF-only passes for the "
-                         "first 128 steps")
+                    help="--guided with the best settings found on the two rooms: the product target, sample "
+                         "weights not relative to their pixel, 16 Adam steps after each of the first 32 passes, "
+                         "BSDF-only passes for the first 256 steps")
     ap.add_argument("--train-steps", type=int, default=1, help="Adam steps of 2^18 samples after a training pass")
     ap.add_argument("--headroom", action="store_true",
                     help="--guided: relMSE at equal spp of guides pre-trained untimed for --headroom-steps steps")
@@ -719,7 +726,8 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.tuned:
-        args.absolute_weights, args.train_steps, args.train_passes, args.warmup_steps = True, 8, 32, 128
+        args.absolute_weights, args.product_target = True, True
+        args.train_steps, args.train_passes, args.warmup_steps = 16, 32, 256
     if args.chains:
         run_chains(args)
         return

@@ -514,7 +514,12 @@ typedef enum gbrt_guide_flags {
   GBRT_GUIDE_EQUAL_WEIGHTS = 1,
   /* Training samples weighted by their share of their pixel's value relative
    * to sqrt(pixel^2 + 0.01) instead of by their radiance alone. */
-  GBRT_GUIDE_PIXEL_RELATIVE = 2
+  GBRT_GUIDE_PIXEL_RELATIVE = 2,
+  /* The guide learns the product of the BSDF, the incident radiance and the
+   * cosine (the radiance each sampled direction reflects towards wo) instead
+   * of the incident radiance times the cosine: the two differ at glossy
+   * vertices, where the product follows the lobe. */
+  GBRT_GUIDE_PRODUCT = 4
 } gbrt_guide_flags;
 
 typedef struct gbrt_guide_stats {

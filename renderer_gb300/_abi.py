@@ -164,7 +164,7 @@ NOALLOC_MAX_BATCH = 65536
 GUIDE_PARAMS, GUIDE_INPUT, GUIDE_OUTPUT, GUIDE_SAMPLE = 24064, 9, 40, 13
 CSG_SPHERE, CSG_BOX, CSG_ISECT, CSG_UNION, CSG_DIFF, CSG_XOR = range(6)
 CSG_MAX_LEAVES = 8
-GUIDE_EQUAL_WEIGHTS, GUIDE_PIXEL_RELATIVE = 1, 2
+GUIDE_EQUAL_WEIGHTS, GUIDE_PIXEL_RELATIVE, GUIDE_PRODUCT = 1, 2, 4
 
 P = C.c_void_p
 

@@ -67,6 +67,7 @@ struct PTParams {
   int record;              // write training records for the guide
   int guide_depth;         // guide vertices i < guide_depth only (0: all)
   int train_relative;      // training weights relative to the sample's pixel
+  int train_product;       // training target BSDF x incident radiance x cos (else radiance x cos)
   const double* film_sum;  // sums of the earlier passes (pixel estimates for the training weights)
   const double* pass_sum;  // sums of the current pass
   double inv_samples;      // 1 / samples per pixel in film_sum + pass_sum
@@ -754,7 +755,7 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
         st.rec[r + ns] = make_float4(nrm.x, nrm.y, nrm.z, wi.x);
         st.rec[r + 2 * ns] = make_float4(wo.x, wo.y, wo.z, wi.y);
         st.rec[r + 3 * ns] = make_float4(na.x, na.y, na.z, wi.z);
-        st.rec[r + 5 * ns] = make_float4((alpha.x + alpha.y + alpha.z) * (1.f / 3.f), 0.f, 0.f, 0.f);
+        st.rec[r + 5 * ns] = make_float4((alpha.x + alpha.y + alpha.z) * (1.f / 3.f), alpha.x, alpha.y, alpha.z);
         z = ((z & 15) + 1) | kRecOpen;
       }
     }
@@ -802,7 +803,10 @@ __global__ void __launch_bounds__(256) k_guide_prep(DeviceScene S, PTState st, i
 // record's snapshot, divided by the throughput up to that direction; the
 // target is its mean over the channels times |cos| at the vertex, and the
 // sample weight target / pdf (pdf: the density the direction was drawn
-// from). With GBRT_GUIDE_PIXEL_RELATIVE the weight is also scaled to the
+// from). With GBRT_GUIDE_PRODUCT the target is the BSDF times that radiance
+// times |cos|: the path's gain after the vertex over its throughput before
+// it (per channel) is already f Li |cos| / pdf, the sample weight.
+// With GBRT_GUIDE_PIXEL_RELATIVE the weight is also scaled to the
 // sample's share of its pixel: times the throughput from the camera to the
 // vertex, over sqrt(p^2 + 0.01) with p the pixel's current estimate (the
 // denominator of relMSE), so that dim regions weigh as much as bright ones.
@@ -822,12 +826,22 @@ __global__ void __launch_bounds__(256) k_guide_collect(PTParams P, PTState st) {
     const size_t b = size_t(kRecComp * r) * ns + slot;
     const float4 r0 = st.rec[b], r1 = st.rec[b + ns], r2 = st.rec[b + 2 * ns], r3 = st.rec[b + 3 * ns],
                  sn = st.rec[b + 4 * ns], r5 = st.rec[b + 5 * ns];
-    float li = 0.f;
-    if (r3.x > 0.f) li += (L.x - sn.x) / r3.x;
-    if (r3.y > 0.f) li += (L.y - sn.y) / r3.y;
-    if (r3.z > 0.f) li += (L.z - sn.z) / r3.z;
-    const float cosi = fabsf(r1.x * r1.w + r1.y * r2.w + r1.z * r3.w);
-    float w = (li * (1.f / 3.f)) * cosi / r0.w;
+    float w;
+    if (P.train_product) {
+      // (gathered after the vertex) / (throughput up to it) = f Li cos / pdf
+      float lr = 0.f;
+      if (r5.y > 0.f) lr += (L.x - sn.x) / r5.y;
+      if (r5.z > 0.f) lr += (L.y - sn.y) / r5.z;
+      if (r5.w > 0.f) lr += (L.z - sn.z) / r5.w;
+      w = lr * (1.f / 3.f);
+    } else {
+      float li = 0.f;
+      if (r3.x > 0.f) li += (L.x - sn.x) / r3.x;
+      if (r3.y > 0.f) li += (L.y - sn.y) / r3.y;
+      if (r3.z > 0.f) li += (L.z - sn.z) / r3.z;
+      const float cosi = fabsf(r1.x * r1.w + r1.y * r2.w + r1.z * r3.w);
+      w = (li * (1.f / 3.f)) * cosi / r0.w;
+    }
     if (P.train_relative) w *= r5.x * inv_pix;
     if (!(w > 0.f) || !isfinite(w)) continue;
     const int e = agg_push(st.tcount);
@@ -1511,6 +1525,7 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     P.record = record ? 1 : 0;
     P.guide_depth = gp->guide_depth;
     P.train_relative = (gp->flags & GBRT_GUIDE_PIXEL_RELATIVE) ? 1 : 0;
+    P.train_product = (gp->flags & GBRT_GUIDE_PRODUCT) ? 1 : 0;
     P.film_sum = d_sum;
     P.pass_sum = d_pass;
     P.inv_samples = 1.0 / (double(spp) * (pass + 1));
