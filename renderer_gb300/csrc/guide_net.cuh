@@ -264,14 +264,25 @@ __device__ __forceinline__ void enc_group(const EncIn& e, int g, float* out) {
       out[2 * q + 1] = co;
     }
   } else {
-    int f0 = 8 * g - 144;
-    float v = f0 < 32 ? e.theta : e.phi;
+    // One-blob bins b0 .. b0 + 7: exp(-(D - q)^2 / 2) with D the distance in
+    // bins from bin b0's centre. Consecutive bins differ by the factor
+    // exp(D - q - 1/2), itself divided by e from one bin to the next, so a
+    // group takes two exponentials. phi wraps around: its distance is taken
+    // from the group's middle, wrapped to [-16, 16] bins (a bin that wraps
+    // the other way lies more than 12.5 bins off, below 1e-33).
+    const int f0 = 8 * g - 144, b0 = f0 & 31;
+    float D = (f0 < 32 ? e.theta : e.phi) * float(kBlob) - (float(b0) + 0.5f);
+    if (f0 >= 32) {
+      const float m = D - 3.5f;
+      D = m - float(kBlob) * rintf(m * (1.f / kBlob)) + 3.5f;
+    }
+    float gq = __expf(-0.5f * D * D), r = __expf(D - 0.5f);
+    out[0] = gq;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      float d = v - (float((f0 + q) & 31) + 0.5f) * (1.f / kBlob);
-      if (f0 >= 32) d -= rintf(d);
-      d *= float(kBlob);
-      out[q] = __expf(-0.5f * d * d);
+    for (int q = 1; q < 8; ++q) {
+      gq *= r;
+      r *= 0.36787944117144233f;  // 1 / e
+      out[q] = gq;
     }
   }
 }
