@@ -72,12 +72,13 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def traffic_per_ray():
-    """DRAM bytes per closest-hit ray from the committed ncu summary, if any."""
+def traffic_per_ray(key="dram_bytes_per_ray"):
+    """DRAM (or, with key="l2_bytes_per_ray", L2) bytes per closest-hit ray
+    from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", "k_extend_icosphere.md")
     if not os.path.exists(p):
         return None
-    m = re.search(r"dram_bytes_per_ray\s*[:=]\s*([0-9.eE+-]+)", open(p).read())
+    m = re.search(key + r"\s*[:=]\s*([0-9.eE+-]+)", open(p).read())
     return float(m.group(1)) if m else None
 
 
@@ -845,10 +846,12 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = tot["ext_rays"] * bytes_per_ray / (tot["ext_ms"] / 1000.0) / 1e9
     tpr = traffic_per_ray()
+    l2pr = traffic_per_ray("l2_bytes_per_ray")
     rays_per_launch = tot["ext_rays"] / max(tot["ext_launch"], 1)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": peak_kind,
                 "traffic": None if tpr is None else tpr * rays_per_launch,
+                "l2_traffic": None if l2pr is None else l2pr * rays_per_launch,
                 "kernel": "k_extend (closest-hit BVH traversal)",
                 "bytes_per_ray": bytes_per_ray, "nodes_per_ray": n_node, "prims_per_ray": n_prim,
                 "launches": tot["ext_launch"], "avg_launch_ms": tot["ext_ms"] / max(tot["ext_launch"], 1),
