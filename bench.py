@@ -674,7 +674,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-rows", type=int, default=64, help="rows in the CPU-baseline sample")
+    ap.add_argument("--cpu-rows", type=int, default=128, help="rows in the CPU-baseline sample (about 11 s on 16 cores)")
     ap.add_argument("--reference-rows", type=int, default=32, help="rows per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-paths", type=int, default=0)
