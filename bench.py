@@ -515,6 +515,60 @@ INSTANCED_WORKLOAD = ("8 instances of one 4,000,000-triangle noise-displaced ter
                       "3840x2160, 1 spp each, max depth 16, RR p=0.5, physical semantics")
 
 
+def guided_views(args, ctx, gs, cams):
+    """The 16 views guided by one network trained online on all of them (2
+    one-sample training passes per view, 4 Adam steps of 2^18 samples after
+    each, product target), then one guided sample per pixel of every view
+    with the trained guide: aggregate paths/s over the views' device time,
+    and the inference rate of the network against the dense-BF16 peak."""
+    from renderer_gb300 import _abi
+    from renderer_gb300.guiding import Guide, guide_params, render_guided, scene_bounds
+    from renderer_gb300.scene import SceneData, render_params
+
+    def cam(c):
+        sc = SceneData()
+        sc.camera = c
+        return sc.camera_struct()
+
+    def prm(seed, flags=0):
+        return render_params(1, 1, 0.5, 16, seed, semantics=_abi.SEM_PHYSICAL, flags=flags)
+
+    g = Guide(ctx, scene_bounds(gs), seed=7)
+    t = time.perf_counter()
+    steps = 0
+    for i, c in enumerate(cams):
+        _, st = render_guided(gs, cam(c), prm(300 + i), g,
+                              guide_params(0.5, passes=2, train_passes=2, steps_per_pass=4, batch_samples=1 << 18,
+                                           learning_rate=1e-2, flags=_abi.GUIDE_PRODUCT))
+        steps += st.train_steps
+    train_s = time.perf_counter() - t
+    ms, paths, ext = 0.0, 0, 0
+    for step in range(args.steps):
+        for i, c in enumerate(cams):
+            _, st = render_guided(gs, cam(c), prm(400 + 16 * step + i), g, guide_params(0.5, passes=1))
+            ms += st.total_ms
+            paths += st.paths
+            ext += st.extension_rays
+    rows, inf_ms = 0, 0.0
+    for i, c in enumerate(cams):
+        _, st = render_guided(gs, cam(c), prm(500 + i, _abi.RENDER_TIME_KERNELS), g, guide_params(0.5, passes=1))
+        rows += st.infer_rows
+        inf_ms += st.infer_ms
+    g.close()
+    f_inf = 2 * (208 * 64 + 64 * 64 + 64 * 64 + 64 * 40)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0))
+    tflops = rows * f_inf / (inf_ms * 1e-3) / 1e12 if inf_ms else None
+    return {"views": len(cams), "resolution": "%dx%d" % (cams[0]["width"], cams[0]["height"]),
+            "paths_per_s": paths / (ms * 1e-3), "ms_per_step": ms / args.steps,
+            "extension_rays_per_path": ext / max(paths, 1),
+            "train": "online on all views: %d Adam steps of 2^18 samples (product target) in %.1f s" % (steps, train_s),
+            "mlp": {"bound": "tensor", "unit": "TFLOP/s", "achieved": tflops, "peak": tc_peak,
+                    "peak_kind": "measured" if "bf16_tflops" in peaks else "fallback",
+                    "frac": tflops / tc_peak if tflops else None, "rows": rows, "ms": inf_ms}}
+
+
 def run_instanced(args):
     """The instanced-terrain scene: 16 views of 3840 x 2160 at one sample per
     pixel in one gbrt_render_batch call (a step = all 16 images). value =
@@ -578,6 +632,8 @@ def run_instanced(args):
             "e2e": {"value": r["e2e"], "unit": "paths/s", "h2d_bytes_per_step": 16 * C.sizeof(_abi.BatchJob),
                     "d2h_bytes_per_step": 16 * cams[0]["width"] * cams[0]["height"] * 12},
             "gpu_launches": r["launches"] * args.steps, "clocks": r["clocks"]}
+    if args.guided_views:
+        line["guided_views"] = guided_views(args, ctx, gs, cams)
     if args.compare_flat:
         del gs
         f = SceneData(materials=s.materials, spheres=s.spheres, lights=s.lights, env=s.env, env_mapping=s.env_mapping,
@@ -720,6 +776,8 @@ def main():
                     help="16 views of the instanced-terrain scene (two-level BVH) through gbrt_render_batch")
     ap.add_argument("--terrain-nx", type=int, default=2000, help="terrain quads along x (2000: 4M triangles)")
     ap.add_argument("--compare-flat", action="store_true", help="with --instanced: also the flattened scene")
+    ap.add_argument("--guided-views", action="store_true",
+                    help="with --instanced: also the 16 views guided by one network trained on them")
     ap.add_argument("--chains", action="store_true",
                     help="paths/s of the Metropolis and energy-redistribution renderers (Cornell box)")
     ap.add_argument("--mlt-chains", type=lambda x: [int(v) for v in x.split(",")], default=[0, 4096, 1 << 20],
