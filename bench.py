@@ -302,15 +302,17 @@ def run_guided(args):
                           "plain": {"relmse": p_err, "ms": st.total_ms}, "guided": rows}))
         return
 
+    # Passes of k x k samples per pixel for both renderers (--pass-side k).
+    k = args.pass_side
     plain = []
     for spp in args.spp_list:
-        img, st = render_guided(gs, cam, prm(1, 1000 + spp), None, guide_params(passes=spp))
-        plain.append((st.total_ms, relmse(img), spp))
+        img, st = render_guided(gs, cam, prm(k, 1000 + spp), None, guide_params(passes=max(1, spp // (k * k))))
+        plain.append((st.total_ms, relmse(img), st.passes * k * k))
     guided = []
     for t, _, spp in plain:
         g = Guide(ctx, bounds, seed=7)
-        img, st = render_guided(gs, cam, prm(1, 2000 + spp), g, train_gp(budget_ms=t))
-        guided.append((st.total_ms, relmse(img), st.passes, st.train_steps, st.train_ms))
+        img, st = render_guided(gs, cam, prm(k, 2000 + spp), g, train_gp(budget_ms=t))
+        guided.append((st.total_ms, relmse(img), st.passes * k * k, st.train_steps, st.train_ms))
         g.close()
     # The network kernels in a trained guide's render, timed per launch.
     g = Guide(ctx, bounds, seed=7)
@@ -331,6 +333,7 @@ def run_guided(args):
             "config": {"workload": workload, "reference_spp": ref_spp,
                        "reference_estimator": "guided" if args.ref_guided else "plain",
                        "reference_ms": ref_ms, "guide_fraction": args.guide_fraction,
+                       "samples_per_pass": args.pass_side ** 2,
                        "guide_depth": args.guide_depth, "warmup_steps": args.warmup_steps,
                        "train": "online, Adam lr 1e-2, %d step(s) of 2^18 samples after %s one-spp pass, "
                                 "sample weights %s, target %s"
@@ -762,6 +765,8 @@ def main():
                          "weights not relative to their pixel, 16 Adam steps after each of the first 32 passes, "
                          "BSDF-only passes for the first 256 steps")
     ap.add_argument("--train-steps", type=int, default=1, help="Adam steps of 2^18 samples after a training pass")
+    ap.add_argument("--pass-side", type=int, default=1,
+                    help="--guided: k x k samples per pixel per pass, for the plain and the guided renderer")
     ap.add_argument("--headroom", action="store_true",
                     help="--guided: relMSE at equal spp of guides pre-trained untimed for --headroom-steps steps")
     ap.add_argument("--headroom-steps", type=lambda x: [int(v) for v in x.split(",")], default=[256, 2048, 8192])
