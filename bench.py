@@ -179,6 +179,7 @@ def run_reference(args, ws, rank, dist):
     print(json.dumps(line))
 
 
+SPP_DEFAULT = [16, 32, 64, 128, 256, 512]
 GUIDED_WORKLOAD = ("two rooms 4x3x3 (albedo 0.7) joined by a 0.2-wide door, 0.3x0.3 area light of radiance 200 "
                    "in the far room, 500,000-triangle displaced grid, Blinn floor (exponent 200), 1024x768, "
                    "physical semantics, max depth 12, RR p=0.5")
@@ -239,7 +240,7 @@ def run_guided(args):
         return guide_params(args.guide_fraction, passes=passes, train_passes=args.train_passes,
                             steps_per_pass=args.train_steps, batch_samples=1 << 18, learning_rate=1e-2,
                             time_budget_ms=budget_ms, guide_depth=args.guide_depth, flags=gflags,
-                            warmup_steps=args.warmup_steps)
+                            warmup_steps=args.warmup_steps, late_pass_samples=args.late_pass_samples)
 
     if args.profile:
         g = Guide(ctx, bounds, seed=1)
@@ -302,17 +303,19 @@ def run_guided(args):
                           "plain": {"relmse": p_err, "ms": st.total_ms}, "guided": rows}))
         return
 
-    # Passes of k x k samples per pixel for both renderers (--pass-side k).
+    # Passes of k x k samples per pixel (--pass-side k; plain: --plain-pass-side
+    # if given); guided passes after training: --late-pass-samples.
     k = args.pass_side
+    kp = args.plain_pass_side or k
     plain = []
     for spp in args.spp_list:
-        img, st = render_guided(gs, cam, prm(k, 1000 + spp), None, guide_params(passes=max(1, spp // (k * k))))
-        plain.append((st.total_ms, relmse(img), st.passes * k * k))
+        img, st = render_guided(gs, cam, prm(kp, 1000 + spp), None, guide_params(passes=max(1, spp // (kp * kp))))
+        plain.append((st.total_ms, relmse(img), st.passes * kp * kp))
     guided = []
     for t, _, spp in plain:
         g = Guide(ctx, bounds, seed=7)
         img, st = render_guided(gs, cam, prm(k, 2000 + spp), g, train_gp(budget_ms=t))
-        guided.append((st.total_ms, relmse(img), st.passes * k * k, st.train_steps, st.train_ms))
+        guided.append((st.total_ms, relmse(img), st.paths // (cam.width * cam.height), st.train_steps, st.train_ms))
         g.close()
     # The network kernels in a trained guide's render, timed per launch.
     g = Guide(ctx, bounds, seed=7)
@@ -333,7 +336,8 @@ def run_guided(args):
             "config": {"workload": workload, "reference_spp": ref_spp,
                        "reference_estimator": "guided" if args.ref_guided else "plain",
                        "reference_ms": ref_ms, "guide_fraction": args.guide_fraction,
-                       "samples_per_pass": args.pass_side ** 2,
+                       "samples_per_pass": {"plain": kp * kp, "guided_training": k * k,
+                                            "guided_late": args.late_pass_samples or k * k},
                        "guide_depth": args.guide_depth, "warmup_steps": args.warmup_steps,
                        "train": "online, Adam lr 1e-2, %d step(s) of 2^18 samples after %s one-spp pass, "
                                 "sample weights %s, target %s"
@@ -751,7 +755,7 @@ def main():
     ap.add_argument("--guided-width", type=int, default=960)
     ap.add_argument("--guided-height", type=int, default=540)
     ap.add_argument("--ref-cache", default="", help="npz file holding (or receiving) the reference render")
-    ap.add_argument("--spp-list", type=lambda x: [int(v) for v in x.split(",")], default=[16, 32, 64, 128, 256, 512])
+    ap.add_argument("--spp-list", type=lambda x: [int(v) for v in x.split(",")], default=SPP_DEFAULT)
     ap.add_argument("--guide-fraction", type=float, default=0.5)
     ap.add_argument("--guide-depth", type=int, default=0, help="guide vertices i < this only (0: all)")
     ap.add_argument("--warmup-steps", type=int, default=0, help="BSDF-only passes until this many training steps")
@@ -763,10 +767,15 @@ def main():
     ap.add_argument("--tuned", action="store_true",
                     help="--guided with the best settings found on the two rooms: the product target, sample "
                          "weights not relative to their pixel, 16 Adam steps after each of the first 32 passes, "
-                         "BSDF-only passes for the first 256 steps")
+                         "BSDF-only passes for the first 256 steps, passes of 16 samples after training; plain "
+                         "at its fastest, 64 samples per pass")
     ap.add_argument("--train-steps", type=int, default=1, help="Adam steps of 2^18 samples after a training pass")
     ap.add_argument("--pass-side", type=int, default=1,
                     help="--guided: k x k samples per pixel per pass, for the plain and the guided renderer")
+    ap.add_argument("--plain-pass-side", type=int, default=0,
+                    help="--guided: k x k samples per pixel per pass of the plain renderer (0: --pass-side)")
+    ap.add_argument("--late-pass-samples", type=int, default=0,
+                    help="--guided: samples per pixel of the guided passes after training (0: as in training)")
     ap.add_argument("--headroom", action="store_true",
                     help="--guided: relMSE at equal spp of guides pre-trained untimed for --headroom-steps steps")
     ap.add_argument("--headroom-steps", type=lambda x: [int(v) for v in x.split(",")], default=[256, 2048, 8192])
@@ -792,6 +801,12 @@ def main():
     if args.tuned:
         args.absolute_weights, args.product_target = True, True
         args.train_steps, args.train_passes, args.warmup_steps = 16, 32, 256
+        # guided passes of 16 samples once training is over; plain at its
+        # fastest pass size (64 samples per pass), so spp from 64 up
+        args.late_pass_samples = args.late_pass_samples or 16
+        args.plain_pass_side = args.plain_pass_side or 8
+        if args.spp_list == SPP_DEFAULT:
+            args.spp_list = [64, 128, 256, 512, 1024]
     if args.chains:
         run_chains(args)
         return

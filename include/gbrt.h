@@ -502,6 +502,12 @@ typedef struct gbrt_guide_params {
   int32_t warmup_steps;   /* while training, passes sample the BSDF only until
                              this many Adam steps are done (0: guide from the
                              pass after the first step) */
+  int32_t late_pass_samples; /* samples per pixel of every pass after the last
+                             training pass (of every pass when the render does
+                             not train), as late_pass_samples x 1 jittered
+                             strata; 0 = x_samples * y_samples like the
+                             training passes. Larger passes keep the GPU full
+                             once the guide no longer changes. */
 } gbrt_guide_params;
 
 typedef enum gbrt_guide_flags {

@@ -124,7 +124,7 @@ class GuideParams(C.Structure):
     _fields_ = [("guide_fraction", C.c_float), ("passes", C.c_int32), ("train_passes", C.c_int32),
                 ("steps_per_pass", C.c_int32), ("batch_samples", C.c_int32), ("learning_rate", C.c_float),
                 ("time_budget_ms", C.c_float), ("guide_depth", C.c_int32), ("flags", C.c_int32),
-                ("warmup_steps", C.c_int32)]
+                ("warmup_steps", C.c_int32), ("late_pass_samples", C.c_int32)]
 
 
 class GuideStats(C.Structure):

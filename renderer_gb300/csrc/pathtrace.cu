@@ -1386,11 +1386,12 @@ __global__ void __launch_bounds__(256) k_pass_deviation(const double* __restrict
 }
 
 // prev_sum += pass_sum; with a deviation (dev != null), weighted += w *
-// pass_sum and wtotal += w for w = n3 / *dev. Thread 0 also adds the pass's
-// training samples (min(*tcount, tcap)) to *tsamples.
+// pass_sum * inv_pass (the pass's mean) and wtotal += w for w = n3 / *dev.
+// Thread 0 also adds the pass's training samples (min(*tcount, tcap)) to
+// *tsamples.
 __global__ void k_pass_combine(const double* __restrict__ pass_sum, double* __restrict__ prev_sum,
-                               double* __restrict__ weighted, size_t n3, const double* dev, double* wtotal,
-                               const int* tcount, int tcap, unsigned long long* tsamples) {
+                               double* __restrict__ weighted, size_t n3, double inv_pass, const double* dev,
+                               double* wtotal, const int* tcount, int tcap, unsigned long long* tsamples) {
   size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const double w = (dev && *dev > 0.0) ? double(n3) / *dev : 0.0;
   if (i == 0) {
@@ -1400,13 +1401,14 @@ __global__ void k_pass_combine(const double* __restrict__ pass_sum, double* __re
   if (i >= n3) return;
   double x = pass_sum[i];
   prev_sum[i] += x;
-  if (w > 0.0) weighted[i] += w * x;
+  if (w > 0.0) weighted[i] += w * x * inv_pass;
 }
 
+// film = (sum over passes of w * pass mean) / (sum of w).
 __global__ void k_finalize_weighted(const double* __restrict__ weighted, float* __restrict__ film, size_t n3,
-                                    double inv_spp, const double* wtotal) {
+                                    const double* wtotal) {
   size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < n3) film[i] = float(weighted[i] * inv_spp / *wtotal);
+  if (i < n3) film[i] = float(weighted[i] / *wtotal);
 }
 
 static unsigned long long pass_seed(unsigned long long seed, int pass) {
@@ -1429,7 +1431,8 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   if (!(prm->termination_prob >= 0.f && prm->termination_prob < 1.f))
     return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: termination probability outside [0, 1)");
   if (!(gp->guide_fraction >= 0.f && gp->guide_fraction <= 1.f) || gp->passes < 0 || gp->train_passes < 0 ||
-      gp->steps_per_pass < 0 || gp->guide_depth < 0 || (gp->passes == 0 && !(gp->time_budget_ms > 0.f)))
+      gp->steps_per_pass < 0 || gp->guide_depth < 0 || gp->late_pass_samples < 0 ||
+      (gp->passes == 0 && !(gp->time_budget_ms > 0.f)))
     return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_guided: bad guide parameters");
   const bool useGuide = g && gp->guide_fraction > 0.f;
   const bool training = useGuide && gp->train_passes > 0 && gp->steps_per_pass > 0;
@@ -1441,9 +1444,18 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
   const unsigned long long npix = (unsigned long long)cam->width * cam->height;
   const int spp = prm->x_samples * prm->y_samples;
+  // Passes after the last training pass may take more samples per pixel
+  // (late_pass_samples x 1 strata), so that they fill the GPU.
+  gbrt_render_params lateParams = *prm;
+  if (gp->late_pass_samples > 0) {
+    lateParams.x_samples = gp->late_pass_samples;
+    lateParams.y_samples = 1;
+  }
+  const int lateSpp = lateParams.x_samples * lateParams.y_samples;
   const unsigned long long total = npix * (unsigned long long)spp;
+  const unsigned long long lateTotal = npix * (unsigned long long)lateSpp;
   long long B = prm->batch_paths > 0 ? prm->batch_paths : (1ll << 23);
-  B = std::max<long long>(1, std::min<long long>(B, (long long)total));
+  B = std::max<long long>(1, std::min<long long>(B, (long long)std::max(total, lateTotal)));
 
   Buffers buf(ctx, stream);
   PTState st;
@@ -1513,12 +1525,16 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   const bool timeK = (prm->flags & GBRT_RENDER_TIME_KERNELS) != 0;
   std::vector<cudaEvent_t> iev;
   gbrt_status status = GBRT_OK;
+  unsigned long long samples = 0, pathsDone = 0;  // per-pixel samples and paths of the passes so far
   for (int pass = 0;; ++pass) {
     if (gp->passes > 0 && pass >= gp->passes) break;
-    PTParams P{};
-    init_params(P, *cam, *prm, total);
-    P.seed = pass_seed(prm->seed, pass);
     const bool record = training && pass < gp->train_passes;
+    const bool late = !record;
+    const int sppPass = late ? lateSpp : spp;
+    const unsigned long long passTotal = late ? lateTotal : total;
+    PTParams P{};
+    init_params(P, *cam, late ? lateParams : *prm, passTotal);
+    P.seed = pass_seed(prm->seed, pass);
     // While training, sample the guide once it has had warmup_steps steps.
     P.guided = (useGuide && g->ready && (!training || steps >= gp->warmup_steps)) ? 1 : 0;
     P.guide_frac = gp->guide_fraction;
@@ -1528,13 +1544,13 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     P.train_product = (gp->flags & GBRT_GUIDE_PRODUCT) ? 1 : 0;
     P.film_sum = d_sum;
     P.pass_sum = d_pass;
-    P.inv_samples = 1.0 / (double(spp) * (pass + 1));
+    P.inv_samples = 1.0 / double(samples + (unsigned long long)sppPass);
     A(cudaMemsetAsync(d_pass, 0, n3 * sizeof(double), stream));
     if (record) A(cudaMemsetAsync(st.tcount, 0, sizeof(int), stream));
     auto kShade = pick_shade(s, true, P.guided || P.record);
-    for (unsigned long long g0 = 0; g0 < total && e == cudaSuccess; g0 += (unsigned long long)B) {
+    for (unsigned long long g0 = 0; g0 < passTotal && e == cudaSuccess; g0 += (unsigned long long)B) {
       P.g0 = g0;
-      P.nb = int(std::min<unsigned long long>((unsigned long long)B, total - g0));
+      P.nb = int(std::min<unsigned long long>((unsigned long long)B, passTotal - g0));
       k_raygen<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
       for (int it = 0; it < P.D; ++it) {
         int cur = it & 1;
@@ -1558,7 +1574,6 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
         kShade<<<cap_grid(shadeGrid, P.nb, 256), 256, 0, stream>>>(s->view, P, st, cur);
         tk.sh<<<cap_grid(shadowGrid, 2ll * P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st);
       }
-      unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
       launch_accumulate(P, st, d_pass, nullptr, stream);
       if (record) k_guide_collect<<<(P.nb + 255) / 256, 256, 0, stream>>>(P, st);
       A(cudaGetLastError());
@@ -1569,14 +1584,17 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     const bool wpass = weighted && pass > 0;
     if (wpass) {
       A(cudaMemsetAsync(d_dev, 0, sizeof(double), stream));
-      k_pass_deviation<<<ctx->num_sms * 4, 256, 0, stream>>>(d_pass, d_sum, n3, 1.0 / spp, 1.0 / (double(spp) * pass),
-                                                             d_dev);
+      k_pass_deviation<<<ctx->num_sms * 4, 256, 0, stream>>>(d_pass, d_sum, n3, 1.0 / sppPass,
+                                                             1.0 / double(samples), d_dev);
     }
-    k_pass_combine<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_pass, d_sum, d_wsum, n3, wpass ? d_dev : nullptr,
-                                                                   d_wtot, record ? st.tcount : nullptr, int(tcap),
+    k_pass_combine<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_pass, d_sum, d_wsum, n3, 1.0 / sppPass,
+                                                                   wpass ? d_dev : nullptr, d_wtot,
+                                                                   record ? st.tcount : nullptr, int(tcap),
                                                                    st.tally + 3);
     A(cudaGetLastError());
     ++passes;
+    samples += (unsigned long long)sppPass;
+    pathsDone += passTotal;
     if (record) {
       // Steps over the pass's samples; their count stays on the device.
       if (timeK) cudaEventRecord(t0, stream);
@@ -1609,9 +1627,9 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   if (timedAtEnd) cudaEventRecord(ev1, stream);
   if (e == cudaSuccess && passes > 0) {
     if (weighted && passes > 1)
-      k_finalize_weighted<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_wsum, d_film, n3, 1.0 / spp, d_wtot);
+      k_finalize_weighted<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_wsum, d_film, n3, d_wtot);
     else
-      k_finalize<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_sum, d_film, n3, 1.0 / (double(spp) * passes));
+      k_finalize<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_sum, d_film, n3, 1.0 / double(samples));
     A(cudaGetLastError());
     A(cudaMemcpyAsync(film, d_film, n3 * sizeof(float), cudaMemcpyDeviceToHost, stream));
   }
@@ -1645,7 +1663,7 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     std::memset(stats, 0, sizeof *stats);
     stats->passes = passes;
     stats->train_steps = steps;
-    stats->paths = (unsigned long long)passes * total;
+    stats->paths = pathsDone;
     stats->train_samples = tally[3];
     stats->total_ms = elapsed;
     stats->train_ms = train_ms;

@@ -84,7 +84,8 @@ class Guide:
 
 
 def guide_params(guide_fraction=0.5, passes=0, train_passes=0, steps_per_pass=0, batch_samples=1 << 18,
-                 learning_rate=1e-2, time_budget_ms=0.0, guide_depth=0, flags=0, warmup_steps=0):
+                 learning_rate=1e-2, time_budget_ms=0.0, guide_depth=0, flags=0, warmup_steps=0,
+                 late_pass_samples=0):
     p = _abi.GuideParams()
     p.guide_fraction = guide_fraction
     p.passes = passes
@@ -96,6 +97,7 @@ def guide_params(guide_fraction=0.5, passes=0, train_passes=0, steps_per_pass=0,
     p.guide_depth = guide_depth
     p.flags = flags
     p.warmup_steps = warmup_steps
+    p.late_pass_samples = late_pass_samples
     return p
 
 

@@ -259,3 +259,34 @@ def test_product_target_is_unbiased_and_helps(ctx):
         assert guided.mean() == pytest.approx(ref.mean(), rel=0.02)
         ratios.append(relmse(guided) / relmse(plain))
     assert min(ratios) < 0.85 and max(ratios) < 1.2, ratios
+
+
+@pytest.mark.gpu
+def test_late_passes_keep_the_expectation(ctx):
+    """late_pass_samples: training passes of 2 x 2 samples per pixel, then
+    passes of 64 samples (64 x 1 strata). With equal pass weights the film is
+    the plain mean of all samples, unbiased by construction; the path count
+    adds up and the image keeps the plain estimator's expectation. The
+    default inverse-deviation weights combine passes of different sizes by
+    their means (looser bound: their weights depend on the passes). A render
+    that does not train takes the late size for every pass."""
+    from renderer_gb300 import _abi
+    from renderer_gb300.guiding import Guide, guide_params, render_guided, scene_bounds
+    from renderer_gb300.workloads import two_rooms_params
+    sc, cam = _small_rooms(ctx, 96, 64, 24)
+    npix = 96 * 64
+    ref, _ = render_guided(sc, cam, two_rooms_params(8, 8, seed=31), None, guide_params(passes=256))
+    for flags, tol, seed in ((_abi.GUIDE_EQUAL_WEIGHTS, 0.02, 32), (0, 0.04, 34)):
+        g = Guide(ctx, scene_bounds(sc), seed=3)
+        gp = guide_params(0.5, passes=14, train_passes=8, steps_per_pass=8, batch_samples=1 << 16,
+                          learning_rate=1e-2, late_pass_samples=64, flags=flags)
+        img, st = render_guided(sc, cam, two_rooms_params(2, 2, seed=seed), g, gp)
+        assert st.passes == 14 and st.train_steps == 64
+        assert st.paths == npix * (8 * 4 + 6 * 64)
+        assert img.mean() == pytest.approx(ref.mean(), rel=tol)
+        if flags:
+            img2, st2 = render_guided(sc, cam, two_rooms_params(1, 1, seed=33), g,
+                                      guide_params(0.5, passes=4, late_pass_samples=64))
+            assert st2.paths == npix * 4 * 64 and st2.train_steps == 0
+            assert img2.mean() == pytest.approx(ref.mean(), rel=0.03)
+        g.close()
