@@ -488,7 +488,8 @@ gbrt_status gbrt_guide_train_step(gbrt_guide* guide, const float* samples,
 typedef struct gbrt_guide_params {
   float guide_fraction;   /* probability of sampling the guide at a
                              non-specular vertex (one-sample MIS), e.g. 0.5 */
-  int32_t passes;         /* passes of x_samples * y_samples per pixel;
+  int32_t passes;         /* passes of x_samples * y_samples per pixel (of
+                             late_pass_samples after training, when set);
                              0 = until time_budget_ms is spent */
   int32_t train_passes;   /* the first train_passes passes record samples and
                              are each followed by steps_per_pass Adam steps */
