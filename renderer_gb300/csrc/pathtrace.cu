@@ -1122,8 +1122,6 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
       if (timeK) mark();
       launches += 3;
     }
-    unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
-    unsigned long long np = p1 - p0 + 1;
     launch_accumulate(P, st, d_sum, d_sumsq, stream);
     ++launches;
     A(cudaGetLastError());
@@ -1322,7 +1320,6 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
       kSh<<<cap_grid(shadowGrid, 2ll * P.nb, kTraceBlock), kTraceBlock, 0, stream>>>(s->view, st);
       launches += 3;
     }
-    unsigned long long p0 = g0 / spp, p1 = (g0 + P.nb - 1) / spp;
     launch_accumulate(P, st, d_sum, d_sumsq, stream);
     ++launches;
     A(cudaGetLastError());
