@@ -14,6 +14,10 @@ repository root: python tests/golden/make_golden.py).
 * cornell_render.npz: the oracle's 32x32 Cornell-box image (2x2 spp, depth 8,
   seed 7, reference semantics) drawn with the counter-based stream that the
   GPU path tracer uses (SplitMix64 over seed, sample id and dimension).
+* cornell_physical_mlt.npz: the same box under the physically based
+  estimator (2x2 spp, depth 8, seed 9), and the oracle's Metropolis image
+  (64 chains, 8 mutations per pixel, bootstrap 500, seed 2) with its normaliser b and
+  acceptance count.
 
 The probe is read from the renderer's source tree; the other fixtures need
 only the oracle (oracle/binding.py builds it).
@@ -130,6 +134,18 @@ def make_cornell():
     out = OracleScene(s).render(s.camera_struct(), params, rng_mode=1)
     np.savez_compressed(os.path.join(HERE, "cornell_render.npz"), film=out["film"], paths=out["paths"],
                         rays=out["rays"], shadow_rays=out["shadow_rays"])
+
+    # the physically based estimator on the same box, and the Metropolis
+    # renderer (64 chains, 8 mutations per pixel, bootstrap 500)
+    from renderer_gb300 import _abi
+    from renderer_gb300.chains import mlt_params
+    from renderer_gb300.scene import render_params
+    phys = OracleScene(s).render(s.camera_struct(), render_params(2, 2, 0.5, 8, 9, semantics=_abi.SEM_PHYSICAL),
+                                 rng_mode=1)
+    mlt = OracleScene(s).render_mlt(s.camera_struct(), render_params(1, 1, 0.0, 5, 2), mlt_params(8, 500), chains=64)
+    np.savez_compressed(os.path.join(HERE, "cornell_physical_mlt.npz"), phys_film=phys["film"],
+                        mlt_film=mlt["film"], mlt_b=mlt["b"], mlt_accepted=mlt["accepted"],
+                        mlt_mutations=mlt["mutations"])
 
 
 if __name__ == "__main__":

@@ -2,8 +2,9 @@
 
 CPU: the library's Radiance reader decodes scanlines of the renderer's own
 shipped light probe exactly as an independent numpy restatement of the
-format does, and the oracle still reproduces its committed ray hits and
-Cornell-box image bit for bit. GPU: the CUDA traversal and path tracer are
+format does, and the oracle still reproduces its committed ray hits, its
+Cornell-box images (reference and physically based estimators) and its
+Metropolis image bit for bit. GPU: the CUDA traversal and path tracer are
 held against the same fixtures, so the comparison does not depend on the
 oracle being built where the GPU runs."""
 import os
@@ -62,6 +63,22 @@ def test_oracle_reproduces_render_fixture():
     assert np.array_equal(out["film"], z["film"])
     assert out["paths"] == int(z["paths"]) == 32 * 32 * 4
 
+
+
+def test_oracle_reproduces_physical_and_metropolis_fixtures():
+    from oracle.binding import OracleScene
+    from renderer_gb300 import _abi
+    from renderer_gb300.chains import mlt_params
+    from renderer_gb300.scene import render_params
+    z = _load("cornell_physical_mlt.npz")
+    s = workloads.cornell_box(32, 32)
+    phys = OracleScene(s).render(s.camera_struct(), render_params(2, 2, 0.5, 8, 9, semantics=_abi.SEM_PHYSICAL),
+                                 rng_mode=1)
+    assert np.array_equal(phys["film"], z["phys_film"])
+    mlt = OracleScene(s).render_mlt(s.camera_struct(), render_params(1, 1, 0.0, 5, 2), mlt_params(8, 500), chains=64)
+    assert np.array_equal(mlt["film"], z["mlt_film"])
+    assert mlt["b"] == float(z["mlt_b"]) and mlt["accepted"] == int(z["mlt_accepted"])
+    assert mlt["mutations"] == int(z["mlt_mutations"]) == 32 * 32 * 8  # met-mutations per pixel
 
 @pytest.mark.gpu
 def test_gpu_trace_matches_ray_fixture(ctx):
