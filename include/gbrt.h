@@ -222,7 +222,15 @@ typedef enum gbrt_scene_flags {
    * traversal speed. Hits are the same; only exact-t ties may resolve
    * differently. A tree too deep for the traversal stack falls back to the
    * host build. gbrt_scene_info then reports max_depth 0 and SAH cost 0. */
-  GBRT_SCENE_GPU_BUILD = 2
+  GBRT_SCENE_GPU_BUILD = 2,
+  /* The physical estimator's next-event estimation samples the environment
+   * map uniformly over the sphere instead of in proportion to its luminance
+   * (importance sampling: a piecewise-constant density over the map's texels
+   * weighted by their solid angle, combined with BSDF sampling by the power
+   * heuristic). For measuring what importance sampling gains; the
+   * renderer's own estimator (GBRT_SEM_REFERENCE) samples it by the cosine
+   * either way (src/environmentmap.cpp:40-54). */
+  GBRT_SCENE_ENV_UNIFORM = 4
 } gbrt_scene_flags;
 
 /* Camera(cop, lookAt, up, fov[radians, full vertical], resolution),
@@ -315,6 +323,36 @@ gbrt_status gbrt_ctx_destroy(gbrt_ctx* ctx);
  * still holds; may be NULL). */
 gbrt_status gbrt_ctx_trim(gbrt_ctx* ctx, uint64_t* reserved_bytes);
 
+/* Host-side fault injection, for tests of the failure paths. The renderer
+ * has no counterpart; it stands in for the conditions the renderer meets with
+ * assert (src/perpixelrenderer.cpp:90-91) or not at all. Every fault is made
+ * on the host or by a bounded wait: none faults, traps or hangs the GPU, and
+ * the context stays usable afterwards. Faults stay set until
+ * GBRT_FAULT_NONE clears them all.
+ *   GBRT_FAULT_ALLOC       arg = n: the device allocations of this context
+ *                          succeed n more times, then one fails as out of
+ *                          memory (the call returns GBRT_ERR_OOM); one-shot.
+ *   GBRT_FAULT_NAN         arg = n > 0: the radiance of every camera sample
+ *                          whose path index is a multiple of n is replaced by
+ *                          NaN before accumulation (counted in
+ *                          gbrt_stats.nonfinite and dropped); 0 turns it off.
+ *   GBRT_FAULT_SMALL_STACK arg != 0: renders trace with a 4-entry traversal
+ *                          stack; a ray that needs more sets the error word and
+ *                          the call returns GBRT_ERR_NUMERIC.
+ *   GBRT_FAULT_GUIDE_WAIT  arg = ns in (0, 1e9]: the guide's kernels issue no
+ *                          tensor-core products and give up waiting for them
+ *                          after arg ns (the call returns GBRT_ERR_TIMEOUT,
+ *                          the kernels' tensor memory is freed); 0 turns it off.
+ */
+typedef enum gbrt_fault {
+  GBRT_FAULT_NONE = 0,
+  GBRT_FAULT_ALLOC = 1,
+  GBRT_FAULT_NAN = 2,
+  GBRT_FAULT_SMALL_STACK = 3,
+  GBRT_FAULT_GUIDE_WAIT = 4
+} gbrt_fault;
+gbrt_status gbrt_debug_fault(gbrt_ctx* ctx, int32_t kind, int64_t arg);
+
 /* ---- scene (replaces scene_builder::getScene + Intersectable::createBVH,
  *      src/sceneast.cpp:673-695, src/intersectable.cpp:11-14,
  *      src/bvh.cpp:67-94). Deep-copies desc to the device and builds the
@@ -381,12 +419,17 @@ gbrt_status gbrt_render_device(gbrt_scene* scene, const gbrt_camera* camera,
  * with the image: d_film_bgr (float) and d_sum (double, required here) and
  * the optional d_sumsq, each H x W x 3 on the device. params->batch_paths = 0
  * means GBRT_NOALLOC_MAX_BATCH; a larger value is rejected with
- * GBRT_ERR_INVALID_ARG. The first call on a device looks up the array's
- * device address; make that first call before any stream capture. All calls
- * in the process share the one array and leave their state in it (each call
- * clears what must start at zero), so calls that overlap on the GPU race:
- * issue them one at a time. GBRT_RENDER_TIME_KERNELS is ignored (stats get
- * host-timed render_ms only). Synchronous. */
+ * GBRT_ERR_INVALID_ARG. The first call on a context looks up the array's
+ * device address (a context created after cudaDeviceReset looks it up again).
+ * That first call, like the first launch of any kernel, may also make the
+ * CUDA driver load this library's kernels and enlarge its per-thread local
+ * memory reservation (the traversal stacks live in local memory, up to 190
+ * entries a thread): callers on a fixed memory budget should make one
+ * warm-up call at start-up, and the first call must come before any stream
+ * capture. All calls in the process share the one array and leave their
+ * state in it (each call clears what must start at zero), so calls that
+ * overlap on the GPU race: issue them one at a time. GBRT_RENDER_TIME_KERNELS
+ * is ignored (stats get host-timed render_ms only). Synchronous. */
 #define GBRT_NOALLOC_MAX_BATCH 65536
 gbrt_status gbrt_render_device_noalloc(gbrt_scene* scene,
                                        const gbrt_camera* camera,

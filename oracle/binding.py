@@ -13,7 +13,11 @@ from renderer_gb300.runtime import HIT_DTYPE, RAY_DTYPE
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
-_lib = None
+# The same source built with the renderer's Release flags, for the timed CPU
+# baseline only (its float results may differ from the parity build's in the
+# last bits).
+TIME_LIB_PATH = os.path.join(HERE, "_build", "liboracle_time.so")
+_libs = {}
 
 
 def build():
@@ -21,12 +25,13 @@ def build():
     return LIB_PATH
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB_PATH):
+def lib(timing=False):
+    """The parity build (default) or, with timing, the timing build."""
+    path = TIME_LIB_PATH if timing else LIB_PATH
+    if path not in _libs:
+        if not os.path.exists(path):
             build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(path)
         P = C.c_void_p
         L.orc_scene_create.restype = P
         L.orc_scene_create.argtypes = [C.POINTER(_abi.SceneDesc), C.c_int]
@@ -50,8 +55,8 @@ def lib():
                                       C.POINTER(_abi.ErptParams), P, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
         L.orc_stream_u.restype = C.c_float
         L.orc_stream_u.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32]
-        _lib = L
-    return _lib
+        _libs[path] = L
+    return _libs[path]
 
 
 def _ptr(a):
@@ -62,24 +67,26 @@ class OracleScene:
     """The renderer's scene (IntersectableList of lights + geometry, median-split
     BVH or a plain list) restated on the CPU."""
 
-    def __init__(self, data, use_bvh=True):
+    def __init__(self, data, use_bvh=True, timing=False):
+        """timing: on the timing build (the CPU baseline), not the parity build."""
         desc, keep = data.to_desc()
         self.data = data
-        self.handle = lib().orc_scene_create(C.byref(desc), 1 if use_bvh else 0)
+        self._L = lib(timing)
+        self.handle = self._L.orc_scene_create(C.byref(desc), 1 if use_bvh else 0)
         if not self.handle:
             raise RuntimeError("orc_scene_create failed")
 
     def intersect(self, rays, threads=0):
         rays = np.ascontiguousarray(rays, RAY_DTYPE)
         hits = np.zeros(len(rays), HIT_DTYPE)
-        lib().orc_trace_closest(self.handle, _ptr(rays), len(rays), _ptr(hits), threads)
+        self._L.orc_trace_closest(self.handle, _ptr(rays), len(rays), _ptr(hits), threads)
         return hits
 
     def occluded(self, rays, ignore_prim=None, threads=0):
         rays = np.ascontiguousarray(rays, RAY_DTYPE)
         occ = np.zeros(len(rays), np.uint8)
         ign = None if ignore_prim is None else np.ascontiguousarray(ignore_prim, np.int32)
-        lib().orc_trace_any(self.handle, _ptr(rays), _ptr(ign), len(rays), _ptr(occ), threads)
+        self._L.orc_trace_any(self.handle, _ptr(rays), _ptr(ign), len(rays), _ptr(occ), threads)
         return occ.astype(bool)
 
     def render(self, camera, params, rng_mode=0, rows=None, threads=0, row_step=1):
@@ -91,7 +98,7 @@ class OracleScene:
         s = np.zeros((H, W, 3), np.float64)
         q = np.zeros((H, W, 3), np.float64)
         paths, rays, sh = C.c_uint64(), C.c_uint64(), C.c_uint64()
-        rc = lib().orc_render(self.handle, C.byref(camera), C.byref(params), rng_mode, r0, r1, row_step, _ptr(film), _ptr(s),
+        rc = self._L.orc_render(self.handle, C.byref(camera), C.byref(params), rng_mode, r0, r1, row_step, _ptr(film), _ptr(s),
                               _ptr(q), threads, C.byref(paths), C.byref(rays), C.byref(sh))
         if rc != 0:
             raise RuntimeError("orc_render failed")
@@ -103,7 +110,7 @@ class OracleScene:
         film = np.zeros((camera.height, camera.width, 3), np.float32)
         b = C.c_double()
         counts = (C.c_uint64 * 4)()
-        if lib().orc_render_mlt(self.handle, C.byref(camera), C.byref(params), C.byref(mp), int(chains), _ptr(film),
+        if self._L.orc_render_mlt(self.handle, C.byref(camera), C.byref(params), C.byref(mp), int(chains), _ptr(film),
                                 C.byref(b), counts) != 0:
             raise RuntimeError("orc_render_mlt failed")
         return dict(film=film, b=b.value, paths=counts[0], mutations=counts[1], accepted=counts[2], chains=counts[3])
@@ -114,14 +121,14 @@ class OracleScene:
         film = np.zeros((camera.height, camera.width, 3), np.float32)
         ed = C.c_double()
         counts = (C.c_uint64 * 4)()
-        if lib().orc_render_erpt(self.handle, C.byref(camera), C.byref(params), C.byref(ep), _ptr(film), C.byref(ed),
+        if self._L.orc_render_erpt(self.handle, C.byref(camera), C.byref(params), C.byref(ep), _ptr(film), C.byref(ed),
                                  counts) != 0:
             raise RuntimeError("orc_render_erpt failed")
         return dict(film=film, ed=ed.value, paths=counts[0], mutations=counts[1], accepted=counts[2], chains=counts[3])
 
     def close(self):
         if self.handle:
-            lib().orc_scene_destroy(self.handle)
+            self._L.orc_scene_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

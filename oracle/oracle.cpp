@@ -949,6 +949,120 @@ struct EnvironmentMap : Light, Material {
   C3 emission(const Hit& hit) const override { return get(hit.ray.d.normalized()); }
   bool emitsLight() const override { return true; }
   V3 outDirection(const Hit&, Sample, float& pdf, C3& b) const override { b = C3(); pdf = 0; return V3(); }
+
+  /* Importance sampling for the physical estimator (not in the renderer,
+   * whose NEE draws the cosine, :40-54). A piecewise-constant density over
+   * the mapping's parameter square, H rows x W cells: lat-long (u, v) =
+   * (atan2(x, -z) / 2 pi + 1/2, acos(y) / pi) with 2 pi^2 sin(theta) of solid
+   * angle per unit area; the angular probe's disc (u, v) = ((cx + 1) / 2,
+   * (cy + 1) / 2), r = theta / pi, 4 pi^2 sin(theta) / theta. A cell weighs
+   * the luminance get() returns for its centre times that factor there; row
+   * and cell CDFs are summed in double and stored in float, and a cell's
+   * density is the product of its float CDF steps times W H. */
+  std::vector<float> marg, cond, dens;
+  bool sampled = false;
+
+  void buildTables() {
+    const double pi = M_PI;
+    std::vector<double> w(size_t(W) * H, 0.0), rs(size_t(H), 0.0);
+    double tot = 0;
+    for (int r = 0; r < H; ++r) {
+      for (int c = 0; c < W; ++c) {
+        double u = (c + 0.5) / W, v = (r + 0.5) / H, jac;
+        V3 d;
+        if (mapping == GBRT_ENV_LATLONG) {
+          double ph = 2 * pi * (u - 0.5), th = pi * v;
+          d = V3(float(std::sin(th) * std::sin(ph)), float(std::cos(th)), float(-std::sin(th) * std::cos(ph)));
+          jac = 2 * pi * pi * std::sin(th);
+        } else {
+          double cx = 2 * u - 1, cy = 2 * v - 1, rr = std::sqrt(cx * cx + cy * cy);
+          if (!(rr < 1)) continue;
+          double th = pi * rr, k = rr > 0 ? std::sin(th) / rr : 0;
+          d = rr > 0 ? V3(float(std::cos(th)), float(k * cx), float(-k * cy)) : V3(1, 0, 0);
+          jac = rr > 0 ? 4 * pi * pi * std::sin(th) / th : 4 * pi * pi;
+        }
+        C3 L = get(d);
+        double l = 0.299 * L.r + 0.587 * L.g + 0.114 * L.b;
+        double x = (l > 0 && std::isfinite(l)) ? l * jac : 0.0;
+        w[size_t(r) * W + c] = x;
+        rs[r] += x;
+      }
+      tot += rs[r];
+    }
+    if (!(tot > 0) || !std::isfinite(tot)) return;
+    marg.assign(size_t(H) + 1, 0.f);
+    cond.assign(size_t(H) * (W + 1), 0.f);
+    dens.assign(size_t(H) * W, 0.f);
+    double acc = 0;
+    for (int r = 0; r < H; ++r) {
+      marg[r] = float(acc / tot);
+      acc += rs[r];
+      double a = 0;
+      for (int c = 0; c < W; ++c) {
+        cond[size_t(r) * (W + 1) + c] = rs[r] > 0 ? float(a / rs[r]) : float(c) / float(W);
+        a += w[size_t(r) * W + c];
+      }
+      cond[size_t(r) * (W + 1) + W] = 1.f;
+    }
+    marg[H] = 1.f;
+    for (int r = 0; r < H; ++r)
+      for (int c = 0; c < W; ++c)
+        dens[size_t(r) * W + c] = (marg[r + 1] - marg[r]) *
+                                  (cond[size_t(r) * (W + 1) + c + 1] - cond[size_t(r) * (W + 1) + c]) * float(W) *
+                                  float(H);
+    sampled = true;
+  }
+  /* Density per solid angle of the unit direction d. */
+  float pdf(V3 d) const {
+    double u, v, jac;
+    if (mapping == GBRT_ENV_LATLONG) {
+      double y = std::min(1.0, std::max(-1.0, double(d.y)));
+      u = std::atan2(double(d.x), double(-d.z)) / (2 * M_PI) + 0.5;
+      v = std::acos(y) / M_PI;
+      jac = 2 * M_PI * M_PI * std::sqrt(std::max(0.0, 1 - y * y));
+    } else {
+      double th = std::acos(std::min(1.0, std::max(-1.0, double(d.x))));
+      double q = std::sqrt(double(d.y) * d.y + double(d.z) * d.z);
+      double f = q > 0 ? th / (q * M_PI) : 0;
+      u = (d.y * f + 1) / 2;
+      v = (-d.z * f + 1) / 2;
+      jac = th > 0 ? 4 * M_PI * M_PI * q / th : 4 * M_PI * M_PI;
+    }
+    if (!(jac > 0)) return 0;
+    int c = std::min(std::max(int(float(u) * W), 0), W - 1), r = std::min(std::max(int(float(v) * H), 0), H - 1);
+    return float(dens[size_t(r) * W + c] / jac);
+  }
+  static int cdfFind(const float* cdf, int n, float x) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) / 2;
+      if (cdf[mid] <= x) lo = mid; else hi = mid;
+    }
+    return lo;
+  }
+  /* Draws a direction with u1 (row) and u2 (cell); false outside the disc. */
+  bool sample(float u1, float u2, V3& d, float& p) const {
+    int r = cdfFind(marg.data(), H, u1);
+    const float* cr = &cond[size_t(r) * (W + 1)];
+    int c = cdfFind(cr, W, u2);
+    float fv = std::min((u1 - marg[r]) / (marg[r + 1] - marg[r]), 0.99999994f);
+    float fu = std::min((u2 - cr[c]) / (cr[c + 1] - cr[c]), 0.99999994f);
+    double u = (float(c) + fu) / float(W), v = (float(r) + fv) / float(H), jac;
+    if (mapping == GBRT_ENV_LATLONG) {
+      double ph = M_PI * (2 * u - 1), th = M_PI * v;
+      d = V3(float(std::sin(th) * std::sin(ph)), float(std::cos(th)), float(-std::sin(th) * std::cos(ph)));
+      jac = 2 * M_PI * M_PI * std::sin(th);
+    } else {
+      double cx = 2 * u - 1, cy = 2 * v - 1, rr = std::sqrt(cx * cx + cy * cy);
+      if (!(rr < 1)) return false;
+      double th = M_PI * rr, k = rr > 0 ? std::sin(th) / rr : 0;
+      d = rr > 0 ? V3(float(std::cos(th)), float(k * cx), float(-k * cy)) : V3(1, 0, 0);
+      jac = rr > 0 ? 4 * M_PI * M_PI * std::sin(th) / th : 4 * M_PI * M_PI;
+    }
+    if (!(jac > 0)) return false;
+    p = float(dens[size_t(r) * W + c] / jac);
+    return p > 0;
+  }
 };
 
 /* --------------------------------------------------------------- Camera -- */
@@ -1029,6 +1143,7 @@ static Scene* buildScene(const gbrt_scene_desc* d, bool useBVH) {
       e->W = d->env->width; e->H = d->env->height; e->mapping = d->env->mapping;
       e->tex.assign(d->env->texels, d->env->texels + size_t(e->W) * e->H * 3);
       e->coef = spec3(L.intensity);
+      if (!(d->flags & GBRT_SCENE_ENV_UNIFORM)) e->buildTables();
       l = e;
     } else l = new BlackLight();
     l->prim = pid;
@@ -1384,7 +1499,8 @@ static C3 physRadiance(const Scene& s, const Ray& primary, int D, float p, U&& u
     }
     if (auto* em = dynamic_cast<const EnvironmentMap*>(h.mat)) {
       V3 dn = ray.d.normalized();
-      float w = prevSpec ? 1.f : powerHeuristic(prevPdf, float(pChoose / (4 * M_PI)));
+      float pe = em->sampled ? em->pdf(dn) : float(1 / (4 * M_PI));
+      float w = prevSpec ? 1.f : powerHeuristic(prevPdf, pChoose * pe);
       Lsum = Lsum + mul(alpha, em->get(dn)) * w;
       break;
     }
@@ -1420,10 +1536,12 @@ static C3 physRadiance(const Scene& s, const Ray& primary, int D, float p, U&& u
         if (ang <= cn->angle) { Le = cn->I * (1 / d.lengthSquared()); pl = pChoose; delta = true; }
         else ok = false;
       } else if (auto* em = dynamic_cast<const EnvironmentMap*>(L)) {
-        wi = Sample(lx, ly).uniformSphere();
+        float pe = float(1 / (4 * M_PI));
+        if (em->sampled) ok = em->sample(lx, ly, wi, pe);
+        else wi = Sample(lx, ly).uniformSphere();
         dist = kInf;
-        Le = em->get(wi);
-        pl = float(pChoose / (4 * M_PI));
+        if (ok) Le = em->get(wi);
+        pl = pChoose * pe;
       } else ok = false;
       if (ok && !Le.isZero()) {
         float pb;

@@ -158,9 +158,11 @@ ENV_ANGULAR, ENV_LATLONG = range(2)
 # gbrt_semantics
 SEM_REFERENCE, SEM_PHYSICAL = range(2)
 # gbrt_scene_flags / gbrt_render_flags
-SCENE_WATERTIGHT, SCENE_GPU_BUILD = 1, 2
+SCENE_WATERTIGHT, SCENE_GPU_BUILD, SCENE_ENV_UNIFORM = 1, 2, 4
 RENDER_TIME_KERNELS, RENDER_COUNT_TRAVERSAL = 1, 2
 NOALLOC_MAX_BATCH = 65536
+# gbrt_fault (host-side fault injection for the failure-path tests)
+FAULT_NONE, FAULT_ALLOC, FAULT_NAN, FAULT_SMALL_STACK, FAULT_GUIDE_WAIT = 0, 1, 2, 3, 4
 GUIDE_PARAMS, GUIDE_INPUT, GUIDE_OUTPUT, GUIDE_SAMPLE = 24064, 9, 40, 13
 CSG_SPHERE, CSG_BOX, CSG_ISECT, CSG_UNION, CSG_DIFF, CSG_XOR = range(6)
 CSG_MAX_LEAVES = 8
@@ -197,6 +199,7 @@ SIGNATURES = [
     ("gbrt_batch_autotune", C.c_int, [P, C.POINTER(BatchJob), C.c_int32, C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int64)]),
     ("gbrt_ctx_trim", C.c_int, [P, C.POINTER(C.c_uint64)]),
+    ("gbrt_debug_fault", C.c_int, [P, C.c_int32, C.c_int64]),
     ("gbrt_render_mlt", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), C.POINTER(MltParams), P,
                                   C.POINTER(ChainStats)]),
     ("gbrt_render_erpt", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), C.POINTER(ErptParams), P,

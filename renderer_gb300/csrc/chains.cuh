@@ -587,7 +587,7 @@ static gbrt_status mlt_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_re
   unsigned long long launches = 0;
 
   PTParams P{};
-  init_params(P, *cam, *prm, 1);
+  init_params(P, s->ctx, *cam, *prm, 1);
   P.seed = prm->seed;
   P.xs = P.ys = P.spp = 1;
   // Bootstrap (src/metropolisrenderer.cpp:77-100): large steps at full length (MetropolisSample
@@ -726,7 +726,7 @@ static gbrt_status erpt_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_r
   const Wave wS = make_wave(s, false), wP = make_wave(s, true);
 
   PTParams P{};
-  init_params(P, *cam, *prm, 1);
+  init_params(P, s->ctx, *cam, *prm, 1);
   P.xs = P.ys = P.spp = 1;
   // computeEd: pixel corners, termination probability 0.1 (its roulette
   // compensation included).

@@ -27,6 +27,16 @@ struct gbrt_ctx {
   std::vector<cudaStream_t> batch_streams;
   int batch_streams_tuned = 4;
   long long batch_paths_tuned = 1ll << 22;
+  // Device address of the no-allocation entry point's file-scope scratch
+  // array, looked up by the first gbrt_render_device_noalloc call on this
+  // context (with its device current).
+  unsigned char* noalloc_scratch = nullptr;
+  // Host-side fault injection for the tests of the failure paths
+  // (gbrt_debug_fault); everything off by default.
+  mutable long long fault_alloc_countdown = -1;  // device allocations that still succeed (-1: off)
+  unsigned long long fault_nan_every = 0;        // every n-th camera sample's radiance becomes NaN
+  bool fault_small_stack = false;                // traversal kernels with a kFaultStack-entry stack
+  unsigned long long fault_guide_wait_ns = 0;    // guide kernels skip their products and wait this long
 };
 
 struct gbrt_scene {
@@ -51,8 +61,25 @@ gbrt_status fail(gbrt_ctx* ctx, gbrt_status st, const std::string& msg);
 gbrt_status cuda_fail(gbrt_ctx* ctx, cudaError_t e, const char* what);
 void clear_error(gbrt_ctx* ctx);
 
+// The injected allocation failure of gbrt_debug_fault: cudaErrorMemoryAllocation
+// for the allocation the countdown reaches, cudaSuccess otherwise. Called
+// before every device allocation the library makes for a context.
+inline cudaError_t fault_alloc(const gbrt_ctx* ctx) {
+  if (!ctx || ctx->fault_alloc_countdown < 0) return cudaSuccess;
+  if (ctx->fault_alloc_countdown == 0) {
+    ctx->fault_alloc_countdown = -1;
+    return cudaErrorMemoryAllocation;
+  }
+  --ctx->fault_alloc_countdown;
+  return cudaSuccess;
+}
+
 // Stream-ordered allocation from the context's pool (cudaFreeAsync frees).
 inline cudaError_t ctx_alloc(const gbrt_ctx* ctx, void** p, size_t bytes, cudaStream_t stream) {
+  if (cudaError_t f = fault_alloc(ctx)) {
+    *p = nullptr;
+    return f;
+  }
   return cudaMallocFromPoolAsync(p, bytes, ctx->pool, stream);
 }
 template <typename T>

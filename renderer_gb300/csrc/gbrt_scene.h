@@ -89,6 +89,16 @@ struct DeviceScene {
   int32_t env_light;      // light index / prim id of the environment map, -1 if none
   int32_t env_w, env_h, env_mapping;
   float env_coef[3];
+  // Importance sampling of the environment by the physical estimator (null
+  // without a map, with a black one or with GBRT_SCENE_ENV_UNIFORM): a
+  // piecewise-constant density over the mapping's parameter square of env_h
+  // rows x env_w cells. env_marg: the rows' CDF (env_h + 1 floats, 0 ... 1);
+  // env_cond: per row the cells' CDF (env_w + 1 floats each); env_dens: per
+  // cell its probability x env_w x env_h (the density over the square),
+  // computed from the float CDFs so that it is exactly what sampling draws.
+  const float* env_marg;
+  const float* env_cond;
+  const float* env_dens;
   // Textures (null when no material uses one): texels of all textures one
   // after the other (3 floats, BGR), per texture (first texel, W, H, -), and
   // per triangle its three texture coordinates (6 floats, input order; the

@@ -165,8 +165,8 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
   auto chain_wait = [&]() -> bool {
     bool fine = true;
     if (t == 0) {
-      mma_commit(bar);
-      fine = mbar_wait(bar, phase);
+      if (net.issue) mma_commit(bar);
+      fine = mbar_wait(bar, phase, net.wait_ns);
     }
     phase ^= 1;
     if (wg_sync_or(bid, !fine)) return false;
@@ -185,11 +185,11 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
     // Layer 1 in two halves of the input.
     write_enc_range<0, kEncA>(sX, t, e);
     wg_handoff(bid);
-    if (t == 0) gemm_k(tmem, sX, 8 * kEncA, sW1, kIn, 8 * kEncA, kHid, false);
+    if (t == 0 && net.issue) gemm_k(tmem, sX, 8 * kEncA, sW1, kIn, 8 * kEncA, kHid, false);
     if (!(ok = chain_wait())) break;
     write_enc_range<kEncA, kEncA + kEncB>(sX, t, e);
     wg_handoff(bid);
-    if (t == 0) gemm_k(tmem, sX, 8 * kEncB, sW1 + kEncA * 128, kIn, 8 * kEncB, kHid, true);
+    if (t == 0 && net.issue) gemm_k(tmem, sX, 8 * kEncB, sW1 + kEncA * 128, kIn, 8 * kEncB, kHid, true);
     if (!(ok = chain_wait())) break;
     hidden_to_smem(lane, sX, t, nullptr);
     // Layers 2 and 3, then the output layer (N = 48, 40 used).
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
   }
   if (!ok) {
     if (t == 0) atomicExch(err, 1);
-    mbar_wait(bar, phase ^ 1);  // the chain that timed out, once more (bounded)
+    mbar_wait(bar, phase ^ 1, net.wait_ns);  // the chain that timed out, once more (bounded)
   }
   tc_fence_before();
   __syncthreads();
@@ -363,8 +363,8 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
   auto sync_chain = [&]() -> bool {
     bool fine = true;
     if (t == 0) {  // one thread polls; the block waits at the barrier
-      mma_commit(bar);
-      fine = mbar_wait(bar, phase);
+      if (net.issue) mma_commit(bar);
+      fine = mbar_wait(bar, phase, net.wait_ns);
     }
     phase ^= 1;
     if (__syncthreads_or(!fine)) return false;
@@ -388,22 +388,22 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
     // ---- forward
     float h[kHid];
     handoff();
-    if (t == 0) gemm_k(tmem + kColScratch, sR, kIn, sW1, kIn, kIn, kHid, false);
+    if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sR, kIn, sW1, kIn, kIn, kHid, false);
     if (!(ok = sync_chain())) break;
     hidden_to_smem(lane + kColScratch, sX1, t, h);
     write_transposed(sR, t, h, kHid);  // X1^T at R + 0
     handoff();
-    if (t == 0) gemm_k(tmem + kColScratch, sX1, kHid, sW2, kHid, kHid, kHid, false);
+    if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sX1, kHid, sW2, kHid, kHid, kHid, false);
     if (!(ok = sync_chain())) break;
     hidden_to_smem(lane + kColScratch, sX2, t, h);
     write_transposed(sR + 16384, t, h, kHid);  // X2^T
     handoff();
-    if (t == 0) gemm_k(tmem + kColScratch, sX2, kHid, sW3, kHid, kHid, kHid, false);
+    if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sX2, kHid, sW3, kHid, kHid, kHid, false);
     if (!(ok = sync_chain())) break;
     hidden_to_smem(lane + kColScratch, sX3, t, h);
     write_transposed(sR + 32768, t, h, kHid);  // X3^T
     handoff();
-    if (t == 0) gemm_k(tmem + kColScratch, sX3, kHid, sW4, kHid, kHid, kOutPad, false);
+    if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sX3, kHid, sW4, kHid, kHid, kOutPad, false);
     if (!(ok = sync_chain())) break;
     {
       float o[kOutPad], g[kOutPad];
@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
     }
     // ---- backward: output layer
     handoff();
-    if (t == 0) {
+    if (t == 0 && net.issue) {
       gemm_k(tmem + kColW4, sR + 32768, kRows, sDT, kRows, kRows, kOutPad, !first);
       gemm_k(tmem + kColScratch, sDR, kOutPad, sW4T, kOutPad, kOutPad, kHid, false);
     }
@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
     backprop_delta(lane + kColScratch, sm + kTX3, sDR, sDT, t);
     // ---- layer 3
     handoff();
-    if (t == 0) {
+    if (t == 0 && net.issue) {
       gemm_k(tmem + kColW3, sR + 16384, kRows, sDT, kRows, kRows, kHid, !first);
       gemm_k(tmem + kColScratch, sDR, kHid, sW3T, kHid, kHid, kHid, false);
     }
@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
     backprop_delta(lane + kColScratch, sm + kTX2, sDR, sDT, t);
     // ---- layer 2
     handoff();
-    if (t == 0) {
+    if (t == 0 && net.issue) {
       gemm_k(tmem + kColW2, sR, kRows, sDT, kRows, kRows, kHid, !first);
       gemm_k(tmem + kColScratch, sDR, kHid, sW2T, kHid, kHid, kHid, false);
     }
@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
       for (int q = 0; q < 8; ++q) st_shared_u16(sR + ik_off(8 * g + q, t, kRows), bf16_bits(fv[q]));
     }
     handoff();
-    if (t == 0) {
+    if (t == 0 && net.issue) {
       gemm_k(tmem + kColW1lo, sR, kRows, sDT, kRows, kRows, kHid, !first);
       gemm_k(tmem + kColW1hi, sR + ik_off(kRows, 0, kRows), kRows, sDT, kRows, kRows, kHid, !first);
     }
@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
   }
   if (!ok) {
     if (t == 0) atomicExch(err, 1);
-    mbar_wait(bar, phase ^ 1);
+    mbar_wait(bar, phase ^ 1, net.wait_ns);
   }
   tc_fence_before();
   __syncthreads();
@@ -525,6 +525,9 @@ __global__ void k_to_bf16(const float* __restrict__ p, __nv_bfloat16* __restrict
 GuideNet view(const gbrt_guide* g) {
   GuideNet v;
   v.w = g->d_w;
+  // An injected fault (gbrt_debug_fault) issues nothing and waits briefly.
+  v.wait_ns = g->ctx->fault_guide_wait_ns ? g->ctx->fault_guide_wait_ns : 1000000000ull;
+  v.issue = g->ctx->fault_guide_wait_ns ? 0 : 1;
   for (int k = 0; k < 3; ++k) {
     v.lo[k] = g->bounds[k];
     float ext = g->bounds[3 + k] - g->bounds[k];

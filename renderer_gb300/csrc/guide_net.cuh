@@ -43,6 +43,8 @@ constexpr float kPi = 3.14159265358979323846f;
 struct GuideNet {
   const __nv_bfloat16* w;  // kParams BF16 values, layout above
   float lo[3], inv_ext[3];  // position normalisation: (p - lo) * inv_ext
+  unsigned long long wait_ns;  // limit of every wait for the tensor cores (1 s)
+  int issue;                   // 0 only under an injected fault: no products are issued or committed
 };
 
 // ------------------------------------------------------------ layout ----
@@ -115,8 +117,8 @@ __device__ __forceinline__ uint64_t global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// Waits for the phase of an mbarrier to complete, for at most ~1 s.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+// Waits for the phase of an mbarrier to complete, for at most limit_ns.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, uint64_t limit_ns) {
   const uint64_t t0 = global_ns();
   for (;;) {
     uint32_t done;
@@ -127,7 +129,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
         : "r"(bar), "r"(phase)
         : "memory");
     if (done) return true;
-    if (global_ns() - t0 > 1000000000ull) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
 }
 

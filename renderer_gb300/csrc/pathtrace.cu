@@ -73,6 +73,7 @@ struct PTParams {
   double inv_samples;      // 1 / samples per pixel in film_sum + pass_sum
   const float* pss;        // primary samples of the Markov-chain renderers: dim d of slot s at pss[d * pss_stride + s]
   int pss_stride;
+  unsigned long long nan_every;  // injected fault: radiance of path indices divisible by this is NaN (0: off)
 };
 
 // Where a path's random numbers come from. StreamSrc: the counter-based
@@ -588,10 +589,17 @@ __device__ __forceinline__ void nee_phys(const DeviceScene& S, const PTState& st
     pl = pChoose;
     delta = true;
   } else if (Lt.type == GBRT_LIGHT_ENV && S.env_light >= 0) {
-    wi = uniform_sphere(lx, ly);
+    // In proportion to the map's luminance (or uniformly over the sphere
+    // without the tables).
+    float pe = 0.25f * kInvPi;
+    if (S.env_marg) {
+      if (!env_sample(S, lx, ly, wi, pe)) return;
+    } else {
+      wi = uniform_sphere(lx, ly);
+    }
     dist = CUDART_INF_F;
     Le = env_get(S, wi);
-    pl = pChoose * (0.25f * kInvPi);
+    pl = pChoose * pe;
   } else {
     return;
   }
@@ -676,7 +684,7 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
     if (envHit) {
       V3f dn = normalize(d);
       V3f Le = env_get(S, dn);
-      float w = prevSpec ? 1.f : power_heuristic(prevPdf, pChoose * (0.25f * kInvPi));
+      float w = prevSpec ? 1.f : power_heuristic(prevPdf, pChoose * (S.env_marg ? env_pdf(S, dn) : 0.25f * kInvPi));
       float4 L4 = st.L[slot];
       L4.x += alpha.x * Le.x * w; L4.y += alpha.y * Le.y * w; L4.z += alpha.z * Le.z * w;
       st.L[slot] = L4;
@@ -867,6 +875,7 @@ __global__ void __launch_bounds__(256) k_accumulate(PTParams P, PTState st, doub
   unsigned long long bad = 0;
   for (unsigned long long g = gb; g < ge; ++g) {
     float4 L = st.L[g - P.g0];
+    if (P.nan_every && g % P.nan_every == 0) L.x = CUDART_NAN_F;
     if (!isfinite(L.x) || !isfinite(L.y) || !isfinite(L.z)) { ++bad; continue; }
     s0 += L.x; s1 += L.y; s2 += L.z;
     q0 += double(L.x) * L.x; q1 += double(L.y) * L.y; q2 += double(L.z) * L.z;
@@ -890,6 +899,7 @@ __global__ void __launch_bounds__(256) k_accumulate_warp(PTParams P, PTState st,
   unsigned long long bad = 0;
   for (unsigned long long g = gb + lane; g < ge; g += 32) {
     float4 L = st.L[g - P.g0];
+    if (P.nan_every && g % P.nan_every == 0) L.x = CUDART_NAN_F;
     if (!isfinite(L.x) || !isfinite(L.y) || !isfinite(L.z)) { ++bad; continue; }
     s0 += L.x; s1 += L.y; s2 += L.z;
     q0 += double(L.x) * L.x; q1 += double(L.y) * L.y; q2 += double(L.z) * L.z;
@@ -980,6 +990,12 @@ static TraceKernels pick_flags(bool count, bool wt, bool shortStack) {
 // shallow enough, the general leaves (CSG objects, instances) only for scenes
 // that have them.
 static TraceKernels pick_kernels(const gbrt_scene* s, bool count) {
+  if (s->ctx->fault_small_stack) {
+    // Injected fault: a stack too small for most trees, so that the overflow
+    // check sets the error word (the call returns GBRT_ERR_NUMERIC).
+    if (s->view.csg_prog || s->view.inst) return {k_extend<false, false, kFaultStack, true>, k_shadow<false, false, kFaultStack, true>};
+    return {k_extend<false, false, kFaultStack, false>, k_shadow<false, false, kFaultStack, false>};
+  }
   const bool shortStack = stack_need(s->max_depth4) <= kShortStack;
   if (s->view.csg_prog || s->view.inst) return pick_flags<true>(count, s->watertight, shortStack);
   return pick_flags<false>(count, s->watertight, shortStack);
@@ -997,8 +1013,10 @@ static void (*pick_shade(const gbrt_scene* s, bool physical, bool guided))(Devic
   return ext ? k_shade_phys<false, true> : k_shade_phys<false, false>;
 }
 
-static void init_params(PTParams& P, const gbrt_camera& cam, const gbrt_render_params& prm, unsigned long long total) {
+static void init_params(PTParams& P, const gbrt_ctx* ctx, const gbrt_camera& cam, const gbrt_render_params& prm,
+                        unsigned long long total) {
   P.cam = make_camera(cam);
+  P.nan_every = ctx->fault_nan_every;
   P.seed = prm.seed;
   P.xs = prm.x_samples;
   P.ys = prm.y_samples;
@@ -1055,7 +1073,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   B = std::max<long long>(B, 1);
 
   PTParams P{};
-  init_params(P, *cam, *prm, total);
+  init_params(P, ctx, *cam, *prm, total);
 
   Buffers buf(ctx, stream);
   PTState st{};
@@ -1213,22 +1231,19 @@ static NoAllocLayout noalloc_layout() {
 constexpr size_t kNoAllocScratchBytes = size_t(20) << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch per device, looked up once per device
-// with that device current (the array's host-side name is not a device
-// address).
-static std::mutex g_noalloc_mu;
-static unsigned char* g_noalloc_ptr[64] = {nullptr};
-
+// Device address of g_noalloc_scratch, looked up once per context with the
+// context's device current (the array's host-side name is not a device
+// address). Kept in the context, not in a process-wide table: a context
+// created after cudaDeviceReset belongs to a new CUDA context in which the
+// module, and so the array, may sit at another address.
 static gbrt_status noalloc_scratch(gbrt_ctx* ctx, unsigned char** out) {
-  if (ctx->device < 0 || ctx->device >= 64) return fail(ctx, GBRT_ERR_UNSUPPORTED, "device index beyond 63");
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[ctx->device]) {
+  if (!ctx->noalloc_scratch) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-    g_noalloc_ptr[ctx->device] = static_cast<unsigned char*>(p);
+    ctx->noalloc_scratch = static_cast<unsigned char*>(p);
   }
-  *out = g_noalloc_ptr[ctx->device];
+  *out = ctx->noalloc_scratch;
   return GBRT_OK;
 }
 
@@ -1285,7 +1300,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
   long long B = prm->batch_paths > 0 ? prm->batch_paths : kNoAllocBatch;
   B = std::max<long long>(1, std::min<long long>(B, (long long)total));
   PTParams P{};
-  init_params(P, *cam, *prm, total);
+  init_params(P, ctx, *cam, *prm, total);
 
   // The array keeps the previous call's contents: clear what starts at zero.
   cudaError_t e = cudaSuccess;
@@ -1530,7 +1545,7 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     const int sppPass = late ? lateSpp : spp;
     const unsigned long long passTotal = late ? lateTotal : total;
     PTParams P{};
-    init_params(P, *cam, late ? lateParams : *prm, passTotal);
+    init_params(P, ctx, *cam, late ? lateParams : *prm, passTotal);
     P.seed = pass_seed(prm->seed, pass);
     // While training, sample the guide once it has had warmup_steps steps.
     P.guided = (useGuide && g->ready && (!training || steps >= gp->warmup_steps)) ? 1 : 0;
@@ -1699,7 +1714,7 @@ static cudaError_t enqueue_job(gbrt_scene* s, const gbrt_camera& cam, const gbrt
   long long B = prm.batch_paths > 0 ? prm.batch_paths : cap;
   B = std::max<long long>(1, std::min<long long>(B, (long long)total));
   PTParams P{};
-  init_params(P, cam, prm, total);
+  init_params(P, s->ctx, cam, prm, total);
   Buffers buf(ctx, stream);
   PTState st;
   std::memset(&st, 0, sizeof st);

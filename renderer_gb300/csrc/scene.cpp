@@ -79,6 +79,7 @@ gbrt_status upload(gbrt_scene* s, const std::vector<T>& host, const T** dst) {
   if (host.empty()) return GBRT_OK;
   void* p = nullptr;
   size_t bytes = host.size() * sizeof(T);
+  GBRT_CUDA_TRY(s->ctx, fault_alloc(s->ctx));
   GBRT_CUDA_TRY(s->ctx, cudaMalloc(&p, bytes));
   s->allocations.push_back(p);
   GBRT_CUDA_TRY(s->ctx, cudaMemcpy(p, host.data(), bytes, cudaMemcpyHostToDevice));
@@ -165,6 +166,74 @@ void relocate_node4(Node4& n, int64_t node0, int64_t rec0) {
 void free_scene(gbrt_scene* s) {
   for (void* p : s->allocations) cudaFree(p);
   s->allocations.clear();
+}
+
+// Importance-sampling tables of an environment map (DeviceScene env_marg /
+// env_cond / env_dens; the sampling itself is shading.cuh env_sample). Cell
+// (r, c) of the mapping's parameter square is weighted by the luminance of
+// the texel its centre looks up, the way EnvironmentMap::get maps directions
+// (src/environmentmap.cpp:57-65 for the angular probe, whose lookup lands
+// one texel before the cell: int(x - 1) truncated, then clamped, rows bounded
+// by the width and columns by the height as in the renderer), times the solid
+// angle per unit parameter area at the centre (lat-long 2 pi^2 sin(theta);
+// angular 4 pi^2 sin(theta) / theta, nothing outside the disc). Sums in
+// double, CDFs rounded to float, each cell's density the product of its float
+// CDF steps (what the sampler draws) times W x H. False for a black map.
+struct EnvTables {
+  std::vector<float> marg, cond, dens;
+};
+
+bool build_env_tables(const float* tex, int W, int H, int mapping, const float coef[3], EnvTables& t) {
+  const double pi = 3.14159265358979323846;
+  std::vector<double> w(size_t(W) * H, 0.0), rowsum(size_t(H), 0.0);
+  double total = 0.0;
+  for (int r = 0; r < H; ++r) {
+    for (int c = 0; c < W; ++c) {
+      const double u = (c + 0.5) / W, v = (r + 0.5) / H;
+      double jac;
+      int tr = r, tc = c;
+      if (mapping == GBRT_ENV_LATLONG) {
+        jac = 2.0 * pi * pi * std::sin(pi * v);
+      } else {
+        const double cx = 2.0 * u - 1.0, cy = 2.0 * v - 1.0, rr = std::sqrt(cx * cx + cy * cy);
+        if (!(rr < 1.0)) continue;
+        jac = rr > 0.0 ? 4.0 * pi * pi * std::sin(pi * rr) / (pi * rr) : 4.0 * pi * pi;
+        const int x = int(u * W - 1.0), y = int(v * H - 1.0);
+        tr = std::min(std::max(std::min(y, W - 1), 0), H - 1);
+        tc = std::min(std::max(std::min(x, H - 1), 0), W - 1);
+      }
+      const float* p = tex + (size_t(tr) * W + tc) * 3;  // BGR
+      const float cb = p[0] * coef[0], cg = p[1] * coef[1], cr = p[2] * coef[2];
+      const double lum = 0.299 * cr + 0.587 * cg + 0.114 * cb;
+      const double x = lum > 0.0 && std::isfinite(lum) ? lum * jac : 0.0;
+      w[size_t(r) * W + c] = x;
+      rowsum[r] += x;
+    }
+    total += rowsum[r];
+  }
+  if (!(total > 0.0) || !std::isfinite(total)) return false;
+  t.marg.assign(size_t(H) + 1, 0.f);
+  t.cond.assign(size_t(H) * (W + 1), 0.f);
+  t.dens.assign(size_t(H) * W, 0.f);
+  double acc = 0.0;
+  for (int r = 0; r < H; ++r) {
+    t.marg[r] = float(acc / total);
+    acc += rowsum[r];
+    float* cr = &t.cond[size_t(r) * (W + 1)];
+    double a = 0.0;
+    for (int c = 0; c < W; ++c) {
+      cr[c] = rowsum[r] > 0.0 ? float(a / rowsum[r]) : float(c) / float(W);
+      a += w[size_t(r) * W + c];
+    }
+    cr[W] = 1.f;
+  }
+  t.marg[H] = 1.f;
+  for (int r = 0; r < H; ++r) {
+    const float dm = t.marg[r + 1] - t.marg[r];
+    const float* cr = &t.cond[size_t(r) * (W + 1)];
+    for (int c = 0; c < W; ++c) t.dens[size_t(r) * W + c] = dm * (cr[c + 1] - cr[c]) * float(W) * float(H);
+  }
+  return true;
 }
 
 }  // namespace
@@ -263,6 +332,36 @@ gbrt_status gbrt_ctx_trim(gbrt_ctx* ctx, uint64_t* reserved_bytes) {
     *reserved_bytes = v;
   }
   return GBRT_OK;
+}
+
+gbrt_status gbrt_debug_fault(gbrt_ctx* ctx, int32_t kind, int64_t arg) {
+  if (!ctx) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_debug_fault: NULL context");
+  clear_error(ctx);
+  switch (kind) {
+    case GBRT_FAULT_NONE:
+      ctx->fault_alloc_countdown = -1;
+      ctx->fault_nan_every = 0;
+      ctx->fault_small_stack = false;
+      ctx->fault_guide_wait_ns = 0;
+      return GBRT_OK;
+    case GBRT_FAULT_ALLOC:
+      if (arg < 0) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_debug_fault: negative allocation count");
+      ctx->fault_alloc_countdown = arg;
+      return GBRT_OK;
+    case GBRT_FAULT_NAN:
+      if (arg < 0) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_debug_fault: negative NaN period");
+      ctx->fault_nan_every = uint64_t(arg);
+      return GBRT_OK;
+    case GBRT_FAULT_SMALL_STACK:
+      ctx->fault_small_stack = arg != 0;
+      return GBRT_OK;
+    case GBRT_FAULT_GUIDE_WAIT:
+      if (arg < 0 || arg > 1000000000) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_debug_fault: wait outside [0, 1 s]");
+      ctx->fault_guide_wait_ns = uint64_t(arg);
+      return GBRT_OK;
+    default:
+      return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_debug_fault: unknown fault kind");
+  }
 }
 
 gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scene** out) {
@@ -770,6 +869,16 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     v.env_h = e->height;
     v.env_mapping = e->mapping;
     for (int k = 0; k < 3; ++k) v.env_coef[k] = d->lights[envLight].intensity[k];
+    EnvTables et;
+    if (!(d->flags & GBRT_SCENE_ENV_UNIFORM) &&
+        build_env_tables(e->texels, e->width, e->height, e->mapping, v.env_coef, et)) {
+      if ((st = upload(s, et.marg, &v.env_marg)) != GBRT_OK || (st = upload(s, et.cond, &v.env_cond)) != GBRT_OK ||
+          (st = upload(s, et.dens, &v.env_dens)) != GBRT_OK) {
+        free_scene(s);
+        delete s;
+        return st;
+      }
+    }
   }
   s->n_leaves = gpuBuilt ? gb.leaves : br.leaves;
   s->max_depth = gpuBuilt ? 0 : br.max_depth;

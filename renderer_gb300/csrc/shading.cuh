@@ -20,6 +20,7 @@ namespace gbrt {
 
 constexpr float kEps = 0.001f;  // EPSILON, src/ray.h:34
 constexpr float kInvPi = 0.318309886183790671537767526745028724f;
+constexpr float kPiF = 3.14159265358979323846f;
 
 struct V3f {
   float x, y, z;
@@ -373,6 +374,101 @@ __device__ __forceinline__ V3f env_get(const DeviceScene& S, V3f d) {
   col = min(max(col, 0), W - 1);
   const float* p = S.env_texels + (size_t(row) * W + col) * 3;
   return v3(__ldg(p) * S.env_coef[0], __ldg(p + 1) * S.env_coef[1], __ldg(p + 2) * S.env_coef[2]);
+}
+
+// ---------------------------------------- environment importance sampling --
+// Physical estimator only (the renderer samples the environment by the
+// cosine, src/environmentmap.cpp:40-54). The environment is sampled from a
+// piecewise-constant density over its mapping's parameter square [0,1)^2,
+// env_h rows x env_w cells, each weighted by the luminance its centre looks
+// up times the solid angle per unit parameter area there (the tables are
+// built at scene creation, scene.cpp build_env_tables). The parameters:
+//   lat-long  u = atan2(x, -z) / 2 pi + 1/2, v = acos(y) / pi (env_get's
+//             own), solid angle per unit area J = 2 pi^2 sin(theta);
+//   angular   u = (cx + 1) / 2, v = (cy + 1) / 2 with (cx, cy) the probe's
+//             disc coordinates, r = |(cx, cy)| = theta / pi (theta measured
+//             from +x), J = 4 pi^2 sin(theta) / theta; outside the disc there
+//             is no direction.
+// A direction's density per solid angle is dens(cell) / J.
+
+// Direction of the parameter point (u, v) and J there; false where there is
+// none (outside the angular disc, or a pole where J vanishes).
+__device__ __forceinline__ bool env_param_dir(const DeviceScene& S, float u, float v, V3f& d, float& jac) {
+  if (S.env_mapping == GBRT_ENV_LATLONG) {
+    float sp, cp, st, ct;
+    sincospif(2.f * u - 1.f, &sp, &cp);
+    sincospif(v, &st, &ct);
+    d = v3(st * sp, ct, -st * cp);
+    jac = (2.f * kPiF * kPiF) * st;
+  } else {
+    const float cx = 2.f * u - 1.f, cy = 2.f * v - 1.f;
+    const float r = sqrtf(cx * cx + cy * cy);
+    if (!(r < 1.f)) return false;
+    if (r == 0.f) {
+      d = v3(1.f, 0.f, 0.f);
+      jac = 4.f * kPiF * kPiF;
+    } else {
+      float st, ct;
+      sincospif(r, &st, &ct);
+      const float s = st / r;
+      d = v3(ct, s * cx, -s * cy);
+      jac = (4.f * kPiF) * s;  // 4 pi^2 sin(pi r) / (pi r)
+    }
+  }
+  return jac > 0.f;
+}
+
+// Density per solid angle with which env_sample draws the unit direction d.
+__device__ __forceinline__ float env_pdf(const DeviceScene& S, V3f d) {
+  const int W = S.env_w, H = S.env_h;
+  float u, v, jac;
+  if (S.env_mapping == GBRT_ENV_LATLONG) {
+    u = atan2f(d.x, -d.z) * (0.5f * kInvPi) + 0.5f;
+    const float yc = fminf(1.f, fmaxf(-1.f, d.y));
+    v = acosf(yc) * kInvPi;
+    jac = (2.f * kPiF * kPiF) * sqrtf(fmaxf(0.f, 1.f - yc * yc));
+  } else {
+    const float th = acosf(fminf(1.f, fmaxf(-1.f, d.x)));
+    const float q = sqrtf(d.y * d.y + d.z * d.z);
+    const float f = q > 0.f ? th / (q * kPiF) : 0.f;
+    u = (d.y * f + 1.f) * 0.5f;
+    v = (-d.z * f + 1.f) * 0.5f;
+    jac = th > 0.f ? (4.f * kPiF * kPiF) * q / th : 4.f * kPiF * kPiF;
+  }
+  if (!(jac > 0.f)) return 0.f;
+  const int col = min(max(int(u * float(W)), 0), W - 1);
+  const int row = min(max(int(v * float(H)), 0), H - 1);
+  return __ldg(&S.env_dens[size_t(row) * W + col]) / jac;
+}
+
+// Index i in [0, n) with cdf[i] <= x < cdf[i + 1] (cdf[0] = 0, cdf[n] = 1,
+// x in [0, 1)); cells of zero width are never returned.
+__device__ __forceinline__ int cdf_find(const float* __restrict__ cdf, int n, float x) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(&cdf[mid]) <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Draws a direction from the environment's density with u1 (row) and u2
+// (cell within the row); its density per solid angle in pdf. False when the
+// point has no direction (the angular disc's corners).
+__device__ __forceinline__ bool env_sample(const DeviceScene& S, float u1, float u2, V3f& d, float& pdf) {
+  const int W = S.env_w, H = S.env_h;
+  const int row = cdf_find(S.env_marg, H, u1);
+  const float m0 = __ldg(&S.env_marg[row]), m1 = __ldg(&S.env_marg[row + 1]);
+  const float* cond = S.env_cond + size_t(row) * (W + 1);
+  const int col = cdf_find(cond, W, u2);
+  const float c0 = __ldg(&cond[col]), c1 = __ldg(&cond[col + 1]);
+  const float fv = fminf((u1 - m0) / (m1 - m0), 0.99999994f);
+  const float fu = fminf((u2 - c0) / (c1 - c0), 0.99999994f);
+  float jac;
+  if (!env_param_dir(S, (float(col) + fu) / float(W), (float(row) + fv) / float(H), d, jac)) return false;
+  pdf = __ldg(&S.env_dens[size_t(row) * W + col]) / jac;
+  return pdf > 0.f;
 }
 
 // ------------------------------------------------ physical semantics -----

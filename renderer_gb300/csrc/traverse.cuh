@@ -50,6 +50,7 @@ namespace gbrt {
 // depth is at most the binary tree's (<= 62, kept by the builder).
 constexpr int kStackSize = 190;  // any tree
 constexpr int kShortStack = 64;  // trees of 4-wide depth <= 21
+constexpr int kFaultStack = 4;   // injected fault (GBRT_FAULT_SMALL_STACK): overflows on most trees
 __host__ __device__ constexpr int stack_need(int depth4) { return 3 * depth4 + 1; }
 constexpr int kTraceBlock = 128;
 

@@ -29,6 +29,17 @@ def pytest_collection_modifyitems(config, items):
             it.add_marker(skip)
 
 
+@pytest.fixture
+def reference_probe():
+    """Path of the renderer's shipped angular light probe
+    (environmentmaps/campus_probe.hdr in its source tree, found through
+    GBRT_REFERENCE_DIR); the test is skipped where the tree is absent."""
+    from tests.golden.make_golden import PROBE
+    if not os.path.exists(PROBE):
+        pytest.skip("the renderer's shipped probe is not present (set GBRT_REFERENCE_DIR)")
+    return PROBE
+
+
 @pytest.fixture(scope="session")
 def gbrt_built():
     """Makes sure the in-tree CUDA library exists (builds it when missing)."""

@@ -30,7 +30,10 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 HERE = os.path.join(ROOT, "tests", "golden")
-PROBE = "/root/reference/environmentmaps/campus_probe.hdr"
+# The renderer's source tree (its shipped light probe is read from it); the
+# GBRT_REFERENCE_DIR environment variable overrides where it is looked for.
+REFERENCE_DIR = os.environ.get("GBRT_REFERENCE_DIR", "/root/reference")
+PROBE = os.path.join(REFERENCE_DIR, "environmentmaps", "campus_probe.hdr")
 PROBE_ROWS = (316, 324)
 
 
@@ -89,6 +92,9 @@ def decode_radiance(data):
 
 
 def make_probe():
+    if not os.path.exists(PROBE):
+        raise SystemExit("make_golden.py: the renderer's light probe %s is missing; point GBRT_REFERENCE_DIR at "
+                         "the renderer's source tree" % PROBE)
     data = open(PROBE, "rb").read()
     img, ranges = decode_radiance(data)
     W = img.shape[1]

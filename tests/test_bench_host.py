@@ -1,6 +1,6 @@
 """Host logic of bench.py (no GPU): the equal-time interpolation, the
 nvidia-smi clock and throttle parser, and the traffic figures read from the
-committed k_extend profile."""
+committed k_extend capture."""
 import math
 
 import pytest
@@ -59,7 +59,14 @@ def test_clock_sampler_without_nvidia_smi():
     assert r["sm_mhz"] is None and r["reasons"] == ["nvidia-smi unavailable"]
 
 
-def test_traffic_figures_come_from_the_committed_profile():
-    dram, l2 = bench.traffic_per_ray(), bench.traffic_per_ray("l2_bytes_per_ray")
-    assert dram == pytest.approx(46.2) and l2 == pytest.approx(164.8)
-    assert bench.traffic_per_ray("no_such_key") is None
+def test_traffic_figures_come_from_the_committed_capture():
+    tr = bench.extend_traffic()
+    assert tr is not None
+    for part in ("camera", "bounce"):
+        d = tr[part]
+        assert d["dram_bytes_per_ray"] == pytest.approx(d["dram_bytes"] / d["rays"])
+        assert d["l2_bytes_per_ray"] == pytest.approx(d["l2_bytes"] / d["rays"])
+        assert 0 < d["dram_bytes_per_ray"] < d["l2_bytes_per_ray"]
+    # a whole frame: one camera launch and eleven bounce launches per wavefront
+    assert tr["camera"]["rays"] == 1024 * 1024 * 64
+    assert tr["bounce"]["launches"] == 11 * tr["camera"]["launches"]

@@ -32,12 +32,10 @@ def test_reader_decodes_probe_scanlines_like_the_restatement(gbrt_built):
     assert tuple(z["full_shape"]) == (640, 640, 3)
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/environmentmaps/campus_probe.hdr"),
-                    reason="the renderer's shipped probe is not present")
-def test_reader_matches_the_whole_probe_sums():
+def test_reader_matches_the_whole_probe_sums(reference_probe):
     from renderer_gb300.scenefile import read_hdr
     z = _load("probe_rows.npz")
-    img = read_hdr("/root/reference/environmentmaps/campus_probe.hdr")
+    img = read_hdr(reference_probe)
     assert np.array_equal(img.astype(np.float64).sum((0, 1)), z["full_sums"])
     assert np.array_equal(img[316:324], z["texels"])
 

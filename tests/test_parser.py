@@ -1,7 +1,6 @@
 """The scene-language parser, OBJ/MTL reader and Radiance reader (pure host
 code in libgbrt.so; no GPU)."""
 import math
-import os
 
 import numpy as np
 import pytest
@@ -180,10 +179,8 @@ def test_rgbe_reader_flat_and_rle(tmp_path):
     np.testing.assert_allclose(out[0, 0], [32 * f, 64 * f, 128 * f])
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/environmentmaps/campus_probe.hdr"),
-                    reason="the renderer's shipped probe is not present")
-def test_reads_the_shipped_angular_probe():
-    img = read_hdr("/root/reference/environmentmaps/campus_probe.hdr")
+def test_reads_the_shipped_angular_probe(reference_probe):
+    img = read_hdr(reference_probe)
     assert img.shape == (640, 640, 3) and np.all(np.isfinite(img)) and img.max() > 1.0
     # an angular probe is black outside the unit disc
     assert img[0, 0].max() == 0 and img[320, 320].max() > 0
