@@ -936,9 +936,11 @@ def main():
     tr = extend_traffic()
     traffic = l2_traffic = dram_frac = None
     if tr is not None:
-        cam, bounce = tot["paths"], tot["ext_rays"] - tot["paths"]
-        traffic = (tr["camera"]["dram_bytes_per_ray"] * cam + tr["bounce"]["dram_bytes_per_ray"] * bounce) / launches
-        l2_traffic = (tr["camera"]["l2_bytes_per_ray"] * cam + tr["bounce"]["l2_bytes_per_ray"] * bounce) / launches
+        n_cam, n_bounce = tot["paths"], tot["ext_rays"] - tot["paths"]
+        traffic = (tr["camera"]["dram_bytes_per_ray"] * n_cam
+                   + tr["bounce"]["dram_bytes_per_ray"] * n_bounce) / launches
+        l2_traffic = (tr["camera"]["l2_bytes_per_ray"] * n_cam
+                      + tr["bounce"]["l2_bytes_per_ray"] * n_bounce) / launches
         dram_frac = traffic / avg_launch_s / 1e9 / peak
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": peak_kind + " (copy bandwidth)",
