@@ -686,9 +686,12 @@ gbrt_status gbrt_parsed_scene_desc(const gbrt_parsed_scene* ps,
                                    int32_t* has_camera);
 void gbrt_parsed_scene_free(gbrt_parsed_scene* ps);
 
-/* Radiance RGBE (.hdr) reader: returns H x W x 3 float BGR in a buffer the
- * caller frees with gbrt_free. (Replaces cv::imread in
- * src/environmentmap.cpp:20-33.) */
+/* Image reader for environment and texture images: Radiance RGBE (.hdr),
+ * PFM, PPM (samples 0..maxval) and PNG (recognised by its signature; 8-bit
+ * samples 0..255 as cv::imread(IMREAD_COLOR) gives them). Returns
+ * H x W x 3 float BGR in a buffer the caller frees with gbrt_free. (Replaces
+ * cv::imread in src/environmentmap.cpp:20-33 and
+ * src/texturematerial.cpp:48-60.) */
 gbrt_status gbrt_read_hdr(const char* path, float** texels_bgr,
                           int32_t* width, int32_t* height);
 void gbrt_free(void* p);

@@ -20,10 +20,9 @@
 // b(left, right, box) node contributes its children (the BVH is rebuilt);
 // box(min, max, m) and isect / union / diff / xor trees of spheres and boxes
 // become CSG objects (a box under an instance must stay axis-aligned).
-// Texture images are read from PPM (P6/P3), PFM and Radiance files
-// (formats the repository decodes itself; PNG/JPEG need an image codec
-// library that is not part of this build) and scaled by 1/255 like the
-// renderer's cv::imread + convertTo; an unreadable image gives DarkMatter.
+// Texture images are read from PNG (image_png.cpp), PPM (P6/P3), PFM and
+// Radiance files, all decoded here, and scaled by 1/255 like the renderer's
+// cv::imread + convertTo; an unreadable image gives DarkMatter.
 // An environment map that fails to load becomes a BlackLight, as in the renderer
 // (src/sceneast.cpp:598-610). As an extension, environmentmap("f", c,
 // "latlong") selects an equirectangular image.
@@ -42,6 +41,7 @@
 #include <vector>
 
 #include "../../include/gbrt.h"
+#include "image_png.h"
 
 namespace {
 
@@ -592,6 +592,17 @@ bool readPPM(const std::string& path, std::vector<float>& bgr, int& W, int& H, s
 }
 
 bool readImage(const std::string& path, std::vector<float>& bgr, int& W, int& H, std::string& why) {
+  {
+    // PNG is recognised by its signature, as cv::imread recognises formats.
+    std::ifstream in(path, std::ios::binary);
+    char sig[8] = {0};
+    if (in && in.read(sig, 8) && gbrt_img::is_png(std::string(sig, 8))) {
+      std::string data;
+      if (!readFile(path, data)) { why = "cannot read " + path; return false; }
+      if (!gbrt_img::decode_png(data, bgr, W, H, why)) { why = path + ": " + why; return false; }
+      return true;
+    }
+  }
   std::string lower = path;
   std::transform(lower.begin(), lower.end(), lower.begin(), ::tolower);
   if (lower.size() >= 4 && lower.substr(lower.size() - 4) == ".pfm") return readPFM(path, bgr, W, H, why);

@@ -4,7 +4,7 @@ triangles from their texture coordinates (default (0,0), (0,1), (1,0)).
 
 CPU: the oracle against closed forms (a constant texture is a diffuse
 material; a textured floor under a point light shows the texel values), the
-parser (texture(...) reads PPM, scales by 1/255, unreadable files give
+parser (texture(...) reads PPM and PNG, scales by 1/255, unreadable files give
 DarkMatter). GPU: path-level parity with the oracle on a scene whose texture
 varies across the image, for both estimators."""
 import math
@@ -120,3 +120,209 @@ def test_textured_path_level_parity(ctx, semantics):
     close = np.isclose(film, orc, rtol=2e-3, atol=1e-5).all(-1)
     assert close.mean() > 0.97, close.mean()
     assert film.mean() == pytest.approx(orc.mean(), rel=5e-3)
+
+
+# ------------------------------------------------------------------ PNG ----
+# An independent PNG writer (Python's zlib for DEFLATE, the filters and Adam7
+# written out here) feeds the library's decoder; the expected image is what
+# cv::imread(IMREAD_COLOR) gives: 8-bit BGR, grey replicated, palette
+# expanded, alpha dropped, 16-bit samples reduced to their high byte.
+import struct
+import zlib
+
+_ADAM7 = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2)]
+_CHANS = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}
+
+
+def _chunk(t, body):
+    return struct.pack(">I", len(body)) + t + body + struct.pack(">I", zlib.crc32(t + body) & 0xFFFFFFFF)
+
+
+def _pack_rows(samples, depth):
+    """(h, w, c) integer samples -> list of packed row byte strings."""
+    h, w, c = samples.shape
+    rows = []
+    for y in range(h):
+        flat = samples[y].reshape(-1).astype(np.int64)
+        if depth == 16:
+            rows.append(flat.astype(">u2").tobytes())
+        elif depth == 8:
+            rows.append(flat.astype(np.uint8).tobytes())
+        else:
+            per = 8 // depth
+            pad = (-len(flat)) % per
+            f = np.concatenate([flat, np.zeros(pad, np.int64)]).reshape(-1, per)
+            shifts = np.array([8 - depth * (k + 1) for k in range(per)])
+            rows.append((f << shifts).sum(1).astype(np.uint8).tobytes())
+    return rows
+
+
+def _filter_rows(rows, bpp, rng):
+    """Applies a random PNG filter (0-4) to each row; returns the filtered stream."""
+    out = bytearray()
+    prev = bytes(len(rows[0])) if rows else b""
+    for r in rows:
+        f = int(rng.integers(0, 5))
+        x, b = np.frombuffer(r, np.uint8).astype(np.int64), np.frombuffer(prev, np.uint8).astype(np.int64)
+        a = np.concatenate([np.zeros(bpp, np.int64), x[:-bpp]]) if len(x) > bpp else np.zeros_like(x)
+        c = np.concatenate([np.zeros(bpp, np.int64), b[:-bpp]]) if len(x) > bpp else np.zeros_like(x)
+        if f == 0:
+            pred = np.zeros_like(x)
+        elif f == 1:
+            pred = a
+        elif f == 2:
+            pred = b
+        elif f == 3:
+            pred = (a + b) >> 1
+        else:
+            p = a + b - c
+            pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+            pred = np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, c))
+        out.append(f)
+        out += ((x - pred) & 255).astype(np.uint8).tobytes()
+        prev = r
+    return bytes(out)
+
+
+def write_png(path, samples, depth, ctype, palette=None, interlace=False, seed=0, level=6,
+              strategy=zlib.Z_DEFAULT_STRATEGY, split_idat=1):
+    h, w, c = samples.shape
+    assert c == _CHANS[ctype]
+    rng = np.random.default_rng(seed)
+    bpp = max(1, c * depth // 8)
+    raw = b""
+    for (x0, y0, dx, dy) in (_ADAM7 if interlace else [(0, 0, 1, 1)]):
+        sub = samples[y0::dy, x0::dx]
+        if sub.size:
+            raw += _filter_rows(_pack_rows(sub, depth), bpp, rng)
+    co = zlib.compressobj(level, zlib.DEFLATED, 15, 8, strategy)
+    z = co.compress(raw) + co.flush()
+    png = b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, int(interlace)))
+    png += _chunk(b"tEXt", b"Comment\x00ancillary chunk")
+    if palette is not None:
+        png += _chunk(b"PLTE", np.asarray(palette, np.uint8).tobytes())
+    step = -(-len(z) // split_idat)
+    for k in range(0, len(z), step):
+        png += _chunk(b"IDAT", z[k:k + step])
+    png += _chunk(b"IEND", b"")
+    path.write_bytes(png)
+
+
+def imread_color(samples, depth, ctype, palette=None):
+    """cv::imread(IMREAD_COLOR) of those samples: (h, w, 3) BGR 0..255."""
+    s = samples.astype(np.int64)
+    if depth == 16:
+        s = s >> 8
+    if ctype == 3:
+        rgb = np.asarray(palette, np.int64)[s[..., 0]]
+    elif ctype in (0, 4):
+        g = s[..., 0] * (255 // ((1 << depth) - 1)) if depth < 8 else s[..., 0]
+        rgb = np.stack([g, g, g], -1)
+    else:
+        rgb = s[..., :3]
+    return rgb[..., ::-1].astype(np.float32)
+
+
+PNG_CASES = [(ct, d) for ct, ds in ((0, (1, 2, 4, 8, 16)), (2, (8, 16)), (3, (1, 2, 4, 8)), (4, (8, 16)),
+                                    (6, (8, 16))) for d in ds]
+
+
+@pytest.mark.parametrize("ctype,depth", PNG_CASES)
+@pytest.mark.parametrize("interlace", [False, True])
+def test_png_decoder_matches_imread_color(tmp_path, ctype, depth, interlace):
+    from renderer_gb300.scenefile import read_hdr
+    rng = np.random.default_rng(ctype * 100 + depth + 7 * interlace)
+    h, w = 13, 11  # odd sizes: partial Adam7 blocks and packed rows with padding bits
+    palette = None
+    top = (1 << depth) - 1
+    if ctype == 3:
+        n = min(1 << depth, 40)
+        palette = rng.integers(0, 256, (n, 3))
+        top = n - 1
+    samples = rng.integers(0, top + 1, (h, w, _CHANS[ctype]))
+    p = tmp_path / "img.png"
+    write_png(p, samples, depth, ctype, palette, interlace, seed=depth, split_idat=3)
+    got = read_hdr(str(p))
+    np.testing.assert_array_equal(got, imread_color(samples, depth, ctype, palette))
+
+
+@pytest.mark.parametrize("level,strategy", [(0, zlib.Z_DEFAULT_STRATEGY), (1, zlib.Z_FIXED), (9, zlib.Z_DEFAULT_STRATEGY),
+                                            (6, zlib.Z_HUFFMAN_ONLY), (6, zlib.Z_RLE)])
+def test_png_deflate_block_kinds(tmp_path, level, strategy):
+    """Stored, fixed-Huffman and dynamic-Huffman blocks, long matches and
+    overlapping copies (a smooth 300 x 200 RGB image with flat runs)."""
+    from renderer_gb300.scenefile import read_hdr
+    y, x = np.mgrid[0:200, 0:300]
+    img = np.stack([(x // 7) % 256, (y * 3) % 256, ((x + y) // 50) * 40 % 256], -1)
+    img[50:90, :, :] = 17  # long runs
+    p = tmp_path / "big.png"
+    write_png(p, img, 8, 2, level=level, strategy=strategy)
+    np.testing.assert_array_equal(read_hdr(str(p)), img[..., ::-1].astype(np.float32))
+
+
+def test_png_rejects_damage(tmp_path):
+    """A flipped byte fails the chunk CRC; a truncated file and a bad zlib
+    stream are refused; a scene texture that fails to decode is DarkMatter."""
+    from renderer_gb300.scenefile import load_scene_string, read_hdr
+    img = np.random.default_rng(3).integers(0, 256, (8, 8, 3))
+    p = tmp_path / "ok.png"
+    write_png(p, img, 8, 2)
+    good = p.read_bytes()
+    for bad in (good[:40] + bytes([good[40] ^ 1]) + good[41:], good[:-20]):
+        q = tmp_path / "bad.png"
+        q.write_bytes(bad)
+        with pytest.raises(Exception):
+            read_hdr(str(q))
+    # a valid CRC around an IDAT whose zlib header is wrong
+    ihdr_end = 8 + 25
+    body = b"\x78\x9c"[::-1] + zlib.compress(b"\x00" * 10)[2:]
+    q = tmp_path / "badz.png"
+    q.write_bytes(good[:ihdr_end] + _chunk(b"IDAT", body) + _chunk(b"IEND", b""))
+    with pytest.raises(Exception):
+        read_hdr(str(q))
+    s = load_scene_string('intersectable = intersectables { sphere([0 0 0], 1, texture("bad.png", [1 1 1], 1)) };',
+                          str(tmp_path))
+    assert s.materials[0]["type"] == _abi.MAT_DARK
+
+
+def test_parser_reads_png_texture(tmp_path):
+    """texture("t.png", ...) in a scene file: the 8-bit image scaled by 1/255,
+    like cv::imread + convertTo (src/texturematerial.cpp:48-60)."""
+    from renderer_gb300.scenefile import load_scene_string
+    img = np.random.default_rng(5).integers(0, 256, (5, 7, 4))
+    write_png(tmp_path / "t.png", img, 8, 6, interlace=True)
+    s = load_scene_string('intersectable = intersectables { t([0 0 0], [1 0 0], [0 1 0], [0 0 1], [0 0 1], '
+                          '[0 0 1], [0 0], [1 0], [0 1], texture("t.png", [1 1 1], 1)) };', str(tmp_path))
+    m = s.materials[0]
+    assert m["type"] == _abi.MAT_TEXTURE
+    np.testing.assert_allclose(s.textures[m["texture"]], img[..., 2::-1] / 255.0, rtol=1e-6)
+
+
+PNG_FLOOR_SCENE = """
+camera = camera([0 3 0.0001], [0 0 0], [0 0 -1], 0.5, 40, 40);
+lights = lights { pointlight([0 2 0], [4 4 4]) };
+intersectable = intersectables {
+  t([-1 0 -1], [1 0 -1], [1 0 1], [0 1 0], [0 1 0], [0 1 0], [0 1], [1 1], [1 0], texture("floor.png", [1 0.9 0.8], 2.2))
+  t([-1 0 -1], [1 0 1], [-1 0 1], [0 1 0], [0 1 0], [0 1 0], [0 1], [1 0], [0 0], texture("floor.png", [1 0.9 0.8], 2.2))
+};
+"""
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("semantics", [_abi.SEM_REFERENCE, _abi.SEM_PHYSICAL])
+def test_png_textured_scene_parity(ctx, tmp_path, semantics):
+    """A scene file with a PNG-textured floor (palette PNG, Adam7): the GPU
+    render against the oracle, path by path, on the parsed scene."""
+    from renderer_gb300.scenefile import load_scene_string
+    from tests.test_gpu_render import gpu_render
+    rng = np.random.default_rng(11)
+    pal = rng.integers(0, 256, (16, 3))
+    write_png(tmp_path / "floor.png", rng.integers(0, 16, (24, 24, 1)), 4, 3, palette=pal, interlace=True)
+    s = load_scene_string(PNG_FLOOR_SCENE, str(tmp_path))
+    assert s.materials[0]["type"] == _abi.MAT_TEXTURE
+    prm = render_params(2, 2, 0.5, 4, 5, semantics=semantics)
+    (film, _, _), _ = gpu_render(ctx, s, prm)
+    orc = OracleScene(s).render(s.camera_struct(), prm, rng_mode=1)["film"]
+    assert film[..., 0].std() > 0.05 * film[..., 0].mean()  # the texture shows
+    close = np.isclose(film, orc, rtol=2e-3, atol=1e-5).all(-1)
+    assert close.mean() > 0.98, close.mean()
