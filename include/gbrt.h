@@ -207,6 +207,11 @@ typedef struct gbrt_scene_desc {
   /* instanced meshes */
   const gbrt_mesh* meshes; int32_t n_meshes;
   const gbrt_instance* instances; int32_t n_instances;
+  /* Optional (NULL: primitive-id order): per primitive id, its position in
+   * the scene's root list (lights first, then the scene's intersectables as
+   * the scene file lists them, src/sceneast.cpp:673-679). Used only with
+   * GBRT_SCENE_LIST_ORDER; gbrt_parsed_scene_desc fills it. */
+  const int32_t* list_rank;
 } gbrt_scene_desc;
 
 typedef enum gbrt_scene_flags {
@@ -230,7 +235,17 @@ typedef enum gbrt_scene_flags {
    * heuristic). For measuring what importance sampling gains; the
    * renderer's own estimator (GBRT_SEM_REFERENCE) samples it by the cosine
    * either way (src/environmentmap.cpp:40-54). */
-  GBRT_SCENE_ENV_UNIFORM = 4
+  GBRT_SCENE_ENV_UNIFORM = 4,
+  /* Exact ties in t between different primitives resolve as the renderer's
+   * IntersectableList does (src/intersectablelist.cpp:29-47: each entry is
+   * tested with the ray shortened to the best hit so far, inclusive, so the
+   * later entry wins), which is what the renderer computes with --no-bvh
+   * (src/sceneast.cpp:681-688): the later primitive in list order
+   * (gbrt_scene_desc.list_rank) wins, and inside a mesh instance the later
+   * mesh triangle. Without the flag an exact tie goes to whichever primitive
+   * the traversal reaches first. Closest hits that are not ties are the same
+   * either way. */
+  GBRT_SCENE_LIST_ORDER = 8
 } gbrt_scene_flags;
 
 /* Camera(cop, lookAt, up, fov[radians, full vertical], resolution),

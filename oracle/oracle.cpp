@@ -1234,12 +1234,27 @@ static Scene* buildScene(const gbrt_scene_desc* d, bool useBVH) {
     auto* inst = new IntersectableInstance();
     std::memcpy(inst->fwd, in.transform, sizeof inst->fwd);
     if (!affineInverse(in.transform, inst->inv)) { delete inst; continue; }
-    inst->child = buildBVH(tris, s->pool);
+    if (useBVH) {
+      inst->child = buildBVH(tris, s->pool);
+    } else {  /* --no-bvh: the mesh's triangles as a list, in file order */
+      auto* ml = new IntersectableList();
+      ml->comps = tris;
+      s->pool.emplace_back(ml);
+      inst->child = ml;
+    }
     inst->prim = pid;
     s->pool.emplace_back(inst);
     top.push_back(inst);
   }
   s->nPrims = pid;
+  /* The root list in the scene's list order (gbrt_scene_desc.list_rank):
+   * with --no-bvh the renderer tests it in that order and the later entry
+   * wins exact ties (src/intersectablelist.cpp:29-47). */
+  if (d->list_rank) {
+    std::stable_sort(top.begin(), top.end(), [&](const Intersectable* a, const Intersectable* b) {
+      return d->list_rank[a->prim] < d->list_rank[b->prim];
+    });
+  }
   if (useBVH && !top.empty()) {
     s->root = buildBVH(top, s->pool);
   } else {

@@ -66,7 +66,8 @@ class SceneDesc(C.Structure):
                 ("csg_nodes", C.POINTER(CsgNode)), ("n_csg_nodes", C.c_int32),
                 ("csg_roots", C.POINTER(C.c_int32)), ("n_csg", C.c_int32),
                 ("meshes", C.POINTER(Mesh)), ("n_meshes", C.c_int32),
-                ("instances", C.POINTER(Instance)), ("n_instances", C.c_int32)]
+                ("instances", C.POINTER(Instance)), ("n_instances", C.c_int32),
+                ("list_rank", C.POINTER(C.c_int32))]
 
 
 class Camera(C.Structure):
@@ -158,7 +159,7 @@ ENV_ANGULAR, ENV_LATLONG = range(2)
 # gbrt_semantics
 SEM_REFERENCE, SEM_PHYSICAL = range(2)
 # gbrt_scene_flags / gbrt_render_flags
-SCENE_WATERTIGHT, SCENE_GPU_BUILD, SCENE_ENV_UNIFORM = 1, 2, 4
+SCENE_WATERTIGHT, SCENE_GPU_BUILD, SCENE_ENV_UNIFORM, SCENE_LIST_ORDER = 1, 2, 4, 8
 RENDER_TIME_KERNELS, RENDER_COUNT_TRAVERSAL = 1, 2
 NOALLOC_MAX_BATCH = 65536
 # gbrt_fault (host-side fault injection for the failure-path tests)

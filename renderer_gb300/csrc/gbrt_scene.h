@@ -114,6 +114,11 @@ struct DeviceScene {
   // Instances (null when none): four float4 each, see above.
   const float4* inst;
   int32_t n_inst;
+  // GBRT_SCENE_LIST_ORDER (both null without it): per primitive id its rank
+  // in the scene's list, and per record its triangle's index in its mesh
+  // (null when the scene has no mesh instances).
+  const int32_t* prim_rank;
+  const int32_t* rec_sub;
 };
 
 // Internal hit encoding of the traversal kernels.

@@ -583,6 +583,7 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   struct MeshTree {
     Collapsed c4;
     std::vector<Rec> recs;  // leaf order
+    std::vector<int32_t> tri_index;  // per leaf-order record, its triangle's index in the mesh
     Box box;
     int64_t node0 = 0, rec0 = 0;
     bool used = false;
@@ -643,7 +644,11 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
     if (mbr.max_depth > kMaxTreeDepth)
       return fail(ctx, GBRT_ERR_UNSUPPORTED, "gbrt_scene_create: mesh BVH deeper than the traversal stack");
     mt.recs.resize(mrecs.size());
-    for (size_t k = 0; k < mbr.order.size(); ++k) mt.recs[k] = mrecs[mbr.order[k]];
+    mt.tri_index.resize(mrecs.size());
+    for (size_t k = 0; k < mbr.order.size(); ++k) {
+      mt.recs[k] = mrecs[mbr.order[k]];
+      mt.tri_index[k] = int32_t(mbr.order[k]);
+    }
     mt.c4 = collapse_bvh4(mbr);
     meshDepth = std::max(meshDepth, mt.c4.max_depth);
     mt.box = mboxes[0];
@@ -802,6 +807,25 @@ gbrt_status gbrt_scene_create(gbrt_ctx* ctx, const gbrt_scene_desc* d, gbrt_scen
   }
   v.n_nodes = gpuBuilt ? gb.n_nodes : int64_t(nodes.size() / 8);
   v.n_recs = int64_t(meta.size());
+  if (d->flags & GBRT_SCENE_LIST_ORDER) {
+    // Tie-breaking by list order: each primitive's rank, and each record's
+    // triangle index within its mesh (0 outside meshes; meshes exist only
+    // with the host build).
+    std::vector<int32_t> rank(static_cast<size_t>(pid));
+    for (int32_t i = 0; i < pid; ++i) rank[size_t(i)] = d->list_rank ? d->list_rank[i] : i;
+    std::vector<int32_t> sub;
+    if (d->n_instances > 0 && !gpuBuilt) {
+      sub.assign(size_t(v.n_recs), 0);
+      for (const MeshTree& mt : meshTrees)
+        if (mt.used) std::copy(mt.tri_index.begin(), mt.tri_index.end(), sub.begin() + mt.rec0);
+    }
+    if ((pid > 0 && (st = upload(s, rank, &v.prim_rank)) != GBRT_OK) ||
+        (!sub.empty() && (st = upload(s, sub, &v.rec_sub)) != GBRT_OK)) {
+      free_scene(s);
+      delete s;
+      return st;
+    }
+  }
   if (d->n_instances > 0) {
     if ((st = upload(s, instTab, &v.inst)) != GBRT_OK) {
       free_scene(s);

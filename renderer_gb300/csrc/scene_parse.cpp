@@ -23,6 +23,9 @@
 // Texture images are read from PNG (image_png.cpp), PPM (P6/P3), PFM and
 // Radiance files, all decoded here, and scaled by 1/255 like the renderer's
 // cv::imread + convertTo; an unreadable image gives DarkMatter.
+// Each primitive's position in the scene's root list (lights, then the
+// intersectables in file order) is kept as gbrt_scene_desc.list_rank, for the
+// list's tie rule under GBRT_SCENE_LIST_ORDER.
 // An environment map that fails to load becomes a BlackLight, as in the renderer
 // (src/sceneast.cpp:598-610). As an extension, environmentmap("f", c,
 // "latlong") selects an equirectangular image.
@@ -796,6 +799,11 @@ struct gbrt_parsed_scene {
   std::vector<MeshData> meshes;
   std::vector<gbrt_mesh> mesh_descs;
   std::vector<gbrt_instance> instances;
+  // The scene's intersectables in the order the scene file lists them
+  // (kind, index within its kind), and the list ranks built from it.
+  enum Kind { kTri, kQuad, kSphere, kPlane, kCsg, kInstance };
+  std::vector<std::pair<int, int64_t>> listed;
+  std::vector<int32_t> list_rank;
 };
 
 namespace {
@@ -809,6 +817,7 @@ struct Builder {
   std::map<std::string, std::vector<LightNode>> lightVars;
   std::map<std::string, CameraNode> camVars;
   std::map<std::string, std::pair<std::vector<ObjTri>, std::map<std::string, MatNode>>> objCache;
+  int inMesh = 0;  // > 0 while a mesh instance's triangles are being emitted
 
   Builder(gbrt_parsed_scene& p, std::string dir) : ps(p), baseDir(std::move(dir)) {}
 
@@ -897,6 +906,7 @@ struct Builder {
       ps.tri_nrm.push_back(m.x); ps.tri_nrm.push_back(m.y); ps.tri_nrm.push_back(m.z);
     }
     if (n) ps.any_smooth = true;
+    if (!inMesh) ps.listed.emplace_back(gbrt_parsed_scene::kTri, int64_t(ps.tri_mat.size()));
     ps.tri_mat.push_back(mat);
   }
 
@@ -933,6 +943,7 @@ struct Builder {
       q.p[k][0] = v.x; q.p[k][1] = v.y; q.p[k][2] = v.z;
     }
     q.material = mat;
+    ps.listed.emplace_back(gbrt_parsed_scene::kQuad, int64_t(ps.quads.size()));
     ps.quads.push_back(q);
   }
 
@@ -961,6 +972,7 @@ struct Builder {
         }
         p.plane[0] = P.x; p.plane[1] = P.y; p.plane[2] = P.z; p.plane[3] = P.w;
         p.material = resolveMat(n->mat);
+        ps.listed.emplace_back(gbrt_parsed_scene::kPlane, int64_t(ps.planes.size()));
         ps.planes.push_back(p);
         break;
       }
@@ -972,12 +984,14 @@ struct Builder {
         s.center[0] = c.x; s.center[1] = c.y; s.center[2] = c.z;
         s.radius = r;
         s.material = resolveMat(n->mat);
+        ps.listed.emplace_back(gbrt_parsed_scene::kSphere, int64_t(ps.spheres.size()));
         ps.spheres.push_back(s);
         break;
       }
       case Node::BOX:  // an AxisAlignedBox is a CSG object of its own
       case Node::CSG: {
         int leaves = 0;
+        ps.listed.emplace_back(gbrt_parsed_scene::kCsg, int64_t(ps.csg_roots.size()));
         ps.csg_roots.push_back(csgNode(n, xf, leaves));
         if (leaves > GBRT_CSG_MAX_LEAVES)
           throw ParseError(GBRT_ERR_UNSUPPORTED, "CSG object with more than 8 spheres and boxes");
@@ -992,6 +1006,7 @@ struct Builder {
           for (int r = 0; r < 3; ++r)
             for (int c = 0; c < 4; ++c) in.transform[4 * r + c] = M.m[r][c];
           in.mesh = meshFor(n->children[0]);
+          ps.listed.emplace_back(gbrt_parsed_scene::kInstance, int64_t(ps.instances.size()));
           ps.instances.push_back(in);
         } else {
           emit(n->children[0], &M);
@@ -1071,7 +1086,9 @@ struct Builder {
     bool smooth = false;
     ps.tri_pos.swap(pos); ps.tri_nrm.swap(nrm); ps.tri_uv.swap(uv); ps.tri_mat.swap(mat);
     std::swap(ps.any_smooth, smooth);
+    ++inMesh;  // the subtree's triangles belong to the mesh, not to the root list
     emit(n, nullptr);
+    --inMesh;
     ps.tri_pos.swap(pos); ps.tri_nrm.swap(nrm); ps.tri_uv.swap(uv); ps.tri_mat.swap(mat);
     std::swap(ps.any_smooth, smooth);
     gbrt_parsed_scene::MeshData md;
@@ -1329,6 +1346,27 @@ gbrt_status gbrt_parsed_scene_desc(const gbrt_parsed_scene* ps, gbrt_scene_desc*
   d->n_csg_nodes = int32_t(ps->csg_nodes.size());
   d->csg_roots = ps->csg_roots.empty() ? nullptr : ps->csg_roots.data();
   d->n_csg = int32_t(ps->csg_roots.size());
+  // List ranks by primitive id: the lights first (the root list's head,
+  // src/sceneast.cpp:676-678), then the intersectables as listed.
+  {
+    // first primitive id of each kind, in gbrt_parsed_scene::Kind order
+    const int64_t nL = d->n_lights;
+    int64_t first[6];
+    first[gbrt_parsed_scene::kTri] = nL;
+    first[gbrt_parsed_scene::kQuad] = first[gbrt_parsed_scene::kTri] + d->n_tri;
+    first[gbrt_parsed_scene::kSphere] = first[gbrt_parsed_scene::kQuad] + d->n_quads;
+    first[gbrt_parsed_scene::kPlane] = first[gbrt_parsed_scene::kSphere] + d->n_spheres;
+    first[gbrt_parsed_scene::kCsg] = first[gbrt_parsed_scene::kPlane] + d->n_planes;
+    first[gbrt_parsed_scene::kInstance] = first[gbrt_parsed_scene::kCsg] + d->n_csg;
+    const int64_t n = first[gbrt_parsed_scene::kInstance] + int64_t(ps->instances.size());
+    mps->list_rank.resize(size_t(n));
+    for (int64_t i = 0; i < n; ++i) mps->list_rank[size_t(i)] = int32_t(i);
+    if (int64_t(ps->listed.size()) == n - nL) {
+      int64_t r = nL;
+      for (const auto& e : ps->listed) mps->list_rank[size_t(first[e.first] + e.second)] = int32_t(r++);
+    }
+    d->list_rank = n ? mps->list_rank.data() : nullptr;
+  }
   mps->mesh_descs.resize(ps->meshes.size());
   for (size_t i = 0; i < ps->meshes.size(); ++i) {
     const auto& m = ps->meshes[i];

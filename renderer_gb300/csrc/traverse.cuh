@@ -407,12 +407,36 @@ __device__ __forceinline__ bool trace_init(const DeviceScene& S, const TRay& r, 
   for (int k = 0; k < S.n_planes; ++k) {
     if (ANY && S.plane_meta[k].x == ignore_prim) continue;
     float t = plane_t(r, __ldg(&S.planes[k]));
-    if (t >= r.tmin && t <= r.tmax && accept_t(t, r.tmin, ts.tcur, ts.found)) {
+    bool take = t >= r.tmin && t <= r.tmax && accept_t(t, r.tmin, ts.tcur, ts.found);
+    if (!ANY && !take && S.prim_rank && ts.found && t == ts.tcur)
+      take = S.prim_rank[S.plane_meta[k].x] > S.prim_rank[ts.bestPrim];  // list order: the later plane
+    if (take) {
       ts.tcur = t; ts.found = true; ts.best = -2 - k; ts.bu = 0.f; ts.bv = 0.f;
+      if (S.prim_rank) ts.bestPrim = S.plane_meta[k].x;
       if (ANY) return true;
     }
   }
   return S.n_nodes <= 0;
+}
+
+// GBRT_SCENE_LIST_ORDER: whether a hit on record rec (primitive prim, in the
+// instance being traversed) at exactly the best t so far comes later in the
+// scene's list than the best hit: by the primitives' (or instances') ranks,
+// then, within one mesh instance, by the mesh triangles' indices. Reached
+// only on exact ties.
+template <bool GEN>
+__device__ __noinline__ bool list_later(const DeviceScene& S, int32_t prim, int32_t rec, const TState& ts) {
+  int32_t top = prim, btop = ts.bestPrim, sub = 0, bsub = 0;
+  if (GEN && ts.inst >= 0) {
+    top = __float_as_int(__ldg(S.inst + 4 * int64_t(ts.inst) + 3).y);
+    sub = S.rec_sub ? S.rec_sub[rec] : 0;
+  }
+  if (GEN && ts.bestInst >= 0) {
+    btop = __float_as_int(__ldg(S.inst + 4 * int64_t(ts.bestInst) + 3).y);
+    bsub = S.rec_sub ? S.rec_sub[ts.best] : 0;
+  }
+  const int32_t a = S.prim_rank[top], b = S.prim_rank[btop];
+  return a != b ? a > b : sub > bsub;
 }
 
 // One traversal step: one 4-wide node or one leaf. ANY: stop at the first
@@ -506,8 +530,11 @@ __device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& wr,
         u = __int_as_float(leaf);
       }
       if (hit && ts.found && !displace) {
-        // strictly closer, and a second half never displaces its first half
-        hit = t < ts.tcur && !(quad == 2 && ts.bestPrim == prim && ts.bestQuad == 1);
+        // strictly closer (or, under GBRT_SCENE_LIST_ORDER, as close and later
+        // in the list), and a second half never displaces its first half
+        bool closer = t < ts.tcur;
+        if (!ANY && !closer && t == ts.tcur && S.prim_rank) closer = list_later<GEN>(S, prim, int32_t(k), ts);
+        hit = closer && !(quad == 2 && ts.bestPrim == prim && ts.bestQuad == 1);
       }
       if (hit) {
         ts.tcur = t; ts.found = true; ts.best = int32_t(k); ts.bu = u; ts.bv = v;

@@ -38,6 +38,7 @@ class SceneData:
     csg_roots: List[int] = field(default_factory=list)
     meshes: List[dict] = field(default_factory=list)     # {"pos" (N, 9), "nrm" (N, 9) or None, "mat" (N,) or None}
     instances: List[tuple] = field(default_factory=list)  # (3x4 object->world transform, mesh index)
+    list_rank: Optional[np.ndarray] = None  # (n_prims,) int32: position in the root list, or None
 
     # ------------------------------------------------------------ building
     def add_material(self, type, kd=(0, 0, 0), ks=(0, 0, 0), exponent=0.0, ior=1.0, coefficient=1.0, texture=-1):
@@ -202,6 +203,12 @@ class SceneData:
             d.n_meshes = len(self.meshes)
             d.instances = iarr
             d.n_instances = len(self.instances)
+        if self.list_rank is not None:
+            rank = np.ascontiguousarray(self.list_rank, np.int32).reshape(-1)
+            if len(rank) != self.n_prims():
+                raise ValueError("list_rank needs one entry per primitive")
+            keep.append(rank)
+            d.list_rank = rank.ctypes.data_as(C.POINTER(C.c_int32))
         return d, keep
 
     def camera_struct(self, width=None, height=None):

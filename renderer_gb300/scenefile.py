@@ -59,6 +59,8 @@ def _from_parsed(ps):
         L = d.lights[i]
         s.lights.append(dict(type=L.type, origin=tuple(L.origin), u=tuple(L.u), v=tuple(L.v),
                              intensity=tuple(L.intensity)))
+    if d.list_rank:
+        s.list_rank = np.ctypeslib.as_array(d.list_rank, shape=(s.n_prims(),)).copy()
     if d.env:
         e = d.env.contents
         s.env = np.ctypeslib.as_array(e.texels, shape=(e.height, e.width, 3)).copy()
