@@ -432,6 +432,77 @@ def run_quality(args):
     print(json.dumps(out))
 
 
+CORNELL_WORKLOAD = ("Cornell box (5 diffuse quads, 0.5x0.5 area light of radiance 15, mirror and glass spheres), "
+                    "256x256, 4x4 jittered spp, max depth 8, RR p=0.5, reference semantics")
+
+
+def run_cornell(args):
+    """Throughput on the Cornell box (256x256, 16 spp, depth 8): GPU paths/s
+    of whole frames (device film, CUDA-event time of gbrt_render_device),
+    end to end through gbrt_render (host film), and the oracle's CPU render
+    of the same frame on all host cores beside it."""
+    import numpy as np
+
+    import renderer_gb300 as rg
+    from oracle.binding import OracleScene
+    from renderer_gb300 import _abi, workloads
+    from renderer_gb300.runtime import Context, GpuScene
+
+    s = workloads.cornell_box(256, 256)
+    cam = s.camera_struct()
+    ctx = Context(0)
+    gs = GpuScene(ctx, s)
+    lib = rg.lib()
+    import torch
+    film = torch.empty(256 * 256 * 3, dtype=torch.float32, device="cuda")
+    fsum = torch.empty(256 * 256 * 3, dtype=torch.float64, device="cuda")
+    hfilm = np.zeros((256, 256, 3), np.float32)
+    prm = workloads.cornell_params(max_depth=8, seed=1)
+
+    def frame_dev():
+        st = _abi.Stats()
+        rg.check(lib.gbrt_render_device(gs.handle, C.byref(cam), C.byref(prm), C.c_void_p(film.data_ptr()),
+                                        C.c_void_p(fsum.data_ptr()), None, C.byref(st)), ctx.handle)
+        return st
+
+    for _ in range(args.warmup):
+        frame_dev()
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    ms, paths, rays, launches = 0.0, 0, 0, 0
+    for _ in range(args.steps):
+        st = frame_dev()
+        ms += st.render_ms
+        paths += st.paths
+        rays += st.extension_rays + st.shadow_rays
+        launches += st.kernel_launches
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        rg.check(lib.gbrt_render(gs.handle, C.byref(cam), C.byref(prm), hfilm.ctypes.data_as(C.c_void_p), None,
+                                 None, None, None), ctx.handle)
+    e2e_s = time.perf_counter() - t
+    clk = clocks.stop()
+    del gs
+    ctx.close()
+    o = OracleScene(s, timing=True)
+    t = time.perf_counter()
+    r = o.render(cam, prm, rng_mode=0, threads=0)
+    cpu_s = time.perf_counter() - t
+    line = {"metric": "paths/s (Cornell box)", "value": paths / (ms / 1000.0), "unit": "paths/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": CORNELL_WORKLOAD, "paths_per_step": paths // args.steps,
+                       "rays_per_s": rays / (ms / 1000.0),
+                       "l2": "scene and path state fit in L2 (a 1M-path frame); whole frames timed back to back"},
+            "e2e": {"value": paths / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": C.sizeof(_abi.Camera) +
+                    C.sizeof(_abi.RenderParams), "d2h_bytes_per_step": 256 * 256 * 3 * 4},
+            "gpu_launches": launches, "clocks": clk,
+            "cpu_baseline": {"value": r["paths"] / cpu_s, "unit": "paths/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "the whole frame (%d paths, %.2f s)" % (r["paths"], cpu_s)}}
+    print(json.dumps(line))
+
+
 BATCH_WORKLOAD = ("64 seeded scenes: diffuse 4x3x4 box, 1-3 noise-displaced meshes (log-uniform 10k-2M triangles), "
                   "2-8 spheres, materials uniform over diffuse/mirror/glass 1.5/Blinn 10-500, 1-4 area lights of "
                   "radiance 5-50, 128^2-1024^2 pixels, 4-256 spp, max depth 8, RR p=0.5, reference semantics, "
@@ -443,18 +514,40 @@ def _batch_scene(i):
     return workloads.batch_scene(i, 0)
 
 
+def _time_batch(fn, jobs, steps):
+    """steps calls of fn(jobs) -> (films, job_ms, stats): device ms, wall ms,
+    paths, rays, launches and the mean per-image device times."""
+    import numpy as np
+    dev_ms, wall_ms, paths, ext, sh, launches, per_image = 0.0, 0.0, 0, 0, 0, 0, []
+    for _ in range(steps):
+        t = time.perf_counter()
+        films, job_ms, st = fn(jobs)
+        wall_ms += 1000 * (time.perf_counter() - t)
+        dev_ms += st.device_ms
+        paths += st.paths
+        ext += st.extension_rays
+        sh += st.shadow_rays
+        launches += st.kernel_launches
+        per_image.append(job_ms)
+    return dict(dev_ms=dev_ms, wall_ms=wall_ms, paths=paths, ext=ext, sh=sh, launches=launches,
+                per_image=np.mean(per_image, 0))
+
+
 def run_batch(args):
-    """Many independent images in one call (gbrt_render_batch): aggregate
-    paths/s and per-image time over the seeded 64-scene batch. A step is the
-    whole batch; value = paths / device span of the batch (films resident),
-    e2e = paths / host wall time of the call (films copied to host memory)."""
+    """Many independent images in one call: aggregate paths/s and per-image
+    time over the seeded 64-scene batch. A step is the whole batch; value =
+    paths / device span of the batch (films resident), e2e = paths / host wall
+    time of the call (films copied to host memory). Default scheduler:
+    per-image wavefronts on concurrent streams (gbrt_render_batch); with
+    --single-launch the line reports the shared-wavefront, graph-replayed
+    batch (gbrt_render_batch_fused) and the stream scheduler beside it."""
     import concurrent.futures as cf
     import multiprocessing as mp
 
     import numpy as np
 
     from renderer_gb300 import _abi
-    from renderer_gb300.batch import BatchJob, autotune, render_batch
+    from renderer_gb300.batch import BatchJob, autotune, autotune_fused, render_batch, render_batch_fused
     from renderer_gb300.runtime import Context, GpuScene
 
     t = time.perf_counter()
@@ -470,25 +563,25 @@ def run_batch(args):
     t = time.perf_counter()
     S, B = autotune(ctx, jobs) if not args.batch_streams else (args.batch_streams, args.batch_paths or (1 << 22))
     tune_s = time.perf_counter() - t
+    fused = None
+    if args.single_launch:
+        t = time.perf_counter()
+        fused = autotune_fused(ctx, jobs)
+        fused["autotune_s"] = time.perf_counter() - t
     for _ in range(args.warmup):
         render_batch(ctx, jobs)
+        if fused:
+            render_batch_fused(ctx, jobs)
     clocks = ClockSampler(0)
     clocks.start()
     time.sleep(0.3)
-    dev_ms, wall_ms, paths, ext, sh, launches = 0.0, 0.0, 0, 0, 0, 0
-    per_image = []
-    for _ in range(args.steps):
-        t = time.perf_counter()
-        films, job_ms, st = render_batch(ctx, jobs)
-        wall_ms += 1000 * (time.perf_counter() - t)
-        dev_ms += st.device_ms
-        paths += st.paths
-        ext += st.extension_rays
-        sh += st.shadow_rays
-        launches += st.kernel_launches
-        per_image.append(job_ms)
+    streams_run = _time_batch(lambda j: render_batch(ctx, j), jobs, args.steps)
+    fused_run = _time_batch(lambda j: render_batch_fused(ctx, j), jobs, args.steps) if fused else None
     clk = clocks.stop()
-    per_image = np.mean(per_image, 0)
+    run = fused_run if fused else streams_run
+    dev_ms, wall_ms, paths, ext, sh, launches = (run[k] for k in ("dev_ms", "wall_ms", "paths", "ext", "sh",
+                                                                  "launches"))
+    per_image = run["per_image"]
     tri = [s.n_tri() for s, _ in scenes]
     spp = [p.x_samples * p.y_samples for _, p in scenes]
     res = [s.camera["width"] for s, _ in scenes]
@@ -510,10 +603,21 @@ def run_batch(args):
                                         "device_max": float(np.max(per_image)),
                                         "device_min": float(np.min(per_image))},
                        "extension_rays_per_path": ext / max(paths, 1), "shadow_rays_per_path": sh / max(paths, 1),
-                       "max_depth": depth},
+                       "max_depth": depth,
+                       "scheduler": "single launch (shared wavefronts, CUDA graph per wavefront)" if fused
+                       else "streams (one wavefront pipeline per image)"},
             "e2e": {"value": paths / (wall_ms / 1000.0), "unit": "paths/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk}
+    if fused:
+        def summary(r):
+            return {"paths_per_s": r["paths"] / (r["dev_ms"] / 1000.0),
+                    "e2e_paths_per_s": r["paths"] / (r["wall_ms"] / 1000.0),
+                    "ms_per_step": r["dev_ms"] / args.steps, "kernel_launches_per_step": r["launches"] // args.steps,
+                    "per_image_ms_median": float(np.median(r["per_image"])),
+                    "per_image_ms_max": float(np.max(r["per_image"]))}
+        line["config"]["designs"] = {"single_launch": dict(summary(fused_run), **fused),
+                                     "streams": dict(summary(streams_run), streams=S, batch_paths=B)}
     print(json.dumps(line))
 
 
@@ -785,7 +889,10 @@ def main():
     ap.add_argument("--batch", action="store_true",
                     help="aggregate paths/s of the seeded 64-scene batch through gbrt_render_batch")
     ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--cornell", action="store_true", help="throughput on the Cornell box (256x256, 16 spp, depth 8)")
     ap.add_argument("--batch-streams", type=int, default=0, help="streams for --batch (0: autotune)")
+    ap.add_argument("--single-launch", action="store_true",
+                    help="with --batch: the shared-wavefront batch under CUDA graphs, beside the stream scheduler")
     ap.add_argument("--instanced", action="store_true",
                     help="16 views of the instanced-terrain scene (two-level BVH) through gbrt_render_batch")
     ap.add_argument("--terrain-nx", type=int, default=2000, help="terrain quads along x (2000: 4M triangles)")
@@ -812,6 +919,9 @@ def main():
         return
     if args.instanced:
         run_instanced(args)
+        return
+    if args.cornell:
+        run_cornell(args)
         return
     if args.batch:
         run_batch(args)

@@ -504,6 +504,47 @@ gbrt_status gbrt_batch_autotune(gbrt_ctx* ctx, const gbrt_batch_job* jobs,
                                 int32_t n, int32_t* streams,
                                 int64_t* batch_paths);
 
+/* The single-launch batch (no counterpart in the renderer). The jobs' paths
+ * are numbered one after the other and every wavefront holds the paths of as
+ * many jobs as it covers, so that each launch of the extend, shade and shadow
+ * kernels serves several images and scenes at once (each slot records its
+ * job; the kernels read the job's scene and parameters from device tables).
+ * One wavefront (set-up, camera rays, max_depth x (extend, shade, shadow),
+ * accumulation) is captured as a CUDA graph and replayed until every path is
+ * done; `pipelines` such graphs run at once on streams of the context
+ * (pipeline k takes wavefronts k, k + pipelines, ...), so that one
+ * wavefront's last, nearly empty bounces overlap another's first ones. Jobs
+ * are numbered smallest first (pixels x spp x max_depth), so that small
+ * images finish in the first wavefronts. All
+ * jobs share one estimator (params.semantics) and one triangle test
+ * (GBRT_SCENE_WATERTIGHT); at most 65,535 jobs; params.batch_paths is
+ * ignored. Every path draws the numbers it draws in gbrt_render, so a job's
+ * film equals its gbrt_render film up to the summation order of the FP64
+ * pixel sums. */
+typedef struct gbrt_batch_schedule {
+  int64_t wavefront_paths;  /* paths per wavefront */
+  int32_t pipelines;        /* wavefront pipelines in flight at once, 1..8 */
+  int32_t trace_block;      /* threads per block of extend and shadow: 64 or 128 */
+  int32_t shade_block;      /* threads per block of shade: 128 or 256 */
+  int32_t pad;
+} gbrt_batch_schedule;
+/* schedule NULL, or a field 0: the value gbrt_batch_autotune_fused chose on
+ * this context (2^24 paths, 2 pipelines, 128 and 256 threads before any
+ * tuning). job_ms (optional): per job, device time from the batch's start to
+ * the end of the wavefront that finishes it. stats->streams is the number of
+ * pipelines; kernel_launches counts the kernels of the replayed graphs and
+ * the final film kernel. */
+gbrt_status gbrt_render_batch_fused(gbrt_ctx* ctx, const gbrt_batch_job* jobs,
+                                    int32_t n,
+                                    const gbrt_batch_schedule* schedule,
+                                    double* job_ms, gbrt_batch_stats* stats);
+/* Renders every job at up to 2 x 2 samples per pixel for wavefronts of 2^20, 2^22 and
+ * 2^24 paths, 1, 2 and 4 pipelines (at most 2^25 paths in flight) and each
+ * pair of tile sizes, keeps the fastest schedule (device time) on the context
+ * and returns it. Films are not written. */
+gbrt_status gbrt_batch_autotune_fused(gbrt_ctx* ctx, const gbrt_batch_job* jobs,
+                                      int32_t n, gbrt_batch_schedule* schedule);
+
 /* ---- neural path guiding. No counterpart in the renderer, whose
  *      integrators sample the BSDF only (src/unidipathtracingintegrator.cpp:
  *      34-46); used with the physical estimator. ---------------------------

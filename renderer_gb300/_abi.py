@@ -97,6 +97,11 @@ class BatchJob(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("params", RenderParams), ("film", C.c_void_p)]
 
 
+class BatchSchedule(C.Structure):
+    _fields_ = [("wavefront_paths", C.c_int64), ("pipelines", C.c_int32), ("trace_block", C.c_int32),
+                ("shade_block", C.c_int32), ("pad", C.c_int32)]
+
+
 class BatchStats(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("nonfinite", C.c_uint64), ("wall_ms", C.c_double), ("streams", C.c_int32), ("pad", C.c_int32),
@@ -199,6 +204,9 @@ SIGNATURES = [
                                     C.POINTER(C.c_double), C.POINTER(BatchStats)]),
     ("gbrt_batch_autotune", C.c_int, [P, C.POINTER(BatchJob), C.c_int32, C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int64)]),
+    ("gbrt_render_batch_fused", C.c_int, [P, C.POINTER(BatchJob), C.c_int32, C.POINTER(BatchSchedule),
+                                          C.POINTER(C.c_double), C.POINTER(BatchStats)]),
+    ("gbrt_batch_autotune_fused", C.c_int, [P, C.POINTER(BatchJob), C.c_int32, C.POINTER(BatchSchedule)]),
     ("gbrt_ctx_trim", C.c_int, [P, C.POINTER(C.c_uint64)]),
     ("gbrt_debug_fault", C.c_int, [P, C.c_int32, C.c_int64]),
     ("gbrt_render_mlt", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), C.POINTER(MltParams), P,

@@ -27,6 +27,8 @@ struct gbrt_ctx {
   std::vector<cudaStream_t> batch_streams;
   int batch_streams_tuned = 4;
   long long batch_paths_tuned = 1ll << 22;
+  // Tuned schedule of gbrt_render_batch_fused.
+  gbrt_batch_schedule fused_tuned{1ll << 24, 2, 128, 256, 0};
   // Device address of the no-allocation entry point's file-scope scratch
   // array, looked up by the first gbrt_render_device_noalloc call on this
   // context (with its device current).

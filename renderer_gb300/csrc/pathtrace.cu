@@ -138,6 +138,45 @@ constexpr int kRecords = 4;
 constexpr int kRecComp = 6;
 constexpr int kRecOpen = 0x100;
 
+// Many images in one wavefront (gbrt_render_batch_fused). The jobs' paths
+// are numbered one after the other (job j owns global path indices
+// [start_j, start_j + total_j)); a wavefront holds global paths [G0, G0 + nb)
+// of any number of jobs, and every slot records its job. A job's parameters
+// carry g0 = G0 - start_j (mod 2^64), rewritten per wavefront, so that
+// g0 + slot is the path's index within its own image, as in a single render.
+struct BatchJob {
+  PTParams P;
+  unsigned long long start, total;  // the job's global path range
+  unsigned long long pix0;          // its first pixel in the batch's film and sums
+  unsigned long long wlane;         // accumulation lanes of the jobs before it in this wavefront (prefix)
+  unsigned long long wnp;           // its pixels in this wavefront
+  int group;                        // lanes per pixel in the accumulation: spp rounded up to 2^k, at most 32
+};
+struct BatchDev {
+  const DeviceScene* scenes;        // per job
+  BatchJob* jobs;
+  const unsigned long long* starts; // per job, start (for the search by path index)
+  unsigned short* job_of;           // per slot
+  unsigned long long* cursor;       // [0] G0, [1] nb, [2] all paths, [3] accumulation lanes of the wavefront
+  double* sum;                      // FP64 sums of all jobs' pixels
+  float* film;                      // films of all jobs
+  unsigned long long stride;        // global paths between this pipeline's wavefronts
+  int n_jobs;
+  int B;                            // wavefront capacity
+  int shared_sum;                   // several pipelines add into the sums: atomics
+};
+
+// The job of global path index g: the last job starting at or before g.
+__device__ __forceinline__ int batch_job_of(const BatchDev& bt, unsigned long long g) {
+  int lo = 0, hi = bt.n_jobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(bt.starts + mid) <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // ------------------------------------------------------------- raygen ----
 // Path length: min(3 + Geometric(p), D) (src/renderer.cpp:52-61), from the
 // uniform ul; D when p is 0.
@@ -182,13 +221,8 @@ __device__ __forceinline__ void camera_dir(const PTParams& P, float sxp, float s
   dz = x * P.cam.u[2] + y * P.cam.v[2] - P.cam.w[2];
 }
 
-__global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
-  int slot = blockIdx.x * blockDim.x + threadIdx.x;
-  if (slot == 0) {
-    st.counts[0] = P.nb;
-    st.work[0] = 0;  // work counter of the first extend
-  }
-  if (slot >= P.nb) return;
+// The camera ray of the path in slot (path index P.g0 + slot of its image).
+__device__ __forceinline__ void raygen_slot(const PTParams& P, const PTState& st, int slot) {
   unsigned long long g = P.g0 + (unsigned long long)slot;
   int pixel, s;
   if (P.idx32) {
@@ -209,6 +243,16 @@ __global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
   // The physical estimator plays Russian roulette per vertex instead.
   const int plen = P.physical ? P.D : ref_path_length(P, stream_u(key, 2));
   start_path(P, st, slot, plen, dx, dy, dz);
+}
+
+__global__ void __launch_bounds__(256) k_raygen(PTParams P, PTState st) {
+  int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot == 0) {
+    st.counts[0] = P.nb;
+    st.work[0] = 0;  // work counter of the first extend
+  }
+  if (slot >= P.nb) return;
+  raygen_slot(P, st, slot);
 }
 
 // Adds a warp's traversal counters to two global totals (all lanes call it).
@@ -232,8 +276,9 @@ __device__ __forceinline__ void warp_add_counters(TraceCounters c, unsigned long
 // counts[0] and zeroes work[0]; k_extend on queue cur zeroes, before shade and
 // shadow run, counts[cur^1] (next extension queue), counts[2] (shadow queue),
 // work[cur^1] (next extend) and work[2] (this iteration's shadow pass).
-template <bool COUNT, bool WT, int STACK, bool GEN>
-__global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState st, int cur) {
+// MS: the scene of each ray is its job's (gbrt_render_batch_fused).
+template <bool COUNT, bool WT, int STACK, bool GEN, bool MS>
+__device__ __forceinline__ void extend_body(const DeviceScene& S, const PTState& st, int cur, const BatchDev& bt) {
   const int n = st.counts[cur];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st.tally[0] += (unsigned long long)n;
@@ -256,15 +301,32 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState s
     TRay r = make_tray(rays[2 * i], rays[2 * i + 1]);
     RawHit h;
     int32_t inst = -1;
-    h.rec = trace_ray<false, COUNT, WT, STACK, GEN>(S, r, -1, h.t, h.u, h.v, st.err, &cnt, &inst);
-    st.hits[i] = h;
-    if (GEN && S.inst) st.hit_inst[i] = inst;
+    if (MS) {
+      const DeviceScene& Sj = bt.scenes[bt.job_of[st.ext_slot[cur][i]]];
+      h.rec = trace_ray<false, COUNT, WT, STACK, GEN>(Sj, r, -1, h.t, h.u, h.v, st.err, &cnt, &inst);
+      st.hits[i] = h;
+      if (GEN && st.hit_inst) st.hit_inst[i] = inst;
+    } else {
+      h.rec = trace_ray<false, COUNT, WT, STACK, GEN>(S, r, -1, h.t, h.u, h.v, st.err, &cnt, &inst);
+      st.hits[i] = h;
+      if (GEN && S.inst) st.hit_inst[i] = inst;
+    }
   }
   if (COUNT) warp_add_counters(cnt, &st.tally[3], &st.tally[4]);
 }
 
 template <bool COUNT, bool WT, int STACK, bool GEN>
-__global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState st) {
+__global__ void __launch_bounds__(kTraceBlock) k_extend(DeviceScene S, PTState st, int cur) {
+  extend_body<COUNT, WT, STACK, GEN, false>(S, st, cur, BatchDev{});
+}
+
+template <bool WT, int STACK, bool GEN>
+__global__ void __launch_bounds__(kTraceBlock) k_extend_ms(PTState st, int cur, BatchDev bt) {
+  extend_body<false, WT, STACK, GEN, true>(bt.scenes[0], st, cur, bt);
+}
+
+template <bool COUNT, bool WT, int STACK, bool GEN, bool MS>
+__device__ __forceinline__ void shadow_body(const DeviceScene& S, const PTState& st, const BatchDev& bt) {
   const int n = st.counts[2];
   if (blockIdx.x == 0 && threadIdx.x == 0) st.tally[1] += (unsigned long long)n;
   unsigned long long* work = st.work + 2;
@@ -280,15 +342,32 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState s
     float4 c = st.sh_c[i];
     TRay r = make_tray(st.sh_ray[2 * i], st.sh_ray[2 * i + 1]);
     float t, u, v;
-    int32_t rec = trace_ray<true, COUNT, WT, STACK, GEN>(S, r, __float_as_int(c.w), t, u, v, st.err, &cnt);
+    const int slot = st.sh_slot[i];
+    int32_t rec;
+    if (MS) {
+      const DeviceScene& Sj = bt.scenes[bt.job_of[slot]];
+      rec = trace_ray<true, COUNT, WT, STACK, GEN>(Sj, r, __float_as_int(c.w), t, u, v, st.err, &cnt);
+    } else {
+      rec = trace_ray<true, COUNT, WT, STACK, GEN>(S, r, __float_as_int(c.w), t, u, v, st.err, &cnt);
+    }
     if (rec == -1) {
-      float4* L = st.L + st.sh_slot[i];
+      float4* L = st.L + slot;
       atomicAdd(&L->x, c.x);
       atomicAdd(&L->y, c.y);
       atomicAdd(&L->z, c.z);
     }
   }
   if (COUNT) warp_add_counters(cnt, &st.tally[5], &st.tally[6]);
+}
+
+template <bool COUNT, bool WT, int STACK, bool GEN>
+__global__ void __launch_bounds__(kTraceBlock) k_shadow(DeviceScene S, PTState st) {
+  shadow_body<COUNT, WT, STACK, GEN, false>(S, st, BatchDev{});
+}
+
+template <bool WT, int STACK, bool GEN>
+__global__ void __launch_bounds__(kTraceBlock) k_shadow_ms(PTState st, BatchDev bt) {
+  shadow_body<false, WT, STACK, GEN, true>(bt.scenes[0], st, bt);
 }
 
 // A persistent grid no larger than a wavefront of `items` needs (each warp
@@ -390,12 +469,16 @@ __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, con
 // Renderer::createPath (src/renderer.cpp:73-104) for one iteration, with the
 // stored-vertex bookkeeping of UniDiPathTracingIntegrator::integrate(path)
 // done in streaming form (see the file comment).
-template <bool EXT, class R>
-__global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTState st, int cur) {
+template <bool EXT, class R, bool MS>
+__device__ __forceinline__ void shade_body(const DeviceScene& S0, const PTParams& P0, const PTState& st, int cur,
+                                           const BatchDev& bt) {
   const int n = st.counts[cur];
   const int nxt = cur ^ 1;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int slot = st.ext_slot[cur][q];
+    const int job = MS ? int(bt.job_of[slot]) : 0;
+    const DeviceScene& S = MS ? bt.scenes[job] : S0;
+    const PTParams& P = MS ? bt.jobs[job].P : P0;
     const RawHit h = st.hits[q];
     const float4 ro = st.ext[cur][2 * q], rd = st.ext[cur][2 * q + 1];
     int4 c = st.ctl[slot];
@@ -544,6 +627,16 @@ __global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTS
   }
 }
 
+template <bool EXT, class R>
+__global__ void __launch_bounds__(256, 4) k_shade(DeviceScene S, PTParams P, PTState st, int cur) {
+  shade_body<EXT, R, false>(S, P, st, cur, BatchDev{});
+}
+
+template <bool EXT>
+__global__ void __launch_bounds__(256, 4) k_shade_ms(PTState st, int cur, BatchDev bt) {
+  shade_body<EXT, StreamSrc, true>(bt.scenes[0], bt.jobs[0].P, st, cur, bt);
+}
+
 // ------------------------------------------------------ shade, physical ----
 // GBRT_SEM_PHYSICAL: next-event estimation with one uniformly chosen light
 // (weighted by the light count), emission on BSDF-sampled hits, both combined
@@ -657,13 +750,18 @@ __device__ __forceinline__ void surface_normal(const DeviceScene& S, const RawHi
   }
 }
 
-template <bool GUIDED, bool EXT>
-__global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P, PTState st, int cur) {
+template <bool GUIDED, bool EXT, bool MS>
+__device__ __forceinline__ void shade_phys_body(const DeviceScene& S0, const PTParams& P0, const PTState& st,
+                                                int cur, const BatchDev& bt) {
   const int n = st.counts[cur];
   const int nxt = cur ^ 1;
-  const float pChoose = S.n_lights > 0 ? 1.f / float(S.n_lights) : 0.f;
+  const float pChoose0 = MS ? 0.f : (S0.n_lights > 0 ? 1.f / float(S0.n_lights) : 0.f);
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int slot = st.ext_slot[cur][q];
+    const int job = MS ? int(bt.job_of[slot]) : 0;
+    const DeviceScene& S = MS ? bt.scenes[job] : S0;
+    const PTParams& P = MS ? bt.jobs[job].P : P0;
+    const float pChoose = MS ? (S.n_lights > 0 ? 1.f / float(S.n_lights) : 0.f) : pChoose0;
     const RawHit h = st.hits[q];
     const float4 ro = st.ext[cur][2 * q], rd = st.ext[cur][2 * q + 1];
     int4 c = st.ctl[slot];
@@ -771,6 +869,16 @@ __global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P
     st.ctl[slot] = make_int4(i + 1, c.y, z, spec ? 1 : 0);
     push_ext(st, nxt, slot, x, wi);
   }
+}
+
+template <bool GUIDED, bool EXT>
+__global__ void __launch_bounds__(256, 4) k_shade_phys(DeviceScene S, PTParams P, PTState st, int cur) {
+  shade_phys_body<GUIDED, EXT, false>(S, P, st, cur, BatchDev{});
+}
+
+template <bool EXT>
+__global__ void __launch_bounds__(256, 4) k_shade_phys_ms(PTState st, int cur, BatchDev bt) {
+  shade_phys_body<false, EXT, true>(bt.scenes[0], bt.jobs[0].P, st, cur, bt);
 }
 
 // ------------------------------------------------------------ guiding ----
@@ -935,6 +1043,137 @@ static void launch_accumulate(const PTParams& P, const PTState& st, double* sum,
 __global__ void k_finalize(const double* sum, float* film, size_t n3, double inv_spp) {
   size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < n3) film[i] = float(sum[i] * inv_spp);
+}
+
+// ---------------------------------------------------- many-image batch ----
+// Start of a wavefront of the fused batch (one block of 1024 threads): nb,
+// every job's g0 for this wavefront, and the accumulation's thread map: job j
+// gets its pixels in the wavefront x group_j lanes, rounded up to whole warps
+// (so that a warp never mixes jobs), as an exclusive prefix.
+__global__ void __launch_bounds__(1024) k_batch_begin(BatchDev bt, PTState st) {
+  __shared__ unsigned long long part[1024];
+  const unsigned long long G0 = bt.cursor[0], all = bt.cursor[2];
+  const unsigned long long nb = G0 < all ? min((unsigned long long)bt.B, all - G0) : 0ull;
+  const unsigned long long G1 = G0 + nb;
+  const int J = bt.n_jobs, per = (J + 1023) / 1024;
+  unsigned long long local = 0;
+  for (int k = 0; k < per; ++k) {
+    const int j = int(threadIdx.x) * per + k;
+    if (j >= J) break;
+    BatchJob& b = bt.jobs[j];
+    b.P.g0 = G0 - b.start;
+    b.P.nb = int(nb);
+    const unsigned long long a = max(G0, b.start), e = min(G1, b.start + b.total);
+    unsigned long long np = 0;
+    if (a < e) {
+      const unsigned long long spp = unsigned(b.P.spp);
+      np = (e - 1 - b.start) / spp - (a - b.start) / spp + 1;
+    }
+    b.wnp = np;
+    const unsigned long long lanes = (np * unsigned(b.group) + 31) & ~31ull;
+    b.wlane = lanes;
+    local += lanes;
+  }
+  part[threadIdx.x] = local;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const unsigned long long v = int(threadIdx.x) >= off ? part[threadIdx.x - off] : 0ull;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  unsigned long long run = part[threadIdx.x] - local;
+  for (int k = 0; k < per; ++k) {
+    const int j = int(threadIdx.x) * per + k;
+    if (j >= J) break;
+    const unsigned long long lanes = bt.jobs[j].wlane;
+    bt.jobs[j].wlane = run;
+    run += lanes;
+  }
+  if (threadIdx.x == 1023) bt.cursor[3] = part[1023];
+  if (threadIdx.x == 0) {
+    bt.cursor[1] = nb;
+    st.counts[0] = int(nb);
+    st.work[0] = 0;  // work counter of the first extend
+  }
+}
+
+// Camera rays of the wavefront: each slot finds its job and starts the path
+// exactly as a single render of that job would.
+__global__ void __launch_bounds__(256) k_raygen_ms(PTState st, BatchDev bt) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((unsigned long long)slot >= bt.cursor[1]) return;
+  const int j = batch_job_of(bt, bt.cursor[0] + (unsigned long long)slot);
+  bt.job_of[slot] = (unsigned short)j;
+  raygen_slot(bt.jobs[j].P, st, slot);
+}
+
+// Per-pixel FP64 sums of the wavefront: a group of lanes per pixel (the
+// job's group size, a power of two up to 32, all within one warp) takes
+// every group-th sample of the pixel's samples in the wavefront, and the
+// group adds its partial sums by shuffles.
+__global__ void __launch_bounds__(256) k_accumulate_ms(PTState st, BatchDev bt) {
+  const unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= bt.cursor[3]) return;  // whole warps: the lane count is a multiple of 32
+  int lo = 0, hi = bt.n_jobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (bt.jobs[mid].wlane <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  const BatchJob& b = bt.jobs[lo];
+  const int G = b.group;  // uniform over the warp
+  const unsigned long long l = t - b.wlane, px = l / unsigned(G);
+  const int sub = int(l % unsigned(G));
+  const bool live = px < b.wnp;
+  const unsigned long long G0 = bt.cursor[0], G1 = G0 + bt.cursor[1];
+  const unsigned long long spp = unsigned(b.P.spp);
+  const unsigned long long a = max(G0, b.start) - b.start, e = min(G1, b.start + b.total) - b.start;
+  const unsigned long long p = a / spp + px;
+  double s0 = 0, s1 = 0, s2 = 0;
+  unsigned long long bad = 0;
+  if (live) {
+    const unsigned long long gb = max(a, p * spp), ge = min(e, (p + 1) * spp);
+    for (unsigned long long g = gb + unsigned(sub); g < ge; g += unsigned(G)) {
+      float4 L = st.L[b.start + g - G0];
+      if (b.P.nan_every && g % b.P.nan_every == 0) L.x = CUDART_NAN_F;
+      if (!isfinite(L.x) || !isfinite(L.y) || !isfinite(L.z)) { ++bad; continue; }
+      s0 += L.x; s1 += L.y; s2 += L.z;
+    }
+  }
+  for (int o = G >> 1; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o, G);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o, G);
+    s2 += __shfl_down_sync(0xffffffffu, s2, o, G);
+    bad += __shfl_down_sync(0xffffffffu, bad, o, G);
+  }
+  if (live && sub == 0) {
+    if (bad) atomicAdd(&st.tally[2], bad);
+    double* o = bt.sum + 3 * (b.pix0 + p);
+    if (bt.shared_sum) {  // a pixel's samples can lie in two pipelines' wavefronts
+      atomicAdd(o, s0); atomicAdd(o + 1, s1); atomicAdd(o + 2, s2);
+    } else {
+      o[0] += s0; o[1] += s1; o[2] += s2;
+    }
+  }
+}
+
+__global__ void k_batch_end(BatchDev bt) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) bt.cursor[0] += bt.stride;
+}
+
+// Films of all jobs from their sums (1 / spp of each job).
+__global__ void k_finalize_ms(BatchDev bt, unsigned long long n3) {
+  const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  const unsigned long long pix = i / 3;
+  int lo = 0, hi = bt.n_jobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (bt.jobs[mid].pix0 <= pix) lo = mid;
+    else hi = mid - 1;
+  }
+  bt.film[i] = float(bt.sum[i] * (1.0 / double(bt.jobs[lo].P.spp)));
 }
 
 // ------------------------------------------------------------- driver ----
@@ -1875,6 +2114,281 @@ static gbrt_status batch_impl(gbrt_ctx* ctx, const gbrt_batch_job* jobs, int n, 
   return status;
 }
 
+// The fused batch's kernels for the jobs' scenes: the general leaves if any
+// scene needs them, the short stack only if every tree is shallow enough.
+struct FusedKernels {
+  void (*ext)(PTState, int, BatchDev);
+  void (*sh)(PTState, BatchDev);
+  void (*shade)(PTState, int, BatchDev);
+};
+template <bool W, int K, bool G>
+static FusedKernels fused_trace(bool physical, bool ext) {
+  FusedKernels f{k_extend_ms<W, K, G>, k_shadow_ms<W, K, G>, nullptr};
+  if (physical) f.shade = ext ? k_shade_phys_ms<true> : k_shade_phys_ms<false>;
+  else f.shade = ext ? k_shade_ms<true> : k_shade_ms<false>;
+  return f;
+}
+template <bool W>
+static FusedKernels fused_pick(bool shortStack, bool gen, bool physical, bool ext) {
+  if (gen) return shortStack ? fused_trace<W, kShortStack, true>(physical, ext) : fused_trace<W, kStackSize, true>(physical, ext);
+  return shortStack ? fused_trace<W, kShortStack, false>(physical, ext) : fused_trace<W, kStackSize, false>(physical, ext);
+}
+
+// gbrt_render_batch_fused: all jobs' paths in one numbering, wavefronts of B
+// paths across jobs. P pipelines (each its own path state, job table copy,
+// stream and graph) take wavefronts k, k + P, k + 2P, ...: while one
+// pipeline's wavefront runs its last, nearly empty bounces, another's runs
+// its full first ones.
+struct FusedPipe {
+  PTState st{};
+  BatchDev bt{};
+  BatchJob* jobs = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+static gbrt_status batch_fused_impl(gbrt_ctx* ctx, const gbrt_batch_job* jobs, int n, const gbrt_batch_schedule& sc,
+                                    bool copy_out, double* job_ms, gbrt_batch_stats* stats) {
+  GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  const auto t0 = std::chrono::steady_clock::now();
+  const int traceBlock = sc.trace_block, shadeBlock = sc.shade_block, P = sc.pipelines;
+  long long B = sc.wavefront_paths;
+  if (n > 65535) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch_fused: more than 65,535 jobs");
+  if (traceBlock != 64 && traceBlock != 128) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch_fused: trace block");
+  if (shadeBlock != 128 && shadeBlock != 256) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch_fused: shade block");
+  if (P < 1 || P > 8) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch_fused: pipelines outside 1..8");
+  if (B < 1) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch_fused: wavefront size");
+  const bool physical = jobs[0].params.semantics == GBRT_SEM_PHYSICAL;
+  const bool wt = jobs[0].scene->watertight;
+  bool gen = false, ext = false, shortStack = true, anyInst = false;
+  int D = 0;
+  unsigned long long total = 0, pixels = 0;
+  // The jobs are numbered smallest first (paths x depth), so that small
+  // images finish in the first wavefronts; pos[j] is job j's place.
+  std::vector<int> ord(static_cast<size_t>(n)), pos(static_cast<size_t>(n));
+  std::vector<double> cost(static_cast<size_t>(n));
+  for (int j = 0; j < n; ++j) {
+    ord[j] = j;
+    const gbrt_render_params& pj = jobs[j].params;
+    cost[j] = double(jobs[j].camera.width) * jobs[j].camera.height * pj.x_samples * pj.y_samples * pj.max_depth;
+  }
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return cost[a] < cost[b]; });
+  for (int k = 0; k < n; ++k) pos[ord[k]] = k;
+  std::vector<BatchJob> hj(static_cast<size_t>(n));
+  std::vector<DeviceScene> hs(static_cast<size_t>(n));
+  std::vector<unsigned long long> starts(static_cast<size_t>(n));
+  for (int k = 0; k < n; ++k) {
+    const int j = ord[k];
+    const gbrt_batch_job& jb = jobs[j];
+    const gbrt_scene* scn = jb.scene;
+    if ((jb.params.semantics == GBRT_SEM_PHYSICAL) != physical || scn->watertight != wt)
+      return fail(ctx, GBRT_ERR_INVALID_ARG,
+                  "gbrt_render_batch_fused: every job needs the same estimator and the same triangle test");
+    gen = gen || scn->view.csg_prog || scn->view.inst;
+    anyInst = anyInst || scn->view.inst;
+    ext = ext || ext_scene(scn);
+    shortStack = shortStack && stack_need(scn->max_depth4) <= kShortStack;
+    D = std::max(D, jb.params.max_depth);
+    const unsigned long long np = (unsigned long long)jb.camera.width * jb.camera.height;
+    const unsigned long long tj = np * (unsigned long long)(jb.params.x_samples * jb.params.y_samples);
+    BatchJob& b = hj[k];
+    std::memset(&b, 0, sizeof b);
+    init_params(b.P, ctx, jb.camera, jb.params, tj);
+    b.start = total;
+    b.total = tj;
+    b.pix0 = pixels;
+    b.group = 1;
+    while (b.group < 32 && b.group < b.P.spp) b.group <<= 1;
+    starts[k] = total;
+    hs[k] = scn->view;
+    total += tj;
+    pixels += np;
+  }
+  B = std::min<long long>(B, (long long)total);
+  if (B > (1ll << 30)) B = 1ll << 30;
+  const unsigned long long waves = (total + (unsigned long long)B - 1) / (unsigned long long)B;
+  const int nP = int(std::min<unsigned long long>((unsigned long long)P, waves));
+  while (int(ctx->batch_streams.size()) < nP) {
+    cudaStream_t q;
+    GBRT_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+    ctx->batch_streams.push_back(q);
+  }
+  cudaStream_t stream = ctx->stream;
+  Buffers buf(ctx, stream);
+  cudaError_t e = cudaSuccess;
+  auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
+  DeviceScene* d_scenes = nullptr;
+  unsigned long long* d_starts = nullptr;
+  double* d_sum = nullptr;
+  float* d_film = nullptr;
+  A(buf.alloc(&d_scenes, size_t(n))); A(buf.alloc(&d_starts, size_t(n)));
+  A(buf.alloc(&d_sum, size_t(pixels) * 3)); A(buf.alloc(&d_film, size_t(pixels) * 3));
+  std::vector<FusedPipe> pipes(static_cast<size_t>(nP));
+  for (int k = 0; k < nP && e == cudaSuccess; ++k) {
+    PTState& st = pipes[k].st;
+    A(buf.alloc(&st.alpha, B)); A(buf.alloc(&st.L, B)); A(buf.alloc(&st.ctl, B));
+    A(buf.alloc(&st.pv_p, B)); A(buf.alloc(&st.pv_n, B)); A(buf.alloc(&st.pv_d, B)); A(buf.alloc(&st.pv_a, B));
+    A(buf.alloc(&st.ext[0], 2 * B)); A(buf.alloc(&st.ext[1], 2 * B));
+    A(buf.alloc(&st.ext_slot[0], B)); A(buf.alloc(&st.ext_slot[1], B));
+    A(buf.alloc(&st.hits, B));
+    if (anyInst) A(buf.alloc(&st.hit_inst, B));
+    A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
+    A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
+    BatchDev& bt = pipes[k].bt;
+    A(buf.alloc(&pipes[k].jobs, size_t(n)));
+    A(buf.alloc(&bt.job_of, size_t(B))); A(buf.alloc(&bt.cursor, 4));
+    bt.scenes = d_scenes;
+    bt.jobs = pipes[k].jobs;
+    bt.starts = d_starts;
+    bt.sum = d_sum;
+    bt.film = d_film;
+    bt.stride = (unsigned long long)nP * (unsigned long long)B;
+    bt.n_jobs = n;
+    bt.B = int(B);
+    bt.shared_sum = nP > 1 ? 1 : 0;
+  }
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gbrt_render_batch_fused buffers");
+  std::vector<unsigned long long> cur0(4 * size_t(nP));
+  for (int k = 0; k < nP; ++k) {
+    cur0[4 * k] = (unsigned long long)k * (unsigned long long)B;
+    cur0[4 * k + 1] = 0;
+    cur0[4 * k + 2] = total;
+    cur0[4 * k + 3] = 0;
+  }
+  A(cudaMemcpyAsync(d_scenes, hs.data(), hs.size() * sizeof(DeviceScene), cudaMemcpyHostToDevice, stream));
+  A(cudaMemcpyAsync(d_starts, starts.data(), starts.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                    stream));
+  A(cudaMemsetAsync(d_sum, 0, size_t(pixels) * 3 * sizeof(double), stream));
+  for (int k = 0; k < nP; ++k) {
+    A(cudaMemcpyAsync(pipes[k].jobs, hj.data(), hj.size() * sizeof(BatchJob), cudaMemcpyHostToDevice, stream));
+    A(cudaMemcpyAsync(pipes[k].bt.cursor, &cur0[4 * k], 4 * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                      stream));
+    A(cudaMemsetAsync(pipes[k].st.tally, 0, 8 * sizeof(unsigned long long), stream));
+    A(cudaMemsetAsync(pipes[k].st.err, 0, sizeof(int), stream));
+  }
+  // The host arrays must outlive the copies; the pipelines start after them.
+  A(cudaStreamSynchronize(stream));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gbrt_render_batch_fused set-up");
+
+  const FusedKernels fk = wt ? fused_pick<true>(shortStack, gen, physical, ext)
+                             : fused_pick<false>(shortStack, gen, physical, ext);
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fk.ext, traceBlock, 0);
+  const int traceGrid = std::max(1, per) * ctx->num_sms;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fk.sh, traceBlock, 0);
+  const int shadowGrid = std::max(1, per) * ctx->num_sms;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fk.shade, shadeBlock, 0);
+  const int shadeGrid = std::max(1, per) * ctx->num_sms;
+  // lanes of a job in a wavefront: (its paths / spp + 2 partial pixels) x
+  // group, group < 2 spp and <= 32, rounded up to a warp: at most 2 paths + 155
+  const unsigned long long lanes = 2ull * (unsigned long long)B + 160ull * (unsigned long long)n;
+  // One wavefront of one pipeline as a graph: grids sized for a full
+  // wavefront; the kernels read the wavefront's actual size from the device.
+  for (int k = 0; k < nP && e == cudaSuccess; ++k) {
+    cudaStream_t q = ctx->batch_streams[k];
+    const PTState& st = pipes[k].st;
+    const BatchDev& bt = pipes[k].bt;
+    A(cudaStreamBeginCapture(q, cudaStreamCaptureModeThreadLocal));
+    if (e != cudaSuccess) break;
+    k_batch_begin<<<1, 1024, 0, q>>>(bt, st);
+    k_raygen_ms<<<unsigned((B + 255) / 256), 256, 0, q>>>(st, bt);
+    for (int it = 0; it < D; ++it) {
+      const int cur = it & 1;
+      fk.ext<<<cap_grid(traceGrid, B, traceBlock), traceBlock, 0, q>>>(st, cur, bt);
+      fk.shade<<<cap_grid(shadeGrid, B, shadeBlock), shadeBlock, 0, q>>>(st, cur, bt);
+      fk.sh<<<cap_grid(shadowGrid, 2 * B, traceBlock), traceBlock, 0, q>>>(st, bt);
+    }
+    k_accumulate_ms<<<unsigned((lanes + 255) / 256), 256, 0, q>>>(st, bt);
+    k_batch_end<<<1, 32, 0, q>>>(bt);
+    cudaError_t ce = cudaStreamEndCapture(q, &pipes[k].graph);
+    A(cudaGetLastError());
+    A(ce);
+    if (e == cudaSuccess) A(cudaGraphInstantiate(&pipes[k].exec, pipes[k].graph, 0));
+  }
+  auto destroy_graphs = [&]() {
+    for (FusedPipe& fp : pipes) {
+      if (fp.exec) cudaGraphExecDestroy(fp.exec);
+      if (fp.graph) cudaGraphDestroy(fp.graph);
+    }
+  };
+  if (e != cudaSuccess) {
+    destroy_graphs();
+    return cuda_fail(ctx, e, "gbrt_render_batch_fused graph");
+  }
+  // Pipeline k runs wavefronts k, k + nP, ...; ev[w] is recorded on its
+  // stream after wavefront w.
+  std::vector<cudaEvent_t> ev(size_t(waves), nullptr);
+  for (auto& x : ev) cudaEventCreate(&x);
+  cudaEvent_t begin = nullptr, done = nullptr;
+  cudaEventCreate(&begin);
+  cudaEventCreate(&done);
+  cudaEventRecord(begin, stream);
+  for (int k = 0; k < nP; ++k) A(cudaStreamWaitEvent(ctx->batch_streams[k], begin, 0));
+  for (unsigned long long w = 0; w < waves && e == cudaSuccess; ++w) {
+    const int k = int(w % (unsigned long long)nP);
+    A(cudaGraphLaunch(pipes[k].exec, ctx->batch_streams[k]));
+    cudaEventRecord(ev[w], ctx->batch_streams[k]);
+  }
+  for (int k = 0; k < nP; ++k) A(cudaStreamWaitEvent(stream, ev[waves - 1 - (waves - 1 - k) % nP], 0));
+  cudaEventRecord(done, stream);
+  const unsigned long long n3 = pixels * 3;
+  k_finalize_ms<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(pipes[0].bt, n3);
+  A(cudaGetLastError());
+  std::vector<unsigned long long> tally(8 * size_t(nP), 0ull);
+  std::vector<int> err(size_t(nP), 0);
+  for (int k = 0; k < nP; ++k) {
+    A(cudaMemcpyAsync(&tally[8 * k], pipes[k].st.tally, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                      stream));
+    A(cudaMemcpyAsync(&err[k], pipes[k].st.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  }
+  if (copy_out) {
+    for (int j = 0; j < n && e == cudaSuccess; ++j) {
+      if (!jobs[j].film) continue;
+      const size_t np = size_t(jobs[j].camera.width) * jobs[j].camera.height;
+      A(cudaMemcpyAsync(jobs[j].film, d_film + 3 * hj[pos[j]].pix0, np * 3 * sizeof(float), cudaMemcpyDeviceToHost,
+                        stream));
+    }
+  }
+  A(cudaStreamSynchronize(stream));
+  double device_ms = 0.0;
+  if (e == cudaSuccess) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, begin, done);
+    device_ms = ms;
+    for (int j = 0; j < n && job_ms; ++j) {
+      // the wavefront that holds the job's last path
+      const BatchJob& b = hj[pos[j]];
+      const unsigned long long w = (b.start + b.total - 1) / (unsigned long long)B;
+      float t = 0.f;
+      cudaEventElapsedTime(&t, begin, ev[w]);
+      job_ms[j] = t;
+    }
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  cudaEventDestroy(begin);
+  cudaEventDestroy(done);
+  destroy_graphs();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gbrt_render_batch_fused");
+  int anyErr = 0;
+  for (int k = 0; k < nP; ++k) anyErr |= err[k];
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    stats->paths = total;
+    for (int k = 0; k < nP; ++k) {
+      stats->extension_rays += tally[8 * k];
+      stats->shadow_rays += tally[8 * k + 1];
+      stats->nonfinite += tally[8 * k + 2];
+    }
+    stats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    stats->streams = nP;
+    stats->batch_paths = B;
+    stats->device_ms = device_ms;
+    stats->kernel_launches = waves * (4ull + 3ull * unsigned(D)) + 1ull;
+  }
+  if (anyErr) return fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render_batch_fused: traversal stack overflow");
+  return GBRT_OK;
+}
+
 }  // namespace gbrt
 
 using namespace gbrt;
@@ -1993,6 +2507,79 @@ gbrt_status gbrt_batch_autotune(gbrt_ctx* ctx, const gbrt_batch_job* jobs, int32
   ctx->batch_paths_tuned = bestB;
   if (streams) *streams = bestS;
   if (batch_paths) *batch_paths = bestB;
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_render_batch_fused(gbrt_ctx* ctx, const gbrt_batch_job* jobs, int32_t n,
+                                    const gbrt_batch_schedule* schedule, double* job_ms, gbrt_batch_stats* stats) {
+  if (!ctx || (n > 0 && !jobs) || n < 0) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch_fused: bad argument");
+  clear_error(ctx);
+  for (int j = 0; j < n; ++j) {
+    gbrt_status st = check_job(ctx, jobs[j]);
+    if (st != GBRT_OK) return st;
+    if (!jobs[j].film) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch_fused: job without a film");
+  }
+  gbrt_batch_schedule sc = ctx->fused_tuned;
+  if (schedule) {
+    if (schedule->wavefront_paths < 0 || schedule->pipelines < 0 || schedule->trace_block < 0 ||
+        schedule->shade_block < 0)
+      return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_batch_fused: negative schedule value");
+    if (schedule->wavefront_paths > 0) sc.wavefront_paths = schedule->wavefront_paths;
+    if (schedule->pipelines > 0) sc.pipelines = schedule->pipelines;
+    if (schedule->trace_block > 0) sc.trace_block = schedule->trace_block;
+    if (schedule->shade_block > 0) sc.shade_block = schedule->shade_block;
+  }
+  if (n == 0) {
+    if (stats) {
+      std::memset(stats, 0, sizeof *stats);
+      stats->batch_paths = sc.wavefront_paths;
+      stats->streams = sc.pipelines;
+    }
+    return GBRT_OK;
+  }
+  return batch_fused_impl(ctx, jobs, n, sc, true, job_ms, stats);
+}
+
+gbrt_status gbrt_batch_autotune_fused(gbrt_ctx* ctx, const gbrt_batch_job* jobs, int32_t n,
+                                      gbrt_batch_schedule* out) {
+  if (!ctx || !jobs || n <= 0) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_batch_autotune_fused: bad argument");
+  clear_error(ctx);
+  // Every job at up to 2 x 2 samples per pixel: the mix of images a
+  // wavefront holds is what the schedule is tuned for.
+  std::vector<gbrt_batch_job> sample(jobs, jobs + n);
+  for (auto& j : sample) {
+    gbrt_status st = check_job(ctx, j);
+    if (st != GBRT_OK) return st;
+    j.params.x_samples = std::min(j.params.x_samples, 2);
+    j.params.y_samples = std::min(j.params.y_samples, 2);
+  }
+  double best = 0.0;
+  gbrt_batch_schedule bestS = ctx->fused_tuned;
+  for (long long B : {1ll << 20, 1ll << 22, 1ll << 24}) {
+    for (int P : {1, 2, 4}) {
+      if ((long long)P * B > (1ll << 25)) continue;  // at most 2^25 paths of state in flight
+      for (int tb : {64, 128}) {
+        for (int sb : {128, 256}) {
+          gbrt_batch_schedule sc{};
+          sc.wavefront_paths = B;
+          sc.pipelines = P;
+          sc.trace_block = tb;
+          sc.shade_block = sb;
+          gbrt_batch_stats st;
+          gbrt_status r = batch_fused_impl(ctx, sample.data(), n, sc, false, nullptr, &st);  // warm-up
+          if (r == GBRT_OK) r = batch_fused_impl(ctx, sample.data(), n, sc, false, nullptr, &st);
+          if (r != GBRT_OK) return r;
+          const double rate = double(st.paths) / std::max(st.device_ms, 1e-6);
+          if (rate > best) {
+            best = rate;
+            bestS = sc;
+          }
+        }
+      }
+    }
+  }
+  ctx->fused_tuned = bestS;
+  if (out) *out = bestS;
   return GBRT_OK;
 }
 

@@ -45,7 +45,7 @@ def test_struct_layout_matches_c(tmp_path):
                "gbrt_scene_desc", "gbrt_camera", "gbrt_render_params", "gbrt_stats", "gbrt_ray", "gbrt_hit",
                "gbrt_guide_params", "gbrt_guide_stats", "gbrt_texture", "gbrt_csg_node", "gbrt_batch_job",
                "gbrt_batch_stats", "gbrt_mlt_params", "gbrt_erpt_params", "gbrt_chain_stats",
-               "gbrt_mesh", "gbrt_instance"]
+               "gbrt_mesh", "gbrt_instance", "gbrt_batch_schedule"]
     src = tmp_path / "sz.c"
     src.write_text('#include <stdio.h>\n#include "gbrt.h"\nint main(void){\n' +
                    "".join('printf("%%zu\\n", sizeof(%s));\n' % s for s in structs) + "return 0;}\n")
@@ -55,7 +55,7 @@ def test_struct_layout_matches_c(tmp_path):
     mirror = [_abi.Material, _abi.Quad, _abi.Sphere, _abi.Plane, _abi.Light, _abi.EnvMap, _abi.SceneDesc,
               _abi.Camera, _abi.RenderParams, _abi.Stats, _abi.Ray, _abi.Hit, _abi.GuideParams, _abi.GuideStats,
               _abi.Texture, _abi.CsgNode, _abi.BatchJob, _abi.BatchStats,
-              _abi.MltParams, _abi.ErptParams, _abi.ChainStats, _abi.Mesh, _abi.Instance]
+              _abi.MltParams, _abi.ErptParams, _abi.ChainStats, _abi.Mesh, _abi.Instance, _abi.BatchSchedule]
     assert sizes == [ctypes.sizeof(m) for m in mirror]
     assert ctypes.sizeof(_abi.Ray) == 32 and ctypes.sizeof(_abi.Hit) == 16
 

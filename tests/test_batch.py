@@ -128,3 +128,100 @@ def test_bad_jobs_are_refused(ctx):
     # an empty batch is a no-op
     films, ms, st = render_batch(ctx, [])
     assert films == [] and st.paths == 0
+
+
+# ------------------------------------------------- single-launch batch ----
+def _alone(ctx, gss, scenes):
+    """Each job rendered by itself through gbrt_render with its own params."""
+    from renderer_gb300 import check, lib
+    out = []
+    for g, (s, p) in zip(gss, scenes):
+        film = np.zeros((s.camera["height"], s.camera["width"], 3), np.float32)
+        cam = s.camera_struct()
+        check(lib().gbrt_render(g.handle, C.byref(cam), C.byref(p), film.ctypes.data_as(C.c_void_p), None, None,
+                                None, None), ctx.handle)
+        out.append(film)
+    return out
+
+
+@pytest.mark.gpu
+def test_fused_batch_equals_individual_renders(ctx):
+    """Wavefronts that cut through jobs and through pixels (B = 2^14 and an
+    odd 10,007), and one wavefront for everything: every film equals the job
+    rendered alone, up to the order of the FP64 pixel sums and of a vertex's
+    shadow-ray additions."""
+    from renderer_gb300.batch import BatchJob, render_batch_fused
+    scenes = [shrunk(i, 48 + 16 * k, 2, 1 + k % 3) for k, i in enumerate(MIXED)]
+    gss = [GpuScene(ctx, s) for s, _ in scenes]
+    jobs = [BatchJob(g, s.camera_struct(), p) for g, (s, p) in zip(gss, scenes)]
+    alone = _alone(ctx, gss, scenes)
+    total = sum(s.camera["width"] ** 2 * p.x_samples * p.y_samples for s, p in scenes)
+    D = max(p.max_depth for _, p in scenes)
+    for B, P, tb, sb in ((1 << 14, 1, 128, 256), (10007, 3, 64, 128), (1 << 24, 2, 128, 128), (1 << 15, 4, 64, 256)):
+        films, ms, st = render_batch_fused(ctx, jobs, wavefront_paths=B, pipelines=P, trace_block=tb, shade_block=sb)
+        for f, a in zip(films, alone):
+            assert np.allclose(f, a, rtol=1e-5, atol=1e-7), np.abs(f - a).max()
+        waves = -(-total // min(B, total))
+        assert st.streams == min(P, waves) and st.batch_paths == min(B, total) and st.paths == total
+        assert st.kernel_launches == waves * (4 + 3 * D) + 1
+        assert st.extension_rays > st.paths and st.nonfinite == 0
+        # the last job ends with the last wavefront; the batch's span also
+        # takes the join of the pipelines' streams
+        assert (ms > 0).all() and 0.9 * st.device_ms <= ms.max() <= st.device_ms * 1.001 + 0.01
+
+
+@pytest.mark.gpu
+def test_fused_batch_physical_with_instances_and_textures(ctx):
+    """The general traversal (mesh instances) and the texture shading in one
+    batch with plain scenes, under the physical estimator."""
+    from renderer_gb300.batch import BatchJob, render_batch_fused
+    from tests.test_instances import instanced_cornell
+    from tests.test_texture import textured_room
+    si, _ = instanced_cornell(40, smooth=False)
+    st_ = textured_room()
+    st_.camera["width"] = st_.camera["height"] = 40
+    plain, _ = shrunk(9, 48, 1, 1)
+    prm = [render_params(2, 2, 0.5, 8, 21, semantics=_abi.SEM_PHYSICAL),
+           render_params(1, 2, 0.5, 6, 22, semantics=_abi.SEM_PHYSICAL),
+           render_params(2, 1, 0.5, 5, 23, semantics=_abi.SEM_PHYSICAL)]
+    scenes = list(zip((si, st_, plain), prm))
+    gss = [GpuScene(ctx, s) for s, _ in scenes]
+    jobs = [BatchJob(g, s.camera_struct(), p) for g, (s, p) in zip(gss, scenes)]
+    alone = _alone(ctx, gss, scenes)
+    films, _, st = render_batch_fused(ctx, jobs, wavefront_paths=5000, pipelines=2)
+    for f, a in zip(films, alone):
+        assert np.allclose(f, a, rtol=1e-5, atol=1e-7), np.abs(f - a).max()
+    # and against the oracle, path by path
+    for f, (s, p) in zip(films, scenes):
+        o = OracleScene(s).render(s.camera_struct(), p, rng_mode=1)["film"].astype(np.float64)
+        close = np.abs(f - o) <= 2e-3 * np.maximum(np.abs(o), 1e-3)
+        assert close.all(-1).mean() >= 0.95
+
+
+@pytest.mark.gpu
+def test_fused_autotune_and_refusals(ctx):
+    from renderer_gb300 import lib
+    from renderer_gb300.batch import BatchJob, _jobs_array, autotune_fused, render_batch_fused
+    scenes = [shrunk(i, 64, 1, 1) for i in SMALL]
+    gss = [GpuScene(ctx, s) for s, _ in scenes]
+    jobs = [BatchJob(g, s.camera_struct(), p) for g, (s, p) in zip(gss, scenes)]
+    c = autotune_fused(ctx, jobs)
+    assert c["wavefront_paths"] in (1 << 20, 1 << 22, 1 << 24) and c["pipelines"] in (1, 2, 4)
+    assert c["trace_block"] in (64, 128) and c["shade_block"] in (128, 256)
+    assert c["pipelines"] * c["wavefront_paths"] <= 1 << 25
+    _, _, st = render_batch_fused(ctx, jobs)
+    total = sum(s.camera["width"] ** 2 for s, _ in scenes)
+    assert st.batch_paths == min(c["wavefront_paths"], total)
+    # one estimator for all jobs
+    mixed = [jobs[0], BatchJob(gss[1], jobs[1].camera, render_params(1, 1, 0.5, 8, 0, semantics=_abi.SEM_PHYSICAL))]
+    with pytest.raises(GbrtError):
+        render_batch_fused(ctx, mixed)
+    with pytest.raises(GbrtError):
+        render_batch_fused(ctx, jobs, trace_block=96)
+    arr = _jobs_array(jobs[:1], None)  # no film
+    s = _abi.BatchStats()
+    assert lib().gbrt_render_batch_fused(ctx.handle, arr, 1, None, None, C.byref(s)) == _abi.ERR_INVALID_ARG
+    with pytest.raises(GbrtError):
+        render_batch_fused(ctx, jobs, pipelines=9)
+    films, ms, st = render_batch_fused(ctx, [])
+    assert films == [] and st.paths == 0
