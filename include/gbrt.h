@@ -452,6 +452,24 @@ gbrt_status gbrt_render_device_noalloc(gbrt_scene* scene,
                                        float* d_film_bgr, double* d_sum,
                                        double* d_sumsq, gbrt_stats* stats);
 
+/* Resumable accumulation in passes (a checkpoint of a long render, e.g. a
+ * 65,536-spp reference, is the FP64 sums plus the number of passes done; the
+ * renderer accumulates one image per process and has none). Renders passes
+ * first_pass .. first_pass + n_passes - 1, pass k with the seed derived from
+ * (params->seed, k) and params' samples per pixel, adding into d_sum (and
+ * d_sumsq when given), which are cleared first only when first_pass is 0;
+ * d_film (device, H x W x 3 BGR) gets the mean of all passes 0 ..
+ * first_pass + n_passes - 1. Rendering passes [0, a) and then, from the
+ * saved sums, [a, b) gives the sums and film of one call over [0, b): the
+ * same paths, the same per-pixel order of the FP64 additions, and only the
+ * order in which a vertex's shadow rays add into its path's radiance (float
+ * atomics) may differ. stats add up over the call's passes. Synchronous. */
+gbrt_status gbrt_render_passes(gbrt_scene* scene, const gbrt_camera* camera,
+                               const gbrt_render_params* params,
+                               int32_t first_pass, int32_t n_passes,
+                               float* d_film_bgr, double* d_sum,
+                               double* d_sumsq, gbrt_stats* stats);
+
 /* ---- output (Tonemapper::map, src/tonemapper.cpp:31-56; the --save-exr,
  *      --save-img and --save-mat writers, src/main.cpp:223-265) ---------- */
 /* rgb: width x height x 3 bytes, RGB order: clamp(255 * c^(1/gamma)) per
@@ -570,6 +588,17 @@ gbrt_status gbrt_guide_create(gbrt_ctx* ctx, const float bounds[6],
 gbrt_status gbrt_guide_destroy(gbrt_guide* guide);
 gbrt_status gbrt_guide_get_weights(gbrt_guide* guide, float* weights,
                                    size_t n);
+/* Checkpoint and resume of training (no counterpart in the renderer): the
+ * FP32 master parameters, Adam's first and second moments (GBRT_GUIDE_PARAMS
+ * floats each, host buffers) and its step count. set_state restores all of
+ * them, so that training continues exactly where the saved guide stopped
+ * (up to the order of the float additions of the gradient), and marks the
+ * guide usable by renders. */
+gbrt_status gbrt_guide_get_state(gbrt_guide* guide, float* params,
+                                 float* adam_m, float* adam_v, int64_t* step);
+gbrt_status gbrt_guide_set_state(gbrt_guide* guide, const float* params,
+                                 const float* adam_m, const float* adam_v,
+                                 int64_t step);
 /* Also resets the optimizer state and marks the guide usable by renders. */
 gbrt_status gbrt_guide_set_weights(gbrt_guide* guide, const float* weights,
                                    size_t n);
@@ -743,8 +772,9 @@ gbrt_status gbrt_parsed_scene_desc(const gbrt_parsed_scene* ps,
 void gbrt_parsed_scene_free(gbrt_parsed_scene* ps);
 
 /* Image reader for environment and texture images: Radiance RGBE (.hdr),
- * PFM, PPM (samples 0..maxval) and PNG (recognised by its signature; 8-bit
- * samples 0..255 as cv::imread(IMREAD_COLOR) gives them). Returns
+ * PFM, PPM (samples 0..maxval), PNG and sequential JPEG (both recognised by
+ * their signatures; 8-bit samples 0..255 as cv::imread(IMREAD_COLOR) gives
+ * them). Returns
  * H x W x 3 float BGR in a buffer the caller frees with gbrt_free. (Replaces
  * cv::imread in src/environmentmap.cpp:20-33 and
  * src/texturematerial.cpp:48-60.) */

@@ -207,6 +207,10 @@ SIGNATURES = [
     ("gbrt_render_batch_fused", C.c_int, [P, C.POINTER(BatchJob), C.c_int32, C.POINTER(BatchSchedule),
                                           C.POINTER(C.c_double), C.POINTER(BatchStats)]),
     ("gbrt_batch_autotune_fused", C.c_int, [P, C.POINTER(BatchJob), C.c_int32, C.POINTER(BatchSchedule)]),
+    ("gbrt_render_passes", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), C.c_int32, C.c_int32,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Stats)]),
+    ("gbrt_guide_get_state", C.c_int, [P, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
+    ("gbrt_guide_set_state", C.c_int, [P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]),
     ("gbrt_ctx_trim", C.c_int, [P, C.POINTER(C.c_uint64)]),
     ("gbrt_debug_fault", C.c_int, [P, C.c_int32, C.c_int64]),
     ("gbrt_render_mlt", C.c_int, [P, C.POINTER(Camera), C.POINTER(RenderParams), C.POINTER(MltParams), P,

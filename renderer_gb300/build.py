@@ -15,8 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgbrt.so")
 
-SOURCES = ["scene.cpp", "bvh_build.cpp", "bvh_gpu.cu", "scene_parse.cpp", "image_png.cpp", "image_out.cu", "trace.cu",
-           "pathtrace.cu", "guide.cu"]
+SOURCES = ["scene.cpp", "bvh_build.cpp", "bvh_gpu.cu", "scene_parse.cpp", "image_png.cpp", "image_jpeg.cpp",
+           "image_out.cu", "trace.cu", "pathtrace.cu", "guide.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",

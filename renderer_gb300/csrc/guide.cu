@@ -703,6 +703,37 @@ gbrt_status gbrt_guide_set_weights(gbrt_guide* g, const float* w, size_t n) {
   return GBRT_OK;
 }
 
+gbrt_status gbrt_guide_get_state(gbrt_guide* g, float* params, float* adam_m, float* adam_v, int64_t* step) {
+  gbrt_status st = check_guide(g);
+  if (st != GBRT_OK) return st;
+  if (!params || !adam_m || !adam_v || !step) return fail(g->ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_get_state: NULL");
+  GBRT_CUDA_TRY(g->ctx, cudaMemcpy(params, g->d_p, kParams * sizeof(float), cudaMemcpyDeviceToHost));
+  GBRT_CUDA_TRY(g->ctx, cudaMemcpy(adam_m, g->d_m, kParams * sizeof(float), cudaMemcpyDeviceToHost));
+  GBRT_CUDA_TRY(g->ctx, cudaMemcpy(adam_v, g->d_v, kParams * sizeof(float), cudaMemcpyDeviceToHost));
+  *step = int64_t(g->step);
+  return GBRT_OK;
+}
+
+gbrt_status gbrt_guide_set_state(gbrt_guide* g, const float* params, const float* adam_m, const float* adam_v,
+                                 int64_t step) {
+  gbrt_status st = check_guide(g);
+  if (st != GBRT_OK) return st;
+  if (!params || !adam_m || !adam_v || step < 0 || step > 0x7fffffff)
+    return fail(g->ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_set_state: bad argument");
+  for (int i = 0; i < kParams; ++i)
+    if (!std::isfinite(params[i]) || !std::isfinite(adam_m[i]) || !(adam_v[i] >= 0.f) || !std::isfinite(adam_v[i]))
+      return fail(g->ctx, GBRT_ERR_INVALID_ARG, "gbrt_guide_set_state: non-finite or negative value");
+  GBRT_CUDA_TRY(g->ctx, cudaMemcpy(g->d_p, params, kParams * sizeof(float), cudaMemcpyHostToDevice));
+  GBRT_CUDA_TRY(g->ctx, cudaMemcpy(g->d_m, adam_m, kParams * sizeof(float), cudaMemcpyHostToDevice));
+  GBRT_CUDA_TRY(g->ctx, cudaMemcpy(g->d_v, adam_v, kParams * sizeof(float), cudaMemcpyHostToDevice));
+  k_to_bf16<<<(kParams + 255) / 256, 256>>>(g->d_p, g->d_w, kParams);
+  GBRT_CUDA_TRY(g->ctx, cudaGetLastError());
+  GBRT_CUDA_TRY(g->ctx, cudaDeviceSynchronize());
+  g->step = int(step);
+  g->ready = true;
+  return GBRT_OK;
+}
+
 gbrt_status gbrt_guide_eval(gbrt_guide* g, const float* inputs, size_t n, float* out) {
   gbrt_status st = check_guide(g);
   if (st != GBRT_OK) return st;

@@ -1288,8 +1288,11 @@ struct Buffers {
   }
 };
 
+// keep_sums: add to d_sum_in / d_sumsq instead of clearing them first (both
+// must then be given); film_scale: the film is sum x film_scale (0: 1 / spp).
 static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render_params* prm, float* d_film,
-                               double* d_sum_in, double* d_sumsq, const volatile int32_t* stop, gbrt_stats* stats) {
+                               double* d_sum_in, double* d_sumsq, const volatile int32_t* stop, gbrt_stats* stats,
+                               bool keep_sums = false, double film_scale = 0.0) {
   gbrt_ctx* ctx = s->ctx;
   if (!cam || !prm || !d_film) return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render: NULL argument");
   if (cam->width <= 0 || cam->height <= 0 || prm->x_samples <= 0 || prm->y_samples <= 0 || prm->max_depth <= 0 ||
@@ -1329,8 +1332,10 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
   if (!d_sum) A(buf.alloc(&d_sum, npix * 3));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "render buffers");
-  A(cudaMemsetAsync(d_sum, 0, npix * 3 * sizeof(double), stream));
-  if (d_sumsq) A(cudaMemsetAsync(d_sumsq, 0, npix * 3 * sizeof(double), stream));
+  if (!keep_sums) {
+    A(cudaMemsetAsync(d_sum, 0, npix * 3 * sizeof(double), stream));
+    if (d_sumsq) A(cudaMemsetAsync(d_sumsq, 0, npix * 3 * sizeof(double), stream));
+  }
   A(cudaMemsetAsync(st.tally, 0, 8 * sizeof(unsigned long long), stream));
   A(cudaMemsetAsync(st.err, 0, sizeof(int), stream));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "render set-up");
@@ -1385,7 +1390,8 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
     if (e != cudaSuccess) break;
   }
   size_t n3 = size_t(npix) * 3;
-  k_finalize<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_sum, d_film, n3, 1.0 / spp);
+  k_finalize<<<unsigned((n3 + 255) / 256), 256, 0, stream>>>(d_sum, d_film, n3,
+                                                             film_scale > 0.0 ? film_scale : 1.0 / spp);
   ++launches;
   cudaEventRecord(ev1, stream);
   A(cudaGetLastError());
@@ -2429,6 +2435,44 @@ gbrt_status gbrt_render(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render
   e = cudaStreamSynchronize(ctx->stream);
   if (st == GBRT_OK && e != cudaSuccess) st = cuda_fail(ctx, e, "gbrt_render copy-out");
   return st;
+}
+
+gbrt_status gbrt_render_passes(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render_params* prm,
+                               int32_t first_pass, int32_t n_passes, float* d_film, double* d_sum, double* d_sumsq,
+                               gbrt_stats* stats) {
+  if (!s) return fail(nullptr, GBRT_ERR_INVALID_ARG, "gbrt_render_passes: NULL scene");
+  gbrt_ctx* ctx = s->ctx;
+  clear_error(ctx);
+  if (!cam || !prm || !d_film || !d_sum || first_pass < 0 || n_passes <= 0 ||
+      int64_t(first_pass) + n_passes > (int64_t(1) << 30))
+    return fail(ctx, GBRT_ERR_INVALID_ARG, "gbrt_render_passes: bad argument");
+  GBRT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  const size_t n3 = size_t(std::max(cam->width, 0)) * size_t(std::max(cam->height, 0)) * 3;
+  if (first_pass == 0) {
+    GBRT_CUDA_TRY(ctx, cudaMemsetAsync(d_sum, 0, n3 * sizeof(double), ctx->stream));
+    if (d_sumsq) GBRT_CUDA_TRY(ctx, cudaMemsetAsync(d_sumsq, 0, n3 * sizeof(double), ctx->stream));
+  }
+  const double spp = double(prm->x_samples) * double(prm->y_samples);
+  gbrt_stats total;
+  std::memset(&total, 0, sizeof total);
+  for (int32_t k = 0; k < n_passes; ++k) {
+    const int32_t pass = first_pass + k;
+    gbrt_render_params p = *prm;
+    p.seed = pass_seed(prm->seed, pass);
+    gbrt_stats st;
+    // the film of the last pass: all passes so far
+    const double scale = 1.0 / (double(pass + 1) * spp);
+    gbrt_status r = render_impl(s, cam, &p, d_film, d_sum, d_sumsq, nullptr, &st, true, scale);
+    if (r != GBRT_OK) return r;
+    total.paths += st.paths;
+    total.extension_rays += st.extension_rays;
+    total.shadow_rays += st.shadow_rays;
+    total.nonfinite += st.nonfinite;
+    total.render_ms += st.render_ms;
+    total.kernel_launches += st.kernel_launches;
+  }
+  if (stats) *stats = total;
+  return GBRT_OK;
 }
 
 gbrt_status gbrt_render_device_noalloc(gbrt_scene* s, const gbrt_camera* cam, const gbrt_render_params* prm,

@@ -20,9 +20,10 @@
 // b(left, right, box) node contributes its children (the BVH is rebuilt);
 // box(min, max, m) and isect / union / diff / xor trees of spheres and boxes
 // become CSG objects (a box under an instance must stay axis-aligned).
-// Texture images are read from PNG (image_png.cpp), PPM (P6/P3), PFM and
-// Radiance files, all decoded here, and scaled by 1/255 like the renderer's
-// cv::imread + convertTo; an unreadable image gives DarkMatter.
+// Texture images are read from PNG (image_png.cpp), JPEG (image_jpeg.cpp),
+// PPM (P6/P3), PFM and Radiance files, all decoded here, and scaled by 1/255
+// like the renderer's cv::imread + convertTo; an unreadable image gives
+// DarkMatter.
 // Each primitive's position in the scene's root list (lights, then the
 // intersectables in file order) is kept as gbrt_scene_desc.list_rank, for the
 // list's tie rule under GBRT_SCENE_LIST_ORDER.
@@ -44,6 +45,7 @@
 #include <vector>
 
 #include "../../include/gbrt.h"
+#include "image_jpeg.h"
 #include "image_png.h"
 
 namespace {
@@ -596,14 +598,20 @@ bool readPPM(const std::string& path, std::vector<float>& bgr, int& W, int& H, s
 
 bool readImage(const std::string& path, std::vector<float>& bgr, int& W, int& H, std::string& why) {
   {
-    // PNG is recognised by its signature, as cv::imread recognises formats.
+    // PNG and JPEG are recognised by their signatures, as cv::imread
+    // recognises formats.
     std::ifstream in(path, std::ios::binary);
     char sig[8] = {0};
-    if (in && in.read(sig, 8) && gbrt_img::is_png(std::string(sig, 8))) {
-      std::string data;
-      if (!readFile(path, data)) { why = "cannot read " + path; return false; }
-      if (!gbrt_img::decode_png(data, bgr, W, H, why)) { why = path + ": " + why; return false; }
-      return true;
+    if (in && in.read(sig, 8)) {
+      const std::string head(sig, 8);
+      const bool png = gbrt_img::is_png(head), jpeg = gbrt_img::is_jpeg(head);
+      if (png || jpeg) {
+        std::string data;
+        if (!readFile(path, data)) { why = "cannot read " + path; return false; }
+        const bool ok = png ? gbrt_img::decode_png(data, bgr, W, H, why) : gbrt_img::decode_jpeg(data, bgr, W, H, why);
+        if (!ok) { why = path + ": " + why; return false; }
+        return true;
+      }
     }
   }
   std::string lower = path;

@@ -47,6 +47,23 @@ class Guide:
         w = np.ascontiguousarray(w, np.float32).reshape(-1)
         check(lib().gbrt_guide_set_weights(self.handle, _ptr(w), w.size), self.ctx.handle)
 
+    def get_state(self):
+        """Checkpoint of training: {"params", "adam_m", "adam_v" (GUIDE_PARAMS
+        float32 each), "step"}."""
+        n = _abi.GUIDE_PARAMS
+        out = {k: np.zeros(n, np.float32) for k in ("params", "adam_m", "adam_v")}
+        step = C.c_int64()
+        check(lib().gbrt_guide_get_state(self.handle, _ptr(out["params"]), _ptr(out["adam_m"]),
+                                         _ptr(out["adam_v"]), C.byref(step)), self.ctx.handle)
+        out["step"] = step.value
+        return out
+
+    def set_state(self, state):
+        """Resumes training from a get_state checkpoint."""
+        a = [np.ascontiguousarray(state[k], np.float32).reshape(-1) for k in ("params", "adam_m", "adam_v")]
+        check(lib().gbrt_guide_set_state(self.handle, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), int(state["step"])),
+              self.ctx.handle)
+
     def eval(self, inputs):
         """inputs (N, 9): point, normal facing the viewer, outgoing direction.
         Returns (N, 40): lobe weights [8], then (mean xyz, kappa) per lobe."""

@@ -4,7 +4,7 @@ triangles from their texture coordinates (default (0,0), (0,1), (1,0)).
 
 CPU: the oracle against closed forms (a constant texture is a diffuse
 material; a textured floor under a point light shows the texel values), the
-parser (texture(...) reads PPM and PNG, scales by 1/255, unreadable files give
+parser (texture(...) reads PPM, PNG and JPEG, scales by 1/255, unreadable files give
 DarkMatter). GPU: path-level parity with the oracle on a scene whose texture
 varies across the image, for both estimators."""
 import math
@@ -324,5 +324,92 @@ def test_png_textured_scene_parity(ctx, tmp_path, semantics):
     (film, _, _), _ = gpu_render(ctx, s, prm)
     orc = OracleScene(s).render(s.camera_struct(), prm, rng_mode=1)["film"]
     assert film[..., 0].std() > 0.05 * film[..., 0].mean()  # the texture shows
+    close = np.isclose(film, orc, rtol=2e-3, atol=1e-5).all(-1)
+    assert close.mean() > 0.98, close.mean()
+
+
+# ----------------------------------------------------------------- JPEG ----
+# The decoder against the standard's reconstruction of the same quantised
+# coefficients (tests/jpeg_writer.py: exact inverse DCT, triangle-filter
+# chroma upsampling, JFIF colour conversion), within one 8-bit unit for the
+# rounding of float arithmetic.
+def _smooth_rgb(h, w, seed):
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w]
+    img = np.stack([128 + 100 * np.sin(x / 5.0 + seed), 128 + 90 * np.cos(y / 7.0), (x * 3 + y * 5) % 256], -1)
+    img = img + rng.normal(0, 12, img.shape)
+    return np.clip(img, 0, 255).astype(np.uint8)
+
+
+QTABLES = {"fine": np.full(64, 2), "coarse": 4 + np.arange(64) // 2}
+
+
+@pytest.mark.parametrize("sub,grey", [((2, 2), False), ((2, 1), False), ((1, 1), False), ((1, 1), True)])
+@pytest.mark.parametrize("qname", ["fine", "coarse"])
+@pytest.mark.parametrize("restart,interleaved", [(0, True), (3, True), (2, False)])
+def test_jpeg_decoder_matches_the_standard(tmp_path, sub, grey, qname, restart, interleaved):
+    from renderer_gb300.scenefile import read_hdr
+    from tests.jpeg_writer import encode, reconstruct
+    img = _smooth_rgb(29, 37, seed=len(qname) + restart)
+    data, comps, layout = encode(img, QTABLES[qname], subsampling=sub, grey=grey, restart=restart,
+                                 interleaved=interleaved)
+    p = tmp_path / "t.jpg"
+    p.write_bytes(data)
+    got = read_hdr(str(p))
+    want = reconstruct(comps, layout, grey=grey)
+    assert got.shape == want.shape == (29, 37, 3)
+    assert np.abs(got - want).max() <= 1.0
+    # and, without chroma subsampling and with fine quantisation, close to
+    # the image that was encoded (a lossy codec)
+    if not grey and qname == "fine" and sub == (1, 1):
+        assert np.abs(got[..., ::-1].astype(np.float64) - img).mean() < 3.0
+
+
+def test_jpeg_refusals(tmp_path):
+    """Progressive (SOF2) and truncated files are refused; a texture that
+    cannot be read is DarkMatter."""
+    from renderer_gb300.scenefile import load_scene_string, read_hdr
+    from tests.jpeg_writer import encode
+    data, _, _ = encode(_smooth_rgb(16, 16, 1), QTABLES["fine"])
+    prog = bytearray(data)
+    i = prog.index(b"\xFF\xC0")
+    prog[i + 1] = 0xC2
+    for bad in (bytes(prog), data[: len(data) // 2], data[:200] + b"\x00" * 50):
+        q = tmp_path / "bad.jpg"
+        q.write_bytes(bad)
+        with pytest.raises(Exception):
+            read_hdr(str(q))
+    s = load_scene_string('intersectable = intersectables { sphere([0 0 0], 1, texture("bad.jpg", [1 1 1], 1)) };',
+                          str(tmp_path))
+    assert s.materials[0]["type"] == _abi.MAT_DARK
+
+
+def test_parser_reads_jpeg_texture(tmp_path):
+    from renderer_gb300.scenefile import load_scene_string
+    from tests.jpeg_writer import encode, reconstruct
+    img = _smooth_rgb(20, 24, 2)
+    data, comps, layout = encode(img, QTABLES["fine"])
+    (tmp_path / "t.jpeg").write_bytes(data)
+    s = load_scene_string('intersectable = intersectables { t([0 0 0], [1 0 0], [0 1 0], [0 0 1], [0 0 1], '
+                          '[0 0 1], [0 0], [1 0], [0 1], texture("t.jpeg", [1 1 1], 1)) };', str(tmp_path))
+    m = s.materials[0]
+    assert m["type"] == _abi.MAT_TEXTURE
+    np.testing.assert_allclose(s.textures[m["texture"]] * 255.0, reconstruct(comps, layout), atol=1.0 + 1e-3)
+
+
+@pytest.mark.gpu
+def test_jpeg_textured_scene_parity(ctx, tmp_path):
+    """The PNG floor scene with a 4:2:0 JPEG texture: GPU against the oracle
+    path by path."""
+    from renderer_gb300.scenefile import load_scene_string
+    from tests.jpeg_writer import encode
+    from tests.test_gpu_render import gpu_render
+    data, _, _ = encode(_smooth_rgb(24, 24, 5), QTABLES["coarse"])
+    (tmp_path / "floor.png").write_bytes(data)  # the scene names floor.png; the format is found by its bytes
+    s = load_scene_string(PNG_FLOOR_SCENE, str(tmp_path))
+    assert s.materials[0]["type"] == _abi.MAT_TEXTURE
+    prm = render_params(2, 2, 0.5, 4, 6)
+    (film, _, _), _ = gpu_render(ctx, s, prm)
+    orc = OracleScene(s).render(s.camera_struct(), prm, rng_mode=1)["film"]
     close = np.isclose(film, orc, rtol=2e-3, atol=1e-5).all(-1)
     assert close.mean() > 0.98, close.mean()
