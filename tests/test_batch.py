@@ -225,3 +225,23 @@ def test_fused_autotune_and_refusals(ctx):
         render_batch_fused(ctx, jobs, pipelines=9)
     films, ms, st = render_batch_fused(ctx, [])
     assert films == [] and st.paths == 0
+
+
+@pytest.mark.gpu
+def test_fused_batch_extreme_wavefronts(ctx):
+    """Wavefronts of a single path (every graph replay shades one path of one
+    job) and of three paths, with 1 x 1 and 5 x 3 images among larger ones:
+    the films still equal the jobs rendered alone."""
+    from renderer_gb300.batch import BatchJob, render_batch_fused
+    scenes = [shrunk(9, 1, 1, 1), shrunk(6, 5, 2, 1), shrunk(8, 12, 1, 2)]
+    scenes[1][0].camera["height"] = 3
+    gss = [GpuScene(ctx, s) for s, _ in scenes]
+    jobs = [BatchJob(g, s.camera_struct(), p) for g, (s, p) in zip(gss, scenes)]
+    alone = _alone(ctx, gss, scenes)
+    total = sum(s.camera["width"] * s.camera["height"] * p.x_samples * p.y_samples for s, p in scenes)
+    for B, P in ((1, 1), (3, 2)):
+        films, ms, st = render_batch_fused(ctx, jobs, wavefront_paths=B, pipelines=P)
+        assert st.paths == total and st.batch_paths == B
+        for f, a in zip(films, alone):
+            assert f.shape == a.shape
+            assert np.allclose(f, a, rtol=1e-5, atol=1e-7), np.abs(f - a).max()
