@@ -234,7 +234,7 @@ def run_guided(args):
         return p
 
     gflags = (0 if args.absolute_weights else _abi.GUIDE_PIXEL_RELATIVE) | (
-        _abi.GUIDE_PRODUCT if args.product_target else 0)
+        _abi.GUIDE_PRODUCT if args.product_target else 0) | (_abi.GUIDE_ASYNC_TRAINING if args.async_train else 0)
 
     def train_gp(budget_ms=0.0, passes=0):
         return guide_params(args.guide_fraction, passes=passes, train_passes=args.train_passes,
@@ -345,7 +345,9 @@ def run_guided(args):
                                    else "each of the first %d" % args.train_passes,
                                    "absolute" if args.absolute_weights else "relative to their pixel",
                                    "BSDF x radiance x cos" if args.product_target else "radiance x cos"),
-                       "passes": "inverse-variance weighted (the first, unguided pass seeds the mean)"},
+                       "passes": "inverse-variance weighted (the first, unguided pass seeds the mean)",
+                       "training_stream": "second stream, overlapping the next pass" if args.async_train
+                       else "the render stream, between passes"},
             "plain": [{"ms": t, "relmse": e, "spp": n} for t, e, n in plain],
             "guided": [{"ms": t, "relmse": e, "spp": n, "train_steps": k, "train_ms": tm}
                        for t, e, n, k, tm in guided],
@@ -866,6 +868,8 @@ def main():
     ap.add_argument("--absolute-weights", action="store_true",
                     help="--guided: training weights not relative to the sample's pixel")
     ap.add_argument("--train-passes", type=int, default=1 << 30, help="passes that train (default: all)")
+    ap.add_argument("--async-train", action="store_true",
+                    help="with --guided: Adam steps on a second stream, overlapping the next pass")
     ap.add_argument("--product-target", action="store_true",
                     help="--guided: the guide learns BSDF x incident radiance x cos (GBRT_GUIDE_PRODUCT)")
     ap.add_argument("--tuned", action="store_true",

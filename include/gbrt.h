@@ -654,7 +654,14 @@ typedef enum gbrt_guide_flags {
    * cosine (the radiance each sampled direction reflects towards wo) instead
    * of the incident radiance times the cosine: the two differ at glossy
    * vertices, where the product follows the lobe. */
-  GBRT_GUIDE_PRODUCT = 4
+  GBRT_GUIDE_PRODUCT = 4,
+  /* The Adam steps after a training pass run on a second stream of the
+   * context while the next pass renders: pass p samples the weights left by
+   * the steps after pass p - 2 (one pass later than without the flag), so
+   * that training and rendering overlap on the GPU. The sample buffers and
+   * the weight snapshots are double-buffered; the call returns after all of
+   * its steps, with the guide's weights those of the last step. */
+  GBRT_GUIDE_ASYNC_TRAINING = 8
 } gbrt_guide_flags;
 
 typedef struct gbrt_guide_stats {

@@ -172,7 +172,7 @@ FAULT_NONE, FAULT_ALLOC, FAULT_NAN, FAULT_SMALL_STACK, FAULT_GUIDE_WAIT = 0, 1, 
 GUIDE_PARAMS, GUIDE_INPUT, GUIDE_OUTPUT, GUIDE_SAMPLE = 24064, 9, 40, 13
 CSG_SPHERE, CSG_BOX, CSG_ISECT, CSG_UNION, CSG_DIFF, CSG_XOR = range(6)
 CSG_MAX_LEAVES = 8
-GUIDE_EQUAL_WEIGHTS, GUIDE_PIXEL_RELATIVE, GUIDE_PRODUCT = 1, 2, 4
+GUIDE_EQUAL_WEIGHTS, GUIDE_PIXEL_RELATIVE, GUIDE_PRODUCT, GUIDE_ASYNC_TRAINING = 1, 2, 4, 8
 
 P = C.c_void_p
 

@@ -551,7 +551,11 @@ cudaError_t train_window(gbrt_guide* g, const float4* samples, const int* avail,
   if (cap > 0 && batch > 0) {
     int tiles = (std::min(batch, cap) + kRows - 1) / kRows;
     int grid = std::min(g->train_grid, tiles);
-    k_guide_train<<<grid, kRows, kTrainSmem, stream>>>(view(g), samples, avail, cap, k, batch, g->d_g, g->d_loss,
+    // Training reads (and Adam writes) the training copy of the BF16
+    // weights when a render trains asynchronously, else the only copy.
+    GuideNet tv = view(g);
+    if (g->d_wt) tv.w = g->d_wt;
+    k_guide_train<<<grid, kRows, kTrainSmem, stream>>>(tv, samples, avail, cap, k, batch, g->d_g, g->d_loss,
                                                        g->d_err);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
@@ -560,8 +564,9 @@ cudaError_t train_window(gbrt_guide* g, const float4* samples, const int* avail,
     g->ready = true;
     const float b1 = 0.9f, b2 = 0.999f;
     float bc1 = float(1.0 - std::pow(double(b1), g->step)), bc2 = float(1.0 - std::pow(double(b2), g->step));
-    k_guide_adam<<<(kParams + 255) / 256, 256, 0, stream>>>(g->d_p, g->d_m, g->d_v, g->d_g, g->d_w, kParams, lr, b1,
-                                                            b2, 1e-8f, bc1, bc2);
+    k_guide_adam<<<(kParams + 255) / 256, 256, 0, stream>>>(g->d_p, g->d_m, g->d_v, g->d_g,
+                                                            g->d_wt ? g->d_wt : g->d_w, kParams, lr, b1, b2, 1e-8f,
+                                                            bc1, bc2);
     e = cudaGetLastError();
   }
   return e;

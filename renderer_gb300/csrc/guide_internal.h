@@ -18,6 +18,11 @@ struct gbrt_guide {
   float* d_v = nullptr;                  // Adam second moments
   float* d_g = nullptr;                  // gradient accumulator
   __nv_bfloat16* d_w = nullptr;          // BF16 copy read by the kernels
+  // While a render trains asynchronously (GBRT_GUIDE_ASYNC_TRAINING): the
+  // BF16 copy that training reads and Adam writes, on the training stream;
+  // d_w then points at the snapshot the current pass infers with. Null
+  // otherwise.
+  __nv_bfloat16* d_wt = nullptr;
   float* d_loss = nullptr;
   int* d_err = nullptr;
   int step = 0;                          // optimizer steps taken

@@ -1728,14 +1728,33 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
   A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
   long long tcap = 0;
+  // Asynchronous training: the Adam steps of pass p's samples run on a second
+  // stream while pass p + 1 renders. Pass p infers with the snapshot wq[p & 1]
+  // of the weights left by the steps of pass p - 2 and collects its samples
+  // into tsamp[p & 1]; the render stream waits for those steps (event
+  // trained[p & 1]) before the pass starts.
+  const bool async = training && (gp->flags & GBRT_GUIDE_ASYNC_TRAINING) != 0;
+  float4* tsampBuf[2] = {nullptr, nullptr};
+  int* tcountBuf[2] = {nullptr, nullptr};
+  __nv_bfloat16* wq[2] = {nullptr, nullptr};
+  __nv_bfloat16* wt = nullptr;
   if (useGuide) {
     A(buf.alloc(&st.gin, 3 * B));
     A(buf.alloc(&st.mix, guide::kMixStride * B));
     if (training) {
       A(buf.alloc(&st.rec, (long long)kRecComp * kRecords * B));
       tcap = std::min<long long>((long long)gp->steps_per_pass * gp->batch_samples, 1ll << 25);
-      A(buf.alloc(&st.tsamp, 4 * tcap));
-      A(buf.alloc(&st.tcount, 1));
+      for (int b = 0; b < (async ? 2 : 1); ++b) {
+        A(buf.alloc(&tsampBuf[b], 4 * tcap));
+        A(buf.alloc(&tcountBuf[b], 1));
+      }
+      st.tsamp = tsampBuf[0];
+      st.tcount = tcountBuf[0];
+      if (async) {
+        A(buf.alloc(&wt, guide::kParams));
+        A(buf.alloc(&wq[0], guide::kParams));
+        A(buf.alloc(&wq[1], guide::kParams));
+      }
     }
   }
   st.tcap = int(tcap);
@@ -1761,7 +1780,46 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
 
   A(cudaMemsetAsync(st.tally, 0, 8 * sizeof(unsigned long long), stream));
   A(cudaMemsetAsync(st.err, 0, sizeof(int), stream));
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "guided render set-up");
+  cudaStream_t ts = stream;  // the training stream
+  cudaEvent_t trained[2] = {nullptr, nullptr}, sampled = nullptr;
+  __nv_bfloat16* const wMain = g ? g->d_w : nullptr;
+  if (async && e == cudaSuccess) {
+    if (ctx->batch_streams.empty()) {
+      cudaStream_t q;
+      A(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+      if (e == cudaSuccess) ctx->batch_streams.push_back(q);
+    }
+    if (e == cudaSuccess) ts = ctx->batch_streams[0];
+    for (__nv_bfloat16* w : {wt, wq[0], wq[1]})
+      A(cudaMemcpyAsync(w, wMain, guide::kParams * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
+    A(cudaEventCreateWithFlags(&trained[0], cudaEventDisableTiming));
+    A(cudaEventCreateWithFlags(&trained[1], cudaEventDisableTiming));
+    A(cudaEventCreateWithFlags(&sampled, cudaEventDisableTiming));
+    // the training stream starts after the copies
+    A(cudaEventRecord(sampled, stream));
+    A(cudaStreamWaitEvent(ts, sampled, 0));
+    if (e == cudaSuccess) g->d_wt = wt;
+  }
+  auto end_async = [&]() {
+    if (!async || !g || !g->d_wt) return;
+    // The render stream waits for every step, and the guide keeps the
+    // weights of the last one.
+    cudaEvent_t done = nullptr;
+    if (cudaEventCreateWithFlags(&done, cudaEventDisableTiming) == cudaSuccess) {
+      cudaEventRecord(done, ts);
+      cudaStreamWaitEvent(stream, done, 0);
+      cudaEventDestroy(done);
+    }
+    cudaMemcpyAsync(wMain, wt, guide::kParams * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream);
+    g->d_w = wMain;
+    g->d_wt = nullptr;
+  };
+  if (e != cudaSuccess) {
+    end_async();
+    for (cudaEvent_t x : {trained[0], trained[1], sampled})
+      if (x) cudaEventDestroy(x);
+    return cuda_fail(ctx, e, "guided render set-up");
+  }
 
   const TraceKernels tk = pick_kernels(s, false);
   int per = 0;
@@ -1783,17 +1841,43 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   std::vector<cudaEvent_t> iev;
   gbrt_status status = GBRT_OK;
   unsigned long long samples = 0, pathsDone = 0;  // per-pixel samples and paths of the passes so far
+  // Asynchronous training: steps issued up to each slot's last training,
+  // whether a slot has a training in flight, and the slot of the last one.
+  int stepsAt[2] = {0, 0}, lastSlot = -1;
+  bool issued[2] = {false, false};
+  const bool readyAtStart = g && g->ready;
   for (int pass = 0;; ++pass) {
     if (gp->passes > 0 && pass >= gp->passes) break;
     const bool record = training && pass < gp->train_passes;
     const bool late = !record;
+    // Steps whose weights this pass infers with.
+    int visible = steps;
+    if (async) {
+      const int b = record ? (pass & 1) : lastSlot;
+      if (b >= 0 && issued[b]) {
+        A(cudaStreamWaitEvent(stream, trained[b], 0));
+        if (!record) {  // after training: both slots' steps are done, the last is newest
+          A(cudaStreamWaitEvent(stream, trained[b ^ 1], 0));
+        }
+        g->d_w = wq[b];
+        visible = stepsAt[b];
+      } else {
+        g->d_w = wq[0];  // the weights the call started with
+        visible = 0;
+      }
+      if (record) {
+        st.tsamp = tsampBuf[pass & 1];
+        st.tcount = tcountBuf[pass & 1];
+      }
+    }
     const int sppPass = late ? lateSpp : spp;
     const unsigned long long passTotal = late ? lateTotal : total;
     PTParams P{};
     init_params(P, ctx, *cam, late ? lateParams : *prm, passTotal);
     P.seed = pass_seed(prm->seed, pass);
     // While training, sample the guide once it has had warmup_steps steps.
-    P.guided = (useGuide && g->ready && (!training || steps >= gp->warmup_steps)) ? 1 : 0;
+    const bool readyNow = async ? (readyAtStart || visible > 0) : (g && g->ready);
+    P.guided = (useGuide && readyNow && (!training || visible >= gp->warmup_steps)) ? 1 : 0;
     P.guide_frac = gp->guide_fraction;
     P.record = record ? 1 : 0;
     P.guide_depth = gp->guide_depth;
@@ -1854,15 +1938,29 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     pathsDone += passTotal;
     if (record) {
       // Steps over the pass's samples; their count stays on the device.
-      if (timeK) cudaEventRecord(t0, stream);
+      // Asynchronously: on the training stream once the pass's samples are
+      // in, then a snapshot of the weights for pass + 2.
+      if (async) {
+        A(cudaEventRecord(sampled, stream));
+        A(cudaStreamWaitEvent(ts, sampled, 0));
+      }
+      if (timeK) cudaEventRecord(t0, ts);
       for (int k = 0; k < gp->steps_per_pass && e == cudaSuccess; ++k) {
         A(guide::train_window(g, st.tsamp, st.tcount, int(tcap), k, gp->batch_samples, gp->learning_rate, true,
-                              stream));
-        g->ready = true;
+                              ts));
+        if (!async) g->ready = true;
         ++steps;
       }
+      if (timeK) cudaEventRecord(t1, ts);
+      if (async) {
+        const int b = pass & 1;
+        A(cudaMemcpyAsync(wq[b], wt, guide::kParams * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, ts));
+        A(cudaEventRecord(trained[b], ts));
+        issued[b] = true;
+        stepsAt[b] = steps;
+        lastSlot = b;
+      }
       if (timeK) {
-        cudaEventRecord(t1, stream);
         A(cudaEventSynchronize(t1));
         float tms = 0.f;
         cudaEventElapsedTime(&tms, t0, t1);
@@ -1880,7 +1978,9 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
       if (elapsed >= gp->time_budget_ms) break;
     }
   }
-  const bool timedAtEnd = gp->passes > 0;
+  end_async();
+  if (async && steps > 0) g->ready = true;
+  const bool timedAtEnd = gp->passes > 0 || async;
   if (timedAtEnd) cudaEventRecord(ev1, stream);
   if (e == cudaSuccess && passes > 0) {
     if (weighted && passes > 1)
@@ -1909,6 +2009,8 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   cudaEventDestroy(ev1);
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
+  for (cudaEvent_t x : {trained[0], trained[1], sampled})
+    if (x) cudaEventDestroy(x);
   for (size_t k = 0; k + 1 < iev.size(); k += 2) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, iev[k], iev[k + 1]);

@@ -292,3 +292,48 @@ def test_late_passes_keep_the_expectation(ctx):
             assert st2.paths == npix * 4 * 64 and st2.train_steps == 0
             assert img2.mean() == pytest.approx(ref.mean(), rel=0.03)
         g.close()
+
+
+@pytest.mark.gpu
+def test_async_training_keeps_the_expectation_and_trains(ctx):
+    """GBRT_GUIDE_ASYNC_TRAINING: the Adam steps run on a second stream while
+    the next pass renders (each pass sampling the weights of the steps two
+    passes back). The render keeps its expectation, every step is taken, the
+    guide ends with the last step's weights (the same as its FP32 master
+    parameters rounded) and helps at equal samples like synchronous
+    training."""
+    from renderer_gb300 import _abi
+    from renderer_gb300.guiding import Guide, guide_params, render_guided, scene_bounds
+    from renderer_gb300.workloads import two_rooms_params
+    sc, cam = _small_rooms(ctx, 128, 96, 24)
+    ref, _ = render_guided(sc, cam, two_rooms_params(8, 8, seed=31), None, guide_params(passes=256))
+    plain, _ = render_guided(sc, cam, two_rooms_params(8, 8, seed=32), None, guide_params(passes=4))
+
+    def relmse(x):
+        return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    ratios = []
+    for seed in (1, 2):
+        g = Guide(ctx, scene_bounds(sc), seed=seed)
+        w0 = g.weights()
+        gp = guide_params(0.5, passes=16, train_passes=16, steps_per_pass=32, batch_samples=1 << 16,
+                          learning_rate=1e-2, flags=_abi.GUIDE_PRODUCT | _abi.GUIDE_ASYNC_TRAINING)
+        trained, st = render_guided(sc, cam, two_rooms_params(8, 8, seed=33 + 2 * seed), g, gp)
+        assert st.train_steps == 512 and st.train_samples > 0 and st.passes == 16
+        state = g.get_state()
+        assert state["step"] == 512 and not np.array_equal(state["params"], w0)
+        # the inference copy is the last step's weights: evaluating the guide
+        # equals evaluating its master parameters set as weights
+        x = np.concatenate([np.random.default_rng(seed).uniform(0, 1, (256, 3)) * 2,
+                            np.tile([0, 1, 0], (256, 1)), np.tile([0, 0, 1], (256, 1))], 1).astype(np.float32)
+        e1 = g.eval(x)
+        h = Guide(ctx, scene_bounds(sc), seed=9)
+        h.set_weights(state["params"])
+        np.testing.assert_allclose(e1, h.eval(x), rtol=1e-5, atol=1e-6)
+        h.close()
+        guided, _ = render_guided(sc, cam, two_rooms_params(8, 8, seed=34 + 2 * seed), g, guide_params(0.5, passes=4))
+        g.close()
+        assert trained.mean() == pytest.approx(ref.mean(), rel=0.02)
+        assert guided.mean() == pytest.approx(ref.mean(), rel=0.02)
+        ratios.append(relmse(guided) / relmse(plain))
+    assert min(ratios) < 0.85 and max(ratios) < 1.2, ratios
