@@ -61,6 +61,7 @@ constexpr int kTW2T = 49152, kTW3T = 57344, kTW4T = 65536;
 constexpr int kTX1 = 71680, kTX2 = 88064, kTX3 = 104448, kTR = 120832, kTDR = 186368, kTDT = 202752;
 constexpr int kTMisc = 219136, kTrainSmem = kTMisc + 64;
 constexpr uint32_t kTrainCols = 512;
+constexpr int kTrainThreads = 2 * kRows;  // two threads per row of a tile
 // TMEM columns of the training kernel.
 constexpr uint32_t kColScratch = 0, kColW1lo = 64, kColW1hi = 128, kColW2 = 192, kColW3 = 256, kColW4 = 320;
 
@@ -278,44 +279,76 @@ __device__ __forceinline__ float loss_grad(const float* o, float wx, float wy, f
   return -w * lq;
 }
 
-// Writes v (64 values of row r) transposed: element (k, r) of a [rows][128]
-// batch-contiguous tile at s.
-__device__ __forceinline__ void write_transposed(uint32_t s, int r, const float* v, int nv) {
-  for (int k = 0; k < nv; ++k) st_shared_u16(s + ik_off(k, r, kRows), bf16_bits(v[k]));
+// Writes v (nv values of row r, features k0 .. k0 + nv - 1) transposed:
+// element (k, r) of a [rows][128] batch-contiguous tile at s.
+__device__ __forceinline__ void write_transposed(uint32_t s, int r, const float* v, int nv, int k0 = 0) {
+  for (int k = 0; k < nv; ++k) st_shared_u16(s + ik_off(k0 + k, r, kRows), bf16_bits(v[k]));
 }
 
-// Reads row r of an interleaved [128][64] BF16 tile.
-__device__ __forceinline__ void read_row64(const uint8_t* base, int r, float* v) {
+// Half of a hidden layer's input for row r: ReLU(TMEM columns [c0, c0 + 32))
+// into an interleaved [128][64] tile at s, the values kept in h.
+__device__ __forceinline__ void hidden_half_to_smem(uint32_t lane_taddr, uint32_t s, int r, int c0, float* h) {
+  float v[32];
+  tmem_ld32(lane_taddr + c0, v);
 #pragma unroll
-  for (int c = 0; c < kHid; c += 8) {
-    uint4 q = *reinterpret_cast<const uint4*>(base + ik_off(r, c, kHid));
-    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+  for (int q = 0; q < 4; ++q)
+    st_shared_v4(s + ik_off(r, c0 + 8 * q, kHid), pack_relu_bf16(v[8 * q], v[8 * q + 1]),
+                 pack_relu_bf16(v[8 * q + 2], v[8 * q + 3]), pack_relu_bf16(v[8 * q + 4], v[8 * q + 5]),
+                 pack_relu_bf16(v[8 * q + 6], v[8 * q + 7]));
+#pragma unroll
+  for (int i = 0; i < 32; ++i) h[i] = fmaxf(v[i], 0.f);
+}
+
+// delta = ReLU'(X) * dX for row r, features [c0, c0 + 32): dX from TMEM
+// scratch, X from the row tile. Writes delta rows (when s_rows != 0) and
+// delta^T.
+__device__ __forceinline__ void backprop_delta_half(uint32_t lane_taddr, const uint8_t* xrow, uint32_t s_rows,
+                                                    uint32_t s_t, int r, int c0) {
+  float x[32], d[32];
+#pragma unroll
+  for (int c = 0; c < 32; c += 8) {
+    uint4 q = *reinterpret_cast<const uint4*>(xrow + ik_off(r, c0 + c, kHid));
+    const __nv_bfloat162* hv = reinterpret_cast<const __nv_bfloat162*>(&q);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      float2 f = __bfloat1622float2(h[i]);
-      v[c + 2 * i] = f.x;
-      v[c + 2 * i + 1] = f.y;
+      float2 f = __bfloat1622float2(hv[i]);
+      x[c + 2 * i] = f.x;
+      x[c + 2 * i + 1] = f.y;
     }
   }
-}
-
-// delta = ReLU'(X) * dX for row r: dX from TMEM scratch, X from the row tile.
-// Writes delta rows (when rows != 0) and delta^T.
-__device__ __forceinline__ void backprop_delta(uint32_t lane_taddr, const uint8_t* xrow, uint32_t s_rows,
-                                               uint32_t s_t, int r) {
-  float x[kHid], d[kHid];
-  read_row64(xrow, r, x);
+  tmem_ld32(lane_taddr + c0, d);
 #pragma unroll
-  for (int c = 0; c < kHid; c += 16) tmem_ld16(lane_taddr + c, d + c);
-#pragma unroll
-  for (int k = 0; k < kHid; ++k) d[k] = x[k] > 0.f ? d[k] : 0.f;
+  for (int k = 0; k < 32; ++k) d[k] = x[k] > 0.f ? d[k] : 0.f;
   if (s_rows) {
 #pragma unroll
-    for (int c = 0; c < kHid; c += 8)
-      st_shared_v4(s_rows + ik_off(r, c, kHid), pack_bf16(d[c], d[c + 1]), pack_bf16(d[c + 2], d[c + 3]),
+    for (int c = 0; c < 32; c += 8)
+      st_shared_v4(s_rows + ik_off(r, c0 + c, kHid), pack_bf16(d[c], d[c + 1]), pack_bf16(d[c + 2], d[c + 3]),
                    pack_bf16(d[c + 4], d[c + 5]), pack_bf16(d[c + 6], d[c + 7]));
   }
-  write_transposed(s_t, r, d, kHid);
+  write_transposed(s_t, r, d, 32, c0);
+}
+
+// Encoding groups [G0, G1) of row r into the full [128][208] row tile, and
+// transposed into the [208][128] tile (both at groups' own feature offsets).
+template <int G0, int G1>
+__device__ __forceinline__ void write_enc_rows(uint32_t s, int r, const EncIn& e) {
+#pragma unroll
+  for (int g = G0; g < G1; ++g) {
+    float f[8];
+    enc_group(e, g, f);
+    st_shared_v4(s + ik_off(r, 8 * g, kIn), pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]),
+                 pack_bf16(f[6], f[7]));
+  }
+}
+template <int G0, int G1>
+__device__ __forceinline__ void write_enc_transposed(uint32_t s, int r, const EncIn& e) {
+#pragma unroll
+  for (int g = G0; g < G1; ++g) {
+    float fv[8];
+    enc_group(e, g, fv);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) st_shared_u16(s + ik_off(8 * g + q, r, kRows), bf16_bits(fv[q]));
+  }
 }
 
 // One optimizer step's gradient over a window of the sample buffer: with
@@ -323,12 +356,19 @@ __device__ __forceinline__ void backprop_delta(uint32_t lane_taddr, const uint8_
 // null), step k uses samples [start, start + n) with start = k * batch mod
 // n_avail and n = min(batch, n_avail - start), read on the device so that
 // the host never waits for the sample count.
-__global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const float4* __restrict__ base,
-                                                        const int* __restrict__ avail, int cap, int k, int batch,
-                                                        float* __restrict__ grad, float* __restrict__ loss_sum,
-                                                        int* err) {
+//
+// Two threads per row (threads t and t + 128, halves 0 and 1, in warps w and
+// w + 4, which read the same TMEM lanes): each encodes 13 of the 26 feature
+// groups, reads back, activates and transposes 32 of a hidden layer's 64
+// columns, and back-propagates 32 of its deltas; the output layer's loss and
+// gradient are computed by half 0. Eight warps per SM instead of four hide
+// more of the per-tile chain's latency.
+__global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideNet net, const float4* __restrict__ base,
+                                                                  const int* __restrict__ avail, int cap, int k,
+                                                                  int batch, float* __restrict__ grad,
+                                                                  float* __restrict__ loss_sum, int* err) {
   extern __shared__ __align__(1024) uint8_t sm[];
-  const int t = threadIdx.x, warp = t >> 5;
+  const int t = threadIdx.x, warp = t >> 5, r = t & (kRows - 1), half = t >> 7, c0 = 32 * half;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kTMisc);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + kTMisc + 8);
   const uint32_t bar = smem_u32(mbar);
@@ -348,7 +388,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
   if (warp == 0) tmem_alloc(smem_u32(tslot), kTrainCols);
   handoff();
   const uint32_t tmem = *tslot;
-  const uint32_t lane = tmem + (uint32_t(warp * 32) << 16);
+  const uint32_t lane = tmem + (uint32_t((warp & 3) * 32) << 16);
   const int n_avail = avail ? min(*avail, cap) : cap;
   const int start = n_avail > 0 ? int((long long)k * batch % n_avail) : 0;
   const int n = min(batch, n_avail - start);
@@ -373,52 +413,56 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
   };
 
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-    const int r = tile * kRows + t;
+    const int row = tile * kRows + r;
     float4 s0 = make_float4(net.lo[0], net.lo[1], net.lo[2], 0.f), s1 = make_float4(0.f, 0.f, 1.f, 0.f),
            s2 = make_float4(0.f, 0.f, 1.f, 0.f), s3 = make_float4(0.f, 0.f, 1.f, 0.f);
-    if (r < n) {
-      s0 = samples[4 * size_t(r)];
-      s1 = samples[4 * size_t(r) + 1];
-      s2 = samples[4 * size_t(r) + 2];
-      s3 = samples[4 * size_t(r) + 3];
+    if (row < n) {
+      s0 = samples[4 * size_t(row)];
+      s1 = samples[4 * size_t(row) + 1];
+      s2 = samples[4 * size_t(row) + 2];
+      s3 = samples[4 * size_t(row) + 3];
     }
-    const float w = r < n ? s0.w * inv_n : 0.f;
+    const float w = row < n ? s0.w * inv_n : 0.f;
     const EncIn e = make_enc(net, s0.x, s0.y, s0.z, s1.x, s1.y, s1.z, s2.x, s2.y, s2.z);
-    write_enc_row(sR, t, e);
+    if (half == 0) write_enc_rows<0, kIn / 16>(sR, r, e);
+    else write_enc_rows<kIn / 16, kIn / 8>(sR, r, e);
     // ---- forward
-    float h[kHid];
+    float hv[32];
     handoff();
     if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sR, kIn, sW1, kIn, kIn, kHid, false);
     if (!(ok = sync_chain())) break;
-    hidden_to_smem(lane + kColScratch, sX1, t, h);
-    write_transposed(sR, t, h, kHid);  // X1^T at R + 0
+    hidden_half_to_smem(lane + kColScratch, sX1, r, c0, hv);
+    write_transposed(sR, r, hv, 32, c0);  // X1^T at R + 0
     handoff();
     if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sX1, kHid, sW2, kHid, kHid, kHid, false);
     if (!(ok = sync_chain())) break;
-    hidden_to_smem(lane + kColScratch, sX2, t, h);
-    write_transposed(sR + 16384, t, h, kHid);  // X2^T
+    hidden_half_to_smem(lane + kColScratch, sX2, r, c0, hv);
+    write_transposed(sR + 16384, r, hv, 32, c0);  // X2^T
     handoff();
     if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sX2, kHid, sW3, kHid, kHid, kHid, false);
     if (!(ok = sync_chain())) break;
-    hidden_to_smem(lane + kColScratch, sX3, t, h);
-    write_transposed(sR + 32768, t, h, kHid);  // X3^T
+    hidden_half_to_smem(lane + kColScratch, sX3, r, c0, hv);
+    write_transposed(sR + 32768, r, hv, 32, c0);  // X3^T
     handoff();
     if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sX3, kHid, sW4, kHid, kHid, kOutPad, false);
     if (!(ok = sync_chain())) break;
-    {
+    if (half == 0) {
       float o[kOutPad], g[kOutPad];
       tmem_ld16(lane + kColScratch, o);
       tmem_ld16(lane + kColScratch + 16, o + 16);
       tmem_ld16(lane + kColScratch + 32, o + 32);
       float ls = loss_grad(o, s3.x, s3.y, s3.z, w, g);
-      if (r < n) loss += ls;
+      if (row < n) loss += ls;
 #pragma unroll
       for (int j = kOut; j < kOutPad; ++j) g[j] = 0.f;
 #pragma unroll
       for (int c = 0; c < kOutPad; c += 8)
-        st_shared_v4(sDR + ik_off(t, c, kOutPad), pack_bf16(g[c], g[c + 1]), pack_bf16(g[c + 2], g[c + 3]),
+        st_shared_v4(sDR + ik_off(r, c, kOutPad), pack_bf16(g[c], g[c + 1]), pack_bf16(g[c + 2], g[c + 3]),
                      pack_bf16(g[c + 4], g[c + 5]), pack_bf16(g[c + 6], g[c + 7]));
-      write_transposed(sDT, t, g, kOutPad);
+      write_transposed(sDT, r, g, kOutPad);
+    } else {
+      // the other half meanwhile: the encoding's second half, transposed, is
+      // not needed until layer 1's weight gradient; nothing to do here
     }
     // ---- backward: output layer
     handoff();
@@ -427,7 +471,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
       gemm_k(tmem + kColScratch, sDR, kOutPad, sW4T, kOutPad, kOutPad, kHid, false);
     }
     if (!(ok = sync_chain())) break;
-    backprop_delta(lane + kColScratch, sm + kTX3, sDR, sDT, t);
+    backprop_delta_half(lane + kColScratch, sm + kTX3, sDR, sDT, r, c0);
     // ---- layer 3
     handoff();
     if (t == 0 && net.issue) {
@@ -435,7 +479,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
       gemm_k(tmem + kColScratch, sDR, kHid, sW3T, kHid, kHid, kHid, false);
     }
     if (!(ok = sync_chain())) break;
-    backprop_delta(lane + kColScratch, sm + kTX2, sDR, sDT, t);
+    backprop_delta_half(lane + kColScratch, sm + kTX2, sDR, sDT, r, c0);
     // ---- layer 2
     handoff();
     if (t == 0 && net.issue) {
@@ -443,16 +487,10 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
       gemm_k(tmem + kColScratch, sDR, kHid, sW2T, kHid, kHid, kHid, false);
     }
     if (!(ok = sync_chain())) break;
-    backprop_delta(lane + kColScratch, sm + kTX1, 0u, sDT, t);
-    // ---- layer 1: the encoding again, transposed, into R (groups of eight
-    // features, unrolled like the row-wise writer)
-#pragma unroll
-    for (int g = 0; g < kIn / 8; ++g) {
-      float fv[8];
-      enc_group(e, g, fv);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) st_shared_u16(sR + ik_off(8 * g + q, t, kRows), bf16_bits(fv[q]));
-    }
+    backprop_delta_half(lane + kColScratch, sm + kTX1, 0u, sDT, r, c0);
+    // ---- layer 1: the encoding again, transposed, into R
+    if (half == 0) write_enc_transposed<0, kIn / 16>(sR, r, e);
+    else write_enc_transposed<kIn / 16, kIn / 8>(sR, r, e);
     handoff();
     if (t == 0 && net.issue) {
       gemm_k(tmem + kColW1lo, sR, kRows, sDT, kRows, kRows, kHid, !first);
@@ -464,28 +502,30 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideNet net, const floa
     __syncthreads();
   }
   if (ok && !first) {
-    // Weight gradients out of TMEM: lane = input feature, column = output.
+    // Weight gradients out of TMEM: lane = input feature, column = output;
+    // half h takes columns [32 h, 32 h + 32) of each block (W4: half 0 the
+    // first 32 of its 48, half 1 the rest).
     float v[16];
-    for (int c = 0; c < kHid; c += 16) {
+    for (int c = c0; c < c0 + 32; c += 16) {
       tmem_ld16(lane + kColW1lo + c, v);
-      for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW1 + (c + i) * kIn + t], v[i]);
+      for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW1 + (c + i) * kIn + r], v[i]);
       tmem_ld16(lane + kColW1hi + c, v);
-      if (kRows + t < kIn)
-        for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW1 + (c + i) * kIn + kRows + t], v[i]);
+      if (kRows + r < kIn)
+        for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW1 + (c + i) * kIn + kRows + r], v[i]);
       tmem_ld16(lane + kColW2 + c, v);
-      if (t < kHid)
-        for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW2 + (c + i) * kHid + t], v[i]);
+      if (r < kHid)
+        for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW2 + (c + i) * kHid + r], v[i]);
       tmem_ld16(lane + kColW3 + c, v);
-      if (t < kHid)
-        for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW3 + (c + i) * kHid + t], v[i]);
+      if (r < kHid)
+        for (int i = 0; i < 16; ++i) atomicAdd(&grad[kOffW3 + (c + i) * kHid + r], v[i]);
     }
-    for (int c = 0; c < kOutPad; c += 16) {
+    for (int c = half ? 32 : 0; c < (half ? kOutPad : 32); c += 16) {
       tmem_ld16(lane + kColW4 + c, v);
-      if (t < kHid)
+      if (r < kHid)
         for (int i = 0; i < 16; ++i)
-          if (c + i < kOut) atomicAdd(&grad[kOffW4 + (c + i) * kHid + t], v[i]);
+          if (c + i < kOut) atomicAdd(&grad[kOffW4 + (c + i) * kHid + r], v[i]);
     }
-    atomicAdd(loss_sum, loss);
+    if (half == 0) atomicAdd(loss_sum, loss);
   }
   if (!ok) {
     if (t == 0) atomicExch(err, 1);
@@ -555,7 +595,7 @@ cudaError_t train_window(gbrt_guide* g, const float4* samples, const int* avail,
     // weights when a render trains asynchronously, else the only copy.
     GuideNet tv = view(g);
     if (g->d_wt) tv.w = g->d_wt;
-    k_guide_train<<<grid, kRows, kTrainSmem, stream>>>(tv, samples, avail, cap, k, batch, g->d_g, g->d_loss,
+    k_guide_train<<<grid, kTrainThreads, kTrainSmem, stream>>>(tv, samples, avail, cap, k, batch, g->d_g, g->d_loss,
                                                        g->d_err);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
