@@ -30,11 +30,18 @@ def nvcc():
     raise RuntimeError("nvcc not found")
 
 
-def _compile(src):
-    obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
+# The checked build (build(checked=True)): the kernels test the indices they
+# follow and report failures in the call's status (GBRT_CHECKED in
+# csrc/gbrt_scene.h); a separate library for tests, not the product path.
+OUT_CHECKED = os.path.join(HERE, "_build_checked")
+LIB_CHECKED = os.path.join(OUT_CHECKED, "libgbrt.so")
+
+
+def _compile(src, out=OUT, extra=()):
+    obj = os.path.join(out, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
     lang = [] if src.endswith(".cu") else ["-x", "c++"]
-    cmd = [nvcc()] + ARCH + COMMON + lang + ["-c", path, "-o", obj]
+    cmd = [nvcc()] + ARCH + COMMON + list(extra) + lang + ["-c", path, "-o", obj]
     if src.endswith(".cu"):
         cmd += ["-Xptxas", "-v"] if os.environ.get("GBRT_PTXAS_VERBOSE") else []
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -43,23 +50,25 @@ def _compile(src):
     return obj, r.stderr
 
 
-def build(verbose=False):
-    os.makedirs(OUT, exist_ok=True)
+def build(verbose=False, checked=False):
+    out, lib = (OUT_CHECKED, LIB_CHECKED) if checked else (OUT, LIB)
+    extra = ("-DGBRT_CHECKED",) if checked else ()
+    os.makedirs(out, exist_ok=True)
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(_compile, SOURCES))
+        results = list(ex.map(lambda src: _compile(src, out, extra), SOURCES))
     objs = [o for o, _ in results]
     if verbose:
         for _, err in results:
             if err:
                 print(err, file=sys.stderr)
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-cudart", "static", "-Xcompiler", "-pthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    print(build(verbose="-v" in sys.argv, checked="--checked" in sys.argv))

@@ -493,6 +493,8 @@ static cudaError_t alloc_state(gbrt_scene* s, Buffers& buf, PTState& st, long lo
   if (s->view.inst) A(buf.alloc(&st.hit_inst, B));
   A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
   A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
+  st.ext_cap = int(B);
+  st.sh_cap = int(2 * B);
   if (e != cudaSuccess) return e;
   A(cudaMemsetAsync(st.tally, 0, 8 * sizeof(unsigned long long), buf.stream));
   A(cudaMemsetAsync(st.err, 0, sizeof(int), buf.stream));
@@ -537,7 +539,7 @@ static gbrt_status chain_finish(gbrt_scene* s, const char* who, const PTState& s
     stats->nonfinite = tally[2];
     stats->render_ms = ms;
   }
-  if (err) return fail(ctx, GBRT_ERR_NUMERIC, std::string(who) + ": traversal stack overflow");
+  if (err) return fail(ctx, GBRT_ERR_NUMERIC, err_text(who, err));
   return GBRT_OK;
 }
 

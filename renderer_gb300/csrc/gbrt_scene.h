@@ -73,6 +73,28 @@ struct alignas(16) DevLight {
   float intensity[3]; // BGR; for the env map: its coefficient
 };
 
+// The checked build (renderer_gb300/build.py with checked=True: -DGBRT_CHECKED)
+// tests the indices the kernels follow (tree nodes, leaf records, instances,
+// hit records, lights, materials, queue slots) before using them. A failed
+// test sets bit 2 of the call's error word and abandons that access; the
+// call then returns GBRT_ERR_NUMERIC. In the normal build the tests compile
+// away.
+#ifdef GBRT_CHECKED
+constexpr bool kChecked = true;
+#else
+constexpr bool kChecked = false;
+#endif
+constexpr int kErrStack = 1, kErrIndex = 2;  // bits of the error word
+#ifdef __CUDACC__
+__device__ __forceinline__ bool in_range(bool ok, int* err) {
+  if (kChecked && !ok) {
+    atomicOr(err, kErrIndex);
+    return false;
+  }
+  return true;
+}
+#endif
+
 // Plain-old-data view of a scene on the device, passed by value to kernels.
 struct DeviceScene {
   const float4* nodes;

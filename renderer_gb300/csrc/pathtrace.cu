@@ -114,6 +114,7 @@ struct PTState {
   float4* sh_c;    // contribution, ignore prim in w (int bits)
   int* sh_slot;
   int* counts;     // [0], [1] extension counts, [2] shadow count
+  int ext_cap, sh_cap;  // entries of each extension queue and of the shadow queue (0: not checked)
   unsigned long long* work;   // work counters of the persistent kernels
   unsigned long long* tally;  // [0] extension rays, [1] shadow rays, [2] non-finite samples
   int* err;
@@ -370,6 +371,14 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow_ms(PTState st, BatchDev 
   shadow_body<false, WT, STACK, GEN, true>(bt.scenes[0], st, bt);
 }
 
+// What the error word of a render says (bits kErrStack, kErrIndex).
+static std::string err_text(const char* who, int err) {
+  std::string m = who;
+  if (err & kErrStack) m += ": traversal stack overflow";
+  if (err & kErrIndex) m += ": index out of range (checked build)";
+  return m;
+}
+
 // A persistent grid no larger than a wavefront of `items` needs (each warp
 // fetches 32 items at a time; a shade thread takes one): small wavefronts
 // then launch a few blocks instead of a full grid that exits at once.
@@ -391,6 +400,7 @@ __device__ __forceinline__ int agg_push(int* counter) {
 
 __device__ __forceinline__ void push_ext(const PTState& st, int nxt, int slot, V3f p, V3f d) {
   int e = agg_push(&st.counts[nxt]);
+  if (!in_range(st.ext_cap == 0 || e < st.ext_cap, st.err)) return;
   st.ext[nxt][2 * e] = make_float4(p.x, p.y, p.z, kEps);
   st.ext[nxt][2 * e + 1] = make_float4(d.x, d.y, d.z, CUDART_INF_F);
   st.ext_slot[nxt][e] = slot;
@@ -459,6 +469,7 @@ __device__ __forceinline__ void nee(const DeviceScene& S, const PTParams& P, con
   V3f c = v3(alpha.x * f.x * Le.x * ac, alpha.y * f.y * Le.y * ac, alpha.z * f.z * Le.z * ac);
   if (is_zero(c)) return;
   int e = agg_push(&st.counts[2]);
+  if (!in_range(st.sh_cap == 0 || e < st.sh_cap, st.err)) return;
   st.sh_ray[2 * e] = make_float4(vx.p.x, vx.p.y, vx.p.z, kEps);
   st.sh_ray[2 * e + 1] = make_float4(sd.x, sd.y, sd.z, stmax);
   st.sh_c[e] = make_float4(c.x, c.y, c.z, __int_as_float(ignore));
@@ -480,6 +491,7 @@ __device__ __forceinline__ void shade_body(const DeviceScene& S0, const PTParams
     const DeviceScene& S = MS ? bt.scenes[job] : S0;
     const PTParams& P = MS ? bt.jobs[job].P : P0;
     const RawHit h = st.hits[q];
+    if (!in_range(h.rec < S.n_recs && h.rec >= -1 - S.n_planes, st.err)) continue;
     const float4 ro = st.ext[cur][2 * q], rd = st.ext[cur][2 * q + 1];
     int4 c = st.ctl[slot];
     int i = c.x, plen = c.y, nst = c.z;
@@ -516,6 +528,7 @@ __device__ __forceinline__ void shade_body(const DeviceScene& S0, const PTParams
         const int kind = __float_as_int(a.w);
         vx.mat = m.y;
         light = m.w;
+        if (!in_range(light < S.n_lights && vx.mat < S.n_materials, st.err)) continue;
         if (EXT && S.tri_uv) hit_texcoords(S, h.rec, h.u, h.v, vx.p, vx.tu, vx.tv);
         if (kind == kRecTriangle) {
           if (m.z >= 0) {
@@ -706,6 +719,7 @@ __device__ __forceinline__ void nee_phys(const DeviceScene& S, const PTState& st
   V3f c = v3(alpha.x * f.x * Le.x * sc, alpha.y * f.y * Le.y * sc, alpha.z * f.z * Le.z * sc);
   if (is_zero(c)) return;
   int e = agg_push(&st.counts[2]);
+  if (!in_range(st.sh_cap == 0 || e < st.sh_cap, st.err)) return;
   st.sh_ray[2 * e] = make_float4(x.x, x.y, x.z, kEps);
   st.sh_ray[2 * e + 1] = make_float4(wi.x, wi.y, wi.z, isinf(dist) ? CUDART_INF_F : dist - kEps);
   st.sh_c[e] = make_float4(c.x, c.y, c.z, __int_as_float(ignore));
@@ -763,6 +777,7 @@ __device__ __forceinline__ void shade_phys_body(const DeviceScene& S0, const PTP
     const PTParams& P = MS ? bt.jobs[job].P : P0;
     const float pChoose = MS ? (S.n_lights > 0 ? 1.f / float(S.n_lights) : 0.f) : pChoose0;
     const RawHit h = st.hits[q];
+    if (!in_range(h.rec < S.n_recs && h.rec >= -1 - S.n_planes, st.err)) continue;
     const float4 ro = st.ext[cur][2 * q], rd = st.ext[cur][2 * q + 1];
     int4 c = st.ctl[slot];
     const int i = c.x;
@@ -791,6 +806,7 @@ __device__ __forceinline__ void shade_phys_body(const DeviceScene& S0, const PTP
     const V3f x = v3(ro.x, ro.y, ro.z) + h.t * d;
     if (h.rec >= 0) {
       const int lt = __ldg(&S.meta[h.rec]).w;
+      if (!in_range(lt < S.n_lights, st.err)) continue;
       if (lt >= 0) {
         // An area light: emission on its front side (AreaLight is one-sided).
         const DevLight& Lt = S.lights[lt];
@@ -1330,6 +1346,8 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
   if (s->view.inst) A(buf.alloc(&st.hit_inst, B));
   A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
   A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
+  st.ext_cap = int(B);
+  st.sh_cap = int(2 * B);
   if (!d_sum) A(buf.alloc(&d_sum, npix * 3));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "render buffers");
   if (!keep_sums) {
@@ -1432,7 +1450,7 @@ static gbrt_status render_impl(gbrt_scene* s, const gbrt_camera* cam, const gbrt
     stats->nodes_any = tally[5];
     stats->prims_any = tally[6];
   }
-  if (err) return fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render: traversal stack overflow");
+  if (err) return fail(ctx, GBRT_ERR_NUMERIC, err_text("gbrt_render", err));
   return status;
 }
 
@@ -1538,6 +1556,8 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
   st.tally = static_cast<unsigned long long*>(at(17));
   st.err = static_cast<int*>(at(18));
   st.hit_inst = s->view.inst ? static_cast<int*>(at(19)) : nullptr;
+  st.ext_cap = int(kNoAllocBatch);
+  st.sh_cap = int(2 * kNoAllocBatch);
 
   const unsigned long long npix = (unsigned long long)cam->width * cam->height;
   const int spp = prm->x_samples * prm->y_samples;
@@ -1609,7 +1629,7 @@ static gbrt_status render_noalloc_impl(gbrt_scene* s, const gbrt_camera* cam, co
     stats->nodes_any = tally[5];
     stats->prims_any = tally[6];
   }
-  if (err) return fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render_device_noalloc: traversal stack overflow");
+  if (err) return fail(ctx, GBRT_ERR_NUMERIC, err_text("gbrt_render_device_noalloc", err));
   return GBRT_OK;
 }
 
@@ -1727,6 +1747,8 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
   if (s->view.inst) A(buf.alloc(&st.hit_inst, B));
   A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
   A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
+  st.ext_cap = int(B);
+  st.sh_cap = int(2 * B);
   long long tcap = 0;
   // Asynchronous training: the Adam steps of pass p's samples run on a second
   // stream while pass p + 1 renders. Pass p infers with the snapshot wq[p & 1]
@@ -2038,7 +2060,7 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     cudaMemsetAsync(g->d_err, 0, sizeof(int), stream);
     return fail(ctx, GBRT_ERR_TIMEOUT, "gbrt_render_guided: a tensor-core wait timed out");
   }
-  if (err) return fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render_guided: traversal stack overflow");
+  if (err) return fail(ctx, GBRT_ERR_NUMERIC, err_text("gbrt_render_guided", err));
   return status;
 }
 
@@ -2076,6 +2098,8 @@ static cudaError_t enqueue_job(gbrt_scene* s, const gbrt_camera& cam, const gbrt
   if (s->view.inst) A(buf.alloc(&st.hit_inst, B));
   A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
   A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
+  st.ext_cap = int(B);
+  st.sh_cap = int(2 * B);
   A(buf.alloc(&d_sum, npix * 3));
   if (e != cudaSuccess) return e;
   A(cudaMemsetAsync(d_sum, 0, npix * 3 * sizeof(double), stream));
@@ -2202,7 +2226,8 @@ static gbrt_status batch_impl(gbrt_ctx* ctx, const gbrt_batch_job* jobs, int n, 
     if (job_ms) job_ms[j] = ms;
     if (ev[2 * j]) cudaEventDestroy(ev[2 * j]);
     if (ev[2 * j + 1]) cudaEventDestroy(ev[2 * j + 1]);
-    if (status == GBRT_OK && h_out[j].err) status = fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render_batch: stack overflow");
+    if (status == GBRT_OK && h_out[j].err)
+      status = fail(ctx, GBRT_ERR_NUMERIC, err_text("gbrt_render_batch", h_out[j].err));
     if (stats) {
       const gbrt_camera& c = jobs[j].camera;
       stats->paths += (unsigned long long)c.width * c.height * jobs[j].params.x_samples * jobs[j].params.y_samples;
@@ -2342,6 +2367,8 @@ static gbrt_status batch_fused_impl(gbrt_ctx* ctx, const gbrt_batch_job* jobs, i
     if (anyInst) A(buf.alloc(&st.hit_inst, B));
     A(buf.alloc(&st.sh_ray, 4 * B)); A(buf.alloc(&st.sh_c, 2 * B)); A(buf.alloc(&st.sh_slot, 2 * B));
     A(buf.alloc(&st.counts, 4)); A(buf.alloc(&st.work, 4)); A(buf.alloc(&st.tally, 8)); A(buf.alloc(&st.err, 1));
+    st.ext_cap = int(B);
+    st.sh_cap = int(2 * B);
     BatchDev& bt = pipes[k].bt;
     A(buf.alloc(&pipes[k].jobs, size_t(n)));
     A(buf.alloc(&bt.job_of, size_t(B))); A(buf.alloc(&bt.cursor, 4));
@@ -2493,7 +2520,7 @@ static gbrt_status batch_fused_impl(gbrt_ctx* ctx, const gbrt_batch_job* jobs, i
     stats->device_ms = device_ms;
     stats->kernel_launches = waves * (4ull + 3ull * unsigned(D)) + 1ull;
   }
-  if (anyErr) return fail(ctx, GBRT_ERR_NUMERIC, "gbrt_render_batch_fused: traversal stack overflow");
+  if (anyErr) return fail(ctx, GBRT_ERR_NUMERIC, err_text("gbrt_render_batch_fused", anyErr));
   return GBRT_OK;
 }
 

@@ -95,6 +95,7 @@ static gbrt_status check_err_word(gbrt_ctx* ctx) {
   int err = 0;
   GBRT_CUDA_TRY(ctx, cudaMemcpyAsync(&err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GBRT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (err & kErrIndex) return fail(ctx, GBRT_ERR_NUMERIC, "trace: index out of range (checked build)");
   if (err) return fail(ctx, GBRT_ERR_NUMERIC, "traversal stack overflow (BVH deeper than supported)");
   return GBRT_OK;
 }

@@ -458,6 +458,7 @@ __device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& wr,
   const int32_t node = ts.node;
   const TRay& r = (GEN && ts.inst >= 0) ? ts.oray : wr;
   if (node >= 0) {
+    if (!in_range(node < S.n_nodes, err)) return true;
     // Offsets (in float4) of the near and far planes of each axis.
     const int nxo = r.ix >= 0.f ? 0 : 1, nyo = r.iy >= 0.f ? 2 : 3, nzo = r.iz >= 0.f ? 4 : 5;
     const float4* np = S.nodes + 8 * int64_t(node);
@@ -479,7 +480,7 @@ __device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& wr,
     cswap(k1, r1, k3, r3);
     cswap(k1, r1, k2, r2);
     if (k1 != CUDART_INF_F) {
-      if (ts.sp + 3 > STACK) { *err = 1; return true; }
+      if (ts.sp + 3 > STACK) { atomicOr(err, kErrStack); return true; }
       if (k3 != CUDART_INF_F) stack[ts.sp++] = r3;
       if (k2 != CUDART_INF_F) stack[ts.sp++] = r2;
       stack[ts.sp++] = r1;
@@ -492,6 +493,7 @@ __device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& wr,
     // Leaf.
     uint32_t lv = ~uint32_t(node);
     int64_t first = int64_t(lv >> 4), count = int64_t(lv & 15u) + 1;
+    if (!in_range(first + count <= S.n_recs, err)) return true;
     for (int64_t k = first; k < first + count; ++k) {
       const float4* rp = S.recs + 3 * k;
       float4 a = __ldg(rp + 0), b = __ldg(rp + 1), c = __ldg(rp + 2);
@@ -514,11 +516,12 @@ __device__ __forceinline__ bool trace_step(const DeviceScene& S, const TRay& wr,
         hit = pgram_test(r, a, b, c, tlim, t, u, v);
       } else if (kind == kRecInstance) {
         // The rest of this leaf after the instance, then the way back.
-        if (ts.sp + 2 > STACK) { *err = 1; return true; }
+        if (ts.sp + 2 > STACK) { atomicOr(err, kErrStack); return true; }
         const int64_t rest = first + count - (k + 1);
         if (rest > 0) stack[ts.sp++] = ~int32_t(uint32_t(k + 1) << 4 | uint32_t(rest - 1));
         stack[ts.sp++] = kInstPop;
         const int in = __float_as_int(b.x);
+        if (!in_range(in >= 0 && in < S.n_inst, err)) return true;
         const float4* M = S.inst + 4 * int64_t(in);
         ts.oray = instance_ray(wr, __ldg(M), __ldg(M + 1), __ldg(M + 2));
         ts.inst = in;

@@ -114,3 +114,46 @@ def test_icosphere_frame_path_level(ctx):
     med = np.median(np.abs(a[~close] - b[~close]) / np.maximum(b[~close], 1e-3)) if (~close).any() else 0.0
     assert med < 1.0
     assert st.extension_rays <= o["rays"]
+
+
+def test_relmse_against_a_65536_sample_fp64_render(ctx):
+    """The image error the renderer's own benchmark states, at its stated
+    sample count: a 65,536-spp FP64-accumulated reference of the Cornell box
+    (64 x 64 pixels here, so that the reference takes a fraction of a second),
+    accumulated in 16 resumable passes of 64 x 64 samples (gbrt_render_passes),
+    against which the GPU's and the oracle's 16-sample images (independent
+    streams) have the same relMSE, the GPU's mean equals the reference's, and
+    relMSE falls as 1 / spp from 16 to 256 samples."""
+    import ctypes as C
+
+    import torch
+
+    import renderer_gb300 as rg
+    from renderer_gb300 import GpuScene, _abi
+    s = workloads.cornell_box(64, 64)
+    gs = GpuScene(ctx, s)
+    cam = s.camera_struct()
+    n3 = 64 * 64 * 3
+    film = torch.zeros(n3, dtype=torch.float32, device="cuda")
+    sums = torch.zeros(n3, dtype=torch.float64, device="cuda")
+    p = workloads.cornell_params(8, seed=4242, x_samples=64, y_samples=64)
+    st = _abi.Stats()
+    for first in (0, 8):  # two calls of 8 passes: the second resumes from the first's sums
+        rg.check(rg.lib().gbrt_render_passes(gs.handle, C.byref(cam), C.byref(p), first, 8,
+                                             C.c_void_p(film.data_ptr()), C.c_void_p(sums.data_ptr()), None,
+                                             C.byref(st)), ctx.handle)
+    ref = (sums.cpu().numpy() / 65536.0).reshape(64, 64, 3)
+    np.testing.assert_allclose(film.cpu().numpy().reshape(64, 64, 3), ref, rtol=1e-6, atol=1e-9)
+    errs = []
+    for spp_side, seed in ((4, 7), (8, 8), (16, 9)):
+        img, _, _, _ = gpu_render(ctx, s, workloads.cornell_params(8, seed=seed, x_samples=spp_side,
+                                                                   y_samples=spp_side))
+        errs.append(relmse(img, ref))
+    o = OracleScene(s).render(cam, workloads.cornell_params(8, seed=7), rng_mode=0)
+    eo = relmse(o["film"], ref)
+    assert errs[0] / eo == pytest.approx(1.0, abs=0.15), (errs[0], eo)
+    # 16 -> 64 -> 256 samples: about 4x less error per step (caustics through
+    # the glass sphere make the error heavy-tailed, hence the wide bounds)
+    assert 2.0 < errs[0] / errs[1] < 8.0 and 2.0 < errs[1] / errs[2] < 8.0, errs
+    img, _, _, _ = gpu_render(ctx, s, workloads.cornell_params(8, seed=7))
+    assert img.mean() / ref.mean() == pytest.approx(1.0, abs=0.02)
