@@ -686,12 +686,15 @@ def run_instanced(args):
     """The instanced-terrain scene: 16 views of 3840 x 2160 at one sample per
     pixel in one gbrt_render_batch call (a step = all 16 images). value =
     paths / device span; e2e = paths / host wall time of the call, the 16
-    films (1.6 GB) copied to host memory. --compare-flat also renders the
+    films (1.6 GB) copied to host memory. --single-launch renders the 16
+    views in one gbrt_render_batch_fused call instead (every kernel launch
+    serves all views, one CUDA graph per wavefront, autotuned schedule) and
+    reports the stream scheduler beside it. --compare-flat also renders the
     same views of the scene with every instance flattened into one tree."""
     import numpy as np
 
     from renderer_gb300 import _abi, workloads
-    from renderer_gb300.batch import BatchJob, render_batch
+    from renderer_gb300.batch import BatchJob, autotune_fused, render_batch, render_batch_fused
     from renderer_gb300.runtime import Context, GpuScene
     from renderer_gb300.scene import SceneData, render_params
 
@@ -704,22 +707,30 @@ def run_instanced(args):
     create_s = time.perf_counter() - t
     info = gs.info()
 
-    def measure(scene, tag):
+    def measure(scene, tag, fused=False):
         jobs = []
         for i, c in enumerate(cams):
             sc = SceneData()
             sc.camera = c
             jobs.append(BatchJob(scene, sc.camera_struct(),
                                  render_params(1, 1, 0.5, 16, 100 + i, semantics=_abi.SEM_PHYSICAL)))
+        tuned = None
+        if fused:
+            t0 = time.perf_counter()
+            tuned = autotune_fused(ctx, jobs)
+            tuned["autotune_s"] = time.perf_counter() - t0
+            call = lambda: render_batch_fused(ctx, jobs)  # noqa: E731
+        else:
+            call = lambda: render_batch(ctx, jobs, streams=4)  # noqa: E731
         for _ in range(args.warmup):
-            render_batch(ctx, jobs, streams=4)
+            call()
         clocks = ClockSampler(0)
         clocks.start()
         time.sleep(0.3)
         dev, wall, paths, ext, sh = 0.0, 0.0, 0, 0, 0
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            films, _, st = render_batch(ctx, jobs, streams=4)
+            films, _, st = call()
             wall += time.perf_counter() - t0
             dev += st.device_ms / 1000.0
             paths += st.paths
@@ -729,9 +740,19 @@ def run_instanced(args):
         return {"value": paths / dev, "e2e": paths / wall, "ms_per_step": 1000 * dev / args.steps,
                 "rays_per_s": (ext + sh) / dev, "extension_rays_per_path": ext / paths,
                 "shadow_rays_per_path": sh / paths, "clocks": clk, "film_mean": float(films[0].mean()),
-                "launches": st.kernel_launches}
+                "launches": st.kernel_launches, "schedule": tuned}
 
     r = measure(gs, "two-level")
+    designs = None
+    if args.single_launch:
+        rf = measure(gs, "two-level", fused=True)
+        designs = {"single_launch": {"paths_per_s": rf["value"], "e2e_paths_per_s": rf["e2e"],
+                                     "ms_per_step": rf["ms_per_step"], "kernel_launches_per_step": rf["launches"],
+                                     "film_mean_view0": rf["film_mean"], **rf["schedule"]},
+                   "streams": {"paths_per_s": r["value"], "e2e_paths_per_s": r["e2e"],
+                               "ms_per_step": r["ms_per_step"], "kernel_launches_per_step": r["launches"],
+                               "film_mean_view0": r["film_mean"], "streams": 4}}
+        r = rf
     tri = len(s.meshes[0]["pos"]) * len(s.instances)
     line = {"metric": "paths/s (instanced terrain, 16 views)", "value": r["value"], "unit": "paths/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
@@ -741,10 +762,14 @@ def run_instanced(args):
                        "scene_generation_s": gen_s, "scene_create_s": create_s, "bvh_nodes": info["nodes"],
                        "rays_per_s": r["rays_per_s"], "extension_rays_per_path": r["extension_rays_per_path"],
                        "shadow_rays_per_path": r["shadow_rays_per_path"],
-                       "l2": "inputs larger than L2 (mesh 4M triangles, path state per stream > 129 MB)"},
+                       "l2": "inputs larger than L2 (mesh 4M triangles, path state per stream > 129 MB)",
+                       "scheduler": "single launch (shared wavefronts, CUDA graph per wavefront)" if designs
+                       else "streams (one wavefront pipeline per view)"},
             "e2e": {"value": r["e2e"], "unit": "paths/s", "h2d_bytes_per_step": 16 * C.sizeof(_abi.BatchJob),
                     "d2h_bytes_per_step": 16 * cams[0]["width"] * cams[0]["height"] * 12},
             "gpu_launches": r["launches"] * args.steps, "clocks": r["clocks"]}
+    if designs:
+        line["config"]["designs"] = designs
     if args.guided_views:
         line["guided_views"] = guided_views(args, ctx, gs, cams)
     if args.compare_flat:
