@@ -53,13 +53,14 @@ constexpr int kInferBuf = kRows * kEncA * 8 * 2;
 constexpr int kInferMisc = kSWEnd + kInferWG * kInferBuf, kInferSmem = kInferMisc + 8 * kInferWG + 16;
 constexpr uint32_t kInferCols = 512;  // 64 per warpgroup, rounded up to a power of two
 
-// Training: weights, transposed weights for dX, three activation tiles, the
-// region R (X0 rows in the forward pass, then the transposed X1..X3 at
-// offsets 0, 16 KB, 32 KB and finally the transposed X0), delta rows and
-// delta^T.
+// Training: weights, transposed weights for dX, the activation rows X1..X3,
+// the region R (the encoded input X0 rows, 53,248 bytes, kept for the weight
+// gradient of layer 1) and the delta rows. The weight gradients read the
+// activation and delta rows as they are (MN-major operands, gemm_mn), so no
+// tile is stored twice.
 constexpr int kTW2T = 49152, kTW3T = 57344, kTW4T = 65536;
-constexpr int kTX1 = 71680, kTX2 = 88064, kTX3 = 104448, kTR = 120832, kTDR = 186368, kTDT = 202752;
-constexpr int kTMisc = 219136, kTrainSmem = kTMisc + 64;
+constexpr int kTX1 = 71680, kTX2 = 88064, kTX3 = 104448, kTR = 120832, kTDR = 186368;
+constexpr int kTMisc = 202752, kTrainSmem = kTMisc + 64;
 constexpr uint32_t kTrainCols = 512;
 constexpr int kTrainThreads = 2 * kRows;  // two threads per row of a tile
 // TMEM columns of the training kernel.
@@ -279,15 +280,9 @@ __device__ __forceinline__ float loss_grad(const float* o, float wx, float wy, f
   return -w * lq;
 }
 
-// Writes v (nv values of row r, features k0 .. k0 + nv - 1) transposed:
-// element (k, r) of a [rows][128] batch-contiguous tile at s.
-__device__ __forceinline__ void write_transposed(uint32_t s, int r, const float* v, int nv, int k0 = 0) {
-  for (int k = 0; k < nv; ++k) st_shared_u16(s + ik_off(k0 + k, r, kRows), bf16_bits(v[k]));
-}
-
 // Half of a hidden layer's input for row r: ReLU(TMEM columns [c0, c0 + 32))
-// into an interleaved [128][64] tile at s, the values kept in h.
-__device__ __forceinline__ void hidden_half_to_smem(uint32_t lane_taddr, uint32_t s, int r, int c0, float* h) {
+// into an interleaved [128][64] tile at s.
+__device__ __forceinline__ void hidden_half_to_smem(uint32_t lane_taddr, uint32_t s, int r, int c0) {
   float v[32];
   tmem_ld32(lane_taddr + c0, v);
 #pragma unroll
@@ -295,15 +290,12 @@ __device__ __forceinline__ void hidden_half_to_smem(uint32_t lane_taddr, uint32_
     st_shared_v4(s + ik_off(r, c0 + 8 * q, kHid), pack_relu_bf16(v[8 * q], v[8 * q + 1]),
                  pack_relu_bf16(v[8 * q + 2], v[8 * q + 3]), pack_relu_bf16(v[8 * q + 4], v[8 * q + 5]),
                  pack_relu_bf16(v[8 * q + 6], v[8 * q + 7]));
-#pragma unroll
-  for (int i = 0; i < 32; ++i) h[i] = fmaxf(v[i], 0.f);
 }
 
 // delta = ReLU'(X) * dX for row r, features [c0, c0 + 32): dX from TMEM
-// scratch, X from the row tile. Writes delta rows (when s_rows != 0) and
-// delta^T.
-__device__ __forceinline__ void backprop_delta_half(uint32_t lane_taddr, const uint8_t* xrow, uint32_t s_rows,
-                                                    uint32_t s_t, int r, int c0) {
+// scratch, X from the row tile; the delta rows go to the tile at s_rows.
+__device__ __forceinline__ void backprop_delta_half(uint32_t lane_taddr, const uint8_t* xrow, uint32_t s_rows, int r,
+                                                    int c0) {
   float x[32], d[32];
 #pragma unroll
   for (int c = 0; c < 32; c += 8) {
@@ -319,17 +311,14 @@ __device__ __forceinline__ void backprop_delta_half(uint32_t lane_taddr, const u
   tmem_ld32(lane_taddr + c0, d);
 #pragma unroll
   for (int k = 0; k < 32; ++k) d[k] = x[k] > 0.f ? d[k] : 0.f;
-  if (s_rows) {
 #pragma unroll
-    for (int c = 0; c < 32; c += 8)
-      st_shared_v4(s_rows + ik_off(r, c0 + c, kHid), pack_bf16(d[c], d[c + 1]), pack_bf16(d[c + 2], d[c + 3]),
-                   pack_bf16(d[c + 4], d[c + 5]), pack_bf16(d[c + 6], d[c + 7]));
-  }
-  write_transposed(s_t, r, d, 32, c0);
+  for (int c = 0; c < 32; c += 8)
+    st_shared_v4(s_rows + ik_off(r, c0 + c, kHid), pack_bf16(d[c], d[c + 1]), pack_bf16(d[c + 2], d[c + 3]),
+                 pack_bf16(d[c + 4], d[c + 5]), pack_bf16(d[c + 6], d[c + 7]));
 }
 
-// Encoding groups [G0, G1) of row r into the full [128][208] row tile, and
-// transposed into the [208][128] tile (both at groups' own feature offsets).
+// Encoding groups [G0, G1) of row r into the full [128][208] row tile (at
+// the groups' own feature offsets).
 template <int G0, int G1>
 __device__ __forceinline__ void write_enc_rows(uint32_t s, int r, const EncIn& e) {
 #pragma unroll
@@ -340,17 +329,6 @@ __device__ __forceinline__ void write_enc_rows(uint32_t s, int r, const EncIn& e
                  pack_bf16(f[6], f[7]));
   }
 }
-template <int G0, int G1>
-__device__ __forceinline__ void write_enc_transposed(uint32_t s, int r, const EncIn& e) {
-#pragma unroll
-  for (int g = G0; g < G1; ++g) {
-    float fv[8];
-    enc_group(e, g, fv);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) st_shared_u16(s + ik_off(8 * g + q, r, kRows), bf16_bits(fv[q]));
-  }
-}
-
 // One optimizer step's gradient over a window of the sample buffer: with
 // n_avail = min(*avail, cap) samples written (n_avail = cap when avail is
 // null), step k uses samples [start, start + n) with start = k * batch mod
@@ -359,10 +337,12 @@ __device__ __forceinline__ void write_enc_transposed(uint32_t s, int r, const En
 //
 // Two threads per row (threads t and t + 128, halves 0 and 1, in warps w and
 // w + 4, which read the same TMEM lanes): each encodes 13 of the 26 feature
-// groups, reads back, activates and transposes 32 of a hidden layer's 64
-// columns, and back-propagates 32 of its deltas; the output layer's loss and
-// gradient are computed by half 0. Eight warps per SM instead of four hide
-// more of the per-tile chain's latency.
+// groups, reads back and activates 32 of a hidden layer's 64 columns, and
+// back-propagates 32 of its deltas; the output layer's loss and gradient are
+// computed by half 0. Eight warps per SM instead of four hide more of the
+// per-tile chain's latency. Weight gradients dW^T = X^T delta read the
+// activation and delta rows MN-major (gemm_mn): the batch rows are the
+// reduction, and the products accumulate in TMEM across the block's tiles.
 __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideNet net, const float4* __restrict__ base,
                                                                   const int* __restrict__ avail, int cap, int k,
                                                                   int batch, float* __restrict__ grad,
@@ -375,8 +355,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideNet net, 
   const uint32_t sW1 = smem_u32(sm + kSW1), sW2 = smem_u32(sm + kSW2), sW3 = smem_u32(sm + kSW3),
                  sW4 = smem_u32(sm + kSW4), sW2T = smem_u32(sm + kTW2T), sW3T = smem_u32(sm + kTW3T),
                  sW4T = smem_u32(sm + kTW4T), sX1 = smem_u32(sm + kTX1), sX2 = smem_u32(sm + kTX2),
-                 sX3 = smem_u32(sm + kTX3), sR = smem_u32(sm + kTR), sDR = smem_u32(sm + kTDR),
-                 sDT = smem_u32(sm + kTDT);
+                 sX3 = smem_u32(sm + kTX3), sR = smem_u32(sm + kTR), sDR = smem_u32(sm + kTDR);
   load_weights(sm + kSW1, net.w + kOffW1, kHid, kIn, kHid, false);
   load_weights(sm + kSW2, net.w + kOffW2, kHid, kHid, kHid, false);
   load_weights(sm + kSW3, net.w + kOffW3, kHid, kHid, kHid, false);
@@ -427,22 +406,18 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideNet net, 
     if (half == 0) write_enc_rows<0, kIn / 16>(sR, r, e);
     else write_enc_rows<kIn / 16, kIn / 8>(sR, r, e);
     // ---- forward
-    float hv[32];
     handoff();
     if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sR, kIn, sW1, kIn, kIn, kHid, false);
     if (!(ok = sync_chain())) break;
-    hidden_half_to_smem(lane + kColScratch, sX1, r, c0, hv);
-    write_transposed(sR, r, hv, 32, c0);  // X1^T at R + 0
+    hidden_half_to_smem(lane + kColScratch, sX1, r, c0);
     handoff();
     if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sX1, kHid, sW2, kHid, kHid, kHid, false);
     if (!(ok = sync_chain())) break;
-    hidden_half_to_smem(lane + kColScratch, sX2, r, c0, hv);
-    write_transposed(sR + 16384, r, hv, 32, c0);  // X2^T
+    hidden_half_to_smem(lane + kColScratch, sX2, r, c0);
     handoff();
     if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sX2, kHid, sW3, kHid, kHid, kHid, false);
     if (!(ok = sync_chain())) break;
-    hidden_half_to_smem(lane + kColScratch, sX3, r, c0, hv);
-    write_transposed(sR + 32768, r, hv, 32, c0);  // X3^T
+    hidden_half_to_smem(lane + kColScratch, sX3, r, c0);
     handoff();
     if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sX3, kHid, sW4, kHid, kHid, kOutPad, false);
     if (!(ok = sync_chain())) break;
@@ -459,42 +434,36 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideNet net, 
       for (int c = 0; c < kOutPad; c += 8)
         st_shared_v4(sDR + ik_off(r, c, kOutPad), pack_bf16(g[c], g[c + 1]), pack_bf16(g[c + 2], g[c + 3]),
                      pack_bf16(g[c + 4], g[c + 5]), pack_bf16(g[c + 6], g[c + 7]));
-      write_transposed(sDT, r, g, kOutPad);
-    } else {
-      // the other half meanwhile: the encoding's second half, transposed, is
-      // not needed until layer 1's weight gradient; nothing to do here
     }
     // ---- backward: output layer
     handoff();
     if (t == 0 && net.issue) {
-      gemm_k(tmem + kColW4, sR + 32768, kRows, sDT, kRows, kRows, kOutPad, !first);
+      gemm_mn(tmem + kColW4, sX3, kHid, sDR, kOutPad, kRows, kOutPad, !first);
       gemm_k(tmem + kColScratch, sDR, kOutPad, sW4T, kOutPad, kOutPad, kHid, false);
     }
     if (!(ok = sync_chain())) break;
-    backprop_delta_half(lane + kColScratch, sm + kTX3, sDR, sDT, r, c0);
+    backprop_delta_half(lane + kColScratch, sm + kTX3, sDR, r, c0);
     // ---- layer 3
     handoff();
     if (t == 0 && net.issue) {
-      gemm_k(tmem + kColW3, sR + 16384, kRows, sDT, kRows, kRows, kHid, !first);
+      gemm_mn(tmem + kColW3, sX2, kHid, sDR, kHid, kRows, kHid, !first);
       gemm_k(tmem + kColScratch, sDR, kHid, sW3T, kHid, kHid, kHid, false);
     }
     if (!(ok = sync_chain())) break;
-    backprop_delta_half(lane + kColScratch, sm + kTX2, sDR, sDT, r, c0);
+    backprop_delta_half(lane + kColScratch, sm + kTX2, sDR, r, c0);
     // ---- layer 2
     handoff();
     if (t == 0 && net.issue) {
-      gemm_k(tmem + kColW2, sR, kRows, sDT, kRows, kRows, kHid, !first);
+      gemm_mn(tmem + kColW2, sX1, kHid, sDR, kHid, kRows, kHid, !first);
       gemm_k(tmem + kColScratch, sDR, kHid, sW2T, kHid, kHid, kHid, false);
     }
     if (!(ok = sync_chain())) break;
-    backprop_delta_half(lane + kColScratch, sm + kTX1, 0u, sDT, r, c0);
-    // ---- layer 1: the encoding again, transposed, into R
-    if (half == 0) write_enc_transposed<0, kIn / 16>(sR, r, e);
-    else write_enc_transposed<kIn / 16, kIn / 8>(sR, r, e);
+    backprop_delta_half(lane + kColScratch, sm + kTX1, sDR, r, c0);
+    // ---- layer 1: input features 0..127 and 128..207 (M = 128 each)
     handoff();
     if (t == 0 && net.issue) {
-      gemm_k(tmem + kColW1lo, sR, kRows, sDT, kRows, kRows, kHid, !first);
-      gemm_k(tmem + kColW1hi, sR + ik_off(kRows, 0, kRows), kRows, sDT, kRows, kRows, kHid, !first);
+      gemm_mn(tmem + kColW1lo, sR, kIn, sDR, kHid, kRows, kHid, !first);
+      gemm_mn(tmem + kColW1hi, sR + 16 * 128, kIn, sDR, kHid, kRows, kHid, !first);
     }
     if (!(ok = sync_chain())) break;
     first = false;

@@ -108,6 +108,24 @@ __device__ __forceinline__ void gemm_k(uint32_t d_tmem, uint32_t sa, int Ka, uin
   }
 }
 
+// A^T B for two interleaved row tiles whose rows are the reduction (the
+// batch): A at sa holds K rows of Ma features, B at sb K rows of Nb features
+// (both laid out by ik_off). Both operands are read MN-major (instruction
+// descriptor bits 15 and 16): a core matrix is 8 rows x 8 consecutive
+// features, the next 8 features 128 bytes on (stride byte offset), the next
+// 8 rows one row group of the tile on (leading byte offset, features x 16).
+// D[m][n] = sum_k A[k][m] B[k][n] with M = 128: rows m >= Ma read the
+// following row group and are not used. Issued by one thread.
+__device__ __forceinline__ void gemm_mn(uint32_t d_tmem, uint32_t sa, int Ma, uint32_t sb, int Nb, int K, int N,
+                                        bool accumulate) {
+  const uint32_t idesc = idesc_bf16(128, N) | (1u << 15) | (1u << 16);
+  for (int kk = 0; kk < K / 16; ++kk) {
+    uint64_t da = smem_desc(sa + kk * 2 * uint32_t(Ma) * 16, uint32_t(Ma) * 16, 128);
+    uint64_t db = smem_desc(sb + kk * 2 * uint32_t(Nb) * 16, uint32_t(Nb) * 16, 128);
+    mma_bf16(d_tmem, da, db, idesc, (accumulate || kk > 0) ? 1u : 0u);
+  }
+}
+
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
