@@ -9,20 +9,22 @@
 // estimated by the tracer's own radiance samples:
 //   loss = -(1/N) sum_s w_s log q(wi_s),   w_s = target_s / pdf_s.
 //
-// Both kernels process tiles of 128 rows, one row per thread of a 128-thread
-// block. Per layer: the threads write the layer input (BF16) into shared
-// memory; one thread issues the tcgen05.mma chain (M = 128, N = layer width,
-// K in steps of 16) into TMEM and commits it to an mbarrier; after the wait
-// every warp reads its 32 TMEM lanes back (tcgen05.ld 32x32b), applies the
-// activation and writes the next layer's input.
+// Both kernels process tiles of 128 rows. Per layer: the threads write the
+// layer input (BF16) into shared memory; one thread issues the tcgen05.mma
+// chain (M = 128, N = layer width, K in steps of 16) into TMEM and commits it
+// to an mbarrier; after the wait every warp reads its 32 TMEM lanes back
+// (tcgen05.ld 32x32b), applies the activation and writes the next layer's
+// input.
 //
-// Training keeps, for the backward pass, the hidden activations both row-wise
-// (for the next layer's product) and transposed (batch-contiguous, for the
-// weight gradients), and computes every product as a K-major A times a
-// K-major B^T:
-//   dX_l   = delta_{l+1} W_{l+1}           A = delta rows, B = W^T
-//   dW_l^T += X_{l-1}^T delta_l            A = X^T (features padded to 128
-//                                          rows), B = delta^T (batch-contiguous)
+// Training keeps, for the backward pass, the encoded input, the hidden
+// activations and the deltas once each, row-wise, and reads the same tiles
+// in the operand order each product needs:
+//   forward  X_l     = ReLU(X_{l-1} W_l^T)    A = X rows, B = W (K-major)
+//   dX_l   = delta_{l+1} W_{l+1}              A = delta rows (K-major),
+//                                             B = W read MN-major
+//   dW_l^T += X_{l-1}^T delta_l               A = X rows, B = delta rows,
+//                                             both MN-major (the batch rows
+//                                             are the reduction; M = 128)
 // The weight-gradient accumulators stay in TMEM across all tiles of a block
 // and are added to global memory once at the end.
 #include <cuda_bf16.h>
@@ -53,14 +55,13 @@ constexpr int kInferBuf = kRows * kEncA * 8 * 2;
 constexpr int kInferMisc = kSWEnd + kInferWG * kInferBuf, kInferSmem = kInferMisc + 8 * kInferWG + 16;
 constexpr uint32_t kInferCols = 512;  // 64 per warpgroup, rounded up to a power of two
 
-// Training: weights, transposed weights for dX, the activation rows X1..X3,
-// the region R (the encoded input X0 rows, 53,248 bytes, kept for the weight
-// gradient of layer 1) and the delta rows. The weight gradients read the
-// activation and delta rows as they are (MN-major operands, gemm_mn), so no
-// tile is stored twice.
-constexpr int kTW2T = 49152, kTW3T = 57344, kTW4T = 65536;
-constexpr int kTX1 = 71680, kTX2 = 88064, kTX3 = 104448, kTR = 120832, kTDR = 186368;
-constexpr int kTMisc = 202752, kTrainSmem = kTMisc + 64;
+// Training: the weights, the activation rows X1..X3, the region R (the
+// encoded input X0 rows, 53,248 bytes, kept for the weight gradient of
+// layer 1) and the delta rows. Every tile is stored once: the weight
+// gradients read the activation and delta rows MN-major (gemm_mn), the dX
+// products the weights MN-major (gemm_k_wmn).
+constexpr int kTX1 = 49152, kTX2 = 65536, kTX3 = 81920, kTR = 98304, kTDR = 151552;
+constexpr int kTMisc = 167936, kTrainSmem = kTMisc + 64;
 constexpr uint32_t kTrainCols = 512;
 constexpr int kTrainThreads = 2 * kRows;  // two threads per row of a tile
 // TMEM columns of the training kernel.
@@ -72,7 +73,7 @@ static_assert(64 * kInferWG <= int(kInferCols), "TMEM columns of the inference b
 static_assert(kEncA + kEncB == kIn / 8, "encoding halves");
 
 // Layer input ReLU(TMEM columns [0, 64)) of row r into an interleaved
-// [128][64] tile at s; also returns the values (for the transposed copy).
+// [128][64] tile at s; also returns the values when h is not null.
 __device__ __forceinline__ void hidden_to_smem(uint32_t lane_taddr, uint32_t s, int r, float* h) {
 #pragma unroll
   for (int c = 0; c < kHid; c += 32) {
@@ -145,10 +146,10 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
   const uint32_t sW1 = smem_u32(sm + kSW1), sW2 = smem_u32(sm + kSW2), sW3 = smem_u32(sm + kSW3),
                  sW4 = smem_u32(sm + kSW4), sX = smem_u32(sm + kSWEnd + wg * kInferBuf), bar = smem_u32(mbar);
   const int bid = 1 + wg;  // named barrier of this warpgroup
-  load_weights(sm + kSW1, net.w + kOffW1, kHid, kIn, kHid, false);
-  load_weights(sm + kSW2, net.w + kOffW2, kHid, kHid, kHid, false);
-  load_weights(sm + kSW3, net.w + kOffW3, kHid, kHid, kHid, false);
-  load_weights(sm + kSW4, net.w + kOffW4, kOut, kHid, kOutPad, false);
+  load_weights(sm + kSW1, net.w + kOffW1, kHid, kIn, kHid);
+  load_weights(sm + kSW2, net.w + kOffW2, kHid, kHid, kHid);
+  load_weights(sm + kSW3, net.w + kOffW3, kHid, kHid, kHid);
+  load_weights(sm + kSW4, net.w + kOffW4, kOut, kHid, kOutPad);
   if (t == 0) mbar_init(bar, 1);
   if (warp == 0) tmem_alloc(smem_u32(tslot), kInferCols);
   handoff();
@@ -353,16 +354,12 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideNet net, 
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + kTMisc + 8);
   const uint32_t bar = smem_u32(mbar);
   const uint32_t sW1 = smem_u32(sm + kSW1), sW2 = smem_u32(sm + kSW2), sW3 = smem_u32(sm + kSW3),
-                 sW4 = smem_u32(sm + kSW4), sW2T = smem_u32(sm + kTW2T), sW3T = smem_u32(sm + kTW3T),
-                 sW4T = smem_u32(sm + kTW4T), sX1 = smem_u32(sm + kTX1), sX2 = smem_u32(sm + kTX2),
+                 sW4 = smem_u32(sm + kSW4), sX1 = smem_u32(sm + kTX1), sX2 = smem_u32(sm + kTX2),
                  sX3 = smem_u32(sm + kTX3), sR = smem_u32(sm + kTR), sDR = smem_u32(sm + kTDR);
-  load_weights(sm + kSW1, net.w + kOffW1, kHid, kIn, kHid, false);
-  load_weights(sm + kSW2, net.w + kOffW2, kHid, kHid, kHid, false);
-  load_weights(sm + kSW3, net.w + kOffW3, kHid, kHid, kHid, false);
-  load_weights(sm + kSW4, net.w + kOffW4, kOut, kHid, kOutPad, false);
-  load_weights(sm + kTW2T, net.w + kOffW2, kHid, kHid, kHid, true);
-  load_weights(sm + kTW3T, net.w + kOffW3, kHid, kHid, kHid, true);
-  load_weights(sm + kTW4T, net.w + kOffW4, kOut, kHid, kOutPad, true);
+  load_weights(sm + kSW1, net.w + kOffW1, kHid, kIn, kHid);
+  load_weights(sm + kSW2, net.w + kOffW2, kHid, kHid, kHid);
+  load_weights(sm + kSW3, net.w + kOffW3, kHid, kHid, kHid);
+  load_weights(sm + kSW4, net.w + kOffW4, kOut, kHid, kOutPad);
   if (t == 0) mbar_init(bar, 1);
   if (warp == 0) tmem_alloc(smem_u32(tslot), kTrainCols);
   handoff();
@@ -439,7 +436,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideNet net, 
     handoff();
     if (t == 0 && net.issue) {
       gemm_mn(tmem + kColW4, sX3, kHid, sDR, kOutPad, kRows, kOutPad, !first);
-      gemm_k(tmem + kColScratch, sDR, kOutPad, sW4T, kOutPad, kOutPad, kHid, false);
+      gemm_k_wmn(tmem + kColScratch, sDR, kOutPad, sW4, kHid, kOutPad, kHid, false);
     }
     if (!(ok = sync_chain())) break;
     backprop_delta_half(lane + kColScratch, sm + kTX3, sDR, r, c0);
@@ -447,7 +444,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideNet net, 
     handoff();
     if (t == 0 && net.issue) {
       gemm_mn(tmem + kColW3, sX2, kHid, sDR, kHid, kRows, kHid, !first);
-      gemm_k(tmem + kColScratch, sDR, kHid, sW3T, kHid, kHid, kHid, false);
+      gemm_k_wmn(tmem + kColScratch, sDR, kHid, sW3, kHid, kHid, kHid, false);
     }
     if (!(ok = sync_chain())) break;
     backprop_delta_half(lane + kColScratch, sm + kTX2, sDR, r, c0);
@@ -455,7 +452,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideNet net, 
     handoff();
     if (t == 0 && net.issue) {
       gemm_mn(tmem + kColW2, sX1, kHid, sDR, kHid, kRows, kHid, !first);
-      gemm_k(tmem + kColScratch, sDR, kHid, sW2T, kHid, kHid, kHid, false);
+      gemm_k_wmn(tmem + kColScratch, sDR, kHid, sW2, kHid, kHid, kHid, false);
     }
     if (!(ok = sync_chain())) break;
     backprop_delta_half(lane + kColScratch, sm + kTX1, sDR, r, c0);

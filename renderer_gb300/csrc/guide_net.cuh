@@ -14,10 +14,12 @@
 // matrices [out][in] one after the other: W1 64x208, W2 64x64, W3 64x64,
 // W4 40x64 (24,064 values).
 //
-// Shared-memory operand layout (tcgen05 "no swizzle", K-major): an R x K
-// BF16 tile is stored as 8 x 8 core matrices of 128 contiguous bytes; the
-// K/8 core matrices of one 8-row group are adjacent (leading byte offset 128)
-// and row groups follow each other (stride byte offset 16 K).
+// Shared-memory operand layout (tcgen05 "no swizzle"): an R x K BF16 tile is
+// stored as 8 x 8 core matrices of 128 contiguous bytes; the K/8 core
+// matrices of one 8-row group are adjacent (leading byte offset 128) and row
+// groups follow each other (stride byte offset 16 K). Read K-major, the rows
+// are M or N; read MN-major (gemm_mn, gemm_k_wmn), the same tile's rows are
+// the reduction and its K columns are M or N.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -126,6 +128,19 @@ __device__ __forceinline__ void gemm_mn(uint32_t d_tmem, uint32_t sa, int Ma, ui
   }
 }
 
+// A (128 x K at sa, K-major as in gemm_k) times B, where B is a weight row
+// tile W [K rows][Nw features] read MN-major: D[m][n] = sum_k A[m][k] W[k][n]
+// (the product with W itself rather than its transpose), N = Nw columns.
+__device__ __forceinline__ void gemm_k_wmn(uint32_t d_tmem, uint32_t sa, int Ka, uint32_t sw, int Nw, int K, int N,
+                                           bool accumulate) {
+  const uint32_t idesc = idesc_bf16(128, N) | (1u << 16);
+  for (int kk = 0; kk < K / 16; ++kk) {
+    uint64_t da = smem_desc(sa + kk * 256, 128, uint32_t(Ka) * 16);
+    uint64_t db = smem_desc(sw + kk * 2 * uint32_t(Nw) * 16, uint32_t(Nw) * 16, 128);
+    mma_bf16(d_tmem, da, db, idesc, (accumulate || kk > 0) ? 1u : 0u);
+  }
+}
+
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -216,28 +231,16 @@ __device__ __forceinline__ uint16_t bf16_bits(float a) {
 }
 
 // Copies a row-major [N][K] BF16 matrix from global memory into the
-// interleaved K-major layout at sbase (rows N..Npad-1 zero); with transpose,
-// stores W^T ([K][N]) instead. All threads of the block take part.
-__device__ __forceinline__ void load_weights(uint8_t* sbase, const __nv_bfloat16* g, int N, int K, int Npad,
-                                             bool transpose) {
+// interleaved layout at sbase (rows N..Npad-1 zero). All threads of the block
+// take part.
+__device__ __forceinline__ void load_weights(uint8_t* sbase, const __nv_bfloat16* g, int N, int K, int Npad) {
   const uint32_t s = smem_u32(sbase);
-  if (!transpose) {
-    const int chunks = Npad * (K / 8);
-    for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
-      int n = c / (K / 8), k8 = c % (K / 8);
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (n < N) v = *reinterpret_cast<const uint4*>(g + size_t(n) * K + k8 * 8);
-      st_shared_v4(s + ik_off(n, k8 * 8, K), v.x, v.y, v.z, v.w);
-    }
-  } else {
-    // W^T: rows = K (inputs), columns = Npad (outputs); element (k, n) = W[n][k].
-    const int total = K * Npad;
-    const uint16_t* gh = reinterpret_cast<const uint16_t*>(g);
-    for (int c = threadIdx.x; c < total; c += blockDim.x) {
-      int k = c / Npad, n = c % Npad;
-      uint16_t v = n < N ? gh[size_t(n) * K + k] : uint16_t(0);
-      st_shared_u16(s + ik_off(k, n, Npad), v);
-    }
+  const int chunks = Npad * (K / 8);
+  for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
+    int n = c / (K / 8), k8 = c % (K / 8);
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (n < N) v = *reinterpret_cast<const uint4*>(g + size_t(n) * K + k8 * 8);
+    st_shared_v4(s + ik_off(n, k8 * 8, K), v.x, v.y, v.z, v.w);
   }
 }
 
