@@ -1003,7 +1003,7 @@ def main():
         print(json.dumps({"profile_frames": 2, "paths": st.paths, "render_ms": st.render_ms,
                           "launches_per_frame": st.kernel_launches, "extension_rays": st.extension_rays,
                           "shadow_rays": st.shadow_rays,
-                          "batch_paths": args.batch_paths or 33554432}))
+                          "batch_paths": args.batch_paths or 67108864}))
         return
 
     # Traversal work of this workload (untimed pass with counters).
@@ -1105,7 +1105,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "paths_per_step": tot["paths"] // args.steps,
                        "bvh_build": "gpu (linear BVH)" if args.gpu_build else "host (binned SAH)",
-                       "l2": "inputs larger than L2 (scene ~240 MB, path state ~10 GB per wavefront)",
+                       "l2": "inputs larger than L2 (scene ~240 MB, path state ~20 GB per wavefront)",
                        "scene_build_ms": info["build_ms"], "bvh_nodes": info["nodes"],
                        "bvh_max_depth": info["max_depth"], "wall_s_timed": wall,
                        "rays_per_s": (tot["ext_rays"] + tot["sh_rays"]) * ws / (ms / 1000.0),

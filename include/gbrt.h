@@ -333,9 +333,9 @@ gbrt_status gbrt_ctx_create(int32_t device, gbrt_ctx** out);
 gbrt_status gbrt_ctx_destroy(gbrt_ctx* ctx);
 /* Per-call device buffers (wavefront state, films) come from a memory pool
  * of the context that keeps freed memory reserved for the next call (about
- * 10 GB after a render with the default wavefront). This returns the
- * reserved, unused part to the driver (and reports how many bytes the pool
- * still holds; may be NULL). */
+ * 20 GB after a render of 2^26 paths or more with the default wavefront).
+ * This returns the reserved, unused part to the driver (and reports how many
+ * bytes the pool still holds; may be NULL). */
 gbrt_status gbrt_ctx_trim(gbrt_ctx* ctx, uint64_t* reserved_bytes);
 
 /* Host-side fault injection, for tests of the failure paths. The renderer
