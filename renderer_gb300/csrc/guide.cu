@@ -57,11 +57,12 @@ constexpr uint32_t kInferCols = 512;  // 64 per warpgroup, rounded up to a power
 
 // Training: the weights, the activation rows X1..X3, the region R (the
 // encoded input X0 rows, 53,248 bytes, kept for the weight gradient of
-// layer 1) and the delta rows. Every tile is stored once: the weight
+// layer 1), the delta rows and the exchange of the loss's lobe terms
+// between the two halves of a row. Every tile is stored once: the weight
 // gradients read the activation and delta rows MN-major (gemm_mn), the dX
 // products the weights MN-major (gemm_k_wmn).
-constexpr int kTX1 = 49152, kTX2 = 65536, kTX3 = 81920, kTR = 98304, kTDR = 151552;
-constexpr int kTMisc = 167936, kTrainSmem = kTMisc + 64;
+constexpr int kTX1 = 49152, kTX2 = 65536, kTX3 = 81920, kTR = 98304, kTDR = 151552, kTXchg = 167936;
+constexpr int kTMisc = kTXchg + 2 * kRows * 16, kTrainSmem = kTMisc + 64;
 constexpr uint32_t kTrainCols = 512;
 constexpr int kTrainThreads = 2 * kRows;  // two threads per row of a tile
 // TMEM columns of the training kernel.
@@ -234,52 +235,108 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
 }
 
 // ------------------------------------------------------------- training ----
-// dLoss/d(raw outputs) of one sample, loss = -w log q(wi).
-__device__ __forceinline__ float loss_grad(const float* o, float wx, float wy, float wz, float w, float* g) {
+// dLoss/d(raw outputs) of one sample, loss = -w log q(wi), with
+//   log q = logsumexp_k lp_k,
+//   lp_k = (o_k - logsumexp_j o_j) + log(kappa_k / (2 pi (1 - exp(-2 kappa_k))))
+//          + kappa_k (mu_k . wi - 1),
+// mu_k the normalised mean outputs and kappa_k = exp(clamp(o_{32+k}, -4, 9));
+// with r_k = exp(lp_k - log q) and p_k the softmax weight:
+//   d/do_k = -w (r_k - p_k),  d/dmean_k = -w r_k kappa_k / |mean_k| (wi - (mu_k . wi) mu_k),
+//   d/do_{32+k} = -w r_k (1 - 2 kappa_k / (exp(2 kappa_k) - 1) + kappa_k (mu_k . wi - 1))
+// inside the clamp (0 outside). The two threads of a row share the lobes:
+// thread half H takes lobes 4H .. 4H + 3. Phase 1 evaluates the weights'
+// normaliser (over all eight) and lp_k of the thread's lobes, and publishes
+// those (four floats per row and half); after a block barrier, phase 2 forms
+// log q from all eight and the gradients of the thread's lobes and writes
+// them, as bfloat16, into its columns of the [128][48] delta row tile.
+struct LossHalf {
+  float lse_a;
+  float lp[4], mx[4], my[4], mz[4], kap[4], cw[4], il[4];
+};
+
+template <int H>
+__device__ __forceinline__ void loss_phase1(const float* o, float wx, float wy, float wz, LossHalf& L,
+                                            float* published) {
   float amax = o[0];
 #pragma unroll
   for (int k = 1; k < kLobes; ++k) amax = fmaxf(amax, o[k]);
   float se = 0.f;
 #pragma unroll
   for (int k = 0; k < kLobes; ++k) se += expf(o[k] - amax);
-  const float lse_a = amax + logf(se);
-  float lp[kLobes], mu[kLobes][3], kap[kLobes], cw[kLobes], il[kLobes];
-  float lmax = -INFINITY;
+  L.lse_a = amax + logf(se);
 #pragma unroll
-  for (int k = 0; k < kLobes; ++k) {
+  for (int j = 0; j < 4; ++j) {
+    const int k = 4 * H + j;
     float x = o[8 + 3 * k], y = o[9 + 3 * k], z = o[10 + 3 * k];
     float l = sqrtf(x * x + y * y + z * z);
     if (l > 1e-12f) {
-      il[k] = 1.f / l;
-      mu[k][0] = x * il[k]; mu[k][1] = y * il[k]; mu[k][2] = z * il[k];
+      L.il[j] = 1.f / l;
+      L.mx[j] = x * L.il[j]; L.my[j] = y * L.il[j]; L.mz[j] = z * L.il[j];
     } else {
-      il[k] = 0.f;
-      mu[k][0] = 0.f; mu[k][1] = 0.f; mu[k][2] = 1.f;
+      L.il[j] = 0.f;
+      L.mx[j] = 0.f; L.my[j] = 0.f; L.mz[j] = 1.f;
     }
-    kap[k] = expf(fminf(fmaxf(o[32 + k], kLogKappaMin), kLogKappaMax));
-    cw[k] = mu[k][0] * wx + mu[k][1] * wy + mu[k][2] * wz;
-    lp[k] = (o[k] - lse_a) + vmf_log_norm(kap[k]) + kap[k] * (cw[k] - 1.f);
-    lmax = fmaxf(lmax, lp[k]);
+    L.kap[j] = expf(fminf(fmaxf(o[32 + k], kLogKappaMin), kLogKappaMax));
+    L.cw[j] = L.mx[j] * wx + L.my[j] * wy + L.mz[j] * wz;
+    L.lp[j] = (o[k] - L.lse_a) + vmf_log_norm(L.kap[j]) + L.kap[j] * (L.cw[j] - 1.f);
   }
+  *reinterpret_cast<float4*>(published) = make_float4(L.lp[0], L.lp[1], L.lp[2], L.lp[3]);
+}
+
+__device__ __forceinline__ void st_shared_v2(uint32_t saddr, uint32_t a, uint32_t b) {
+  asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(saddr), "r"(a), "r"(b) : "memory");
+}
+
+template <int H>
+__device__ __forceinline__ float loss_phase2(const float* o, float wx, float wy, float wz, float w, const LossHalf& L,
+                                             const float* other, uint32_t s_rows, int r) {
+  const float4 q = *reinterpret_cast<const float4*>(other);
+  float lp[kLobes];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) lp[4 * H + j] = L.lp[j];
+  lp[4 * (1 - H) + 0] = q.x; lp[4 * (1 - H) + 1] = q.y; lp[4 * (1 - H) + 2] = q.z; lp[4 * (1 - H) + 3] = q.w;
+  float lmax = -INFINITY;
+#pragma unroll
+  for (int k = 0; k < kLobes; ++k) lmax = fmaxf(lmax, lp[k]);
   float sq = 0.f;
 #pragma unroll
   for (int k = 0; k < kLobes; ++k) sq += expf(lp[k] - lmax);
   const float lq = lmax + logf(sq);
+  float gw[4], gm[12], gk[4];
 #pragma unroll
-  for (int k = 0; k < kLobes; ++k) {
-    float rk = expf(lp[k] - lq);
-    float pk = expf(o[k] - lse_a);
-    g[k] = -w * (rk - pk);
-    float s = -w * rk * kap[k] * il[k];
-    g[8 + 3 * k] = s * (wx - cw[k] * mu[k][0]);
-    g[9 + 3 * k] = s * (wy - cw[k] * mu[k][1]);
-    g[10 + 3 * k] = s * (wz - cw[k] * mu[k][2]);
+  for (int j = 0; j < 4; ++j) {
+    const int k = 4 * H + j;
+    float rk = expf(L.lp[j] - lq);
+    float pk = expf(o[k] - L.lse_a);
+    gw[j] = -w * (rk - pk);
+    float s = -w * rk * L.kap[j] * L.il[j];
+    gm[3 * j] = s * (wx - L.cw[j] * L.mx[j]);
+    gm[3 * j + 1] = s * (wy - L.cw[j] * L.my[j]);
+    gm[3 * j + 2] = s * (wz - L.cw[j] * L.mz[j]);
     bool inside = o[32 + k] > kLogKappaMin && o[32 + k] < kLogKappaMax;
-    float dk = 1.f - 2.f * kap[k] / expm1f(2.f * kap[k]) + kap[k] * (cw[k] - 1.f);
-    g[32 + k] = inside ? -w * rk * dk : 0.f;
+    float dk = 1.f - 2.f * L.kap[j] / expm1f(2.f * L.kap[j]) + L.kap[j] * (L.cw[j] - 1.f);
+    gk[j] = inside ? -w * rk * dk : 0.f;
+  }
+  // Columns: weights 0-7, means 8-31 (three per lobe), kappas 32-39, 40-47
+  // zero; 16-byte chunks of eight columns, the halves' shares aligned to 8 bytes.
+  const uint32_t row = s_rows + ik_off(r, 0, kOutPad);
+  if (H == 0) {
+    st_shared_v2(row, pack_bf16(gw[0], gw[1]), pack_bf16(gw[2], gw[3]));                  // cols 0-3
+    st_shared_v4(row + 128, pack_bf16(gm[0], gm[1]), pack_bf16(gm[2], gm[3]), pack_bf16(gm[4], gm[5]),
+                 pack_bf16(gm[6], gm[7]));                                                  // cols 8-15
+    st_shared_v2(row + 256, pack_bf16(gm[8], gm[9]), pack_bf16(gm[10], gm[11]));          // cols 16-19
+    st_shared_v2(row + 512, pack_bf16(gk[0], gk[1]), pack_bf16(gk[2], gk[3]));            // cols 32-35
+  } else {
+    st_shared_v2(row + 8, pack_bf16(gw[0], gw[1]), pack_bf16(gw[2], gw[3]));              // cols 4-7
+    st_shared_v2(row + 256 + 8, pack_bf16(gm[0], gm[1]), pack_bf16(gm[2], gm[3]));        // cols 20-23
+    st_shared_v4(row + 384, pack_bf16(gm[4], gm[5]), pack_bf16(gm[6], gm[7]), pack_bf16(gm[8], gm[9]),
+                 pack_bf16(gm[10], gm[11]));                                                // cols 24-31
+    st_shared_v2(row + 512 + 8, pack_bf16(gk[0], gk[1]), pack_bf16(gk[2], gk[3]));        // cols 36-39
+    st_shared_v4(row + 640, 0u, 0u, 0u, 0u);                                                // cols 40-47
   }
   return -w * lq;
 }
+
 
 // Half of a hidden layer's input for row r: ReLU(TMEM columns [c0, c0 + 32))
 // into an interleaved [128][64] tile at s.
@@ -418,19 +475,22 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideNet net, 
     handoff();
     if (t == 0 && net.issue) gemm_k(tmem + kColScratch, sX3, kHid, sW4, kHid, kHid, kOutPad, false);
     if (!(ok = sync_chain())) break;
-    if (half == 0) {
-      float o[kOutPad], g[kOutPad];
-      tmem_ld16(lane + kColScratch, o);
-      tmem_ld16(lane + kColScratch + 16, o + 16);
+    {
+      // the loss and the output layer's delta, lobes split between the halves
+      float o[kOutPad];
+      tmem_ld32(lane + kColScratch, o);
       tmem_ld16(lane + kColScratch + 32, o + 32);
-      float ls = loss_grad(o, s3.x, s3.y, s3.z, w, g);
-      if (row < n) loss += ls;
-#pragma unroll
-      for (int j = kOut; j < kOutPad; ++j) g[j] = 0.f;
-#pragma unroll
-      for (int c = 0; c < kOutPad; c += 8)
-        st_shared_v4(sDR + ik_off(r, c, kOutPad), pack_bf16(g[c], g[c + 1]), pack_bf16(g[c + 2], g[c + 3]),
-                     pack_bf16(g[c + 4], g[c + 5]), pack_bf16(g[c + 6], g[c + 7]));
+      float* xchg = reinterpret_cast<float*>(sm + kTXchg);
+      float* mine = xchg + 4 * (half * kRows + r);
+      const float* other = xchg + 4 * ((1 - half) * kRows + r);
+      LossHalf L;
+      if (half == 0) loss_phase1<0>(o, s3.x, s3.y, s3.z, L, mine);
+      else loss_phase1<1>(o, s3.x, s3.y, s3.z, L, mine);
+      __syncthreads();
+      float ls;
+      if (half == 0) ls = loss_phase2<0>(o, s3.x, s3.y, s3.z, w, L, other, sDR, r);
+      else ls = loss_phase2<1>(o, s3.x, s3.y, s3.z, w, L, other, sDR, r);
+      if (half == 0 && row < n) loss += ls;
     }
     // ---- backward: output layer
     handoff();
