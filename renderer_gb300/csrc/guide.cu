@@ -74,8 +74,8 @@ static_assert(64 * kInferWG <= int(kInferCols), "TMEM columns of the inference b
 static_assert(kEncA + kEncB == kIn / 8, "encoding halves");
 
 // Layer input ReLU(TMEM columns [0, 64)) of row r into an interleaved
-// [128][64] tile at s; also returns the values when h is not null.
-__device__ __forceinline__ void hidden_to_smem(uint32_t lane_taddr, uint32_t s, int r, float* h) {
+// [128][64] tile at s.
+__device__ __forceinline__ void hidden_to_smem(uint32_t lane_taddr, uint32_t s, int r) {
 #pragma unroll
   for (int c = 0; c < kHid; c += 32) {
     float v[32];
@@ -85,10 +85,6 @@ __device__ __forceinline__ void hidden_to_smem(uint32_t lane_taddr, uint32_t s, 
       st_shared_v4(s + ik_off(r, c + 8 * q, kHid), pack_relu_bf16(v[8 * q], v[8 * q + 1]),
                    pack_relu_bf16(v[8 * q + 2], v[8 * q + 3]), pack_relu_bf16(v[8 * q + 4], v[8 * q + 5]),
                    pack_relu_bf16(v[8 * q + 6], v[8 * q + 7]));
-    if (h) {
-#pragma unroll
-      for (int i = 0; i < 32; ++i) h[c + i] = fmaxf(v[i], 0.f);
-    }
   }
 }
 
@@ -195,7 +191,7 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
     wg_handoff(bid);
     if (t == 0 && net.issue) gemm_k(tmem, sX, 8 * kEncB, sW1 + kEncA * 128, kIn, 8 * kEncB, kHid, true);
     if (!(ok = chain_wait())) break;
-    hidden_to_smem(lane, sX, t, nullptr);
+    hidden_to_smem(lane, sX, t);
     // Layers 2 and 3, then the output layer (N = 48, 40 used).
     for (int layer = 1; layer < 4; ++layer) {
       wg_handoff(bid);
@@ -206,7 +202,7 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
       }
       if (!(ok = chain_wait())) break;
       if (layer < 3) {
-        hidden_to_smem(lane, sX, t, nullptr);
+        hidden_to_smem(lane, sX, t);
       } else {
         float o[kOutPad];
         tmem_ld32(lane, o);
