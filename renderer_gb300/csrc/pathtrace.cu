@@ -986,8 +986,40 @@ __global__ void __launch_bounds__(256) k_guide_collect(PTParams P, PTState st) {
 }
 
 // --------------------------------------------------------- accumulate ----
+// Float-float running sum (Knuth's TwoSum: every addition's rounding error is
+// carried in lo), so that a batch's samples of a pixel are summed to about
+// 2^-48 relative, the accuracy of an FP64 sum, with FP32 operations only: the
+// GB300's FP64 pipe runs at a small fraction of its FP32 rate, and one FP64
+// conversion and addition per sample and channel was most of the
+// accumulation's time. Each pixel's float-float sums are added into the FP64
+// pixel sums once per batch. Squares enter as exact product pairs (fmaf).
+struct FSum {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+  }
+  __device__ __forceinline__ void add_square(float x) {
+    const float p = x * x;
+    add(p);
+    lo += fmaf(x, x, -p);
+  }
+  __device__ __forceinline__ void merge(float h, float l) {
+    add(h);
+    lo += l;
+  }
+  __device__ __forceinline__ void shfl_merge(int offset, int width = 32) {
+    const float h = __shfl_down_sync(0xffffffffu, hi, offset, width);
+    const float l = __shfl_down_sync(0xffffffffu, lo, offset, width);
+    merge(h, l);
+  }
+  __device__ __forceinline__ double value() const { return double(hi) + double(lo); }
+};
+
 // One thread per pixel touched by the batch; samples of a pixel are
-// contiguous slots. FP64 sums; non-finite samples are counted and dropped.
+// contiguous slots. Non-finite samples are counted and dropped.
 __global__ void __launch_bounds__(256) k_accumulate(PTParams P, PTState st, double* sum, double* sumsq) {
   unsigned long long p0 = P.g0 / unsigned(P.spp);
   unsigned long long p1 = (P.g0 + unsigned(P.nb) - 1) / unsigned(P.spp);
@@ -995,19 +1027,19 @@ __global__ void __launch_bounds__(256) k_accumulate(PTParams P, PTState st, doub
   if (p > p1) return;
   unsigned long long gb = max(P.g0, p * unsigned(P.spp));
   unsigned long long ge = min(P.g0 + unsigned(P.nb), (p + 1) * unsigned(P.spp));
-  double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0;
+  FSum s0, s1, s2, q0, q1, q2;
   unsigned long long bad = 0;
   for (unsigned long long g = gb; g < ge; ++g) {
     float4 L = st.L[g - P.g0];
     if (P.nan_every && g % P.nan_every == 0) L.x = CUDART_NAN_F;
     if (!isfinite(L.x) || !isfinite(L.y) || !isfinite(L.z)) { ++bad; continue; }
-    s0 += L.x; s1 += L.y; s2 += L.z;
-    q0 += double(L.x) * L.x; q1 += double(L.y) * L.y; q2 += double(L.z) * L.z;
+    s0.add(L.x); s1.add(L.y); s2.add(L.z);
+    if (sumsq) { q0.add_square(L.x); q1.add_square(L.y); q2.add_square(L.z); }
   }
   if (bad) atomicAdd(&st.tally[2], bad);
   size_t o = size_t(p) * 3;
-  sum[o] += s0; sum[o + 1] += s1; sum[o + 2] += s2;
-  if (sumsq) { sumsq[o] += q0; sumsq[o + 1] += q1; sumsq[o + 2] += q2; }
+  sum[o] += s0.value(); sum[o + 1] += s1.value(); sum[o + 2] += s2.value();
+  if (sumsq) { sumsq[o] += q0.value(); sumsq[o + 1] += q1.value(); sumsq[o + 2] += q2.value(); }
 }
 
 // The same with one warp per pixel, for many samples per pixel.
@@ -1019,29 +1051,25 @@ __global__ void __launch_bounds__(256) k_accumulate_warp(PTParams P, PTState st,
   if (p > p1) return;  // whole warps leave together
   const unsigned long long gb = max(P.g0, p * unsigned(P.spp));
   const unsigned long long ge = min(P.g0 + unsigned(P.nb), (p + 1) * unsigned(P.spp));
-  double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0;
+  FSum s0, s1, s2, q0, q1, q2;
   unsigned long long bad = 0;
   for (unsigned long long g = gb + lane; g < ge; g += 32) {
     float4 L = st.L[g - P.g0];
     if (P.nan_every && g % P.nan_every == 0) L.x = CUDART_NAN_F;
     if (!isfinite(L.x) || !isfinite(L.y) || !isfinite(L.z)) { ++bad; continue; }
-    s0 += L.x; s1 += L.y; s2 += L.z;
-    q0 += double(L.x) * L.x; q1 += double(L.y) * L.y; q2 += double(L.z) * L.z;
+    s0.add(L.x); s1.add(L.y); s2.add(L.z);
+    if (sumsq) { q0.add_square(L.x); q1.add_square(L.y); q2.add_square(L.z); }
   }
   for (int o = 16; o > 0; o >>= 1) {
-    s0 += __shfl_down_sync(0xffffffffu, s0, o);
-    s1 += __shfl_down_sync(0xffffffffu, s1, o);
-    s2 += __shfl_down_sync(0xffffffffu, s2, o);
-    q0 += __shfl_down_sync(0xffffffffu, q0, o);
-    q1 += __shfl_down_sync(0xffffffffu, q1, o);
-    q2 += __shfl_down_sync(0xffffffffu, q2, o);
+    s0.shfl_merge(o); s1.shfl_merge(o); s2.shfl_merge(o);
+    if (sumsq) { q0.shfl_merge(o); q1.shfl_merge(o); q2.shfl_merge(o); }
     bad += __shfl_down_sync(0xffffffffu, bad, o);
   }
   if (lane == 0) {
     if (bad) atomicAdd(&st.tally[2], bad);
     size_t o = size_t(p) * 3;
-    sum[o] += s0; sum[o + 1] += s1; sum[o + 2] += s2;
-    if (sumsq) { sumsq[o] += q0; sumsq[o + 1] += q1; sumsq[o + 2] += q2; }
+    sum[o] += s0.value(); sum[o + 1] += s1.value(); sum[o + 2] += s2.value();
+    if (sumsq) { sumsq[o] += q0.value(); sumsq[o + 1] += q1.value(); sumsq[o + 2] += q2.value(); }
   }
 }
 
@@ -1146,7 +1174,7 @@ __global__ void __launch_bounds__(256) k_accumulate_ms(PTState st, BatchDev bt) 
   const unsigned long long spp = unsigned(b.P.spp);
   const unsigned long long a = max(G0, b.start) - b.start, e = min(G1, b.start + b.total) - b.start;
   const unsigned long long p = a / spp + px;
-  double s0 = 0, s1 = 0, s2 = 0;
+  FSum s0, s1, s2;
   unsigned long long bad = 0;
   if (live) {
     const unsigned long long gb = max(a, p * spp), ge = min(e, (p + 1) * spp);
@@ -1154,22 +1182,20 @@ __global__ void __launch_bounds__(256) k_accumulate_ms(PTState st, BatchDev bt) 
       float4 L = st.L[b.start + g - G0];
       if (b.P.nan_every && g % b.P.nan_every == 0) L.x = CUDART_NAN_F;
       if (!isfinite(L.x) || !isfinite(L.y) || !isfinite(L.z)) { ++bad; continue; }
-      s0 += L.x; s1 += L.y; s2 += L.z;
+      s0.add(L.x); s1.add(L.y); s2.add(L.z);
     }
   }
   for (int o = G >> 1; o > 0; o >>= 1) {
-    s0 += __shfl_down_sync(0xffffffffu, s0, o, G);
-    s1 += __shfl_down_sync(0xffffffffu, s1, o, G);
-    s2 += __shfl_down_sync(0xffffffffu, s2, o, G);
+    s0.shfl_merge(o, G); s1.shfl_merge(o, G); s2.shfl_merge(o, G);
     bad += __shfl_down_sync(0xffffffffu, bad, o, G);
   }
   if (live && sub == 0) {
     if (bad) atomicAdd(&st.tally[2], bad);
     double* o = bt.sum + 3 * (b.pix0 + p);
     if (bt.shared_sum) {  // a pixel's samples can lie in two pipelines' wavefronts
-      atomicAdd(o, s0); atomicAdd(o + 1, s1); atomicAdd(o + 2, s2);
+      atomicAdd(o, s0.value()); atomicAdd(o + 1, s1.value()); atomicAdd(o + 2, s2.value());
     } else {
-      o[0] += s0; o[1] += s1; o[2] += s2;
+      o[0] += s0.value(); o[1] += s1.value(); o[2] += s2.value();
     }
   }
 }

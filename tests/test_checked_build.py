@@ -60,9 +60,14 @@ with Context(0) as ctx:
     from renderer_gb300.guiding import Guide, guide_params, render_guided, scene_bounds
     gr = GpuScene(ctx, scenes["cornell"])
     guide = Guide(ctx, scene_bounds(gr), seed=1)
-    film, st = render_guided(gr, scenes["cornell"].camera_struct(), render_params(1, 1, 0.5, 8, 5, semantics=_abi.SEM_PHYSICAL),
-                             guide, guide_params(0.5, passes=4, train_passes=4, steps_per_pass=2, batch_samples=1 << 14))
+    gcam = scenes["cornell"].camera_struct()
+    gpar = render_params(1, 1, 0.5, 8, 5, semantics=_abi.SEM_PHYSICAL)
+    film, st = render_guided(gr, gcam, gpar, guide,
+                             guide_params(0.5, passes=4, train_passes=4, steps_per_pass=2, batch_samples=1 << 14))
     out["guided_mean"] = np.array([film.mean()])
+    # a fixed network (no training): inference and guided shading are deterministic
+    guide.set_weights(np.random.default_rng(3).normal(0.0, 0.1, _abi.GUIDE_PARAMS).astype(np.float32))
+    out["guided_fixed"], _ = render_guided(gr, gcam, gpar, guide, guide_params(0.5, passes=2))
     guide.close()
     from renderer_gb300.batch import BatchJob, render_batch_fused
     jobs = [BatchJob(GpuScene(ctx, scenes[k]), scenes[k].camera_struct(), render_params(2, 1, 0.5, 6, 9))
@@ -90,8 +95,11 @@ def test_checked_build_renders_the_same_images(tmp_path):
     b = _run(LIB_PATH, tmp_path / "normal.npz")
     assert set(a.files) == set(b.files) and len(a.files) >= 12
     for k in a.files:
-        if k == "guided_mean":  # training gathers gradients with float atomics
-            assert a[k][0] == pytest.approx(b[k][0], rel=0.05)
+        if k == "guided_mean":
+            # training gathers gradients with float atomics, so the two guides
+            # differ in their last bits and the guided paths part ways: the
+            # images are two estimates of one mean (4 spp of a 48 x 48 box)
+            assert a[k][0] == pytest.approx(b[k][0], rel=0.2)
         elif k == "trace_prim":
             assert np.array_equal(a[k], b[k])
         else:
