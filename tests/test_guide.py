@@ -213,7 +213,7 @@ def test_guided_render_is_unbiased_and_helps(ctx):
         return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
 
     ratios = []
-    for seed in (1, 2):
+    for seed in (1, 2, 3):
         g = Guide(ctx, scene_bounds(sc), seed=seed)
         gp = guide_params(0.5, passes=16, train_passes=16, steps_per_pass=32, batch_samples=1 << 16,
                           learning_rate=1e-2)
@@ -225,11 +225,13 @@ def test_guided_render_is_unbiased_and_helps(ctx):
         assert guided.mean() == pytest.approx(ref.mean(), rel=0.02)
         ratios.append(relmse(guided) / relmse(plain))
     # Training is not bit-reproducible (samples and gradients are gathered
-    # with atomics) and its result varies: over repeated runs the ratio of one
-    # guide was 0.52-0.77 in most runs, about 1.0 in some and once 1.41 (this
-    # radiance target sends guided directions past the glossy floor's lobe;
-    # the product target, tested below, does not). Of two guides trained
-    # independently, the better one helps and neither hurts badly.
+    # with atomics, and Adam turns the last-bit differences of near-zero
+    # gradients into different steps) and its result varies: over guide seeds
+    # 1-8 in one run the ratio was 0.52-1.07 (median 0.67), and a guide's
+    # ratio once reached 1.41 (this radiance target sends guided directions
+    # past the glossy floor's lobe; the product target, tested below, does
+    # not). Of three guides trained independently, the best one helps and
+    # none hurts badly.
     assert min(ratios) < 0.85 and max(ratios) < 1.6, ratios
 
 
