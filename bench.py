@@ -234,8 +234,7 @@ def run_guided(args):
         return p
 
     gflags = (0 if args.absolute_weights else _abi.GUIDE_PIXEL_RELATIVE) | (
-        _abi.GUIDE_PRODUCT if args.product_target else 0) | (_abi.GUIDE_ASYNC_TRAINING if args.async_train else 0) | (
-        _abi.GUIDE_LEARNED_SELECTION if args.learned_selection else 0)
+        _abi.GUIDE_PRODUCT if args.product_target else 0) | (_abi.GUIDE_ASYNC_TRAINING if args.async_train else 0)
 
     def train_gp(budget_ms=0.0, passes=0):
         return guide_params(args.guide_fraction, passes=passes, train_passes=args.train_passes,
@@ -348,9 +347,7 @@ def run_guided(args):
                                    "BSDF x radiance x cos" if args.product_target else "radiance x cos"),
                        "passes": "inverse-variance weighted (the first, unguided pass seeds the mean)",
                        "training_stream": "second stream, overlapping the next pass" if args.async_train
-                       else "the render stream, between passes",
-                       "selection": "learned per vertex (network output)" if args.learned_selection
-                       else "fixed fraction %g" % args.guide_fraction},
+                       else "the render stream, between passes"},
             "plain": [{"ms": t, "relmse": e, "spp": n} for t, e, n in plain],
             "guided": [{"ms": t, "relmse": e, "spp": n, "train_steps": k, "train_ms": tm}
                        for t, e, n, k, tm in guided],
@@ -898,9 +895,6 @@ def main():
     ap.add_argument("--train-passes", type=int, default=1 << 30, help="passes that train (default: all)")
     ap.add_argument("--async-train", action="store_true",
                     help="with --guided: Adam steps on a second stream, overlapping the next pass")
-    ap.add_argument("--learned-selection", action="store_true",
-                    help="with --guided: each vertex samples the guide with the network's own selection "
-                         "probability (GBRT_GUIDE_LEARNED_SELECTION) instead of --guide-fraction")
     ap.add_argument("--product-target", action="store_true",
                     help="--guided: the guide learns BSDF x incident radiance x cos (GBRT_GUIDE_PRODUCT)")
     ap.add_argument("--tuned", action="store_true",

@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define GBRT_ABI_VERSION 2
+#define GBRT_ABI_VERSION 1
 
 typedef enum gbrt_status {
   GBRT_OK = 0,
@@ -573,21 +573,15 @@ gbrt_status gbrt_batch_autotune_fused(gbrt_ctx* ctx, const gbrt_batch_job* jobs,
  * accumulation; FP32 master weights and Adam state live on the device. */
 typedef struct gbrt_guide gbrt_guide;
 /* Parameters: row-major [out][in] matrices W1 64x208, W2 64x64, W3 64x64,
- * W4 41x64, concatenated. */
-#define GBRT_GUIDE_PARAMS 24128
+ * W4 40x64, concatenated. */
+#define GBRT_GUIDE_PARAMS 24064
 /* One network input: point, normal facing the viewer, outgoing direction. */
 #define GBRT_GUIDE_INPUT 9
-/* One mixture: lobe weights [8], then (mean x, y, z, kappa) for each lobe,
- * then the probability c of sampling the guide rather than the BSDF at the
- * vertex (0.1 + 0.6 sigmoid of the last output; renders use it with
- * GBRT_GUIDE_LEARNED_SELECTION). */
-#define GBRT_GUIDE_OUTPUT 41
+/* One mixture: lobe weights [8], then (mean x, y, z, kappa) for each lobe. */
+#define GBRT_GUIDE_OUTPUT 40
 /* One training sample: point, normal, outgoing direction, sampled incident
- * direction, weight = target / pdf, and the BSDF's sampling density p at the
- * direction. p = 0: loss = -mean(weight * log q(direction)); p > 0: the
- * mixture the renderer samples with learned selection,
- * loss = -mean(weight * log(c q + (1 - c) p)), which also trains c. */
-#define GBRT_GUIDE_SAMPLE 14
+ * direction, weight = target / pdf (loss = -mean(weight * log q(direction))). */
+#define GBRT_GUIDE_SAMPLE 13
 
 gbrt_status gbrt_guide_create(gbrt_ctx* ctx, const float bounds[6],
                               uint64_t seed, gbrt_guide** out);
@@ -667,12 +661,7 @@ typedef enum gbrt_guide_flags {
    * that training and rendering overlap on the GPU. The sample buffers and
    * the weight snapshots are double-buffered; the call returns after all of
    * its steps, with the guide's weights those of the last step. */
-  GBRT_GUIDE_ASYNC_TRAINING = 8,
-  /* Each guided vertex samples the guide with the network's own selection
-   * probability c (GBRT_GUIDE_OUTPUT) instead of guide_fraction, one-sample
-   * MIS with pdf c q + (1 - c) p_bsdf, and the training samples carry the
-   * BSDF density so that c is learned with the mixture objective. */
-  GBRT_GUIDE_LEARNED_SELECTION = 16
+  GBRT_GUIDE_ASYNC_TRAINING = 8
 } gbrt_guide_flags;
 
 typedef struct gbrt_guide_stats {

@@ -9,12 +9,9 @@ only, src/unidipathtracingintegrator.cpp:34-46):
             sin/cos(2^j pi v), j = 0..11, per coordinate; theta / pi and
             phi / 2pi + 1/2 of the outgoing direction as 32 Gaussian bins each
             (sigma = 1 / 32, phi wrapped)
-  network   208 -> 64 -> 64 -> 64 -> 41, ReLU, no biases
-  output    softmax lobe weights, normalised means, kappa = exp(clamp(b, -4, 9)),
-            and the selection probability c = 0.1 + 0.6 sigmoid(b)
-  loss      -(1/N) sum w log q(wi), q the vMF mixture; samples that carry the
-            BSDF density p > 0 at wi also train c on -w log(c q(wi) + (1 - c) p)
-            with q held fixed (its gradient reaches the network through c only)
+  network   208 -> 64 -> 64 -> 64 -> 40, ReLU, no biases
+  output    softmax lobe weights, normalised means, kappa = exp(clamp(b, -4, 9))
+  loss      -(1/N) sum w log q(wi), q the vMF mixture
 
 With bf16=True the layer inputs and the weights are rounded to bfloat16 as
 the tensor-core kernels do (straight through for the gradient), so the GPU
@@ -25,10 +22,9 @@ import math
 import numpy as np
 import torch
 
-K_IN, K_HID, K_OUT, LOBES, BANDS, BLOB = 208, 64, 41, 8, 12, 32
-SEL_MIN, SEL_RANGE = 0.1, 0.6
+K_IN, K_HID, K_OUT, LOBES, BANDS, BLOB = 208, 64, 40, 8, 12, 32
 LOGK_MIN, LOGK_MAX = -4.0, 9.0
-SHAPES = [(64, 208), (64, 64), (64, 64), (41, 64)]
+SHAPES = [(64, 208), (64, 64), (64, 64), (40, 64)]
 N_PARAMS = sum(a * b for a, b in SHAPES)
 
 
@@ -73,7 +69,7 @@ def encode(inputs, bounds):
 
 
 def forward(w, x0, bf16=True):
-    """Raw outputs (N, 41) of the network on encoded inputs x0."""
+    """Raw outputs (N, 40) of the network on encoded inputs x0."""
     W = split(w)
     r = _bf16 if bf16 else (lambda t: t)
     W = [r(m) for m in W]
@@ -83,20 +79,14 @@ def forward(w, x0, bf16=True):
     return h @ W[3].T
 
 
-def selection(o):
-    """The probability of sampling the guide, from the raw outputs."""
-    return SEL_MIN + SEL_RANGE * torch.sigmoid(o[:, 40])
-
-
 def decode(o):
-    """Raw outputs -> (N, 41) mixture: weights [8], then (mean xyz, kappa) x 8,
-    then the selection probability."""
+    """Raw outputs -> (N, 40) mixture: weights [8], then (mean xyz, kappa) x 8."""
     pi = torch.softmax(o[:, :LOBES], 1)
     m = o[:, 8:32].reshape(-1, LOBES, 3)
     mu = m / torch.linalg.norm(m, dim=2, keepdim=True)
     kap = torch.exp(torch.clamp(o[:, 32:40], LOGK_MIN, LOGK_MAX))
     lobes = torch.cat([mu, kap[:, :, None]], 2).reshape(-1, 4 * LOBES)
-    return torch.cat([pi, lobes, selection(o)[:, None]], 1)
+    return torch.cat([pi, lobes], 1)
 
 
 def log_q(o, wi):
@@ -110,45 +100,18 @@ def log_q(o, wi):
     return torch.logsumexp(logpi + logf, 1)
 
 
-def _objective(w, samples, bounds, bf16, lq_fixed):
+def loss_and_grad(w, samples, bounds, bf16=True):
+    """Loss -(1/N) sum w log q and its gradient (N_PARAMS,) for samples
+    (N, 13): point, normal, outgoing, sampled direction, weight."""
     s = np.asarray(samples, np.float32)
+    wt = torch.tensor(np.asarray(w, np.float64), requires_grad=True)
     x0 = encode(s[:, 0:9], bounds)
-    o = forward(w, x0, bf16)
+    o = forward(wt, x0, bf16)
     wi = torch.as_tensor(s[:, 9:12], dtype=torch.float64)
     weight = torch.as_tensor(s[:, 12], dtype=torch.float64)
-    p = torch.as_tensor(s[:, 13], dtype=torch.float64)
-    lq = log_q(o, wi)
-    lq0 = lq.detach() if lq_fixed is None else torch.as_tensor(lq_fixed, dtype=torch.float64)
-    c = selection(o)
-    mixed = torch.log(c * torch.exp(lq0) + (1 - c) * torch.clamp(p, min=0.0))
-    loss = -(weight * lq).sum() / len(s)
-    objective = loss - (weight * torch.where(p > 0, mixed, torch.zeros_like(mixed))).sum() / len(s)
-    return loss, objective, lq.detach()
-
-
-def loss_and_grad(w, samples, bounds, bf16=True):
-    """Loss -(1/N) sum w log q and the gradient (N_PARAMS,) of the training
-    objective, for samples (N, 14): point, normal, outgoing, sampled
-    direction, weight, BSDF density p at the direction. The objective is the
-    loss plus, for samples with p > 0, -(1/N) w log(c q + (1 - c) p) with q
-    held fixed (it trains the selection probability c only)."""
-    wt = torch.tensor(np.asarray(w, np.float64), requires_grad=True)
-    loss, objective, _ = _objective(wt, samples, bounds, bf16, None)
-    objective.backward()
+    loss = -(weight * log_q(o, wi)).sum() / len(s)
+    loss.backward()
     return float(loss.detach()), wt.grad.numpy().copy()
-
-
-def sample_log_q(w, samples, bounds, bf16=True):
-    """log q(wi) of every sample (the values the selection term holds fixed)."""
-    with torch.no_grad():
-        return _objective(torch.as_tensor(np.asarray(w, np.float64)), samples, bounds, bf16, None)[2].numpy()
-
-
-def objective_value(w, samples, bounds, lq_fixed, bf16=True):
-    """The training objective's value with the selection term's log q fixed
-    at lq_fixed (so that finite differences give loss_and_grad's gradient)."""
-    with torch.no_grad():
-        return float(_objective(torch.as_tensor(np.asarray(w, np.float64)), samples, bounds, bf16, lq_fixed)[1])
 
 
 def mixture(w, inputs, bounds, bf16=True):
@@ -157,11 +120,11 @@ def mixture(w, inputs, bounds, bf16=True):
 
 
 def mixture_pdf(mix, wi):
-    """Density of the mixtures (N, 40 or 41) at the unit directions wi (N, 3)."""
+    """Density of the mixtures (N, 40) at the unit directions wi (N, 3)."""
     mix = np.asarray(mix, np.float64)
     wi = np.asarray(wi, np.float64)
     pi = mix[:, :8]
-    lob = mix[:, 8:40].reshape(-1, 8, 4)
+    lob = mix[:, 8:].reshape(-1, 8, 4)
     c = (lob[:, :, :3] * wi[:, None, :]).sum(2)
     k = lob[:, :, 3]
     f = k / (2 * math.pi * (-np.expm1(-2 * k))) * np.exp(k * (c - 1))

@@ -169,11 +169,10 @@ RENDER_TIME_KERNELS, RENDER_COUNT_TRAVERSAL = 1, 2
 NOALLOC_MAX_BATCH = 65536
 # gbrt_fault (host-side fault injection for the failure-path tests)
 FAULT_NONE, FAULT_ALLOC, FAULT_NAN, FAULT_SMALL_STACK, FAULT_GUIDE_WAIT = 0, 1, 2, 3, 4
-GUIDE_PARAMS, GUIDE_INPUT, GUIDE_OUTPUT, GUIDE_SAMPLE = 24128, 9, 41, 14
+GUIDE_PARAMS, GUIDE_INPUT, GUIDE_OUTPUT, GUIDE_SAMPLE = 24064, 9, 40, 13
 CSG_SPHERE, CSG_BOX, CSG_ISECT, CSG_UNION, CSG_DIFF, CSG_XOR = range(6)
 CSG_MAX_LEAVES = 8
 GUIDE_EQUAL_WEIGHTS, GUIDE_PIXEL_RELATIVE, GUIDE_PRODUCT, GUIDE_ASYNC_TRAINING = 1, 2, 4, 8
-GUIDE_LEARNED_SELECTION = 16
 
 P = C.c_void_p
 

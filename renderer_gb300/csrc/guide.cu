@@ -72,8 +72,6 @@ static_assert(kTrainSmem <= 232448, "training tile exceeds the shared memory of 
 static_assert(kInferSmem <= 232448, "inference block exceeds the shared memory of a block");
 static_assert(64 * kInferWG <= int(kInferCols), "TMEM columns of the inference block");
 static_assert(kEncA + kEncB == kIn / 8, "encoding halves");
-static_assert(kParams == GBRT_GUIDE_PARAMS && kOut == GBRT_GUIDE_OUTPUT && GBRT_GUIDE_SAMPLE == 14,
-              "the guide's sizes in the C ABI");
 
 // Layer input ReLU(TMEM columns [0, 64)) of row r into an interleaved
 // [128][64] tile at s.
@@ -194,7 +192,7 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
     if (t == 0 && net.issue) gemm_k(tmem, sX, 8 * kEncB, sW1 + kEncA * 128, kIn, 8 * kEncB, kHid, true);
     if (!(ok = chain_wait())) break;
     hidden_to_smem(lane, sX, t);
-    // Layers 2 and 3, then the output layer (N = 48, 41 used).
+    // Layers 2 and 3, then the output layer (N = 48, 40 used).
     for (int layer = 1; layer < 4; ++layer) {
       wg_handoff(bid);
       if (t == 0) {
@@ -241,13 +239,7 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_guide_infer(GuideNet net,
 // with r_k = exp(lp_k - log q) and p_k the softmax weight:
 //   d/do_k = -w (r_k - p_k),  d/dmean_k = -w r_k kappa_k / |mean_k| (wi - (mu_k . wi) mu_k),
 //   d/do_{32+k} = -w r_k (1 - 2 kappa_k / (exp(2 kappa_k) - 1) + kappa_k (mu_k . wi - 1))
-// inside the clamp (0 outside). A sample that carries the BSDF's density
-// p > 0 at wi also trains the selection probability c = 0.1 + 0.6
-// sigmoid(o_40) of learned selection, on the mixture the renderer samples,
-// -w log(c q + (1 - c) p) with q held fixed:
-//   d/do_40 = -w (q - p) / (c q + (1 - c) p) * 0.6 sigmoid (1 - sigmoid);
-// the guide itself keeps its own objective (the gradients above).
-// The two threads of a row share the lobes:
+// inside the clamp (0 outside). The two threads of a row share the lobes:
 // thread half H takes lobes 4H .. 4H + 3. Phase 1 evaluates the weights'
 // normaliser (over all eight) and lp_k of the thread's lobes, and publishes
 // those (four floats per row and half); after a block barrier, phase 2 forms
@@ -292,8 +284,8 @@ __device__ __forceinline__ void st_shared_v2(uint32_t saddr, uint32_t a, uint32_
 }
 
 template <int H>
-__device__ __forceinline__ float loss_phase2(const float* o, float wx, float wy, float wz, float w, float pb,
-                                             const LossHalf& L, const float* other, uint32_t s_rows, int r) {
+__device__ __forceinline__ float loss_phase2(const float* o, float wx, float wy, float wz, float w, const LossHalf& L,
+                                             const float* other, uint32_t s_rows, int r) {
   const float4 q = *reinterpret_cast<const float4*>(other);
   float lp[kLobes];
 #pragma unroll
@@ -306,13 +298,6 @@ __device__ __forceinline__ float loss_phase2(const float* o, float wx, float wy,
 #pragma unroll
   for (int k = 0; k < kLobes; ++k) sq += expf(lp[k] - lmax);
   const float lq = lmax + logf(sq);
-  float gz = 0.f;
-  if (pb > 0.f) {  // learned selection: c's objective is the sampled mixture
-    const float sg = 1.f / (1.f + expf(-o[kSel]));
-    const float c = kSelMin + kSelRange * sg;
-    const float qv = expf(lq);
-    gz = -w * (qv - pb) / (c * qv + (1.f - c) * pb) * (kSelRange * sg * (1.f - sg));
-  }
   float gw[4], gm[12], gk[4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
@@ -328,9 +313,8 @@ __device__ __forceinline__ float loss_phase2(const float* o, float wx, float wy,
     float dk = 1.f - 2.f * L.kap[j] / expm1f(2.f * L.kap[j]) + L.kap[j] * (L.cw[j] - 1.f);
     gk[j] = inside ? -w * rk * dk : 0.f;
   }
-  // Columns: weights 0-7, means 8-31 (three per lobe), kappas 32-39, the
-  // selection logit 40, 41-47 zero; 16-byte chunks of eight columns, the
-  // halves' shares aligned to 8 bytes.
+  // Columns: weights 0-7, means 8-31 (three per lobe), kappas 32-39, 40-47
+  // zero; 16-byte chunks of eight columns, the halves' shares aligned to 8 bytes.
   const uint32_t row = s_rows + ik_off(r, 0, kOutPad);
   if (H == 0) {
     st_shared_v2(row, pack_bf16(gw[0], gw[1]), pack_bf16(gw[2], gw[3]));                  // cols 0-3
@@ -344,7 +328,7 @@ __device__ __forceinline__ float loss_phase2(const float* o, float wx, float wy,
     st_shared_v4(row + 384, pack_bf16(gm[4], gm[5]), pack_bf16(gm[6], gm[7]), pack_bf16(gm[8], gm[9]),
                  pack_bf16(gm[10], gm[11]));                                                // cols 24-31
     st_shared_v2(row + 512 + 8, pack_bf16(gk[0], gk[1]), pack_bf16(gk[2], gk[3]));        // cols 36-39
-    st_shared_v4(row + 640, pack_bf16(gz, 0.f), 0u, 0u, 0u);                               // cols 40-47
+    st_shared_v4(row + 640, 0u, 0u, 0u, 0u);                                                // cols 40-47
   }
   return -w * lq;
 }
@@ -500,8 +484,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideNet net, 
       else loss_phase1<1>(o, s3.x, s3.y, s3.z, L, mine);
       __syncthreads();
       float ls;
-      if (half == 0) ls = loss_phase2<0>(o, s3.x, s3.y, s3.z, w, s3.w, L, other, sDR, r);
-      else ls = loss_phase2<1>(o, s3.x, s3.y, s3.z, w, s3.w, L, other, sDR, r);
+      if (half == 0) ls = loss_phase2<0>(o, s3.x, s3.y, s3.z, w, L, other, sDR, r);
+      else ls = loss_phase2<1>(o, s3.x, s3.y, s3.z, w, L, other, sDR, r);
       if (half == 0 && row < n) loss += ls;
     }
     // ---- backward: output layer
@@ -836,29 +820,24 @@ gbrt_status gbrt_guide_eval(gbrt_guide* g, const float* inputs, size_t n, float*
   if (e == cudaSuccess) e = ctx_alloc(g->ctx, &d_mix, kMixStride * n * sizeof(float4), s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = launch_infer(g, d_in, nullptr, int(n), d_mix, s);
-  std::vector<float4> mixes(kMixStride * n);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(mixes.data(), d_mix, mixes.size() * sizeof(float4), cudaMemcpyDeviceToHost, s);
+    e = cudaMemcpy2DAsync(out, 10 * sizeof(float4), d_mix, kMixStride * sizeof(float4), 10 * sizeof(float4), n,
+                          cudaMemcpyDeviceToHost, s);
   if (d_in) cudaFreeAsync(d_in, s);
   if (d_mix) cudaFreeAsync(d_mix, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(g->ctx, e, "gbrt_guide_eval");
-  // per row: the 40 floats of (pi0..7, (mean, kappa) x 8), then the selection probability
-  for (size_t i = 0; i < n; ++i) {
-    std::memcpy(out + GBRT_GUIDE_OUTPUT * i, &mixes[kMixStride * i], 40 * sizeof(float));
-    out[GBRT_GUIDE_OUTPUT * i + 40] = mixes[kMixStride * i + 12].x;
-  }
   return read_err(g, s);
 }
 
 static gbrt_status upload_samples(gbrt_guide* g, const float* samples, size_t n, float4** d_out) {
   std::vector<float4> h(4 * n);
   for (size_t i = 0; i < n; ++i) {
-    const float* r = samples + GBRT_GUIDE_SAMPLE * i;
+    const float* r = samples + 13 * i;
     h[4 * i] = make_float4(r[0], r[1], r[2], r[12]);
     h[4 * i + 1] = make_float4(r[3], r[4], r[5], 0.f);
     h[4 * i + 2] = make_float4(r[6], r[7], r[8], 0.f);
-    h[4 * i + 3] = make_float4(r[9], r[10], r[11], r[13]);
+    h[4 * i + 3] = make_float4(r[9], r[10], r[11], 0.f);
   }
   cudaStream_t s = g->ctx->stream;
   cudaError_t e = ctx_alloc(g->ctx, d_out, h.size() * sizeof(float4), s);

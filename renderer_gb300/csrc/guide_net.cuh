@@ -6,16 +6,13 @@
 //                coordinate as sin/cos(2^j pi v), j = 0..11 (2 x 72), and the
 //                outgoing direction as a one-blob encoding of theta / pi and
 //                phi / 2pi with 32 Gaussian bins each (64)
-//   layers 208 -> 64 -> 64 -> 64 -> 41, ReLU between, no biases, BF16
+//   layers 208 -> 64 -> 64 -> 64 -> 40, ReLU between, no biases, BF16
 //          operands with FP32 accumulation on the tensor cores (tcgen05)
 //   output 8 lobes: softmax weights (8), mean directions (8 x 3, normalised),
-//          concentrations kappa = exp(clamp(b, -4, 9)) (8), and the
-//          probability of sampling the guide rather than the BSDF at the
-//          vertex, c = 0.1 + 0.6 sigmoid(b) (1; used by renders with
-//          GBRT_GUIDE_LEARNED_SELECTION)
+//          concentrations kappa = exp(clamp(b, -4, 9)) (8)
 // Parameters, FP32 master copy and BF16 copy alike, are four row-major
 // matrices [out][in] one after the other: W1 64x208, W2 64x64, W3 64x64,
-// W4 41x64 (24,128 values).
+// W4 40x64 (24,064 values).
 //
 // Shared-memory operand layout (tcgen05 "no swizzle"): an R x K BF16 tile is
 // stored as 8 x 8 core matrices of 128 contiguous bytes; the K/8 core
@@ -32,9 +29,7 @@
 namespace gbrt {
 namespace guide {
 
-constexpr int kIn = 208, kHid = 64, kOut = 41, kOutPad = 48, kLobes = 8, kRows = 128;
-constexpr int kSel = 40;  // output of the selection logit
-constexpr float kSelMin = 0.1f, kSelRange = 0.6f;
+constexpr int kIn = 208, kHid = 64, kOut = 40, kOutPad = 48, kLobes = 8, kRows = 128;
 constexpr int kBands = 12, kBlob = 32;
 constexpr int kW1 = kHid * kIn, kW2 = kHid * kHid, kW3 = kHid * kHid, kW4 = kOut * kHid;
 constexpr int kOffW1 = 0, kOffW2 = kW1, kOffW3 = kW1 + kW2, kOffW4 = kW1 + kW2 + kW3;
@@ -42,9 +37,8 @@ constexpr int kParams = kW1 + kW2 + kW3 + kW4;
 constexpr float kLogKappaMin = -4.f, kLogKappaMax = 9.f;
 // A stored mixture: (pi0..3), (pi4..7), (mean, kappa) per lobe, then the
 // normalised lobe weights c_k = pi_k kappa_k / (2 pi (1 - exp(-2 kappa_k)))
-// in two float4, so that q(w) = sum_k c_k exp(kappa_k (mean_k . w - 1)),
-// then (selection probability, 0, 0, 0).
-constexpr int kMixStride = 13;
+// in two float4, so that q(w) = sum_k c_k exp(kappa_k (mean_k . w - 1)).
+constexpr int kMixStride = 12;
 constexpr float kPi = 3.14159265358979323846f;
 
 // Device view of a network.
@@ -334,7 +328,6 @@ struct Mixture {
   float pi[kLobes];
   float mx[kLobes], my[kLobes], mz[kLobes];
   float kappa[kLobes];
-  float sel;
 };
 
 // log of the vMF normalisation kappa / (2 pi (1 - exp(-2 kappa))).
@@ -342,7 +335,7 @@ __device__ __forceinline__ float vmf_log_norm(float k) {
   return logf(k) - logf(2.f * kPi) - logf(-expm1f(-2.f * k));
 }
 
-// Decodes the 41 raw outputs with the fast intrinsics (__expf, rsqrtf,
+// Decodes the 40 raw outputs with the fast intrinsics (__expf, rsqrtf,
 // __frcp_rn): relative errors of a few 1e-7, below the bfloat16 rounding of
 // the layers that produced the outputs.
 __device__ __forceinline__ void decode_mixture(const float* o, Mixture& m) {
@@ -369,7 +362,6 @@ __device__ __forceinline__ void decode_mixture(const float* o, Mixture& m) {
     }
     m.kappa[k] = __expf(fminf(fmaxf(o[32 + k], kLogKappaMin), kLogKappaMax));
   }
-  m.sel = kSelMin + kSelRange * __frcp_rn(1.f + __expf(-o[kSel]));
 }
 
 // 1 - exp(-x) for x >= 0: its Taylor series to x^4 below 1/8 (relative error
@@ -392,7 +384,6 @@ __device__ __forceinline__ void store_mixture(float4* out, const Mixture& m) {
   for (int k = 0; k < kLobes; ++k) out[2 + k] = make_float4(m.mx[k], m.my[k], m.mz[k], m.kappa[k]);
   out[10] = make_float4(c[0], c[1], c[2], c[3]);
   out[11] = make_float4(c[4], c[5], c[6], c[7]);
-  out[12] = make_float4(m.sel, 0.f, 0.f, 0.f);
 }
 
 // Mixture pdf (solid angle) of the unit direction (x, y, z).

@@ -64,7 +64,6 @@ struct PTParams {
   int physical;            // GBRT_SEM_PHYSICAL
   int guided;              // sample non-specular vertices from the guide's mixtures too
   float guide_frac;        // probability of sampling the guide (one-sample MIS)
-  int learned_sel;         // the guide's own per-vertex selection probability instead of guide_frac
   int record;              // write training records for the guide
   int guide_depth;         // guide vertices i < guide_depth only (0: all)
   int train_relative;      // training weights relative to the sample's pixel
@@ -130,15 +129,14 @@ struct PTState {
 };
 
 // Training records of the guide: the first kRecords guided vertices of a
-// path. Record component c of record r of a slot is rec[(7 r + c) nslots +
+// path. Record component c of record r of a slot is rec[(6 r + c) nslots +
 // slot]: (point, pdf), (normal, wi.x), (wo, wi.y), (throughput after the
 // vertex, wi.z), (radiance of the path when the next vertex was reached),
-// (mean throughput before the vertex, throughput before the vertex), (the
-// BSDF's sampling density at wi, -, -, -; with learned selection only).
+// (mean throughput before the vertex, -, -, -).
 // ctl.z of a guided path: records written (low 4 bits), kRecOpen while the
 // last record waits for its radiance snapshot.
 constexpr int kRecords = 4;
-constexpr int kRecComp = 7;
+constexpr int kRecComp = 6;
 constexpr int kRecOpen = 0x100;
 
 // Many images in one wavefront (gbrt_render_batch_fused). The jobs' paths
@@ -843,29 +841,25 @@ __device__ __forceinline__ void shade_phys_body(const DeviceScene& S0, const PTP
     const bool depthOk = P.guide_depth == 0 || i < P.guide_depth;
     const bool guideHere = GUIDED && P.guided && depthOk && b.kind >= 1 && b.kind <= 3;
     const float4* M = guideHere ? st.mix + guide::kMixStride * size_t(q) : nullptr;
-    // probability of sampling the guide here: the network's own (learned
-    // selection) or the fixed fraction
-    const float frac = (GUIDED && M && P.learned_sel) ? M[12].x : P.guide_frac;
-    if (b.kind <= 3 && S.n_lights > 0) nee_phys(S, st, slot, key, base, b, x, nrm, wo, alpha, M, frac);
+    if (b.kind <= 3 && S.n_lights > 0) nee_phys(S, st, slot, key, base, b, x, nrm, wo, alpha, M, P.guide_frac);
     V3f wi, wgt;
-    float pdf, pbsdf;
+    float pdf;
     bool spec;
     const float u0 = stream_u(key, base), u1 = stream_u(key, base + 1), u2 = stream_u(key, base + 2);
     if (guideHere) {
-      if (stream_u(key, base + 7) < frac) {
+      if (stream_u(key, base + 7) < P.guide_frac) {
         guide::mixture_sample(M, u0, u1, u2, wi.x, wi.y, wi.z);
       } else if (!phys_sample(b, nrm, wo, flipped, u0, u1, u2, wi, wgt, pdf, spec)) {
         continue;
       }
-      V3f f = phys_eval(b, nrm, wo, wi, pbsdf);
-      pdf = frac * guide::mixture_pdf(M, wi.x, wi.y, wi.z) + (1.f - frac) * pbsdf;
+      float pb;
+      V3f f = phys_eval(b, nrm, wo, wi, pb);
+      pdf = P.guide_frac * guide::mixture_pdf(M, wi.x, wi.y, wi.z) + (1.f - P.guide_frac) * pb;
       if (is_zero(f) || !(pdf > 0.f)) continue;
       wgt = (dot(nrm, wi) / pdf) * f;
       spec = false;
     } else if (!phys_sample(b, nrm, wo, flipped, u0, u1, u2, wi, wgt, pdf, spec)) {
       continue;
-    } else {
-      pbsdf = pdf;
     }
     V3f na = mulc(alpha, wgt);
     if (i + 1 >= 3 && P.term_p > 0.f) {
@@ -884,7 +878,6 @@ __device__ __forceinline__ void shade_phys_body(const DeviceScene& S0, const PTP
         st.rec[r + 2 * ns] = make_float4(wo.x, wo.y, wo.z, wi.y);
         st.rec[r + 3 * ns] = make_float4(na.x, na.y, na.z, wi.z);
         st.rec[r + 5 * ns] = make_float4((alpha.x + alpha.y + alpha.z) * (1.f / 3.f), alpha.x, alpha.y, alpha.z);
-        if (P.learned_sel) st.rec[r + 6 * ns] = make_float4(pbsdf, 0.f, 0.f, 0.f);
         z = ((z & 15) + 1) | kRecOpen;
       }
     }
@@ -988,10 +981,7 @@ __global__ void __launch_bounds__(256) k_guide_collect(PTParams P, PTState st) {
     st.tsamp[4 * size_t(e)] = make_float4(r0.x, r0.y, r0.z, w);
     st.tsamp[4 * size_t(e) + 1] = make_float4(r1.x, r1.y, r1.z, 0.f);
     st.tsamp[4 * size_t(e) + 2] = make_float4(r2.x, r2.y, r2.z, 0.f);
-    // the BSDF density at wi with learned selection (the sample then trains
-    // the mixture objective and the selection probability), else 0
-    const float pb = P.learned_sel ? st.rec[b + 6 * ns].x : 0.f;
-    st.tsamp[4 * size_t(e) + 3] = make_float4(r1.w, r2.w, r3.w, pb);
+    st.tsamp[4 * size_t(e) + 3] = make_float4(r1.w, r2.w, r3.w, 0.f);
   }
 }
 
@@ -1941,7 +1931,6 @@ static gbrt_status render_guided_impl(gbrt_scene* s, const gbrt_camera* cam, con
     P.guide_depth = gp->guide_depth;
     P.train_relative = (gp->flags & GBRT_GUIDE_PIXEL_RELATIVE) ? 1 : 0;
     P.train_product = (gp->flags & GBRT_GUIDE_PRODUCT) ? 1 : 0;
-    P.learned_sel = (gp->flags & GBRT_GUIDE_LEARNED_SELECTION) ? 1 : 0;
     P.film_sum = d_sum;
     P.pass_sum = d_pass;
     P.inv_samples = 1.0 / double(samples + (unsigned long long)sppPass);

@@ -66,17 +66,14 @@ class Guide:
 
     def eval(self, inputs):
         """inputs (N, 9): point, normal facing the viewer, outgoing direction.
-        Returns (N, 41): lobe weights [8], then (mean xyz, kappa) per lobe,
-        then the probability of sampling the guide (learned selection)."""
+        Returns (N, 40): lobe weights [8], then (mean xyz, kappa) per lobe."""
         x = np.ascontiguousarray(inputs, np.float32).reshape(-1, _abi.GUIDE_INPUT)
         out = np.zeros((len(x), _abi.GUIDE_OUTPUT), np.float32)
         check(lib().gbrt_guide_eval(self.handle, _ptr(x), len(x), _ptr(out)), self.ctx.handle)
         return out
 
     def gradient(self, samples):
-        """samples (N, 14): point, normal, outgoing, sampled direction,
-        weight, and the BSDF's density at the direction (> 0: the mixture
-        objective of learned selection; 0: the guide's density alone).
+        """samples (N, 13): point, normal, outgoing, sampled direction, weight.
         Returns (gradient of the loss, loss)."""
         s = np.ascontiguousarray(samples, np.float32).reshape(-1, _abi.GUIDE_SAMPLE)
         g = np.zeros(_abi.GUIDE_PARAMS, np.float32)

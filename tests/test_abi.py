@@ -31,7 +31,7 @@ def test_library_loads_and_exports_every_symbol(gbrt_built):
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert not missing, missing
     lib.gbrt_abi_version.restype = ctypes.c_int32
-    assert lib.gbrt_abi_version() == 2
+    assert lib.gbrt_abi_version() == 1
 
 
 def test_exports_are_c_symbols(gbrt_built):

@@ -119,8 +119,7 @@ def test_guide_wait_timeout_returns_timeout_and_frees_tensor_memory(fctx):
     n = 4096
     x = np.concatenate([rng.uniform(box[:3], box[3:], (n, 3)), unit(rng.normal(size=(n, 3))),
                         unit(rng.normal(size=(n, 3)))], 1).astype(np.float32)
-    samples = np.concatenate([x, unit(rng.normal(size=(n, 3))), rng.exponential(1.0, (n, 1)), np.zeros((n, 1))],
-                             1).astype(np.float32)
+    samples = np.concatenate([x, unit(rng.normal(size=(n, 3))), rng.exponential(1.0, (n, 1))], 1).astype(np.float32)
     guide = Guide(fctx, box, seed=4)
     want = guide.eval(x)
     g0, l0 = guide.gradient(samples)
