@@ -515,7 +515,7 @@ gbrt_status gbrt_render_batch(gbrt_ctx* ctx, const gbrt_batch_job* jobs,
                               int32_t n, int32_t streams, int64_t batch_paths,
                               double* job_ms, gbrt_batch_stats* stats);
 /* Renders up to 8 of the jobs at one sample per pixel with 1, 2, 4 and 8
- * streams and wavefronts of 2^20, 2^22 and 2^24 paths, keeps the fastest pair on
+ * streams and wavefronts of 2^22 and 2^24 paths, keeps the fastest pair on
  * the context (for later calls with 0s) and returns it. Films are not
  * written. */
 gbrt_status gbrt_batch_autotune(gbrt_ctx* ctx, const gbrt_batch_job* jobs,
